@@ -1,0 +1,174 @@
+// Device-side state of one BUSseq chain and the constants of the model.
+//
+// Layout in HBM (N cells in batch-contiguous order, G genes, Gp = G rounded up
+// to GENE_TILE so every row starts on a 512-byte boundary):
+//   Y, X        int32  [N][Gp]   observed counts / imputed underlying counts
+//   y0m, zm     uint32 [N][Gp/32] bit masks: Y == 0, dropout indicator Z
+//   beta, L     [K][Gp]          (reference layout k*G+g)
+//   nu, phi     [B][Gp]          (reference layout b*G+g)
+//   E           [B][K][Gp]       exp(alpha_g + beta_kg + nu_bg), kept current
+//   W, delta, Dexp = exp(delta)  [N]
+//   perm        [N]              cells sorted by (batch, cell type), rebuilt
+//                                after every W update
+//   gchunk      int4 [cap_g]     gene-pass work list: {b, k, first, count} runs
+//                                of <= CG cells of one (batch, type) segment
+//   ctile       int4 [cap_c]     cell-pass work list: runs of <= CELL_TILE cells
+//   part        f64 [cap_g][4][Gp] per-chunk partial sums of the gene passes
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace bq {
+
+// ---- hyper-parameters of the model (BUSseq_gpu.cu:12-32) ------------------
+constexpr float P_INIT_BOUND = 0.5f;
+constexpr float TAU0_INIT = 0.005f;
+constexpr float GAMMA0_INIT = 0.0f;
+constexpr float GAMMA1_INIT = -0.3f;
+constexpr float PHI_INIT = 5.0f;
+constexpr double XI_PI = 2.0;
+constexpr double SIGMA2_ALPHA = 5.0;
+constexpr double SIGMA2_NU = 5.0;
+constexpr double SIGMA2_DELTA = 5.0;
+constexpr double SIGMA2_GAMMA0 = 3.0;
+constexpr double KAPPA_GAMMA1 = 0.001;
+constexpr double TAU_GAMMA1 = 0.01;
+constexpr double KAPPA_PHI = 1.0;
+constexpr double TAU_PHI = 0.1;
+constexpr double A_P = 1.0;
+constexpr double B_P = 3.0;
+constexpr double A_TAU0 = 2.0;
+constexpr double B_TAU0 = 0.01;
+constexpr double TAU1 = 100.0;
+constexpr float RW_STEP = 0.1f;  // random-walk proposal s.d. of alpha, beta, nu, delta, gamma0
+
+// ---- launch geometry -------------------------------------------------------
+constexpr int GENE_TILE = 128;     // genes per gene-pass CTA (one per thread)
+constexpr int CELL_TILE = 8;       // cells per cell-pass CTA
+constexpr int CELL_THREADS = 256;  // threads of a cell-pass CTA (4 genes each per step)
+constexpr int MAX_B = 128;
+constexpr int MAX_K = 64;
+constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
+constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
+constexpr int PHI_TAB = 16;        // small-count table of lgamma differences
+
+// ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
+enum Stage : int {
+  STAGE_ZX_GAMMA_ALPHA_L = 0,  // Z/X, gamma0, gamma1, alpha, L (and p, tau0 at the tail)
+  STAGE_PTAU_BETA_NU = 1,      // (p, tau0 already drawn) beta, nu
+  STAGE_DELTA = 2,
+  STAGE_PHI = 3,
+  STAGE_W = 4,
+  STAGE_PI = 5,                // pi, then the new cell order
+  N_STAGES = 6
+};
+
+// Proposal families (bit mask for the proposal kernel).
+enum PropMask : int {
+  PROP_GAMMA = 1, PROP_ALPHA = 2, PROP_BETA = 4, PROP_NU = 8, PROP_DELTA = 16, PROP_PHI = 32,
+  PROP_ALL = 63
+};
+
+struct DevState {
+  // dimensions and run configuration
+  int B, K;
+  int64_t G, N, Gp, Gw;
+  int n_tiles;      // ceil(G / GENE_TILE)
+  int cap_g, CG;    // gene-pass chunk capacity and chunk length
+  int cap_c;        // cell-pass tile capacity
+  int n_static;     // CTAs evaluating the static (Y > 0) gamma terms
+  int ymax;         // largest observed count
+  int w_update;     // 0: MH with uniform proposal (reference), 1: K-way Gibbs
+  int n_burnin, n_unchanged, keep_draws, n_kept;
+  uint64_t seed;
+
+  // data
+  const int32_t* Y;
+  int32_t* X;
+  const uint32_t* y0m;
+  uint32_t* zm;
+  const int32_t* batch_of;   // [N]
+  const int32_t* batch_off;  // [B+1]
+  const int32_t* yhist;      // [B][ymax+1] counts of Y values (Y > 0 entries only)
+
+  // parameters (float) and indicators
+  int32_t* W;
+  int8_t* L;
+  float* alpha;
+  float* mu_alpha;
+  float* beta;
+  float* nu;
+  float* mu_nu;    // [B]
+  float* delta;
+  float* mu_delta;
+  float* Dexp;
+  float* phi;
+  float* gamma;    // [2][B]
+  float* pi;       // [B][K]
+  float* p_tau0;   // [2]
+  float* E;        // [B][K][Gp]
+
+  // proposals of the current sweep
+  float* alpha_p;
+  float* beta_p;   // [K][Gp]
+  float* nu_p;     // [B][Gp]
+  float* delta_p;  // [N]
+  float* phi_p;    // [B][Gp]
+  float* gamma_p;  // [2][B]
+
+  // cell order and work lists
+  int32_t* perm;
+  int4* gchunk;
+  int4* ctile;
+  int32_t* seg_cnt;  // [B][K]
+
+  // scratch (partial sums and completion counters)
+  double* part;    // [cap_g][NSLOT][Gp]
+  double* gpart;   // [cap_g * n_tiles][GSLOT]
+  double* gstat;   // [n_static][4]
+  double* tpart;   // [n_tiles][2]
+  unsigned* cnt_tile;  // [n_tiles]
+  unsigned* cnt_glob;  // [4]
+
+  int* iter;       // sweep index, advanced on the device at the end of a sweep
+  int* err;        // sampler / numerical error bits
+
+  // log acceptance ratios of the last sweep (likelihood + prior), double
+  double* lr_gamma;  // [2][B]
+  double* lr_alpha;  // [G]
+  double* lr_beta;   // [K][G]
+  double* lr_nu;     // [B][G]
+  double* lr_delta;  // [N]
+  double* lr_phi;    // [B][G]
+  double* lr_W;      // [N]
+
+  // posterior accumulators (kept sweeps)
+  double* acc_alpha;
+  double* acc_beta;   // [K][G]
+  double* acc_L;      // [K][G]
+  double* acc_nu;     // [B][G]
+  double* acc_delta;  // [N]
+  double* acc_phi;    // [B][G]
+  double* acc_gamma;  // [2B]
+  double* acc_pi;     // [B*K]
+  double* acc_ptau;   // [2]
+  int32_t* acc_wcnt;  // [N][K]
+
+  // preserved draws, [kept sweep][scalar] (only when keep_draws)
+  float* keep_gamma;
+  float* keep_alpha;
+  float* keep_beta;   // (K-1)*G per sweep
+  int8_t* keep_L;     // (K-1)*G per sweep
+  float* keep_ptau;
+  float* keep_nu;     // (B-1)*G per sweep
+  float* keep_delta;
+  float* keep_phi;    // B*G per sweep
+  int16_t* keep_W;
+  float* keep_pi;
+};
+
+// eta = alpha + beta + nu, always summed in this order so that every kernel
+// rounds it identically.
+__device__ __forceinline__ float eta3(float a, float b, float n) { return (a + b) + n; }
+
+}  // namespace bq

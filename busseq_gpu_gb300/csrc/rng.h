@@ -1,0 +1,273 @@
+// Counter-based random numbers and the distribution samplers behind every
+// conditional update of the BUSseq Gibbs sweep.
+//
+// The reference draws from one stored cuRAND XORWOW state per (cell, gene)
+// entry (BUSseq_gpu.cu:220-224, 48 bytes each, 4.8 GB at N = G = 10^4) and
+// from R's rgamma (BUSseq_gpu.cu:34-197).  This build stores no generator
+// state at all: every draw is a pure function of
+//     (seed, stream id, entity index, sweep index, block number)
+// through Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11).  A conditional update keys its
+// stream by the entity it updates (entry i*G+g, gene g, cell i, ...), so the
+// draws do not depend on launch shape, thread mapping or processing order,
+// and a CPU restatement can consume exactly the same uniforms.
+//
+// Samplers (all written from the published methods named beside them):
+//   normal   : Box-Muller, cosine branch only (Box and Muller 1958)
+//   gamma    : Marsaglia and Tsang (2000), with the U^(1/a) boost for a < 1
+//   poisson  : sequential inversion for lambda < 10, PTRS transformed
+//              rejection with squeeze (Hormann 1993) for lambda >= 10
+//   NB       : gamma-Poisson mixture, as the reference's rnbinom
+//              (BUSseq_gpu.cu:199-210)
+//
+// Everything here is single precision on the device; every rejection loop
+// has an iteration cap that raises a flag instead of spinning forever.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define BQ_HD __host__ __device__ __forceinline__
+#else
+#define BQ_HD inline
+#endif
+
+namespace bq {
+
+// ---------------------------------------------------------------------------
+// Stream ids: one per kind of random decision in a sweep.
+// ---------------------------------------------------------------------------
+enum StreamId : uint32_t {
+  SID_ZX = 1,            // entry i*G+g : Z Bernoulli, NB proposal, MH accept
+  SID_GAMMA = 2,         // batch b     : gamma0 proposal (u0,u1), gamma0 accept (u2), gamma1 accept (u3)
+  SID_GAMMA1_PROP = 3,   // batch b     : gamma1 proposal (Gamma draw)
+  SID_ALPHA = 4,         // gene g      : proposal (u0,u1), accept (u2)
+  SID_L = 5,             // (k-1)*G+g   : indicator L
+  SID_P = 6,             // 0           : p ~ Beta (two Gamma draws)
+  SID_TAU0 = 7,          // 0           : tau0 (one Gamma draw)
+  SID_BETA = 8,          // (k-1)*G+g   : proposal (u0,u1), accept (u2)
+  SID_NU = 9,            // (b-1)*G+g   : proposal (u0,u1), accept (u2)
+  SID_DELTA = 10,        // cell i      : proposal (u0,u1), accept (u2)
+  SID_PHI_PROP = 11,     // b*G+g       : proposal (Gamma draw)
+  SID_PHI_ACC = 12,      // b*G+g       : accept (u0)
+  SID_W = 13,            // cell i      : proposal / categorical (u0), accept (u1)
+  SID_PI = 14,           // b*K+k       : Dirichlet component (Gamma draw)
+  SID_INIT_W = 20,       // cell i      : initial cell type
+  SID_INIT_L = 21,       // k*G+g       : initial indicator L
+  SID_SIM = 30           // synthetic-data generator (not used by the sampler)
+};
+
+// Iteration caps of the rejection samplers.  Hitting one sets an error bit.
+constexpr int GAMMA_MAX_ITER = 64;
+constexpr int POISSON_MAX_ITER = 64;
+constexpr int POISSON_INV_MAX_K = 256;
+constexpr float POISSON_MAX_LAMBDA = 1.0e9f;
+enum SamplerErr : int { ERR_GAMMA_CAP = 1, ERR_POISSON_CAP = 2 };
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10
+// ---------------------------------------------------------------------------
+struct U32x4 { uint32_t x, y, z, w; };
+
+BQ_HD void mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+#if defined(__CUDA_ARCH__)
+  hi = __umulhi(a, b);
+  lo = a * b;
+#else
+  const uint64_t p = (uint64_t)a * (uint64_t)b;
+  hi = (uint32_t)(p >> 32);
+  lo = (uint32_t)p;
+#endif
+}
+
+BQ_HD U32x4 philox4x32_10(U32x4 c, uint32_t k0, uint32_t k1) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(0xD2511F53u, c.x, hi0, lo0);
+    mulhilo32(0xCD9E8D57u, c.z, hi1, lo1);
+    c = U32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+  }
+  return c;
+}
+
+// Uniform on the open interval (0,1): (2m+1) * 2^-24 with m the top 23 bits.
+// Every value is exact in float and in double, so a double-precision
+// restatement sees the very same numbers.
+BQ_HD float u32_to_unit(uint32_t r) {
+  return ((float)(r >> 9) + 0.5f) * 1.1920928955078125e-07f;
+}
+
+// Counter layout: x = entity bits 0..31, y = entity bits 32..47 | stream<<16,
+// z = block number within the stream, w = sweep index.  Key = seed.
+struct Stream {
+  uint32_t k0, k1, c0, c1, blk, it;
+  uint32_t b0, b1, b2, b3;
+  int n;
+  BQ_HD Stream(uint64_t seed, uint32_t sid, uint64_t entity, uint32_t iter)
+      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), c0((uint32_t)entity),
+        c1(((uint32_t)(entity >> 32) & 0xFFFFu) | (sid << 16)), blk(0), it(iter),
+        b0(0), b1(0), b2(0), b3(0), n(0) {}
+  BQ_HD uint32_t next_u32() {
+    if (n == 0) {
+      const U32x4 r = philox4x32_10(U32x4{c0, c1, blk, it}, k0, k1);
+      ++blk;
+      b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w;
+      n = 4;
+    }
+    const uint32_t v = b0;
+    b0 = b1; b1 = b2; b2 = b3;
+    --n;
+    return v;
+  }
+  BQ_HD float uniform() { return u32_to_unit(next_u32()); }
+};
+
+// ---------------------------------------------------------------------------
+// Single-precision math shims (device intrinsics vs. host libm)
+// ---------------------------------------------------------------------------
+BQ_HD float cospi2f(float u) {  // cos(2*pi*u)
+#if defined(__CUDA_ARCH__)
+  return cospif(2.0f * u);
+#else
+  return (float)cos(6.283185307179586 * (double)u);
+#endif
+}
+
+BQ_HD float bq_lgammaf(float x) {
+#if defined(__CUDA_ARCH__)
+  return lgammaf(x);
+#else
+  return (float)lgamma((double)x);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Samplers
+// ---------------------------------------------------------------------------
+// Standard normal: z = sqrt(-2 log u1) cos(2 pi u2).  Consumes 2 uniforms.
+BQ_HD float normal(Stream& s) {
+  const float u1 = s.uniform();
+  const float u2 = s.uniform();
+  return sqrtf(-2.0f * logf(u1)) * cospi2f(u2);
+}
+
+// Gamma(shape a, scale 1), Marsaglia and Tsang (2000).  Each try consumes a
+// normal (2 uniforms) and, unless 1 + c z <= 0, one more uniform.  Shapes
+// below one draw Gamma(a+1) and multiply by U^(1/a) (one more uniform).
+BQ_HD float gamma_mt(Stream& s, float a, int* err) {
+  if (!(a > 0.0f)) return 0.0f;
+  const bool boost = a < 1.0f;
+  const float aa = boost ? a + 1.0f : a;
+  const float d = aa - (1.0f / 3.0f);
+  const float c = 1.0f / sqrtf(9.0f * d);
+  float x = d;
+  int it = 0;
+  for (; it < GAMMA_MAX_ITER; ++it) {
+    const float z = normal(s);
+    float v = 1.0f + c * z;
+    if (v <= 0.0f) continue;
+    v = v * v * v;
+    const float u = s.uniform();
+    const float z2 = z * z;
+    if (u < 1.0f - 0.0331f * (z2 * z2)) { x = d * v; break; }
+    if (logf(u) < 0.5f * z2 + d * (1.0f - v + logf(v))) { x = d * v; break; }
+  }
+  if (it == GAMMA_MAX_ITER) *err |= ERR_GAMMA_CAP;
+  if (boost) {
+    const float u = s.uniform();
+    x = x * expf(logf(u) / a);
+  }
+  return x;
+}
+
+// Poisson(lambda).  Inversion below 10 (one uniform), PTRS above (two
+// uniforms per try).
+BQ_HD int poisson(Stream& s, float lam, int* err) {
+  if (!(lam > 0.0f)) return 0;
+  if (lam > POISSON_MAX_LAMBDA) lam = POISSON_MAX_LAMBDA;
+  if (lam < 10.0f) {
+    const float u = s.uniform();
+    float p = expf(-lam);
+    float F = p;
+    int k = 0;
+    while (u > F && k < POISSON_INV_MAX_K) {
+      ++k;
+      p = p * (lam / (float)k);
+      const float Fn = F + p;
+      if (Fn == F) break;  // the cumulative sum stopped growing
+      F = Fn;
+    }
+    return k;
+  }
+  const float slam = sqrtf(lam);
+  const float loglam = logf(lam);
+  const float b = 0.931f + 2.53f * slam;
+  const float a = -0.059f + 0.02483f * b;
+  const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+  const float vr = 0.9277f - 3.6224f / (b - 2.0f);
+  for (int it = 0; it < POISSON_MAX_ITER; ++it) {
+    const float U = s.uniform() - 0.5f;
+    const float V = s.uniform();
+    const float us = 0.5f - fabsf(U);
+    const float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+    if (us >= 0.07f && V <= vr) return (int)kf;
+    if (kf < 0.0f || (us < 0.013f && V > us)) continue;
+    const float lhs = logf(V) + logf(invalpha) - logf(a / (us * us) + b);
+    const float rhs = -lam + kf * loglam - bq_lgammaf(kf + 1.0f);
+    if (lhs <= rhs) return (int)kf;
+  }
+  *err |= ERR_POISSON_CAP;
+  return (int)lam;
+}
+
+// Negative binomial with mean mu and size phi, as Gamma(phi, mu/phi) then
+// Poisson (the reference's rnbinom, BUSseq_gpu.cu:199-210).
+BQ_HD int negbin(Stream& s, float mu, float phi, int* err) {
+  const float g = gamma_mt(s, phi, err);
+  return poisson(s, g * (mu / phi), err);
+}
+
+// ---------------------------------------------------------------------------
+// Numerically stable differences used by every Metropolis ratio
+// ---------------------------------------------------------------------------
+BQ_HD float softplusf(float t) {
+  return t > 0.0f ? t + log1pf(expf(-t)) : log1pf(expf(t));
+}
+
+// softplus(t + dlt) - softplus(t) without cancellation.
+BQ_HD float softplus_diff(float t, float dlt) {
+  if (fabsf(dlt) < 0.5f) {
+    const float sig = 1.0f / (1.0f + expf(-t));
+    return log1pf(sig * expm1f(dlt));
+  }
+  return softplusf(t + dlt) - softplusf(t);
+}
+
+// lgamma(z + dlt) - lgamma(z) for z > 0, z + dlt > 0, without cancellation.
+// For z, z + dlt >= 8 it uses the difference of Stirling's series
+//   lgamma(z) = (z - 1/2) log z - z + log(2 pi)/2 + 1/(12z) - 1/(360z^3) + 1/(1260z^5) - ...
+// rearranged as (z' - 1/2) log1p(dlt/z) + dlt (log z - 1) + S(z') - S(z);
+// smaller arguments are shifted up with lgamma(x+1) = lgamma(x) + log x.
+BQ_HD float stirling_tail(float z) {
+  const float r = 1.0f / z;
+  const float r2 = r * r;
+  return r * (1.0f / 12.0f - r2 * (1.0f / 360.0f - r2 * (1.0f / 1260.0f)));
+}
+
+BQ_HD float lgamma_diff(float z, float dlt) {
+  float acc = 0.0f;
+  float zz = z;
+  for (int j = 0; j < 8 && (zz < 8.0f || zz + dlt < 8.0f); ++j) {
+    acc -= log1pf(dlt / zz);
+    zz += 1.0f;
+  }
+  const float zp = zz + dlt;
+  return acc + (zp - 0.5f) * log1pf(dlt / zz) + dlt * (logf(zz) - 1.0f) +
+         (stirling_tail(zp) - stirling_tail(zz));
+}
+
+}  // namespace bq

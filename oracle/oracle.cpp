@@ -1,0 +1,934 @@
+// ===========================================================================
+// FP64 CPU oracle of the BUSseq Gibbs sweep -- TEST INFRASTRUCTURE ONLY.
+//
+// This file is the checker.  Only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference arm of bench.py load it; the product library never
+// links, loads or calls it.
+//
+// It restates, in double precision and in plain C++, the conditional updates
+// of the reference BUSseq_gpu.cu (Anguscgm/BUSseq_gpu):
+//   Z/X            BUSseq_gpu.cu:484-512
+//   gamma0/gamma1  BUSseq_gpu.cu:514-600   (driver :1274-1297)
+//   alpha          BUSseq_gpu.cu:602-632   (driver :1299-1307)
+//   L, p, tau0     BUSseq_gpu.cu:634-668   (driver :1309-1321)
+//   beta           BUSseq_gpu.cu:670-707   (driver :1323-1332)
+//   nu             BUSseq_gpu.cu:709-737   (driver :1334-1345)
+//   delta          BUSseq_gpu.cu:739-778   (driver :1347-1359)
+//   phi            BUSseq_gpu.cu:780-818   (driver :1361-1375)
+//   W (MH)         BUSseq_gpu.cu:820-854   (driver :1377-1385), plus the K-way
+//                  categorical (Gibbs) draw of the same conditional
+//   pi             BUSseq_gpu.cu:856-890   (driver :1387-1398)
+//   init           BUSseq_gpu.cu:369-482, :1163-1244
+//   posterior      BUSseq_gpu.cu:1557-1608, :938-959
+//   BIC            BUSseq_gpu.cu:967-1024, :1815-1843
+//
+// Randomness: the reference uses cuRAND XORWOW and R's rgamma; neither is
+// reproduced.  The oracle instead consumes the SAME counter-based uniforms as
+// the CUDA kernels (Philox4x32-10 keyed by seed, stream id, entity, sweep),
+// restated here independently of the product header, and runs double
+// precision versions of the same published samplers (Box-Muller,
+// Marsaglia-Tsang gamma, inversion / Hormann PTRS Poisson) in the same
+// consumption order.  Every comparison that decides a discrete outcome
+// records a normalised margin, so a test can tell a genuine disagreement from
+// a near-tie that single-precision kernels may legitimately decide the other
+// way.
+//
+// Parity of the likelihood formulas with the reference itself is pinned by
+// golden vectors produced by the reference's own kernels
+// (tests/golden/make_ref_golden.py, oracle/ref_harness.cpp).
+// ===========================================================================
+#include <stdint.h>
+#include <math.h>
+#include <string.h>
+#include <stdlib.h>
+#include <vector>
+#include <algorithm>
+#include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+// ---- hyper-parameters: BUSseq_gpu.cu:12-32 --------------------------------
+constexpr double TAU0_INIT = 0.005;
+constexpr double GAMMA0_INIT = 0.0;
+constexpr double GAMMA1_INIT = -0.3;
+constexpr double PHI_INIT = 5.0;
+constexpr double XI_PI = 2.0;
+constexpr double SIGMA2_ALPHA = 5.0;
+constexpr double SIGMA2_NU = 5.0;
+constexpr double SIGMA2_DELTA = 5.0;
+constexpr double SIGMA2_GAMMA0 = 3.0;
+constexpr double KAPPA_GAMMA1 = 0.001;
+constexpr double TAU_GAMMA1 = 0.01;
+constexpr double KAPPA_PHI = 1.0;
+constexpr double TAU_PHI = 0.1;
+constexpr double A_P = 1.0;
+constexpr double B_P = 3.0;
+constexpr double A_TAU0 = 2.0;
+constexpr double B_TAU0 = 0.01;
+constexpr double TAU1 = 100.0;
+
+// ---- stream ids (must agree with the kernels' counter layout) -------------
+enum : uint32_t {
+  SID_ZX = 1, SID_GAMMA = 2, SID_GAMMA1_PROP = 3, SID_ALPHA = 4, SID_L = 5,
+  SID_P = 6, SID_TAU0 = 7, SID_BETA = 8, SID_NU = 9, SID_DELTA = 10,
+  SID_PHI_PROP = 11, SID_PHI_ACC = 12, SID_W = 13, SID_PI = 14,
+  SID_INIT_W = 20, SID_INIT_L = 21
+};
+
+// ---- Philox4x32-10 (Salmon et al., SC'11), restated -----------------------
+static inline void philox(uint32_t ctr[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * ctr[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * ctr[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ ctr[1] ^ k0;
+    const uint32_t n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ ctr[3] ^ k1;
+    const uint32_t n3 = (uint32_t)p0;
+    ctr[0] = n0; ctr[1] = n1; ctr[2] = n2; ctr[3] = n3;
+  }
+}
+
+struct Stream {
+  uint32_t key0, key1, cx, cy, block, iter;
+  uint32_t buf[4];
+  int used;
+  Stream(uint64_t seed, uint32_t sid, uint64_t ent, uint32_t it)
+      : key0((uint32_t)(seed & 0xFFFFFFFFu)), key1((uint32_t)(seed >> 32)),
+        cx((uint32_t)(ent & 0xFFFFFFFFu)),
+        cy((uint32_t)((ent >> 32) & 0xFFFFu) | (sid << 16)), block(0), iter(it), used(4) {}
+  uint32_t u32() {
+    if (used == 4) {
+      uint32_t c[4] = {cx, cy, block, iter};
+      philox(c, key0, key1);
+      ++block;
+      memcpy(buf, c, sizeof(buf));
+      used = 0;
+    }
+    return buf[used++];
+  }
+  // (2m+1) 2^-24, m = top 23 bits: the same value the kernels use in float.
+  double unif() { return ((double)(u32() >> 9) + 0.5) / 8388608.0; }
+};
+
+// ---- margins ---------------------------------------------------------------
+static inline void mark(double* mg, double diff, double scale) {
+  if (!mg) return;
+  const double m = fabs(diff) / scale;
+  if (m < *mg) *mg = m;
+}
+
+// ---- samplers (double precision, same consumption order as the kernels) ---
+static double normal(Stream& s) {
+  const double u1 = s.unif();
+  const double u2 = s.unif();
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586476925 * u2);
+}
+
+static double gamma_mt(Stream& s, double a, double* mg) {
+  if (!(a > 0.0)) return 0.0;
+  const bool boost = a < 1.0;
+  mark(mg, a - 1.0, 1.0);
+  const double aa = boost ? a + 1.0 : a;
+  const double d = aa - 1.0 / 3.0;
+  const double c = 1.0 / sqrt(9.0 * d);
+  double x = d;
+  for (int it = 0; it < 64; ++it) {
+    const double z = normal(s);
+    double v = 1.0 + c * z;
+    mark(mg, v, 1.0 + fabs(c * z));
+    if (v <= 0.0) continue;
+    v = v * v * v;
+    const double u = s.unif();
+    const double z2 = z * z;
+    const double sq = 1.0 - 0.0331 * (z2 * z2);
+    mark(mg, u - sq, 1.0 + 0.0331 * z2 * z2);
+    if (u < sq) { x = d * v; break; }
+    const double lhs = log(u);
+    const double rhs = 0.5 * z2 + d * (1.0 - v + log(v));
+    mark(mg, lhs - rhs, 1.0 + fabs(lhs) + 0.5 * z2 + d * (1.0 + v + fabs(log(v))));
+    if (lhs < rhs) { x = d * v; break; }
+  }
+  if (boost) {
+    const double u = s.unif();
+    x = x * exp(log(u) / a);
+  }
+  return x;
+}
+
+static int poisson(Stream& s, double lam, double* mg) {
+  if (!(lam > 0.0)) return 0;
+  if (lam > 1.0e9) lam = 1.0e9;
+  mark(mg, lam - 10.0, 10.0);
+  if (lam < 10.0) {
+    const double u = s.unif();
+    double p = exp(-lam);
+    double F = p;
+    int k = 0;
+    for (;;) {
+      mark(mg, u - F, 1.0);
+      if (!(u > F) || k >= 256) break;
+      ++k;
+      p = p * (lam / (double)k);
+      const double Fn = F + p;
+      if (Fn == F) break;
+      F = Fn;
+    }
+    return k;
+  }
+  const double slam = sqrt(lam);
+  const double loglam = log(lam);
+  const double b = 0.931 + 2.53 * slam;
+  const double a = -0.059 + 0.02483 * b;
+  const double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int it = 0; it < 64; ++it) {
+    const double U = s.unif() - 0.5;
+    const double V = s.unif();
+    const double us = 0.5 - fabs(U);
+    const double arg = (2.0 * a / us + b) * U + lam + 0.43;
+    const double kf = floor(arg);
+    mark(mg, std::min(arg - kf, kf + 1.0 - arg), 1.0 + lam);
+    mark(mg, us - 0.07, 1.0);
+    mark(mg, V - vr, 1.0);
+    if (us >= 0.07 && V <= vr) return (int)kf;
+    mark(mg, us - 0.013, 1.0);
+    mark(mg, V - us, 1.0);
+    if (kf < 0.0 || (us < 0.013 && V > us)) continue;
+    const double lhs = log(V) + log(invalpha) - log(a / (us * us) + b);
+    const double rhs = -lam + kf * loglam - lgamma(kf + 1.0);
+    mark(mg, lhs - rhs, 1.0 + fabs(lhs) + lam + fabs(kf * loglam));
+    if (lhs <= rhs) return (int)kf;
+  }
+  return (int)lam;
+}
+
+static int negbin(Stream& s, double mu, double phi, double* mg) {
+  const double g = gamma_mt(s, phi, mg);
+  return poisson(s, g * (mu / phi), mg);
+}
+
+static inline double softplus(double t) {
+  return t > 0.0 ? t + log1p(exp(-t)) : log1p(exp(t));
+}
+
+// (phi + X) * [log(phi + e^{m + new}) - log(phi + e^{m + old})] - (new - old) X
+// is minus the reference's fill_prop_* term; this returns the term itself:
+//   (new - old) X + (phi + X) (log(phi + e^{m+old}) - log(phi + e^{m+new}))
+static inline double nb_shift_term(double xold, double xnew, double m, double phi, int X) {
+  return (xnew - xold) * X + (phi + X) * (log(phi + exp(m + xold)) - log(phi + exp(m + xnew)));
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+// Full sampler state in double precision.  Layouts follow the reference:
+// beta/L [k*G+g], nu/phi [b*G+g], gamma [0/1*B+b], pi [b*K+k], X/Y/Z [i*G+g].
+typedef struct orc_state {
+  int32_t B, K;
+  int64_t G, N;
+  const int32_t* n_b;
+  const int32_t* Y;
+  int32_t* X;
+  uint8_t* Z;
+  int32_t* W;
+  int8_t* L;
+  double* alpha;
+  double* mu_alpha;
+  double* beta;
+  double* nu;
+  double* mu_nu;      // [B], entry 0 unused (0)
+  double* delta;
+  double* mu_delta;
+  double* phi;
+  double* gamma;
+  double* pi;
+  double* p_tau0;     // [2] = {p, tau0}
+  uint64_t seed;
+} orc_state;
+
+// Diagnostics of the last stage run.  Any pointer may be NULL.
+typedef struct orc_debug {
+  double* lr_gamma;   // [2B]  log acceptance ratio (likelihood + prior) of gamma0, gamma1
+  double* lr_alpha;   // [G]
+  double* lr_beta;    // [K*G] (k >= 1 used)
+  double* lr_nu;      // [B*G] (b >= 1 used)
+  double* lr_delta;   // [N]
+  double* lr_phi;     // [B*G]
+  double* lr_W;       // [N]  MH: log ratio; Gibbs: unused
+  double* mg_zx;      // [N*G] min normalised margin of the entry's discrete decisions
+  double* mg_gamma;   // [2B]  |log u - log r|
+  double* mg_alpha;   // [G]
+  double* mg_L;       // [K*G]
+  double* mg_beta;    // [K*G]
+  double* mg_nu;      // [B*G]
+  double* mg_delta;   // [N]
+  double* mg_phi;     // [B*G]
+  double* mg_W;       // [N]
+  double* mg_ptau;    // [2]
+  double* mg_pi;      // [B*K]
+} orc_debug;
+
+enum { ORC_STAGE_ZX_GAMMA_ALPHA_L = 0, ORC_STAGE_PTAU_BETA_NU = 1, ORC_STAGE_DELTA = 2,
+       ORC_STAGE_PHI = 3, ORC_STAGE_W = 4, ORC_STAGE_PI = 5 };
+
+static inline std::vector<int64_t> batch_offsets(const orc_state* st) {
+  std::vector<int64_t> off(st->B + 1, 0);
+  for (int b = 0; b < st->B; ++b) off[b + 1] = off[b] + st->n_b[b];
+  return off;
+}
+
+static inline int batch_of(const std::vector<int64_t>& off, int64_t i) {
+  int b = 0;
+  while (i >= off[b + 1]) ++b;
+  return b;
+}
+
+static inline double mu_of(const orc_state* st, int b, int64_t i, int64_t g) {
+  const int64_t G = st->G;
+  return exp(st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->nu[b * G + g] + st->delta[i]);
+}
+
+// --- Z / X : BUSseq_gpu.cu:484-512 -----------------------------------------
+static void stage_zx(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t N = st->N, G = st->G;
+  const int B = st->B;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    const double g0 = st->gamma[b], g1 = st->gamma[B + b];
+    for (int64_t g = 0; g < G; ++g) {
+      const int64_t pos = i * G + g;
+      double mg = INFINITY;
+      if (st->Y[pos] == 0) {
+        Stream s(st->seed, SID_ZX, (uint64_t)pos, (uint32_t)iter);
+        int z;
+        if (st->X[pos] == 0) {
+          const double u = s.unif();
+          const double thr = 1.0 / (1.0 + exp(g0));
+          mark(&mg, u - thr, 1.0);
+          z = u > thr;
+        } else {
+          z = 1;
+        }
+        st->Z[pos] = (uint8_t)z;
+        if (z) {
+          const double mu = mu_of(st, b, i, g);
+          const int xn = negbin(s, mu, st->phi[b * G + g], &mg);
+          const double u = s.unif();
+          // log[(1 + e^{-g0-g1 Xold}) / (1 + e^{-g0-g1 Xnew})]
+          const double lr = softplus(-g0 - g1 * st->X[pos]) - softplus(-g0 - g1 * xn);
+          const double lu = log(u);
+          mark(&mg, lu - lr, 1.0 + fabs(lu) + fabs(lr));
+          if (lu <= lr) st->X[pos] = xn;
+        } else {
+          st->X[pos] = 0;
+        }
+      }
+      if (dbg && dbg->mg_zx) dbg->mg_zx[pos] = mg;
+    }
+  }
+}
+
+// --- gamma0 then gamma1 : BUSseq_gpu.cu:514-600 -----------------------------
+static void stage_gamma(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t G = st->G;
+  const int B = st->B;
+  auto off = batch_offsets(st);
+  for (int b = 0; b < B; ++b) {
+    Stream s(st->seed, SID_GAMMA, (uint64_t)b, (uint32_t)iter);
+    const double u0 = s.unif(), u1 = s.unif();
+    const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
+    const double ua0 = s.unif(), ua1 = s.unif();
+    double g0 = st->gamma[b];
+    const double g1 = st->gamma[B + b];
+    const double g0n = g0 + 0.1 * z;
+    Stream sg(st->seed, SID_GAMMA1_PROP, (uint64_t)b, (uint32_t)iter);
+    const double g1n = -gamma_mt(sg, -10.0 * g1, nullptr) * 0.1;
+    const int64_t lo = off[b] * G, hi = off[b + 1] * G;
+    // gamma0: sum of (g0n - g0) Z - [sp(g0n + g1 X) - sp(g0 + g1 X)]
+    double lr0 = 0.0;
+#pragma omp parallel for reduction(+ : lr0)
+    for (int64_t pos = lo; pos < hi; ++pos) {
+      const int X = st->X[pos], Z = st->Z[pos];
+      double prop, prev, t;
+      t = g0n + g1 * X;
+      prop = g0n * Z - softplus(t);
+      t = g0 + g1 * X;
+      prev = g0 * Z - softplus(t);
+      lr0 += prop - prev;
+    }
+    const double prior0 = (g0 * g0 - g0n * g0n) / (2.0 * SIGMA2_GAMMA0);
+    const double l0 = log(ua0);
+    if (dbg && dbg->lr_gamma) dbg->lr_gamma[b] = lr0 + prior0;
+    if (dbg && dbg->mg_gamma) dbg->mg_gamma[b] = fabs(l0 - (prior0 + lr0));
+    if (l0 <= prior0 + lr0) { g0 = g0n; st->gamma[b] = g0n; }
+    // gamma1 with the updated gamma0
+    double lr1 = 0.0;
+#pragma omp parallel for reduction(+ : lr1)
+    for (int64_t pos = lo; pos < hi; ++pos) {
+      const int X = st->X[pos], Z = st->Z[pos];
+      const double prop = g1n * X * Z - softplus(g0 + g1n * X);
+      const double prev = g1 * X * Z - softplus(g0 + g1 * X);
+      lr1 += prop - prev;
+    }
+    const double pv = -g1, nv = -g1n;
+    const double prior1 = (KAPPA_GAMMA1 - 1.0) * (log(nv) - log(pv)) + TAU_GAMMA1 * (pv - nv) -
+                          lgamma(10.0 * nv) + (10.0 * nv - 1.0) * log(pv) + 10.0 * nv * (log(10.0) + 1.0) +
+                          lgamma(10.0 * pv) - (10.0 * pv - 1.0) * log(nv) - 10.0 * pv * (log(10.0) + 1.0);
+    const double l1 = log(ua1);
+    if (dbg && dbg->lr_gamma) dbg->lr_gamma[B + b] = lr1 + prior1;
+    if (dbg && dbg->mg_gamma) dbg->mg_gamma[B + b] = fabs(l1 - (prior1 + lr1));
+    if (l1 <= prior1 + lr1) st->gamma[B + b] = g1n;
+  }
+}
+
+// --- alpha : BUSseq_gpu.cu:602-632 ------------------------------------------
+static void stage_alpha(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t N = st->N, G = st->G;
+  auto off = batch_offsets(st);
+  std::vector<int> bat(N);
+  for (int64_t i = 0; i < N; ++i) bat[i] = batch_of(off, i);
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    Stream s(st->seed, SID_ALPHA, (uint64_t)g, (uint32_t)iter);
+    const double u0 = s.unif(), u1 = s.unif();
+    const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
+    const double ua = s.unif();
+    const double a = st->alpha[g], an = a + 0.1 * z;
+    double lr = 0.0;
+    for (int64_t i = 0; i < N; ++i) {
+      const int b = bat[i];
+      const double phi = st->phi[b * G + g];
+      const double m = st->beta[(int64_t)st->W[i] * G + g] + st->nu[b * G + g] + st->delta[i];
+      lr += nb_shift_term(a, an, m, phi, st->X[i * G + g]);
+    }
+    const double ma = st->mu_alpha[g];
+    const double prior = ((a - ma) * (a - ma) - (an - ma) * (an - ma)) / (2.0 * SIGMA2_ALPHA);
+    const double lu = log(ua);
+    if (dbg && dbg->lr_alpha) dbg->lr_alpha[g] = lr + prior;
+    if (dbg && dbg->mg_alpha) dbg->mg_alpha[g] = fabs(lu - (lr + prior));
+    if (lu <= lr + prior) st->alpha[g] = an;
+  }
+}
+
+// --- L : BUSseq_gpu.cu:634-648 ----------------------------------------------
+static void stage_L(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t G = st->G;
+  const int K = st->K;
+  const double p = st->p_tau0[0], tau0 = st->p_tau0[1];
+#pragma omp parallel for schedule(static)
+  for (int64_t pos = G; pos < (int64_t)K * G; ++pos) {
+    const double bt = st->beta[pos];
+    const double lo = log(p) - log(1.0 - p) - (log(TAU1) - log(tau0)) / 2.0 +
+                      bt * bt * (1.0 / (2.0 * tau0) - 1.0 / (2.0 * TAU1));
+    Stream s(st->seed, SID_L, (uint64_t)(pos - G), (uint32_t)iter);
+    const double u = s.unif();
+    const double thr = 1.0 / (1.0 + exp(lo));
+    if (dbg && dbg->mg_L) dbg->mg_L[pos] = fabs(u - thr);
+    st->L[pos] = (int8_t)(u > thr ? 1 : 0);
+  }
+}
+
+// --- p, tau0 : BUSseq_gpu.cu:650-668, driver :1313-1321 ---------------------
+static void stage_ptau(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t G = st->G;
+  const int K = st->K;
+  int64_t cnt = 0;
+  double bsq = 0.0;
+  for (int64_t pos = G; pos < (int64_t)K * G; ++pos) {
+    cnt += st->L[pos];
+    if (st->L[pos] == 0) bsq += st->beta[pos] * st->beta[pos];
+  }
+  const double tot = (double)G * (double)(K - 1);
+  double mgp = INFINITY, mgt = INFINITY;
+  Stream sp(st->seed, SID_P, 0, (uint32_t)iter);
+  const double ga = gamma_mt(sp, (double)cnt + A_P, &mgp);
+  const double gb = gamma_mt(sp, tot - (double)cnt + B_P, &mgp);
+  st->p_tau0[0] = ga / (ga + gb);
+  Stream stt(st->seed, SID_TAU0, 0, (uint32_t)iter);
+  const double shape = A_TAU0 + (tot - (double)cnt) / 2.0;
+  const double rate = B_TAU0 + bsq / 2.0;
+  st->p_tau0[1] = 1.0 / (gamma_mt(stt, shape, &mgt) * (1.0 / rate));
+  if (dbg && dbg->mg_ptau) { dbg->mg_ptau[0] = mgp; dbg->mg_ptau[1] = mgt; }
+}
+
+// --- beta : BUSseq_gpu.cu:670-707 -------------------------------------------
+static void stage_beta(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t N = st->N, G = st->G;
+  const int K = st->K;
+  auto off = batch_offsets(st);
+  std::vector<int> bat(N);
+  for (int64_t i = 0; i < N; ++i) bat[i] = batch_of(off, i);
+  const double tau0 = st->p_tau0[1];
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    std::vector<double> lr(K, 0.0), bn(K, 0.0), ua(K, 0.0);
+    for (int k = 1; k < K; ++k) {
+      Stream s(st->seed, SID_BETA, (uint64_t)((k - 1) * G + g), (uint32_t)iter);
+      const double u0 = s.unif(), u1 = s.unif();
+      const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
+      ua[k] = s.unif();
+      bn[k] = st->beta[k * G + g] + 0.1 * z;
+    }
+    for (int64_t i = 0; i < N; ++i) {
+      const int k = st->W[i];
+      if (k == 0) continue;
+      const int b = bat[i];
+      const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
+      lr[k] += nb_shift_term(st->beta[k * G + g], bn[k], m, st->phi[b * G + g], st->X[i * G + g]);
+    }
+    for (int k = 1; k < K; ++k) {
+      const int64_t pos = k * G + g;
+      const double bo = st->beta[pos];
+      const double var = st->L[pos] == 1 ? TAU1 : tau0;
+      const double prior = (bo * bo - bn[k] * bn[k]) / (2.0 * var);
+      const double lu = log(ua[k]);
+      if (dbg && dbg->lr_beta) dbg->lr_beta[pos] = lr[k] + prior;
+      if (dbg && dbg->mg_beta) dbg->mg_beta[pos] = fabs(lu - (lr[k] + prior));
+      if (lu <= lr[k] + prior) st->beta[pos] = bn[k];
+    }
+  }
+}
+
+// --- nu : BUSseq_gpu.cu:709-737 ---------------------------------------------
+static void stage_nu(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t G = st->G;
+  const int B = st->B;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    for (int b = 1; b < B; ++b) {
+      const int64_t pos = b * G + g;
+      Stream s(st->seed, SID_NU, (uint64_t)((b - 1) * G + g), (uint32_t)iter);
+      const double u0 = s.unif(), u1 = s.unif();
+      const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
+      const double ua = s.unif();
+      const double vo = st->nu[pos], vn = vo + 0.1 * z;
+      double lr = 0.0;
+      for (int64_t i = off[b]; i < off[b + 1]; ++i) {
+        const double m = st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->delta[i];
+        lr += nb_shift_term(vo, vn, m, st->phi[pos], st->X[i * G + g]);
+      }
+      const double mn = st->mu_nu[b];
+      const double prior = ((vo - mn) * (vo - mn) - (vn - mn) * (vn - mn)) / (2.0 * SIGMA2_NU);
+      const double lu = log(ua);
+      if (dbg && dbg->lr_nu) dbg->lr_nu[pos] = lr + prior;
+      if (dbg && dbg->mg_nu) dbg->mg_nu[pos] = fabs(lu - (lr + prior));
+      if (lu <= lr + prior) st->nu[pos] = vn;
+    }
+  }
+}
+
+// --- delta : BUSseq_gpu.cu:739-778 ------------------------------------------
+static void stage_delta(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t N = st->N, G = st->G;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    if (i == off[b]) continue;  // first cell of each batch stays at 0
+    Stream s(st->seed, SID_DELTA, (uint64_t)i, (uint32_t)iter);
+    const double u0 = s.unif(), u1 = s.unif();
+    const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
+    const double ua = s.unif();
+    const double dn = st->delta[i] + 0.1 * z, d = st->delta[i];
+    const int k = st->W[i];
+    double lr = 0.0;
+    for (int64_t g = 0; g < G; ++g) {
+      const double m = st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g];
+      lr += nb_shift_term(d, dn, m, st->phi[b * G + g], st->X[i * G + g]);
+    }
+    const double md = st->mu_delta[i];
+    const double prior = ((d - md) * (d - md) - (dn - md) * (dn - md)) / (2.0 * SIGMA2_DELTA);
+    const double lu = log(ua);
+    if (dbg && dbg->lr_delta) dbg->lr_delta[i] = lr + prior;
+    if (dbg && dbg->mg_delta) dbg->mg_delta[i] = fabs(lu - (lr + prior));
+    if (lu <= lr + prior) st->delta[i] = dn;
+  }
+}
+
+// --- phi : BUSseq_gpu.cu:780-818 --------------------------------------------
+static void stage_phi(orc_state* st, int iter, orc_debug* dbg) {
+  const int64_t G = st->G;
+  const int B = st->B;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    for (int b = 0; b < B; ++b) {
+      const int64_t pos = b * G + g;
+      Stream sp(st->seed, SID_PHI_PROP, (uint64_t)pos, (uint32_t)iter);
+      const double po = st->phi[pos];
+      const double pn = gamma_mt(sp, po, nullptr);
+      Stream sa(st->seed, SID_PHI_ACC, (uint64_t)pos, (uint32_t)iter);
+      const double ua = sa.unif();
+      double lr = 0.0;
+      for (int64_t i = off[b]; i < off[b + 1]; ++i) {
+        const int X = st->X[i * G + g];
+        const double eta = exp(st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->nu[pos] + st->delta[i]);
+        lr += lgamma(pn + X) + pn * log(pn) - lgamma(pn) - (pn + X) * log(pn + eta) + lgamma(po) +
+              (po + X) * log(po + eta) - lgamma(po + X) - po * log(po);
+      }
+      const double prior = (KAPPA_PHI - po) * log(pn) - (KAPPA_PHI - pn) * log(po) + (1.0 - TAU_PHI) * (pn - po) +
+                           lgamma(po) - lgamma(pn);
+      const double lu = log(ua);
+      if (dbg && dbg->lr_phi) dbg->lr_phi[pos] = lr + prior;
+      if (dbg && dbg->mg_phi) dbg->mg_phi[pos] = fabs(lu - (lr + prior));
+      if (lu <= lr + prior) st->phi[pos] = pn;
+    }
+  }
+}
+
+// --- W : BUSseq_gpu.cu:820-854 (MH) and the K-way categorical --------------
+static void stage_W(orc_state* st, int iter, int w_update, orc_debug* dbg) {
+  const int64_t N = st->N, G = st->G;
+  const int K = st->K;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    const int k = st->W[i];
+    Stream s(st->seed, SID_W, (uint64_t)i, (uint32_t)iter);
+    if (w_update == 0) {
+      const uint32_t r0 = s.u32();
+      const int kn = (int)(((uint64_t)r0 * (uint64_t)K) >> 32);
+      const double ua = s.unif();
+      double lr = 0.0;
+      for (int64_t g = 0; g < G; ++g) {
+        const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
+        lr += nb_shift_term(st->beta[(int64_t)k * G + g], st->beta[(int64_t)kn * G + g], m, st->phi[b * G + g],
+                            st->X[i * G + g]);
+      }
+      const double rhs = log(st->pi[b * K + kn] / st->pi[b * K + k]) + lr;
+      const double lu = log(ua);
+      if (dbg && dbg->lr_W) dbg->lr_W[i] = rhs;
+      if (dbg && dbg->mg_W) dbg->mg_W[i] = (kn == k) ? INFINITY : fabs(lu - rhs);
+      if (lu <= rhs) st->W[i] = kn;
+    } else {
+      const double u = s.unif();
+      std::vector<double> lp(K, 0.0);
+      for (int kk = 0; kk < K; ++kk) {
+        if (kk == k) continue;
+        double lr = 0.0;
+        for (int64_t g = 0; g < G; ++g) {
+          const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
+          lr += nb_shift_term(st->beta[(int64_t)k * G + g], st->beta[(int64_t)kk * G + g], m, st->phi[b * G + g],
+                              st->X[i * G + g]);
+        }
+        lp[kk] = lr;
+      }
+      double mx = -INFINITY;
+      for (int kk = 0; kk < K; ++kk) {
+        lp[kk] += log(st->pi[b * K + kk]);
+        mx = std::max(mx, lp[kk]);
+      }
+      double tot = 0.0;
+      for (int kk = 0; kk < K; ++kk) tot += exp(lp[kk] - mx);
+      const double target = u * tot;
+      double cum = 0.0, mg = INFINITY;
+      int pick = K - 1;
+      bool done = false;
+      for (int kk = 0; kk < K; ++kk) {
+        cum += exp(lp[kk] - mx);
+        mg = std::min(mg, fabs(cum - target) / tot);
+        if (!done && target < cum) { pick = kk; done = true; }
+      }
+      if (dbg && dbg->mg_W) dbg->mg_W[i] = mg;
+      st->W[i] = pick;
+    }
+  }
+}
+
+// --- pi : BUSseq_gpu.cu:856-890 (a correct Dirichlet draw) ------------------
+static void stage_pi(orc_state* st, int iter, orc_debug* dbg) {
+  const int B = st->B, K = st->K;
+  auto off = batch_offsets(st);
+  for (int b = 0; b < B; ++b) {
+    std::vector<int64_t> cnt(K, 0);
+    for (int64_t i = off[b]; i < off[b + 1]; ++i) cnt[st->W[i]]++;
+    std::vector<double> gk(K);
+    double tot = 0.0;
+    for (int k = 0; k < K; ++k) {
+      Stream s(st->seed, SID_PI, (uint64_t)(b * K + k), (uint32_t)iter);
+      double mg = INFINITY;
+      gk[k] = gamma_mt(s, (double)cnt[k] + XI_PI, &mg);
+      if (dbg && dbg->mg_pi) dbg->mg_pi[b * K + k] = mg;
+      tot += gk[k];
+    }
+    for (int k = 0; k < K; ++k) st->pi[b * K + k] = gk[k] / tot;
+  }
+}
+
+int orc_stage(orc_state* st, int stage, int iter, int n_unchanged, int w_update, orc_debug* dbg) {
+  switch (stage) {
+    case ORC_STAGE_ZX_GAMMA_ALPHA_L:
+      stage_zx(st, iter, dbg);
+      stage_gamma(st, iter, dbg);
+      stage_alpha(st, iter, dbg);
+      stage_L(st, iter, dbg);
+      return 0;
+    case ORC_STAGE_PTAU_BETA_NU:
+      if (iter >= n_unchanged) stage_ptau(st, iter, dbg);
+      stage_beta(st, iter, dbg);
+      stage_nu(st, iter, dbg);
+      return 0;
+    case ORC_STAGE_DELTA: stage_delta(st, iter, dbg); return 0;
+    case ORC_STAGE_PHI: stage_phi(st, iter, dbg); return 0;
+    case ORC_STAGE_W: stage_W(st, iter, w_update, dbg); return 0;
+    case ORC_STAGE_PI: stage_pi(st, iter, dbg); return 0;
+    default: return -1;
+  }
+}
+
+// Fine-grained entry points (one reference block each), for unit tests.
+int orc_step(orc_state* st, const char* which, int iter, int w_update, orc_debug* dbg) {
+  if (!strcmp(which, "zx")) stage_zx(st, iter, dbg);
+  else if (!strcmp(which, "gamma")) stage_gamma(st, iter, dbg);
+  else if (!strcmp(which, "alpha")) stage_alpha(st, iter, dbg);
+  else if (!strcmp(which, "L")) stage_L(st, iter, dbg);
+  else if (!strcmp(which, "ptau")) stage_ptau(st, iter, dbg);
+  else if (!strcmp(which, "beta")) stage_beta(st, iter, dbg);
+  else if (!strcmp(which, "nu")) stage_nu(st, iter, dbg);
+  else if (!strcmp(which, "delta")) stage_delta(st, iter, dbg);
+  else if (!strcmp(which, "phi")) stage_phi(st, iter, dbg);
+  else if (!strcmp(which, "W")) stage_W(st, iter, w_update, dbg);
+  else if (!strcmp(which, "pi")) stage_pi(st, iter, dbg);
+  else return -1;
+  return 0;
+}
+
+// One whole sweep in the reference's order (BUSseq_gpu.cu:1267-1398).
+int orc_sweep(orc_state* st, int iter, int n_unchanged, int w_update) {
+  for (int s = 0; s <= ORC_STAGE_PI; ++s) orc_stage(st, s, iter, n_unchanged, w_update, nullptr);
+  return 0;
+}
+
+// --- initialisation : BUSseq_gpu.cu:369-482, :1163-1244 ---------------------
+// orc_init_given_W: everything of the reference's initialisation that does
+// not draw random numbers, for a given W.  delta from library sizes
+// (first_delta_W, :419-443), raw means (fill_raw_means + selective_mean,
+// :369-382 / :1210-1221), gamma/phi/nu (first_gamma, first_nu_phi), beta
+// (first_beta_L without L), alpha = mu_alpha, X = Y, Z = 0, mu_nu (fill_mu_nu +
+// mean_on_gpu + first_mu_nu, :1232-1241), mu_delta, pi (first_pi).  Optional
+// outputs: raw means [b][k][g] and batch means [b].
+int orc_init_given_W(orc_state* st, double* raw_out, double* batch_means_out) {
+  const int64_t N = st->N, G = st->G;
+  const int B = st->B, K = st->K;
+  auto off = batch_offsets(st);
+  std::vector<int64_t> lib(N, 0);
+#pragma omp parallel for
+  for (int64_t i = 0; i < N; ++i) {
+    int64_t s = 0;
+    for (int64_t g = 0; g < G; ++g) s += st->Y[i * G + g];
+    lib[i] = s;
+  }
+  for (int b = 0; b < B; ++b)
+    for (int k = 0; k < K; ++k) st->pi[b * K + k] = (k + 1) / (K * (K + 1) / 2.0);
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    st->delta[i] = log((double)lib[i]) - log((double)lib[off[b]]);
+  }
+  std::vector<double> raw((size_t)B * K * G, 0.0);
+  std::vector<int64_t> cnt((size_t)B * K, 0);
+  std::vector<int> bat(N);
+  for (int64_t i = 0; i < N; ++i) { bat[i] = batch_of(off, i); cnt[bat[i] * K + st->W[i]]++; }
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    for (int64_t i = 0; i < N; ++i)
+      raw[((size_t)bat[i] * K + st->W[i]) * G + g] += log(1.0 + st->Y[i * G + g] / exp(st->delta[i]));
+    for (int b = 0; b < B; ++b)
+      for (int k = 0; k < K; ++k) {
+        const int64_t c = cnt[b * K + k];
+        double& r = raw[((size_t)b * K + k) * G + g];
+        r = c == 0 ? 0.0 : r / (double)c;
+      }
+  }
+  for (int b = 0; b < B; ++b) { st->gamma[b] = GAMMA0_INIT; st->gamma[B + b] = GAMMA1_INIT; }
+  for (int64_t pos = 0; pos < (int64_t)B * G; ++pos) {
+    st->phi[pos] = PHI_INIT;
+    const int b = (int)(pos / G);
+    const int64_t g = pos % G;
+    if (b == 0) { st->nu[pos] = 0.0; continue; }
+    double t1 = 0.0, t2 = 0.0;
+    for (int k = 0; k < K; ++k) {
+      t1 += raw[((size_t)b * K + k) * G + g];
+      t2 += raw[(size_t)k * G + g];
+    }
+    st->nu[pos] = (t1 - t2) / K;
+  }
+  for (int64_t pos = 0; pos < (int64_t)K * G; ++pos)
+    st->beta[pos] = pos < G ? 0.0 : raw[pos] - raw[pos % G];
+  for (int64_t pos = 0; pos < N * G; ++pos) { st->X[pos] = st->Y[pos]; st->Z[pos] = 0; }
+  for (int64_t g = 0; g < G; ++g) { st->alpha[g] = raw[g]; st->mu_alpha[g] = raw[g]; }
+  std::vector<double> mb(B, 0.0);
+  for (int b = 0; b < B; ++b) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s)
+    for (int64_t i = off[b]; i < off[b + 1]; ++i)
+      for (int64_t g = 0; g < G; ++g) s += log(1.0 + st->Y[i * G + g] / exp(st->delta[i]));
+    mb[b] = s / ((double)st->n_b[b] * (double)G);
+  }
+  st->mu_nu[0] = 0.0;
+  for (int b = 1; b < B; ++b) st->mu_nu[b] = mb[b] - mb[0];
+  for (int64_t i = 0; i < N; ++i) st->mu_delta[i] = st->delta[i];
+  if (raw_out) memcpy(raw_out, raw.data(), sizeof(double) * raw.size());
+  if (batch_means_out) memcpy(batch_means_out, mb.data(), sizeof(double) * B);
+  return 0;
+}
+
+// Full initialisation: W ~ Cat(pi_init) per cell (first_delta_W), the
+// deterministic part above, L ~ its prior odds (first_beta_L), p = p0 (the
+// caller's value; the reference draws it with srand(seed); rand()), tau0.
+int orc_init(orc_state* st, double p0) {
+  const int64_t N = st->N, G = st->G;
+  const int K = st->K;
+  auto off = batch_offsets(st);
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    Stream s(st->seed, SID_INIT_W, (uint64_t)i, 0u);
+    const double u = s.unif();
+    int k = 0;
+    double acc = (0 + 1) / (K * (K + 1) / 2.0);
+    while (u > acc && k < K - 1) { ++k; acc += (k + 1) / (K * (K + 1) / 2.0); }
+    st->W[i] = k;
+    (void)b;
+  }
+  orc_init_given_W(st, nullptr, nullptr);
+  const double log_rat_base = log(p0 / (1.0 - p0)) + (log(TAU0_INIT) - log(TAU1)) / 2.0;
+  for (int64_t pos = 0; pos < (int64_t)K * G; ++pos) {
+    if (pos < G) { st->L[pos] = 0; continue; }
+    const double lr = log_rat_base + st->beta[pos] * st->beta[pos] * (1.0 / TAU0_INIT - 1.0 / TAU1) / 2.0;
+    Stream s(st->seed, SID_INIT_L, (uint64_t)pos, 0u);
+    st->L[pos] = (int8_t)(s.unif() > 1.0 / (1.0 + exp(lr)) ? 1 : 0);
+  }
+  st->p_tau0[0] = p0;
+  st->p_tau0[1] = TAU0_INIT;
+  return 0;
+}
+
+// --- BIC : BUSseq_gpu.cu:967-1024 and :1833 ---------------------------------
+// Uses the posterior estimates stored in the state's parameter arrays.
+// Per-(i,k) partials are returned in ll_ik [k*N+i] when non-NULL.
+double orc_bic(const orc_state* st, double* ll_ik) {
+  const int64_t N = st->N, G = st->G;
+  const int B = st->B, K = st->K;
+  auto off = batch_offsets(st);
+  std::vector<double> part((size_t)K * N, 0.0);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t ik = 0; ik < (int64_t)K * N; ++ik) {
+    const int k = (int)(ik / N);
+    const int64_t i = ik % N;
+    const int b = batch_of(off, i);
+    const double g0 = st->gamma[b], g1 = st->gamma[B + b];
+    double acc = 0.0;
+    for (int64_t g = 0; g < G; ++g) {
+      const double mu = exp(st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g] + st->delta[i]);
+      const double phi = st->phi[b * G + g];
+      const int Y = st->Y[i * G + g];
+      const double pbgk = mu / (mu + phi);
+      double logp, log1mp;
+      if (pbgk < exp(-250.0)) { logp = -250.0; log1mp = log(1.0 - pbgk); }
+      else if (1.0 - pbgk < exp(-250.0)) { logp = log(pbgk); log1mp = -250.0; }
+      else { logp = log(pbgk); log1mp = log(1.0 - pbgk); }
+      if (Y) {
+        acc += -log(1.0 + exp(g0 + g1 * Y)) + lgamma(phi + Y) - lgamma(1.0 + Y) - lgamma(phi) + Y * logp +
+               phi * log1mp;
+      } else {
+        const int x_max = (int)(3.0 * mu);
+        double s = phi * log1mp;
+        for (int x = 1; x < x_max; ++x) {
+          const double t = g0 + g1 * x - log(1.0 + exp(g0 + g1 * x)) + lgamma(phi + x) - lgamma(1.0 + x) -
+                           lgamma(phi) + x * logp + phi * log1mp;
+          if (t > s) s = t + log(1.0 + exp(s - t));
+          else s += log(1.0 + exp(t - s));
+        }
+        acc += s;
+      }
+    }
+    part[(size_t)k * N + i] = acc;
+  }
+  double ll = 0.0;
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    double mx = part[i];
+    for (int k = 1; k < K; ++k) mx = std::max(mx, part[(size_t)k * N + i]);
+    double s = 0.0;
+    for (int k = 0; k < K; ++k) s += st->pi[b * K + k] * exp(part[(size_t)k * N + i] - mx);
+    ll += mx + log(s);
+  }
+  if (ll_ik) memcpy(ll_ik, part.data(), sizeof(double) * part.size());
+  const double nparam = (double)((B + G) * K + 2 * B + G * (B * 2 - 1) + N - B);
+  return -2.0 * ll + log((double)G * (double)N) * nparam;
+}
+
+// Raw uniforms of one stream, for cross-checking the kernels' generator.
+void orc_uniforms(uint64_t seed, uint32_t sid, uint64_t ent, uint32_t iter, int n, double* out) {
+  Stream s(seed, sid, ent, iter);
+  for (int j = 0; j < n; ++j) out[j] = s.unif();
+}
+
+void orc_philox(const uint32_t ctr_in[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+  uint32_t c[4] = {ctr_in[0], ctr_in[1], ctr_in[2], ctr_in[3]};
+  philox(c, k0, k1);
+  memcpy(out, c, sizeof(c));
+}
+
+// Samplers, exposed for distribution tests of the oracle itself.
+void orc_sample_gamma(uint64_t seed, double a, int n, double* out) {
+  for (int j = 0; j < n; ++j) {
+    Stream s(seed, 40u, (uint64_t)j, 0u);
+    out[j] = gamma_mt(s, a, nullptr);
+  }
+}
+void orc_sample_poisson(uint64_t seed, double lam, int n, int32_t* out) {
+  for (int j = 0; j < n; ++j) {
+    Stream s(seed, 41u, (uint64_t)j, 0u);
+    out[j] = poisson(s, lam, nullptr);
+  }
+}
+void orc_sample_negbin(uint64_t seed, double mu, double phi, int n, int32_t* out) {
+  for (int j = 0; j < n; ++j) {
+    Stream s(seed, 42u, (uint64_t)j, 0u);
+    out[j] = negbin(s, mu, phi, nullptr);
+  }
+}
+
+// Per-term likelihood differences exactly as the reference's fill_prop_*
+// kernels write them, for pinning against the reference's own outputs.
+double orc_term_shift(double xold, double xnew, double m, double phi, int X) {
+  return nb_shift_term(xold, xnew, m, phi, X);
+}
+double orc_term_phi(double po, double pn, double eta, int X) {
+  return lgamma(pn + X) + pn * log(pn) - lgamma(pn) - (pn + X) * log(pn + eta) + lgamma(po) +
+         (po + X) * log(po + eta) - lgamma(po + X) - po * log(po);
+}
+double orc_term_gamma0(double g0o, double g0n, double g1, int X, int Z) {
+  return (g0n * Z - softplus(g0n + g1 * X)) - (g0o * Z - softplus(g0o + g1 * X));
+}
+double orc_term_gamma1(double g0, double g1o, double g1n, int X, int Z) {
+  return (g1n * X * Z - softplus(g0 + g1n * X)) - (g1o * X * Z - softplus(g0 + g1o * X));
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+}  // extern "C"
