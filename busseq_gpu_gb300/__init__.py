@@ -1,0 +1,338 @@
+"""GB300-native BUSseq Gibbs sampler.
+
+Python front-end over the C ABI of ``libbusseq_gb300.so`` (include/busseq_gb300.h).
+The compute path is the library's sm_103a CUDA kernels; there is no CPU
+fallback: if the library has not been built, or no GPU is present, the calls
+fail loudly.
+
+    from busseq_gpu_gb300 import Sampler, simulate
+    Y, W_true, _ = simulate([300, 300, 200, 200], G=3000, K=5, seed=13579)
+    s = Sampler(Y, [300, 300, 200, 200], K=5, seed=13579)
+    s.run(n_iter=4000, n_burnin=2000, n_unchanged=500)
+    est = s.estimates()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "Sampler", "BusseqError", "simulate", "read_counts", "lib", "library_path", "CONFIG_SIM", "STAGES",
+    "W_MH", "W_GIBBS",
+]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_PKG, "lib", "libbusseq_gb300.so")
+CLI_PATH = os.path.join(_PKG, "bin", "busseq")
+
+W_MH = 0
+W_GIBBS = 1
+STAGES = {"zx_gamma_alpha_L": 0, "beta_nu": 1, "delta": 2, "phi": 3, "W": 4, "pi": 5}
+
+_PI32 = C.POINTER(C.c_int32)
+_PU8 = C.POINTER(C.c_uint8)
+_PI8 = C.POINTER(C.c_int8)
+_PF = C.POINTER(C.c_float)
+_PD = C.POINTER(C.c_double)
+
+
+class Dims(C.Structure):
+    _fields_ = [("B", C.c_int32), ("K", C.c_int32), ("G", C.c_int64), ("n_b", _PI32)]
+
+
+class Options(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
+                ("device", C.c_int32), ("chunk_cells", C.c_int32), ("reserved", C.c_int32 * 8)]
+
+
+class Estimates(C.Structure):
+    _fields_ = [("Z", _PI32), ("X", _PI32), ("gamma", _PD), ("alpha", _PD), ("L", _PD), ("beta", _PD),
+                ("p_tau0", _PD), ("nu", _PD), ("delta", _PD), ("phi", _PD), ("W", _PI32), ("pi", _PD)]
+
+
+class Preserved(C.Structure):
+    _fields_ = [("gamma", _PD), ("alpha", _PD), ("L", _PI32), ("beta", _PD), ("p_tau0", _PD), ("nu", _PD),
+                ("delta", _PD), ("phi", _PD), ("W", _PI32), ("pi", _PD)]
+
+
+class State(C.Structure):
+    _fields_ = [("X", _PI32), ("Z", _PU8), ("W", _PI32), ("L", _PI8), ("alpha", _PF), ("mu_alpha", _PF),
+                ("beta", _PF), ("nu", _PF), ("mu_nu", _PF), ("delta", _PF), ("mu_delta", _PF), ("phi", _PF),
+                ("gamma", _PF), ("pi", _PF), ("p_tau0", _PF)]
+
+
+class LogRatios(C.Structure):
+    _fields_ = [("gamma", _PD), ("alpha", _PD), ("beta", _PD), ("nu", _PD), ("delta", _PD), ("phi", _PD),
+                ("W", _PD)]
+
+
+class SimParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("alpha_lo", "alpha_hi", "de_frac", "beta_lo", "beta_hi", "nu_step",
+                                          "nu_sd", "delta_sd", "phi_lo", "phi_hi", "pi_conc", "gamma0", "gamma1")]
+
+
+class BusseqError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("busseq error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load libbusseq_gb300.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise BusseqError(-4, "%s is not built; run __graft_entry__.build() first" % _LIB_PATH)
+    L = C.CDLL(_LIB_PATH)
+    H = C.c_void_p
+    sigs = {
+        "busseq_create": ([C.POINTER(Dims), C.c_void_p, C.c_int32, C.POINTER(Options), C.POINTER(H)], C.c_int),
+        "busseq_destroy": ([H], None),
+        "busseq_run": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+        "busseq_begin": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+        "busseq_sweeps": ([H, C.c_int32], C.c_int),
+        "busseq_finish": ([H], C.c_int),
+        "busseq_synchronize": ([H], C.c_int),
+        "busseq_get_estimates": ([H, C.POINTER(Estimates)], C.c_int),
+        "busseq_get_preserved": ([H, C.POINTER(Preserved)], C.c_int),
+        "busseq_bic": ([H, _PD], C.c_int),
+        "busseq_get_state": ([H, C.POINTER(State)], C.c_int),
+        "busseq_set_state": ([H, C.POINTER(State)], C.c_int),
+        "busseq_run_stage": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+        "busseq_get_log_ratios": ([H, C.POINTER(LogRatios)], C.c_int),
+        "busseq_set_stream": ([H, C.c_void_p], C.c_int),
+        "busseq_profile": ([H, C.c_int32, _PD, C.c_int32, _PI32], C.c_int),
+        "busseq_kernel_name": ([C.c_int32], C.c_char_p),
+        "busseq_kernel_bytes": ([H, C.c_int32], C.c_double),
+        "busseq_launches_per_sweep": ([H, C.c_int32], C.c_int),
+        "busseq_read_counts": ([C.c_char_p, C.c_int64, C.c_int64, _PI32], C.c_int),
+        "busseq_write_outputs": ([H, C.c_char_p, C.c_int32], C.c_int),
+        "busseq_simulate": ([C.POINTER(Dims), C.POINTER(SimParams), C.c_uint64, _PI32, _PI32, _PI32], C.c_int),
+        "busseq_last_error": ([], C.c_char_p),
+        "busseq_version": ([], C.c_char_p),
+    }
+    for name, (args, res) in sigs.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise BusseqError(rc, lib().busseq_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+# Parameters of the generative model behind each benchmark configuration.
+CONFIG_SIM = {
+    "default": dict(alpha_lo=0.5, alpha_hi=2.5, de_frac=0.2, beta_lo=1.5, beta_hi=3.0, nu_step=0.5, nu_sd=0.2,
+                    delta_sd=0.2, phi_lo=5.0, phi_hi=20.0, pi_conc=2.0, gamma0=-0.5, gamma1=-0.2),
+}
+CONFIG_SIM["wide"] = dict(CONFIG_SIM["default"], de_frac=0.15, phi_lo=2.0, phi_hi=30.0)
+
+
+def simulate(n_b, G: int, K: int, seed: int, **params):
+    """Draw (Y [N,G] int32, W_true [N], X_true [N,G]) from the BUSseq model on the host."""
+    prm = dict(CONFIG_SIM["default"])
+    prm.update(params)
+    n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+    N = int(n_b.sum())
+    Y = np.zeros((N, G), np.int32)
+    W = np.zeros(N, np.int32)
+    X = np.zeros((N, G), np.int32)
+    d = Dims(len(n_b), K, G, _p(n_b, _PI32))
+    sp = SimParams(**prm)
+    _check(lib().busseq_simulate(C.byref(d), C.byref(sp), int(seed), _p(Y, _PI32), _p(W, _PI32), _p(X, _PI32)))
+    return Y, W, X
+
+
+def read_counts(path: str, N: int, G: int) -> np.ndarray:
+    out = np.zeros((N, G), np.int32)
+    _check(lib().busseq_read_counts(path.encode(), N, G, _p(out, _PI32)))
+    return out
+
+
+class Sampler:
+    """One BUSseq chain on one GPU (mirrors the reference program's pipeline:
+    read counts -> initialise -> sweeps -> posterior -> files)."""
+
+    def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
+                 keep_draws: bool = False, device: int = 0, chunk_cells: int = 0):
+        L = lib()
+        self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+        self.B, self.K = len(self.n_b), int(K)
+        self.N = int(self.n_b.sum())
+        if isinstance(w_update, str):
+            w_update = {"mh": W_MH, "gibbs": W_GIBBS}[w_update]
+        opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
+                      keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells))
+        on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
+        if on_dev:
+            assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2
+            self.G = int(Y.shape[1])
+            yptr = C.c_void_p(Y.data_ptr())
+        else:
+            Yh = np.ascontiguousarray(Y, dtype=np.int32)
+            self.G = int(Yh.shape[1])
+            yptr = Yh.ctypes.data_as(C.c_void_p)
+            self._Yh = Yh
+        if (Y.shape[0] if on_dev else self._Yh.shape[0]) != self.N:
+            raise ValueError("Y has %d rows, n_b sums to %d" % (Y.shape[0], self.N))
+        self._dims = Dims(self.B, self.K, self.G, _p(self.n_b, _PI32))
+        h = C.c_void_p()
+        _check(L.busseq_create(C.byref(self._dims), yptr, int(on_dev), C.byref(opt), C.byref(h)))
+        self._h = h
+        self._Yh = None
+        self.n_kept = 0
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().busseq_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def run(self, n_iter: int, n_burnin: int, n_unchanged: int):
+        _check(lib().busseq_run(self._h, n_iter, n_burnin, n_unchanged))
+        self.n_kept = n_iter - n_burnin
+
+    def begin(self, n_iter: int, n_burnin: int, n_unchanged: int):
+        _check(lib().busseq_begin(self._h, n_iter, n_burnin, n_unchanged))
+        self.n_kept = n_iter - n_burnin
+
+    def sweeps(self, count: int):
+        _check(lib().busseq_sweeps(self._h, count))
+
+    def synchronize(self):
+        _check(lib().busseq_synchronize(self._h))
+
+    def finish(self):
+        _check(lib().busseq_finish(self._h))
+
+    # -- results ---------------------------------------------------------------
+    def estimates(self, with_XZ: bool = True) -> dict:
+        B, K, G, N = self.B, self.K, self.G, self.N
+        o = {"gamma": np.zeros((2, B)), "alpha": np.zeros(G), "L": np.zeros((max(K - 1, 1), G)),
+             "beta": np.zeros((K, G)), "p_tau0": np.zeros(2), "nu": np.zeros((B, G)), "delta": np.zeros(N),
+             "phi": np.zeros((B, G)), "W": np.zeros(N, np.int32), "pi": np.zeros((B, K))}
+        e = Estimates()
+        for k, v in o.items():
+            setattr(e, k, _p(v, _PI32 if v.dtype == np.int32 else _PD))
+        if with_XZ:
+            o["X"] = np.zeros((N, G), np.int32)
+            o["Z"] = np.zeros((N, G), np.int32)
+            e.X, e.Z = _p(o["X"], _PI32), _p(o["Z"], _PI32)
+        _check(lib().busseq_get_estimates(self._h, C.byref(e)))
+        return o
+
+    def preserved(self) -> dict:
+        B, K, G, N, n = self.B, self.K, self.G, self.N, self.n_kept
+        o = {"gamma": np.zeros((2 * B, n)), "alpha": np.zeros((G, n)), "L": np.zeros(((K - 1) * G, n), np.int32),
+             "beta": np.zeros(((K - 1) * G, n)), "p_tau0": np.zeros((2, n)), "nu": np.zeros(((B - 1) * G, n)),
+             "delta": np.zeros((N, n)), "phi": np.zeros((B * G, n)), "W": np.zeros((N, n), np.int32),
+             "pi": np.zeros((B * K, n))}
+        p = Preserved()
+        for k, v in o.items():
+            setattr(p, k, _p(v, _PI32 if v.dtype == np.int32 else _PD))
+        _check(lib().busseq_get_preserved(self._h, C.byref(p)))
+        return o
+
+    def bic(self) -> float:
+        v = C.c_double()
+        _check(lib().busseq_bic(self._h, C.byref(v)))
+        return v.value
+
+    def write_outputs(self, prefix: str, print_preserved: bool = False):
+        _check(lib().busseq_write_outputs(self._h, prefix.encode(), int(print_preserved)))
+
+    # -- state and stages ------------------------------------------------------
+    def _state_arrays(self):
+        B, K, G, N = self.B, self.K, self.G, self.N
+        return {"X": np.zeros((N, G), np.int32), "Z": np.zeros((N, G), np.uint8), "W": np.zeros(N, np.int32),
+                "L": np.zeros((K, G), np.int8), "alpha": np.zeros(G, np.float32),
+                "mu_alpha": np.zeros(G, np.float32), "beta": np.zeros((K, G), np.float32),
+                "nu": np.zeros((B, G), np.float32), "mu_nu": np.zeros(B, np.float32),
+                "delta": np.zeros(N, np.float32), "mu_delta": np.zeros(N, np.float32),
+                "phi": np.zeros((B, G), np.float32), "gamma": np.zeros((2, B), np.float32),
+                "pi": np.zeros((B, K), np.float32), "p_tau0": np.zeros(2, np.float32)}
+
+    @staticmethod
+    def _ptr_for(v):
+        return {np.int32: _PI32, np.uint8: _PU8, np.int8: _PI8, np.float32: _PF}[v.dtype.type]
+
+    def get_state(self) -> dict:
+        o = self._state_arrays()
+        s = State()
+        for k, v in o.items():
+            setattr(s, k, _p(v, self._ptr_for(v)))
+        _check(lib().busseq_get_state(self._h, C.byref(s)))
+        return o
+
+    def set_state(self, st: dict):
+        ref = self._state_arrays()
+        s = State()
+        keep = []
+        for k, v in ref.items():
+            if k not in st:
+                continue
+            a = np.ascontiguousarray(st[k], dtype=v.dtype).reshape(v.shape)
+            keep.append(a)
+            setattr(s, k, _p(a, self._ptr_for(a)))
+        _check(lib().busseq_set_state(self._h, C.byref(s)))
+
+    def run_stage(self, stage, it: int, n_unchanged: int = 1 << 30):
+        if isinstance(stage, str):
+            stage = STAGES[stage]
+        _check(lib().busseq_run_stage(self._h, int(stage), int(it), int(n_unchanged)))
+
+    def log_ratios(self) -> dict:
+        B, K, G, N = self.B, self.K, self.G, self.N
+        o = {"gamma": np.zeros((2, B)), "alpha": np.zeros(G), "beta": np.zeros((K, G)), "nu": np.zeros((B, G)),
+             "delta": np.zeros(N), "phi": np.zeros((B, G)), "W": np.zeros(N)}
+        r = LogRatios()
+        for k, v in o.items():
+            setattr(r, k, _p(v, _PD))
+        _check(lib().busseq_get_log_ratios(self._h, C.byref(r)))
+        return o
+
+    # -- measurement -------------------------------------------------------------
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().busseq_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def profile(self, n_sweeps: int) -> dict:
+        ms = np.zeros(16)
+        n = C.c_int32()
+        _check(lib().busseq_profile(self._h, n_sweeps, _p(ms, _PD), 16, C.byref(n)))
+        return {lib().busseq_kernel_name(i).decode(): float(ms[i]) for i in range(n.value)}
+
+    def kernel_bytes(self, i: int) -> float:
+        return float(lib().busseq_kernel_bytes(self._h, i))
+
+    def launches_per_sweep(self, kept: bool) -> int:
+        return int(lib().busseq_launches_per_sweep(self._h, int(kept)))

@@ -167,6 +167,12 @@ struct DevState {
   float* keep_pi;
 };
 
+// Posterior estimates on the device (double precision).
+struct Estimates {
+  double *gamma, *alpha, *L, *beta, *ptau, *nu, *delta, *phi, *pi;
+  int32_t* W;
+};
+
 // eta = alpha + beta + nu, always summed in this order so that every kernel
 // rounds it identically.
 __device__ __forceinline__ float eta3(float a, float b, float n) { return (a + b) + n; }

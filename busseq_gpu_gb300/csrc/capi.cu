@@ -1,0 +1,799 @@
+// C ABI of the GB300 BUSseq sampler: memory, initialisation, CUDA-graph
+// sweeps, stages, summaries.  See include/busseq_gb300.h for the contract.
+#include "busseq_gb300.h"
+#include "busseq_dev.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <climits>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                                   \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));        \
+  } while (0)
+
+#define LAUNCH_CHECK(name)                                                                            \
+  do {                                                                                                \
+    cudaError_t e_ = cudaGetLastError();                                                              \
+    if (e_ != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "launch of %s: %s", name, cudaGetErrorString(e_)); \
+  } while (0)
+
+int64_t round_up(int64_t a, int64_t m) { return (a + m - 1) / m * m; }
+unsigned blocks_for(int64_t n, int t) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+
+const char* const kKernelNames[] = {"k_propose", "k_zx_alpha", "k_beta_nu", "k_delta",
+                                    "k_phi",     "k_w",        "k_sort_pi", "k_posterior"};
+constexpr int kNumKernels = 8;
+
+}  // namespace
+
+struct busseq_handle {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  bq::DevState s{};
+  busseq_options opt{};
+  std::vector<int32_t> n_b, off;
+  std::vector<void*> allocs;
+  int static_rows = 0;
+  // run
+  bool begun = false, finished = false;
+  int n_iter = 0, n_burnin = 0, n_unchanged = 0, iter_host = 0, n_kept = 0;
+  cudaGraphExec_t g_burn = nullptr, g_keep = nullptr;
+  std::vector<void*> run_allocs;  // accumulators and kept draws of the current run
+  // summaries
+  bq::Estimates est{};
+  double* ll_ik = nullptr;
+  double* bic_out = nullptr;
+  bool est_valid = false;
+
+  ~busseq_handle() {
+    if (g_burn) cudaGraphExecDestroy(g_burn);
+    if (g_keep) cudaGraphExecDestroy(g_keep);
+    for (void* p : run_allocs) cudaFree(p);
+    for (void* p : allocs) cudaFree(p);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  template <class T>
+  int alloc(T** p, size_t count, bool run_scoped = false) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(BUSSEQ_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    e = cudaMemsetAsync(q, 0, bytes, stream);
+    if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+    (run_scoped ? run_allocs : allocs).push_back(q);
+    *p = static_cast<T*>(q);
+    return BUSSEQ_OK;
+  }
+};
+
+#define TRY(x)                   \
+  do {                           \
+    int r_ = (x);                \
+    if (r_ != BUSSEQ_OK) return r_; \
+  } while (0)
+
+namespace {
+
+int check_device_error(busseq_handle* h) {
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  int err = 0;
+  CUDA_TRY(cudaMemcpy(&err, h->s.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    return fail(BUSSEQ_ERR_SAMPLER, "a device rejection sampler reached its iteration cap (flags 0x%x)", err);
+  }
+  return BUSSEQ_OK;
+}
+
+// Enqueue the launches of one sweep on `st` (used for graph capture, for
+// profiling and for direct launches).
+int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const bq::DevState& s) {
+  using namespace bq;
+  const dim3 gene_grid(s.n_tiles, s.cap_g);
+  switch (which) {
+    case 0:
+      k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(s, PROP_ALL);
+      LAUNCH_CHECK("k_propose");
+      break;
+    case 1:
+      k_zx_alpha<<<dim3(s.n_tiles, s.cap_g + h->static_rows), GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_zx_alpha");
+      break;
+    case 2:
+      k_beta_nu<<<gene_grid, GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_beta_nu");
+      break;
+    case 3:
+      k_delta<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
+      LAUNCH_CHECK("k_delta");
+      break;
+    case 4:
+      k_phi<<<gene_grid, GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_phi");
+      break;
+    case 5:
+      if (s.w_update == BUSSEQ_W_GIBBS) k_w_gibbs<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
+      else k_w_mh<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
+      LAUNCH_CHECK("k_w");
+      break;
+    case 6:
+      k_sort_pi<<<s.B, 1024, 0, st>>>(s, 1, kept ? 0 : 1);
+      LAUNCH_CHECK("k_sort_pi");
+      break;
+    case 7: {
+      const unsigned nb = (unsigned)std::min<int64_t>(blocks_for((int64_t)s.K * s.G, 256), 152 * 8);
+      k_posterior<<<nb, 256, 0, st>>>(s, 1);
+      LAUNCH_CHECK("k_posterior");
+      break;
+    }
+    default:
+      return fail(BUSSEQ_ERR_ARG, "no kernel %d", which);
+  }
+  return BUSSEQ_OK;
+}
+
+int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
+  const int n = kept ? 8 : 7;
+  for (int k = 0; k < n; ++k) TRY(launch_kernel(h, k, st, kept, h->s));
+  return BUSSEQ_OK;
+}
+
+int capture(busseq_handle* h, int kept, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal));
+  const int r = launch_sweep(h, h->own_stream, kept);
+  cudaError_t e = cudaStreamEndCapture(h->own_stream, &g);
+  if (r != BUSSEQ_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return BUSSEQ_OK;
+}
+
+int ensure_estimates(busseq_handle* h) {
+  bq::Estimates& e = h->est;
+  const int64_t G = h->s.G, N = h->s.N;
+  const int B = h->s.B, K = h->s.K;
+  if (!e.alpha) {
+    TRY(h->alloc(&e.gamma, 2 * B));
+    TRY(h->alloc(&e.alpha, G));
+    TRY(h->alloc(&e.L, std::max<int64_t>(1, (K - 1) * G)));
+    TRY(h->alloc(&e.beta, K * G));
+    TRY(h->alloc(&e.ptau, 2));
+    TRY(h->alloc(&e.nu, B * G));
+    TRY(h->alloc(&e.delta, N));
+    TRY(h->alloc(&e.phi, B * G));
+    TRY(h->alloc(&e.pi, B * K));
+    TRY(h->alloc(&e.W, N));
+  }
+  if (!h->est_valid) {
+    bq::k_finalize<<<std::min<unsigned>(blocks_for((int64_t)K * G, 256), 152 * 8), 256, 0, h->stream>>>(
+        h->s, e, h->finished ? h->n_kept : 0);
+    LAUNCH_CHECK("k_finalize");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->est_valid = true;
+  }
+  return BUSSEQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* busseq_last_error(void) { return g_err.c_str(); }
+
+int busseq_internal_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
+                         int32_t* kept_draws) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  *B = h->s.B;
+  *K = h->s.K;
+  *G = h->s.G;
+  *N = h->s.N;
+  *n_kept = h->finished ? h->n_kept : 0;
+  *kept_draws = h->s.keep_draws;
+  return BUSSEQ_OK;
+}
+const char* busseq_version(void) { return "busseq_gb300 0.1 (sm_103a)"; }
+
+int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, const busseq_options* optp,
+                  busseq_handle** out) {
+  if (!dims || !Y || !out) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  const int B = dims->B, K = dims->K;
+  const int64_t G = dims->G;
+  if (B < 2) return fail(BUSSEQ_ERR_ARG, "The batch number must be greater than one.");
+  if (B > BUSSEQ_MAX_BATCHES) return fail(BUSSEQ_ERR_ARG, "at most %d batches are supported", BUSSEQ_MAX_BATCHES);
+  if (K < 1 || K > BUSSEQ_MAX_TYPES) return fail(BUSSEQ_ERR_ARG, "K must be in 1..%d", BUSSEQ_MAX_TYPES);
+  if (G < 1) return fail(BUSSEQ_ERR_ARG, "G must be positive");
+  if (!dims->n_b) return fail(BUSSEQ_ERR_ARG, "n_b is NULL");
+  int64_t N = 0;
+  for (int b = 0; b < B; ++b) {
+    if (dims->n_b[b] < K)
+      return fail(BUSSEQ_ERR_ARG, "The sample size in any batch must be greater than the assumed cell type number.");
+    N += dims->n_b[b];
+  }
+  if (N >= INT_MAX) return fail(BUSSEQ_ERR_ARG, "too many cells");
+  busseq_options opt{};
+  if (optp) opt = *optp;
+  else opt.p0 = 0.25;
+  if (!(opt.p0 > 0.0 && opt.p0 < 1.0)) return fail(BUSSEQ_ERR_ARG, "p0 must be in (0, 1)");
+  CUDA_TRY(cudaSetDevice(opt.device));
+
+  busseq_handle* h = new busseq_handle();
+  h->device = opt.device;
+  h->opt = opt;
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(BUSSEQ_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  h->stream = h->own_stream;
+  h->n_b.assign(dims->n_b, dims->n_b + B);
+  h->off.assign(B + 1, 0);
+  for (int b = 0; b < B; ++b) h->off[b + 1] = h->off[b] + h->n_b[b];
+  const int r = [&]() -> int {
+    bq::DevState& s = h->s;
+    s.B = B;
+    s.K = K;
+    s.G = G;
+    s.N = N;
+    s.Gp = round_up(G, bq::GENE_TILE);
+    s.Gw = s.Gp / 32;
+    s.n_tiles = (int)((G + bq::GENE_TILE - 1) / bq::GENE_TILE);
+    s.CG = opt.chunk_cells > 0 ? opt.chunk_cells : 256;
+    s.cap_g = 0;
+    s.cap_c = 0;
+    for (int b = 0; b < B; ++b) {
+      s.cap_g += h->n_b[b] / s.CG + K;
+      s.cap_c += h->n_b[b] / bq::CELL_TILE + K;
+    }
+    s.w_update = opt.w_update == BUSSEQ_W_GIBBS ? BUSSEQ_W_GIBBS : BUSSEQ_W_MH;
+    s.seed = opt.seed;
+    s.n_burnin = 0;
+    s.n_unchanged = INT_MAX;
+    const int64_t Gp = s.Gp;
+    int32_t* Yd;
+    TRY(h->alloc(&Yd, N * Gp));
+    s.Y = Yd;
+    TRY(h->alloc(&s.X, N * Gp));
+    uint32_t* y0m;
+    TRY(h->alloc(&y0m, N * s.Gw));
+    s.y0m = y0m;
+    TRY(h->alloc(&s.zm, N * s.Gw));
+    int32_t *bo, *boff;
+    TRY(h->alloc(&bo, N));
+    TRY(h->alloc(&boff, B + 1));
+    s.batch_of = bo;
+    s.batch_off = boff;
+    TRY(h->alloc(&s.W, N));
+    TRY(h->alloc(&s.L, K * Gp));
+    TRY(h->alloc(&s.alpha, Gp));
+    TRY(h->alloc(&s.mu_alpha, Gp));
+    TRY(h->alloc(&s.beta, K * Gp));
+    TRY(h->alloc(&s.nu, B * Gp));
+    TRY(h->alloc(&s.mu_nu, B));
+    TRY(h->alloc(&s.delta, N));
+    TRY(h->alloc(&s.mu_delta, N));
+    TRY(h->alloc(&s.Dexp, N));
+    TRY(h->alloc(&s.phi, B * Gp));
+    TRY(h->alloc(&s.gamma, 2 * B));
+    TRY(h->alloc(&s.pi, B * K));
+    TRY(h->alloc(&s.p_tau0, 2));
+    TRY(h->alloc(&s.E, (int64_t)B * K * Gp));
+    TRY(h->alloc(&s.alpha_p, Gp));
+    TRY(h->alloc(&s.beta_p, K * Gp));
+    TRY(h->alloc(&s.nu_p, B * Gp));
+    TRY(h->alloc(&s.delta_p, N));
+    TRY(h->alloc(&s.phi_p, B * Gp));
+    TRY(h->alloc(&s.gamma_p, 2 * B));
+    TRY(h->alloc(&s.perm, N));
+    TRY(h->alloc(&s.gchunk, s.cap_g));
+    TRY(h->alloc(&s.ctile, s.cap_c));
+    TRY(h->alloc(&s.seg_cnt, B * K));
+    TRY(h->alloc(&s.part, (int64_t)s.cap_g * bq::NSLOT * Gp));
+    TRY(h->alloc(&s.gpart, (int64_t)s.cap_g * s.n_tiles * bq::GSLOT));
+    TRY(h->alloc(&s.tpart, (int64_t)s.n_tiles * bq::MAX_B));
+    TRY(h->alloc(&s.cnt_tile, s.n_tiles));
+    TRY(h->alloc(&s.cnt_glob, 8));
+    TRY(h->alloc(&s.iter, 1));
+    TRY(h->alloc(&s.err, 1));
+    TRY(h->alloc(&s.lr_gamma, 2 * B));
+    TRY(h->alloc(&s.lr_alpha, G));
+    TRY(h->alloc(&s.lr_beta, K * G));
+    TRY(h->alloc(&s.lr_nu, B * G));
+    TRY(h->alloc(&s.lr_delta, N));
+    TRY(h->alloc(&s.lr_phi, B * G));
+    TRY(h->alloc(&s.lr_W, N));
+    TRY(h->alloc(&h->ll_ik, (int64_t)K * N));
+    TRY(h->alloc(&h->bic_out, 2));
+    int64_t* libsize;
+    int *ymax_d, *bad;
+    TRY(h->alloc(&libsize, N));
+    TRY(h->alloc(&ymax_d, 1));
+    TRY(h->alloc(&bad, 1));
+
+    // ---- upload ----------------------------------------------------------
+    CUDA_TRY(cudaMemcpy2DAsync(Yd, Gp * sizeof(int32_t), Y, G * sizeof(int32_t), G * sizeof(int32_t), N,
+                               Y_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    std::vector<int32_t> bo_h(N);
+    for (int b = 0; b < B; ++b)
+      for (int64_t i = h->off[b]; i < h->off[b + 1]; ++i) bo_h[i] = b;
+    CUDA_TRY(cudaMemcpyAsync(bo, bo_h.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(boff, h->off.data(), (B + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    const float ptau0[2] = {(float)opt.p0, bq::TAU0_INIT};
+    CUDA_TRY(cudaMemcpyAsync(s.p_tau0, ptau0, sizeof(ptau0), cudaMemcpyHostToDevice, h->stream));
+    const int big = INT_MAX;
+    CUDA_TRY(cudaMemcpyAsync(bad, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+
+    // ---- initialisation (BUSseq_gpu.cu:1163-1244) --------------------------
+    bq::k_init_scan<<<(unsigned)N, 256, 0, h->stream>>>(s, libsize, ymax_d);
+    LAUNCH_CHECK("k_init_scan");
+    int ymax = 0;
+    CUDA_TRY(cudaMemcpyAsync(&ymax, ymax_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (ymax < 0) return fail(BUSSEQ_ERR_ARG, "counts must be non-negative");
+    if (ymax > (1 << 26)) return fail(BUSSEQ_ERR_ARG, "counts above 2^26 are not supported");
+    s.ymax = std::max(ymax, 1);
+    s.n_static = B * ((s.ymax + bq::GENE_TILE - 1) / bq::GENE_TILE);
+    h->static_rows = (s.n_static + s.n_tiles - 1) / s.n_tiles;
+    int32_t* hist;
+    TRY(h->alloc(&hist, (int64_t)B * (s.ymax + 1)));
+    s.yhist = hist;
+    TRY(h->alloc(&s.gstat, (int64_t)s.n_static * 4));
+    bq::k_init_hist<<<(unsigned)N, 256, 0, h->stream>>>(s, hist);
+    LAUNCH_CHECK("k_init_hist");
+    bq::k_init_w_delta<<<blocks_for(N, 256), 256, 0, h->stream>>>(s, libsize, bad);
+    LAUNCH_CHECK("k_init_w_delta");
+    int bad_h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&bad_h, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (bad_h != INT_MAX) return fail(BUSSEQ_ERR_ARG, "cell %d has no counts (library size 0)", bad_h);
+    bq::k_sort_pi<<<B, 1024, 0, h->stream>>>(s, 0, 0);
+    LAUNCH_CHECK("k_sort_pi");
+    bq::k_init_raw<<<dim3(s.n_tiles, s.cap_g), bq::GENE_TILE, 0, h->stream>>>(s);
+    LAUNCH_CHECK("k_init_raw");
+    const int64_t nfin = std::max<int64_t>(std::max<int64_t>(N, (int64_t)B * Gp), (int64_t)B * K);
+    bq::k_init_finish<<<blocks_for(nfin, 256), 256, 0, h->stream>>>(s, 1);
+    LAUNCH_CHECK("k_init_finish");
+    CUDA_TRY(cudaMemcpyAsync(s.X, s.Y, (size_t)N * Gp * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(cudaMemsetAsync(s.zm, 0, (size_t)N * s.Gw * sizeof(uint32_t), h->stream));
+    CUDA_TRY(cudaMemsetAsync(s.iter, 0, sizeof(int), h->stream));
+    return check_device_error(h);
+  }();
+  if (r != BUSSEQ_OK) {
+    delete h;
+    return r;
+  }
+  *out = h;
+  return BUSSEQ_OK;
+}
+
+void busseq_destroy(busseq_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+}
+
+int busseq_begin(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_unchanged) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (n_iter < 0 || n_burnin < 0) return fail(BUSSEQ_ERR_ARG, "iteration counts must be non-negative");
+  if (n_burnin > n_iter) return fail(BUSSEQ_ERR_ARG, "Burn-in iterations must be less than total number of iterations.");
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (h->g_burn) { cudaGraphExecDestroy(h->g_burn); h->g_burn = nullptr; }
+  if (h->g_keep) { cudaGraphExecDestroy(h->g_keep); h->g_keep = nullptr; }
+  for (void* p : h->run_allocs) cudaFree(p);
+  h->run_allocs.clear();
+  bq::DevState& s = h->s;
+  const int64_t G = s.G, N = s.N;
+  const int B = s.B, K = s.K;
+  h->n_iter = n_iter;
+  h->n_burnin = n_burnin;
+  h->n_unchanged = n_unchanged;
+  h->n_kept = n_iter - n_burnin;
+  h->iter_host = 0;
+  h->finished = false;
+  h->est_valid = false;
+  s.n_burnin = n_burnin;
+  s.n_unchanged = n_unchanged;
+  s.n_kept = h->n_kept;
+  s.keep_draws = (h->opt.keep_draws && h->n_kept > 0) ? 1 : 0;
+  TRY(h->alloc(&s.acc_alpha, G, true));
+  TRY(h->alloc(&s.acc_beta, K * G, true));
+  TRY(h->alloc(&s.acc_L, K * G, true));
+  TRY(h->alloc(&s.acc_nu, B * G, true));
+  TRY(h->alloc(&s.acc_delta, N, true));
+  TRY(h->alloc(&s.acc_phi, B * G, true));
+  TRY(h->alloc(&s.acc_gamma, 2 * B, true));
+  TRY(h->alloc(&s.acc_pi, B * K, true));
+  TRY(h->alloc(&s.acc_ptau, 2, true));
+  TRY(h->alloc(&s.acc_wcnt, N * K, true));
+  s.keep_gamma = s.keep_alpha = s.keep_beta = s.keep_ptau = s.keep_nu = s.keep_delta = s.keep_phi = s.keep_pi =
+      nullptr;
+  s.keep_L = nullptr;
+  s.keep_W = nullptr;
+  if (s.keep_draws) {
+    const int64_t nk = h->n_kept;
+    TRY(h->alloc(&s.keep_gamma, nk * 2 * B, true));
+    TRY(h->alloc(&s.keep_alpha, nk * G, true));
+    TRY(h->alloc(&s.keep_beta, nk * std::max(1, K - 1) * G, true));
+    TRY(h->alloc(&s.keep_L, nk * std::max(1, K - 1) * G, true));
+    TRY(h->alloc(&s.keep_ptau, nk * 2, true));
+    TRY(h->alloc(&s.keep_nu, nk * (B - 1) * G, true));
+    TRY(h->alloc(&s.keep_delta, nk * N, true));
+    TRY(h->alloc(&s.keep_phi, nk * B * G, true));
+    TRY(h->alloc(&s.keep_W, nk * N, true));
+    TRY(h->alloc(&s.keep_pi, nk * B * K, true));
+  }
+  CUDA_TRY(cudaMemsetAsync(s.iter, 0, sizeof(int), h->stream));
+  CUDA_TRY(cudaMemsetAsync(s.cnt_tile, 0, s.n_tiles * sizeof(unsigned), h->stream));
+  CUDA_TRY(cudaMemsetAsync(s.cnt_glob, 0, 8 * sizeof(unsigned), h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  TRY(capture(h, 0, &h->g_burn));
+  TRY(capture(h, 1, &h->g_keep));
+  h->begun = true;
+  return BUSSEQ_OK;
+}
+
+int busseq_sweeps(busseq_handle* h, int32_t count) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (!h->begun) return fail(BUSSEQ_ERR_STATE, "busseq_begin has not been called");
+  if (count < 0 || h->iter_host + count > h->n_iter)
+    return fail(BUSSEQ_ERR_ARG, "requested sweeps exceed the run length (%d of %d done)", h->iter_host, h->n_iter);
+  for (int c = 0; c < count; ++c) {
+    cudaGraphExec_t g = h->iter_host < h->n_burnin ? h->g_burn : h->g_keep;
+    CUDA_TRY(cudaGraphLaunch(g, h->stream));
+    ++h->iter_host;
+  }
+  return BUSSEQ_OK;
+}
+
+int busseq_synchronize(busseq_handle* h) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  return check_device_error(h);
+}
+
+int busseq_finish(busseq_handle* h) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (!h->begun || h->iter_host != h->n_iter)
+    return fail(BUSSEQ_ERR_STATE, "the run is not complete (%d of %d sweeps)", h->iter_host, h->n_iter);
+  TRY(check_device_error(h));
+  h->finished = true;
+  h->est_valid = false;
+  return ensure_estimates(h);
+}
+
+int busseq_run(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_unchanged) {
+  TRY(busseq_begin(h, n_iter, n_burnin, n_unchanged));
+  TRY(busseq_sweeps(h, n_iter));
+  return busseq_finish(h);
+}
+
+int busseq_get_estimates(busseq_handle* h, busseq_estimates* o) {
+  if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  TRY(ensure_estimates(h));
+  const bq::DevState& s = h->s;
+  const int64_t G = s.G, N = s.N;
+  const int B = s.B, K = s.K;
+  const bq::Estimates& e = h->est;
+  auto cp = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (dst) CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return BUSSEQ_OK;
+  };
+  TRY(cp(o->gamma, e.gamma, 2 * B * sizeof(double)));
+  TRY(cp(o->alpha, e.alpha, G * sizeof(double)));
+  if (K > 1) TRY(cp(o->L, e.L, (K - 1) * G * sizeof(double)));
+  TRY(cp(o->beta, e.beta, K * G * sizeof(double)));
+  TRY(cp(o->p_tau0, e.ptau, 2 * sizeof(double)));
+  TRY(cp(o->nu, e.nu, B * G * sizeof(double)));
+  TRY(cp(o->delta, e.delta, N * sizeof(double)));
+  TRY(cp(o->phi, e.phi, B * G * sizeof(double)));
+  TRY(cp(o->W, e.W, N * sizeof(int32_t)));
+  TRY(cp(o->pi, e.pi, B * K * sizeof(double)));
+  if (o->X) CUDA_TRY(cudaMemcpy2D(o->X, G * 4, s.X, s.Gp * 4, G * 4, N, cudaMemcpyDeviceToHost));
+  if (o->Z) {
+    std::vector<uint32_t> zm((size_t)N * s.Gw);
+    CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < N; ++i)
+      for (int64_t g = 0; g < G; ++g) o->Z[i * G + g] = (zm[i * s.Gw + (g >> 5)] >> (g & 31)) & 1u;
+  }
+  return BUSSEQ_OK;
+}
+
+int busseq_get_preserved(busseq_handle* h, busseq_preserved* o) {
+  if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  const bq::DevState& s = h->s;
+  if (!h->finished) return fail(BUSSEQ_ERR_STATE, "no finished run");
+  if (!s.keep_draws) return fail(BUSSEQ_ERR_STATE, "draws were not kept (set keep_draws)");
+  const int64_t nk = h->n_kept, G = s.G, N = s.N;
+  const int B = s.B, K = s.K;
+  // device layout [kept][scalar] -> reference layout [scalar][kept]
+  auto tr_f = [&](double* dst, const float* src, int64_t nscal) -> int {
+    if (!dst || nscal <= 0) return BUSSEQ_OK;
+    std::vector<float> buf((size_t)nk * nscal);
+    CUDA_TRY(cudaMemcpy(buf.data(), src, buf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int64_t it = 0; it < nk; ++it)
+      for (int64_t j = 0; j < nscal; ++j) dst[j * nk + it] = buf[it * nscal + j];
+    return BUSSEQ_OK;
+  };
+  TRY(tr_f(o->gamma, s.keep_gamma, 2 * B));
+  TRY(tr_f(o->alpha, s.keep_alpha, G));
+  TRY(tr_f(o->beta, s.keep_beta, (K - 1) * G));
+  TRY(tr_f(o->p_tau0, s.keep_ptau, 2));
+  TRY(tr_f(o->nu, s.keep_nu, (B - 1) * G));
+  TRY(tr_f(o->delta, s.keep_delta, N));
+  TRY(tr_f(o->phi, s.keep_phi, B * G));
+  TRY(tr_f(o->pi, s.keep_pi, B * K));
+  if (o->L && K > 1) {
+    const int64_t ns = (K - 1) * G;
+    std::vector<int8_t> buf((size_t)nk * ns);
+    CUDA_TRY(cudaMemcpy(buf.data(), s.keep_L, buf.size(), cudaMemcpyDeviceToHost));
+    for (int64_t it = 0; it < nk; ++it)
+      for (int64_t j = 0; j < ns; ++j) o->L[j * nk + it] = buf[it * ns + j];
+  }
+  if (o->W) {
+    std::vector<int16_t> buf((size_t)nk * N);
+    CUDA_TRY(cudaMemcpy(buf.data(), s.keep_W, buf.size() * 2, cudaMemcpyDeviceToHost));
+    for (int64_t it = 0; it < nk; ++it)
+      for (int64_t j = 0; j < N; ++j) o->W[j * nk + it] = buf[it * N + j];
+  }
+  return BUSSEQ_OK;
+}
+
+int busseq_bic(busseq_handle* h, double* bic) {
+  if (!h || !bic) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  TRY(ensure_estimates(h));
+  bq::k_bic_cell<<<(unsigned)h->s.N, 256, 0, h->stream>>>(h->s, h->est, h->ll_ik);
+  LAUNCH_CHECK("k_bic_cell");
+  bq::k_bic_total<<<1, 1024, 0, h->stream>>>(h->s, h->est, h->ll_ik, h->bic_out);
+  LAUNCH_CHECK("k_bic_total");
+  double out[2];
+  CUDA_TRY(cudaMemcpyAsync(out, h->bic_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *bic = out[0];
+  return BUSSEQ_OK;
+}
+
+int busseq_get_state(busseq_handle* h, busseq_state* o) {
+  if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const bq::DevState& s = h->s;
+  const int64_t G = s.G, N = s.N, Gp = s.Gp;
+  const int B = s.B, K = s.K;
+  auto rows = [&](void* dst, const void* src, size_t esz, int64_t nrows) -> int {
+    if (dst) CUDA_TRY(cudaMemcpy2D(dst, G * esz, src, Gp * esz, G * esz, nrows, cudaMemcpyDeviceToHost));
+    return BUSSEQ_OK;
+  };
+  auto flat = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (dst) CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return BUSSEQ_OK;
+  };
+  TRY(rows(o->X, s.X, 4, N));
+  if (o->Z) {
+    std::vector<uint32_t> zm((size_t)N * s.Gw);
+    CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < N; ++i)
+      for (int64_t g = 0; g < G; ++g) o->Z[i * G + g] = (uint8_t)((zm[i * s.Gw + (g >> 5)] >> (g & 31)) & 1u);
+  }
+  TRY(flat(o->W, s.W, N * 4));
+  TRY(rows(o->L, s.L, 1, K));
+  TRY(flat(o->alpha, s.alpha, G * 4));
+  TRY(flat(o->mu_alpha, s.mu_alpha, G * 4));
+  TRY(rows(o->beta, s.beta, 4, K));
+  TRY(rows(o->nu, s.nu, 4, B));
+  TRY(flat(o->mu_nu, s.mu_nu, B * 4));
+  TRY(flat(o->delta, s.delta, N * 4));
+  TRY(flat(o->mu_delta, s.mu_delta, N * 4));
+  TRY(rows(o->phi, s.phi, 4, B));
+  TRY(flat(o->gamma, s.gamma, 2 * B * 4));
+  TRY(flat(o->pi, s.pi, B * K * 4));
+  TRY(flat(o->p_tau0, s.p_tau0, 2 * 4));
+  return BUSSEQ_OK;
+}
+
+int busseq_set_state(busseq_handle* h, const busseq_state* in) {
+  if (!h || !in) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  bq::DevState& s = h->s;
+  const int64_t G = s.G, N = s.N, Gp = s.Gp;
+  const int B = s.B, K = s.K;
+  auto rows = [&](void* dst, const void* src, size_t esz, int64_t nrows) -> int {
+    if (src) CUDA_TRY(cudaMemcpy2D(dst, Gp * esz, src, G * esz, G * esz, nrows, cudaMemcpyHostToDevice));
+    return BUSSEQ_OK;
+  };
+  auto flat = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (src) CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return BUSSEQ_OK;
+  };
+  if (in->W) {
+    for (int64_t i = 0; i < N; ++i)
+      if (in->W[i] < 0 || in->W[i] >= K) return fail(BUSSEQ_ERR_ARG, "W[%lld] out of range", (long long)i);
+  }
+  TRY(rows(s.X, in->X, 4, N));
+  if (in->Z) {
+    std::vector<uint32_t> zm((size_t)N * s.Gw, 0u);
+    for (int64_t i = 0; i < N; ++i)
+      for (int64_t g = 0; g < G; ++g)
+        if (in->Z[i * G + g]) zm[i * s.Gw + (g >> 5)] |= 1u << (g & 31);
+    CUDA_TRY(cudaMemcpy(s.zm, zm.data(), zm.size() * 4, cudaMemcpyHostToDevice));
+  }
+  TRY(flat(s.W, in->W, N * 4));
+  TRY(rows(s.L, in->L, 1, K));
+  TRY(flat(s.alpha, in->alpha, G * 4));
+  TRY(flat(s.mu_alpha, in->mu_alpha, G * 4));
+  TRY(rows(s.beta, in->beta, 4, K));
+  TRY(rows(s.nu, in->nu, 4, B));
+  TRY(flat(s.mu_nu, in->mu_nu, B * 4));
+  TRY(flat(s.delta, in->delta, N * 4));
+  TRY(flat(s.mu_delta, in->mu_delta, N * 4));
+  TRY(rows(s.phi, in->phi, 4, B));
+  TRY(flat(s.gamma, in->gamma, 2 * B * 4));
+  TRY(flat(s.pi, in->pi, B * K * 4));
+  TRY(flat(s.p_tau0, in->p_tau0, 2 * 4));
+  const int64_t nfin = std::max<int64_t>(std::max<int64_t>(N, (int64_t)B * Gp), (int64_t)B * K);
+  bq::k_init_finish<<<blocks_for(nfin, 256), 256, 0, h->stream>>>(s, 0);
+  LAUNCH_CHECK("k_init_finish");
+  bq::k_sort_pi<<<B, 1024, 0, h->stream>>>(s, 0, 0);
+  LAUNCH_CHECK("k_sort_pi");
+  h->est_valid = false;
+  return check_device_error(h);
+}
+
+int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_unchanged) {
+  using namespace bq;
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (iter < 0) return fail(BUSSEQ_ERR_ARG, "iter must be non-negative");
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaMemcpyAsync(h->s.iter, &iter, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  DevState s = h->s;
+  s.n_unchanged = n_unchanged;
+  cudaStream_t st = h->stream;
+  const unsigned pb = blocks_for(propose_count(s), 256);
+  switch (stage) {
+    case BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L:
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA);
+      LAUNCH_CHECK("k_propose");
+      TRY(launch_kernel(h, 1, st, 0, s));
+      break;
+    case BUSSEQ_STAGE_BETA_NU:
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU);
+      LAUNCH_CHECK("k_propose");
+      TRY(launch_kernel(h, 2, st, 0, s));
+      break;
+    case BUSSEQ_STAGE_DELTA:
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_DELTA);
+      LAUNCH_CHECK("k_propose");
+      TRY(launch_kernel(h, 3, st, 0, s));
+      break;
+    case BUSSEQ_STAGE_PHI:
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_PHI);
+      LAUNCH_CHECK("k_propose");
+      TRY(launch_kernel(h, 4, st, 0, s));
+      break;
+    case BUSSEQ_STAGE_W:
+      TRY(launch_kernel(h, 5, st, 0, s));
+      break;
+    case BUSSEQ_STAGE_PI:
+      k_sort_pi<<<s.B, 1024, 0, st>>>(s, 1, 0);
+      LAUNCH_CHECK("k_sort_pi");
+      break;
+    default:
+      return fail(BUSSEQ_ERR_ARG, "unknown stage %d", stage);
+  }
+  h->est_valid = false;
+  return check_device_error(h);
+}
+
+int busseq_get_log_ratios(busseq_handle* h, busseq_log_ratios* o) {
+  if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const bq::DevState& s = h->s;
+  auto cp = [&](double* dst, const double* src, int64_t n) -> int {
+    if (dst) CUDA_TRY(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return BUSSEQ_OK;
+  };
+  TRY(cp(o->gamma, s.lr_gamma, 2 * s.B));
+  TRY(cp(o->alpha, s.lr_alpha, s.G));
+  TRY(cp(o->beta, s.lr_beta, (int64_t)s.K * s.G));
+  TRY(cp(o->nu, s.lr_nu, (int64_t)s.B * s.G));
+  TRY(cp(o->delta, s.lr_delta, s.N));
+  TRY(cp(o->phi, s.lr_phi, (int64_t)s.B * s.G));
+  TRY(cp(o->W, s.lr_W, s.N));
+  return BUSSEQ_OK;
+}
+
+int busseq_set_stream(busseq_handle* h, void* cuda_stream) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+  return BUSSEQ_OK;
+}
+
+const char* busseq_kernel_name(int32_t i) { return (i >= 0 && i < kNumKernels) ? kKernelNames[i] : ""; }
+
+int busseq_profile(busseq_handle* h, int32_t n_sweeps, double* ms_avg, int32_t cap, int32_t* n_out) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (n_sweeps <= 0) return fail(BUSSEQ_ERR_ARG, "n_sweeps must be positive");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const int nk = 7;  // one burn-in sweep: every kernel but the posterior accumulation
+  std::vector<cudaEvent_t> ev((size_t)nk * 2 * n_sweeps);
+  for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+  int r = BUSSEQ_OK;
+  for (int sw = 0; sw < n_sweeps && r == BUSSEQ_OK; ++sw)
+    for (int k = 0; k < nk && r == BUSSEQ_OK; ++k) {
+      cudaEventRecord(ev[((size_t)sw * nk + k) * 2], h->stream);
+      r = launch_kernel(h, k, h->stream, 0, h->s);
+      cudaEventRecord(ev[((size_t)sw * nk + k) * 2 + 1], h->stream);
+    }
+  if (r == BUSSEQ_OK) r = check_device_error(h);
+  std::vector<double> tot(nk, 0.0);
+  if (r == BUSSEQ_OK)
+    for (int sw = 0; sw < n_sweeps; ++sw)
+      for (int k = 0; k < nk; ++k) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[((size_t)sw * nk + k) * 2], ev[((size_t)sw * nk + k) * 2 + 1]);
+        tot[k] += ms;
+      }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (r != BUSSEQ_OK) return r;
+  for (int k = 0; k < nk && k < cap; ++k) ms_avg[k] = tot[k] / n_sweeps;
+  if (n_out) *n_out = nk;
+  h->est_valid = false;
+  return BUSSEQ_OK;
+}
+
+double busseq_kernel_bytes(busseq_handle* h, int32_t i) {
+  if (!h) return 0.0;
+  const double E = (double)h->s.N * (double)h->s.G;
+  const double params = 8.0 * ((double)h->s.K * h->s.G + 2.0 * h->s.B * h->s.G + h->s.N);
+  switch (i) {
+    case 0: return params;                   // proposals
+    case 1: return 8.25 * E;                 // read X, write X, Y==0 mask in, Z mask out
+    case 2: return 4.0 * E;                  // read X
+    case 3: return 4.0 * E;
+    case 4: return 4.0 * E;
+    case 5: return 4.0 * E;
+    case 6: return 8.0 * h->s.N;             // W in, cell order out
+    case 7: return params;
+    default: return 0.0;
+  }
+}
+
+int busseq_launches_per_sweep(busseq_handle* h, int32_t kept) {
+  (void)h;
+  return kept ? 8 : 7;
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+// busseq -- drop-in replacement of the reference BUSseq_gpu executable.
+//
+// Same command line (getopt "B:N:G:K:s:c:i:b:u:po:", BUSseq_gpu.cu:1048),
+// same defaults and derived defaults (:1028-1111), same checks and messages
+// (:1120-1134), same stdout phase lines and output files (:1118-2018).
+// Options the reference does not have are long options only:
+//   --w-update=mh|gibbs   W move (default mh, the reference's)
+//   --device=D            CUDA device ordinal
+//   --stats               print per-phase wall times to stderr
+#include "busseq_gb300.h"
+
+#include <getopt.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+
+#include <chrono>
+#include <vector>
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+[[noreturn]] void die_lib(const char* what) {
+  fprintf(stderr, "busseq: %s: %s\n", what, busseq_last_error());
+  exit(1);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  int B = 4;
+  std::vector<int32_t> n_b = {300, 300, 200, 200};
+  n_b.resize(200, 0);
+  long G = 3000;
+  int K = 5;
+  int seed = 0;
+  char count_data[4096] = "count_data/demo_count.txt";
+  int n_iter = 4000, n_burnin = 2000, n_unchanged = 500;
+  int print_preserved = 0;
+  char output_file[4096] = "demo_output";
+  char n_file[4096] = "";
+  int n_file_flag = 0, burnin_flag = 1, unchanged_flag = 1, seed_flag = 1;
+  int w_update = BUSSEQ_W_MH, device = 0, stats = 0;
+
+  static struct option longopts[] = {{"w-update", required_argument, nullptr, 1000},
+                                     {"device", required_argument, nullptr, 1001},
+                                     {"stats", no_argument, nullptr, 1002},
+                                     {nullptr, 0, nullptr, 0}};
+  int opt;
+  while ((opt = getopt_long(argc, argv, "B:N:G:K:s:c:i:b:u:po:", longopts, nullptr)) != -1) {
+    switch (opt) {
+      case 'B': B = atoi(optarg); break;
+      case 'N': n_file_flag = 1; snprintf(n_file, sizeof(n_file), "%s", optarg); break;
+      case 'G': G = atol(optarg); break;
+      case 'K': K = atoi(optarg); break;
+      case 's': seed_flag = 0; seed = atoi(optarg); break;
+      case 'c': snprintf(count_data, sizeof(count_data), "%s", optarg); break;
+      case 'i': n_iter = atoi(optarg); break;
+      case 'b': burnin_flag = 0; n_burnin = atoi(optarg); break;
+      case 'u': unchanged_flag = 0; n_unchanged = atoi(optarg); break;
+      case 'p': print_preserved = 1; break;
+      case 'o': snprintf(output_file, sizeof(output_file), "%s", optarg); break;
+      case 1000:
+        if (!strcmp(optarg, "gibbs")) w_update = BUSSEQ_W_GIBBS;
+        else if (!strcmp(optarg, "mh")) w_update = BUSSEQ_W_MH;
+        else { fprintf(stderr, "--w-update must be mh or gibbs\n"); return 1; }
+        break;
+      case 1001: device = atoi(optarg); break;
+      case 1002: stats = 1; break;
+      default:
+        printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
+               "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
+               "[-p print_preserved] [-o output_prefix] \n",
+               argv[0]);
+        exit(1);
+    }
+  }
+  if (B > BUSSEQ_MAX_BATCHES || B > (int)n_b.size()) {
+    printf("At most %d batches are supported.\n", BUSSEQ_MAX_BATCHES);
+    return -1;
+  }
+  if (argc > 1) {
+    if (n_file_flag) {
+      FILE* f = fopen(n_file, "r");
+      if (!f) { printf("Cannot open the batch-size file %s.\n", n_file); return -1; }
+      for (int b = 0; b < B; ++b)
+        if (fscanf(f, "%d", &n_b[b]) != 1) { printf("Cannot read %d batch sizes from %s.\n", B, n_file); return -1; }
+      fclose(f);
+    }
+    if (burnin_flag) n_burnin = n_iter / 2;
+    if (unchanged_flag) n_unchanged = (0.3 * n_iter > 500) ? (int)(0.3 * n_iter) : 500;
+  }
+  if (seed_flag) {
+    struct timeval tv;
+    gettimeofday(&tv, nullptr);
+    seed = (int)tv.tv_usec;
+  }
+  printf("Seed is %d\n", seed);
+  if (n_burnin > n_iter) {
+    printf("Burn-in iterations must be less than total number of iterations.\n");
+    return -1;
+  }
+  if (B < 2) {
+    printf("The batch number must be greater than one.\n");
+    return -1;
+  }
+  for (int b = 0; b < B; ++b)
+    if (n_b[b] < K) {
+      printf("The sample size in any batch must be greater than the assumed cell type number.\n");
+      return -1;
+    }
+  int64_t N = 0;
+  for (int b = 0; b < B; ++b) N += n_b[b];
+  fflush(stdout);
+
+  double t0 = now_s();
+  printf("Start reading file.\n");
+  fflush(stdout);
+  std::vector<int32_t> Y((size_t)N * G);
+  if (busseq_read_counts(count_data, N, G, Y.data()) != BUSSEQ_OK) die_lib("reading the count file");
+  double t1 = now_s();
+
+  printf("Start initialization.\n");
+  fflush(stdout);
+  srand((unsigned)seed);
+  const double p0 = ((double)rand() * 0.5) / RAND_MAX;  // p_init_bound = 0.5 (BUSseq_gpu.cu:1172-1173)
+  busseq_dims dims{B, K, G, n_b.data()};
+  busseq_options o{};
+  o.seed = (uint64_t)(uint32_t)seed;
+  o.p0 = p0 > 0.0 ? p0 : 1e-9;
+  o.w_update = w_update;
+  o.keep_draws = print_preserved;
+  o.device = device;
+  busseq_handle* h = nullptr;
+  if (busseq_create(&dims, Y.data(), 0, &o, &h) != BUSSEQ_OK) die_lib("initialisation");
+  std::vector<int32_t>().swap(Y);
+  double t2 = now_s();
+
+  printf("Start MCMC.\n");
+  fflush(stdout);
+  if (busseq_begin(h, n_iter, n_burnin, n_unchanged) != BUSSEQ_OK) die_lib("starting the run");
+  if (busseq_sweeps(h, n_burnin) != BUSSEQ_OK || busseq_synchronize(h) != BUSSEQ_OK) die_lib("burn-in");
+  printf("Burnin completed. Start recording iterations.\n");
+  fflush(stdout);
+  if (busseq_sweeps(h, n_iter - n_burnin) != BUSSEQ_OK || busseq_synchronize(h) != BUSSEQ_OK) die_lib("sampling");
+  double t3 = now_s();
+
+  printf("Start posterior inference.\n");
+  fflush(stdout);
+  if (busseq_finish(h) != BUSSEQ_OK) die_lib("posterior inference");
+  printf("Start writing output files.\n");
+  if (print_preserved) printf("Start writing preserved iterations.\n");
+  fflush(stdout);
+  if (busseq_write_outputs(h, output_file, print_preserved) != BUSSEQ_OK) die_lib("writing outputs");
+  double t4 = now_s();
+  if (stats) {
+    fprintf(stderr,
+            "{\"read_s\": %.3f, \"init_s\": %.3f, \"mcmc_s\": %.3f, \"iters_per_s\": %.2f, \"post_write_s\": %.3f}\n",
+            t1 - t0, t2 - t1, t3 - t2, n_iter / (t3 - t2 > 0 ? t3 - t2 : 1e-9), t4 - t3);
+  }
+  busseq_destroy(h);
+  return 0;
+}

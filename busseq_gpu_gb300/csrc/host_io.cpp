@@ -1,0 +1,257 @@
+// Count-file parser and output writers with the reference's formats.
+//
+// Reading: BUSseq_gpu.cu:1143-1161 reads N*G integers with fscanf("%d"); here
+// the whole file is read once and parsed by every host thread (two passes:
+// count the tokens of each slice, then parse each slice into its place).
+// Writing: BUSseq_gpu.cu:1610-2018 -- tab-separated rows, "%lf" for floating
+// point, "%d" for integers; rows are formatted in parallel and written in order.
+#include "busseq_gb300.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <functional>
+#include <string>
+#include <thread>
+#include <vector>
+
+extern "C" int busseq_internal_set_error(int code, const char* msg);
+
+namespace {
+
+int nthreads() {
+  const unsigned n = std::thread::hardware_concurrency();
+  return n == 0 ? 1 : (int)std::min(n, 64u);
+}
+
+inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+
+// Parses [b, e): counts tokens (out == NULL) or stores them.  Returns the
+// number of tokens, or -1 (and *bad = position) on a malformed token.
+int64_t parse_slice(const char* b, const char* e, int32_t* out, int64_t cap, const char** bad) {
+  int64_t n = 0;
+  const char* p = b;
+  while (p < e) {
+    while (p < e && is_space(*p)) ++p;
+    if (p >= e) break;
+    bool neg = false;
+    if (*p == '-' || *p == '+') { neg = *p == '-'; ++p; }
+    if (p >= e || *p < '0' || *p > '9') { *bad = p; return -1; }
+    int64_t v = 0;
+    while (p < e && *p >= '0' && *p <= '9') {
+      v = v * 10 + (*p - '0');
+      if (v > 2147483647LL) { *bad = p; return -1; }
+      ++p;
+    }
+    if (p < e && !is_space(*p)) { *bad = p; return -1; }
+    if (out) {
+      if (n >= cap) { *bad = p; return -1; }
+      out[n] = (int32_t)(neg ? -v : v);
+    }
+    ++n;
+  }
+  return n;
+}
+
+struct Table {
+  int64_t rows = 0, cols = 0;
+  // formats cell (r, c) into buf, returns length
+  std::function<int(int64_t, int64_t, char*)> cell;
+  bool trailing_tab_no_newline = false;  // the _post_p.txt layout
+};
+
+int fmt_int(int64_t v, char* buf) {
+  char tmp[24];
+  int n = 0;
+  const bool neg = v < 0;
+  uint64_t u = neg ? (uint64_t)(-v) : (uint64_t)v;
+  do { tmp[n++] = (char)('0' + u % 10); u /= 10; } while (u);
+  int k = 0;
+  if (neg) buf[k++] = '-';
+  while (n) buf[k++] = tmp[--n];
+  return k;
+}
+
+int fmt_lf(double v, char* buf) { return snprintf(buf, 64, "%f", v); }
+
+int write_table(const std::string& path, const Table& t) {
+  FILE* f = fopen(path.c_str(), "wb");
+  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("cannot open " + path + " for writing").c_str());
+  const int nt = nthreads();
+  const int64_t rows_per_task = std::max<int64_t>(1, (int64_t)(1 << 20) / std::max<int64_t>(1, t.cols));
+  std::vector<std::string> bufs(nt);
+  int64_t r0 = 0;
+  bool ok = true;
+  while (r0 < t.rows && ok) {
+    std::vector<std::thread> th;
+    for (int w = 0; w < nt; ++w) {
+      const int64_t a = r0 + w * rows_per_task, b = std::min(t.rows, a + rows_per_task);
+      bufs[w].clear();
+      if (a >= b) continue;
+      th.emplace_back([&, w, a, b]() {
+        std::string& s = bufs[w];
+        s.reserve((size_t)((b - a) * t.cols * 10));
+        char cell[80];
+        for (int64_t r = a; r < b; ++r) {
+          for (int64_t c = 0; c < t.cols; ++c) {
+            const int n = t.cell(r, c, cell);
+            s.append(cell, (size_t)n);
+            if (t.trailing_tab_no_newline) s.push_back('\t');
+            else s.push_back(c + 1 < t.cols ? '\t' : '\n');
+          }
+        }
+      });
+    }
+    for (auto& x : th) x.join();
+    for (int w = 0; w < nt; ++w)
+      if (!bufs[w].empty() && fwrite(bufs[w].data(), 1, bufs[w].size(), f) != bufs[w].size()) ok = false;
+    r0 += (int64_t)nt * rows_per_task;
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + path).c_str());
+  return BUSSEQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
+  if (!path || !out || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
+  FILE* f = fopen(path, "rb");
+  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open count file ") + path).c_str());
+  fseek(f, 0, SEEK_END);
+  const long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  std::vector<char> buf((size_t)std::max(0L, sz));
+  const size_t got = sz > 0 ? fread(buf.data(), 1, (size_t)sz, f) : 0;
+  fclose(f);
+  if ((long)got != sz) return busseq_internal_set_error(BUSSEQ_ERR_IO, "short read of the count file");
+  const int nt = std::max(1, std::min(nthreads(), (int)(sz / (1 << 16)) + 1));
+  std::vector<const char*> starts(nt + 1);
+  const char* base = buf.data();
+  const char* end = base + sz;
+  starts[0] = base;
+  starts[nt] = end;
+  for (int t = 1; t < nt; ++t) {
+    const char* p = base + (size_t)sz * t / nt;
+    if (p < starts[t - 1]) p = starts[t - 1];
+    while (p < end && !is_space(*p)) ++p;  // never split a token
+    starts[t] = p;
+  }
+  std::vector<int64_t> cnt(nt, 0);
+  std::vector<const char*> bad(nt, nullptr);
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]() { cnt[t] = parse_slice(starts[t], starts[t + 1], nullptr, 0, &bad[t]); });
+    for (auto& x : th) x.join();
+  }
+  int64_t total = 0;
+  for (int t = 0; t < nt; ++t) {
+    if (cnt[t] < 0) {
+      char msg[160];
+      snprintf(msg, sizeof(msg), "malformed count at byte %lld of %s", (long long)(bad[t] - base), path);
+      return busseq_internal_set_error(BUSSEQ_ERR_IO, msg);
+    }
+    total += cnt[t];
+  }
+  if (total != N * G) {
+    char msg[200];
+    snprintf(msg, sizeof(msg), "count file %s holds %lld numbers, expected N*G = %lld", path, (long long)total,
+             (long long)(N * G));
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, msg);
+  }
+  std::vector<int64_t> pre(nt + 1, 0);
+  for (int t = 0; t < nt; ++t) pre[t + 1] = pre[t] + cnt[t];
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]() { parse_slice(starts[t], starts[t + 1], out + pre[t], cnt[t], &bad[t]); });
+    for (auto& x : th) x.join();
+  }
+  for (int64_t i = 0; i < N * G; ++i)
+    if (out[i] < 0) return busseq_internal_set_error(BUSSEQ_ERR_IO, "negative count in the count file");
+  return BUSSEQ_OK;
+}
+
+int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
+                         int32_t* kept_draws);
+
+int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
+  if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
+  int32_t B, K, nk, kd;
+  int64_t G, N;
+  int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
+  if (r) return r;
+  std::vector<int32_t> Z((size_t)N * G), X((size_t)N * G), W(N);
+  std::vector<double> gamma(2 * B), alpha(G), L((size_t)std::max(1, K - 1) * G), beta((size_t)K * G), ptau(2),
+      nu((size_t)B * G), delta(N), phi((size_t)B * G), pi((size_t)B * K);
+  busseq_estimates e{};
+  e.Z = Z.data(); e.X = X.data(); e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
+  e.beta = beta.data(); e.p_tau0 = ptau.data(); e.nu = nu.data(); e.delta = delta.data();
+  e.phi = phi.data(); e.W = W.data(); e.pi = pi.data();
+  if ((r = busseq_get_estimates(h, &e))) return r;
+  const std::string pre(prefix);
+  auto ints = [](const std::vector<int32_t>& v, int64_t cols) {
+    Table t;
+    t.rows = (int64_t)v.size() / cols;
+    t.cols = cols;
+    t.cell = [&v, cols](int64_t r, int64_t c, char* b) { return fmt_int(v[r * cols + c], b); };
+    return t;
+  };
+  auto dbls = [](const double* v, int64_t rows, int64_t cols) {
+    Table t;
+    t.rows = rows;
+    t.cols = cols;
+    t.cell = [v, cols](int64_t r, int64_t c, char* b) { return fmt_lf(v[r * cols + c], b); };
+    return t;
+  };
+  // _post_Z, _post_X: last sweep's state (BUSseq_gpu.cu:1613-1645)
+  if ((r = write_table(pre + "_post_Z.txt", ints(Z, G)))) return r;
+  if ((r = write_table(pre + "_post_X.txt", ints(X, G)))) return r;
+  if ((r = write_table(pre + "_post_gamma.txt", dbls(gamma.data(), 2, B)))) return r;
+  if ((r = write_table(pre + "_post_alpha.txt", dbls(alpha.data(), G, 1)))) return r;
+  if ((r = write_table(pre + "_post_L.txt", dbls(L.data(), K - 1, G)))) return r;
+  for (int64_t g = 0; g < G; ++g) beta[g] = 0.0;  // the first row is printed as literal zeros
+  if ((r = write_table(pre + "_post_beta.txt", dbls(beta.data(), K, G)))) return r;
+  {
+    Table t = dbls(ptau.data(), 1, 2);
+    t.trailing_tab_no_newline = true;  // "p\ttau0\t" without a newline (BUSseq_gpu.cu:1725-1727)
+    if ((r = write_table(pre + "_post_p.txt", t))) return r;
+  }
+  for (int64_t g = 0; g < G; ++g) nu[g] = 0.0;
+  if ((r = write_table(pre + "_post_nu.txt", dbls(nu.data(), B, G)))) return r;
+  if ((r = write_table(pre + "_post_delta.txt", dbls(delta.data(), N, 1)))) return r;
+  if ((r = write_table(pre + "_post_phi.txt", dbls(phi.data(), B, G)))) return r;
+  if ((r = write_table(pre + "_post_W.txt", ints(W, 1)))) return r;
+  if ((r = write_table(pre + "_post_pi.txt", dbls(pi.data(), B, K)))) return r;
+  double bic = 0.0;
+  if ((r = busseq_bic(h, &bic))) return r;
+  if ((r = write_table(pre + "_BIC.txt", dbls(&bic, 1, 1)))) return r;
+  if (!print_preserved) return BUSSEQ_OK;
+  if (!kd || nk <= 0) return busseq_internal_set_error(BUSSEQ_ERR_STATE, "no kept draws to print (keep_draws off)");
+  const int64_t n = nk;
+  std::vector<double> pg((size_t)2 * B * n), pa((size_t)G * n), pb((size_t)(K - 1) * G * n), pp((size_t)2 * n),
+      pn((size_t)(B - 1) * G * n), pd((size_t)N * n), pf((size_t)B * G * n), ppi((size_t)B * K * n);
+  std::vector<int32_t> pL((size_t)(K - 1) * G * n), pW((size_t)N * n);
+  busseq_preserved p{};
+  p.gamma = pg.data(); p.alpha = pa.data(); p.L = pL.data(); p.beta = pb.data(); p.p_tau0 = pp.data();
+  p.nu = pn.data(); p.delta = pd.data(); p.phi = pf.data(); p.W = pW.data(); p.pi = ppi.data();
+  if ((r = busseq_get_preserved(h, &p))) return r;
+  if ((r = write_table(pre + "_preserved_gamma.txt", dbls(pg.data(), 2 * B, n)))) return r;
+  if ((r = write_table(pre + "_preserved_alpha.txt", dbls(pa.data(), G, n)))) return r;
+  if ((r = write_table(pre + "_preserved_L.txt", ints(pL, n)))) return r;
+  if ((r = write_table(pre + "_preserved_beta.txt", dbls(pb.data(), (K - 1) * G, n)))) return r;
+  if ((r = write_table(pre + "_preserved_p.txt", dbls(pp.data(), 2, n)))) return r;
+  if ((r = write_table(pre + "_preserved_nu.txt", dbls(pn.data(), (B - 1) * G, n)))) return r;
+  if ((r = write_table(pre + "_preserved_delta.txt", dbls(pd.data(), N, n)))) return r;
+  if ((r = write_table(pre + "_preserved_phi.txt", dbls(pf.data(), B * G, n)))) return r;
+  if ((r = write_table(pre + "_preserved_W.txt", ints(pW, n)))) return r;
+  if ((r = write_table(pre + "_preserved_pi.txt", dbls(ppi.data(), B * K, n)))) return r;
+  return BUSSEQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,352 @@
+// Initialisation, posterior summaries and BIC.
+//
+// Initialisation restates BUSseq_gpu.cu:1163-1244 (kernels :369-482) as a
+// handful of passes instead of the reference's B*K*G*3 single-block launches:
+//   k_init_scan    Y == 0 bit masks, library sizes, largest count
+//   k_init_hist    histogram of the positive counts per batch (gamma statistics)
+//   k_init_w_delta W ~ Cat(pi_init), delta = log(lib_i) - log(lib_first of batch)
+//   k_sort_pi      cell order (no pi draw)
+//   k_init_raw     raw means of log(1 + Y e^-delta) per (batch, type, gene) and
+//                  alpha, beta, nu, L from them; mu_nu from the batch means
+//   k_init_finish  phi, gamma, pi, mu_delta, exp(delta), exp(alpha+beta+nu)
+// Summaries: k_finalize (posterior means, P(L=1), W mode; :1557-1608) and
+// k_bic_cell + k_bic_total (:967-1024, :1815-1843).
+#include "kernels_common.cuh"
+
+namespace bq {
+
+__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax) {
+  const int64_t i = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ long long sh_sum[32];
+  __shared__ int sh_max[32];
+  long long sum = 0;
+  int mx = 0;
+  for (int64_t w = warp; w < s.Gw; w += nw) {
+    const int64_t g = w * 32 + lane;
+    const int y = g < s.G ? s.Y[i * s.Gp + g] : 1;
+    const unsigned m = __ballot_sync(0xffffffffu, y == 0);
+    if (lane == 0) const_cast<uint32_t*>(s.y0m)[i * s.Gw + w] = m;
+    if (g < s.G) {
+      sum += y;
+      mx = max(mx, y);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  if (lane == 0) { sh_sum[warp] = sum; sh_max[warp] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    int m = 0;
+    for (int w = 0; w < nw; ++w) { t += sh_sum[w]; m = max(m, sh_max[w]); }
+    libsize[i] = t;
+    atomicMax(ymax, m);
+  }
+}
+
+// Histogram of Y > 0 per batch; warp-aggregated so that repeated small values
+// cost one atomic per distinct value per warp.
+__global__ void k_init_hist(DevState s, int32_t* hist) {
+  const int64_t i = blockIdx.x;
+  const int b = s.batch_of[i];
+  const int lane = threadIdx.x & 31;
+  int32_t* h = hist + (int64_t)b * (s.ymax + 1);
+  for (int64_t g0 = (int64_t)(threadIdx.x & ~31); g0 < s.Gp; g0 += blockDim.x) {
+    const int64_t g = g0 + lane;
+    const int y = g < s.G ? s.Y[i * s.Gp + g] : 0;
+    const unsigned same = __match_any_sync(0xffffffffu, y);
+    if (y > 0 && __ffs(same) - 1 == lane) atomicAdd(&h[y], __popc(same));
+  }
+}
+
+__global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.N) return;
+  const int b = s.batch_of[i];
+  const int K = s.K;
+  Stream st(s.seed, SID_INIT_W, (uint64_t)i, 0u);
+  const float u = st.uniform();
+  // pi_init[k] = (k+1) / (K(K+1)/2), first_pi (BUSseq_gpu.cu:392-397)
+  const double den = K * (K + 1) / 2.0;
+  int k = 0;
+  double acc = 1.0 / den;
+  while ((double)u > acc && k < K - 1) { ++k; acc += (k + 1) / den; }
+  s.W[i] = k;
+  const int64_t l = libsize[i], l0 = libsize[s.batch_off[b]];
+  if (l <= 0) atomicMin(bad_cell, (int)i);
+  s.delta[i] = (float)(log((double)l) - log((double)l0));
+}
+
+// Raw means and the parameters derived from them.  Gene-pass layout: CTA =
+// (gene tile, chunk of one (batch, type) segment).  Tile tails compute, per
+// gene, raw[b][k] = mean over the segment of log(1 + Y e^-delta), then
+//   alpha = mu_alpha = raw[0][0], beta_k = raw[0][k] - raw[0][0],
+//   nu_b = (sum_k raw[b][k] - sum_k raw[0][k]) / K, L_k ~ prior odds;
+// the last tile turns the batch sums into mu_nu (BUSseq_gpu.cu:1232-1241).
+__global__ void __launch_bounds__(GENE_TILE) k_init_raw(DevState s) {
+  __shared__ double sh[(GENE_TILE / 32) * MAX_B];
+  __shared__ int sh_flag;
+  const int tid = threadIdx.x;
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int4 ch = s.gchunk[row];
+  const int start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + tid;
+  const bool valid = g < s.G;
+  if (len > 0 && valid) {
+    double acc = 0.0;
+    for (int j0 = 0; j0 < len; j0 += 32) {
+      const int jn = min(32, len - j0);
+      float f = 0.0f;
+      for (int jj = 0; jj < jn; ++jj) {
+        const int i = s.perm[start + j0 + jj];
+        const float y = (float)s.Y[(int64_t)i * Gp + g];
+        f += log1pf(y * expf(-s.delta[i]));
+      }
+      acc += f;
+    }
+    s.part[(int64_t)row * NSLOT * Gp + g] = acc;
+  }
+  if (!arrive_last(&s.cnt_tile[tile], (unsigned)s.cap_g, &sh_flag)) return;
+  const int B = s.B, K = s.K;
+  double bsum[MAX_B];
+  for (int b = 0; b < B; ++b) bsum[b] = 0.0;
+  if (valid) {
+    const double p0 = s.p_tau0[0];
+    const double log_rat_base = log(p0 / (1.0 - p0)) + (log((double)TAU0_INIT) - log(TAU1)) / 2.0;
+    double raw0[MAX_K];
+    double nusum0 = 0.0;
+    for (int b = 0; b < B; ++b) {
+      double rsum = 0.0;
+      for (int k = 0; k < K; ++k) {
+        double sumbk = 0.0;
+        for (int c = 0; c < s.cap_g; ++c) {
+          const int4 cc = s.gchunk[c];
+          if (cc.w == 0 || cc.x != b || cc.y != k) continue;
+          sumbk += __ldcg(&s.part[(int64_t)c * NSLOT * Gp + g]);
+        }
+        const int n = s.seg_cnt[b * K + k];
+        const double raw = n == 0 ? 0.0 : sumbk / n;
+        bsum[b] += sumbk;
+        rsum += raw;
+        if (b == 0) raw0[k] = raw;
+      }
+      if (b == 0) {
+        nusum0 = rsum;
+        s.nu[g] = 0.0f;
+      } else {
+        s.nu[(int64_t)b * Gp + g] = (float)((rsum - nusum0) / K);
+      }
+    }
+    s.alpha[g] = (float)raw0[0];
+    s.mu_alpha[g] = (float)raw0[0];
+    s.beta[g] = 0.0f;
+    s.L[g] = 0;
+    for (int k = 1; k < K; ++k) {
+      const double bt = raw0[k] - raw0[0];
+      s.beta[(int64_t)k * Gp + g] = (float)bt;
+      const double lr = log_rat_base + bt * bt * (1.0 / TAU0_INIT - 1.0 / TAU1) / 2.0;
+      const float u = uniform_at(s.seed, SID_INIT_L, (uint64_t)k * (uint64_t)s.G + (uint64_t)g, 0u, 0);
+      s.L[(int64_t)k * Gp + g] = (double)u > 1.0 / (1.0 + exp(lr)) ? 1 : 0;
+    }
+  }
+  // per-tile batch sums -> tpart[tile][b]
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int b = 0; b < B; ++b) {
+    const double v = warp_sum(bsum[b]);
+    if (lane == 0) sh[warp * MAX_B + b] = v;
+  }
+  __syncthreads();
+  if (tid < B) {
+    double t = 0.0;
+    for (int w = 0; w < GENE_TILE / 32; ++w) t += sh[w * MAX_B + tid];
+    s.tpart[(int64_t)tile * MAX_B + tid] = t;
+  }
+  if (!arrive_last(&s.cnt_glob[3], (unsigned)s.n_tiles, &sh_flag)) return;
+  if (tid < B) {
+    double t = 0.0;
+    for (int tt = 0; tt < s.n_tiles; ++tt) t += __ldcg(&s.tpart[(int64_t)tt * MAX_B + tid]);
+    sh[tid] = t / ((double)(s.batch_off[tid + 1] - s.batch_off[tid]) * (double)s.G);
+  }
+  __syncthreads();
+  if (tid < B) s.mu_nu[tid] = tid == 0 ? 0.0f : (float)(sh[tid] - sh[0]);
+}
+
+// Parameters that do not come from the data, and the derived tables.
+// Padded genes get harmless values (beta = nu = 0, phi = 1, E = 1).
+__global__ void k_init_finish(DevState s, int fresh) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t Gp = s.Gp, G = s.G;
+  const int B = s.B, K = s.K;
+  if (fresh) {
+    if (t < B) { s.gamma[t] = GAMMA0_INIT; s.gamma[B + t] = GAMMA1_INIT; }
+    if (t < (int64_t)B * K) s.pi[t] = (float)(((t % K) + 1) / (K * (K + 1) / 2.0));
+    if (t < (int64_t)B * Gp) s.phi[t] = (t % Gp) < G ? PHI_INIT : 1.0f;
+    if (t < s.N) s.mu_delta[t] = s.delta[t];
+    if (t == 0) s.p_tau0[1] = TAU0_INIT;
+  }
+  if (t < s.N) s.Dexp[t] = expf(s.delta[t]);
+  if (t < Gp && t >= G) {
+    s.alpha[t] = 0.0f;
+    for (int k = 0; k < K; ++k) s.beta[(int64_t)k * Gp + t] = 0.0f;
+    for (int b = 0; b < B; ++b) {
+      s.nu[(int64_t)b * Gp + t] = 0.0f;
+      s.phi[(int64_t)b * Gp + t] = 1.0f;
+    }
+  }
+  if (t < Gp) {
+    const float a = t < G ? s.alpha[t] : 0.0f;
+    for (int b = 0; b < B; ++b) {
+      const float nv = s.nu[(int64_t)b * Gp + t];
+      for (int k = 0; k < K; ++k)
+        s.E[((int64_t)b * K + k) * Gp + t] = t < G ? expf(eta3(a, s.beta[(int64_t)k * Gp + t], nv)) : 1.0f;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Posterior summaries: means over kept sweeps, P(L = 1), W mode.
+// est layout: gamma[2B] alpha[G] L[(K-1)G] beta[K G] ptau[2] nu[B G] delta[N] phi[B G] pi[B K]
+// ---------------------------------------------------------------------------
+__global__ void k_finalize(DevState s, Estimates e, int n_kept) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = s.G, Gp = s.Gp, N = s.N;
+  const int B = s.B, K = s.K;
+  const bool have = n_kept > 0;
+  const double inv = have ? 1.0 / n_kept : 0.0;
+  for (int64_t t = t0; t < (int64_t)K * G; t += stride) {
+    const int k = (int)(t / G);
+    const int64_t g = t % G;
+    if (k == 0) {
+      e.alpha[g] = have ? s.acc_alpha[g] * inv : s.alpha[g];
+      e.beta[g] = 0.0;
+    } else {
+      e.beta[t] = have ? s.acc_beta[t] * inv : s.beta[(int64_t)k * Gp + g];
+      e.L[t - G] = have ? s.acc_L[t] * inv : s.L[(int64_t)k * Gp + g];
+    }
+  }
+  for (int64_t t = t0; t < (int64_t)B * G; t += stride) {
+    const int b = (int)(t / G);
+    const int64_t g = t % G;
+    e.phi[t] = have ? s.acc_phi[t] * inv : s.phi[(int64_t)b * Gp + g];
+    e.nu[t] = b == 0 ? 0.0 : (have ? s.acc_nu[t] * inv : s.nu[(int64_t)b * Gp + g]);
+  }
+  for (int64_t i = t0; i < N; i += stride) {
+    e.delta[i] = have ? s.acc_delta[i] * inv : s.delta[i];
+    if (have) {
+      int best = 0, bc = s.acc_wcnt[i * K];
+      for (int k = 1; k < K; ++k) {
+        const int c = s.acc_wcnt[i * K + k];
+        if (c > bc) { bc = c; best = k; }
+      }
+      e.W[i] = best;
+    } else {
+      e.W[i] = s.W[i];
+    }
+  }
+  for (int64_t t = t0; t < 2 * B; t += stride) e.gamma[t] = have ? s.acc_gamma[t] * inv : s.gamma[t];
+  for (int64_t t = t0; t < (int64_t)B * K; t += stride) e.pi[t] = have ? s.acc_pi[t] * inv : s.pi[t];
+  for (int64_t t = t0; t < 2; t += stride) e.ptau[t] = have ? s.acc_ptau[t] * inv : s.p_tau0[t];
+}
+
+// ---------------------------------------------------------------------------
+// BIC.  Per cell i and type k: sum over genes of the dropout-marginal
+// log-likelihood of Y (BUSseq_gpu.cu:967-1007), with the estimates.
+// For Y = 0 the reference sums NB(x) * P(drop | x) over x = 0 .. floor(3 mu)-1
+// in log space; here the same sum is evaluated with the NB recurrence
+//   log NB(x) = log NB(x-1) + log((phi + x - 1) / x) + log p
+// and stops once the terms are past the NB mode and 30 nats below the running
+// sum (the summand is then decreasing, so the rest cannot matter in float).
+// ---------------------------------------------------------------------------
+__device__ double bic_zero_term(double mu, double logp, double log1mp, float phi, float g0, float g1) {
+  const double x_max_d = 3.0 * mu;
+  // the series is cut at 2^24 terms (it is negligible long before, unless mu is absurd)
+  const int x_max = x_max_d > 16777216.0 ? 16777216 : (int)x_max_d;
+  float sacc = (float)(phi * log1mp);
+  float lnb = sacc;
+  const float lp = (float)logp;
+  const double mode_d = phi > 1.0f ? floor((phi - 1.0) * mu / phi) : 0.0;
+  for (int x = 1; x < x_max; ++x) {
+    lnb += logf((phi + (float)(x - 1)) / (float)x) + lp;
+    const float s = fmaf(g1, (float)x, g0);
+    const float ls = s - softplusf(s);  // log(sigmoid(g0 + g1 x))
+    const float tt = ls + lnb;
+    if (tt > sacc) sacc = tt + log1pf(expf(sacc - tt));
+    else sacc = sacc + log1pf(expf(tt - sacc));
+    if (g1 < 0.0f && (double)x > mode_d && tt < sacc - 30.0f) break;
+  }
+  return (double)sacc;
+}
+
+__global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik) {
+  __shared__ double sh[8 * MAX_K];
+  const int64_t i = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int b = s.batch_of[i];
+  const int B = s.B, K = s.K;
+  const int64_t G = s.G, Gp = s.Gp;
+  const double g0 = e.gamma[b], g1 = e.gamma[B + b];
+  const double di = e.delta[i];
+  double acc[MAX_K];
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (int64_t g = tid; g < G; g += blockDim.x) {
+    const int y = s.Y[i * Gp + g];
+    const double phi = e.phi[(int64_t)b * G + g];
+    const double an = e.alpha[g] + e.nu[(int64_t)b * G + g] + di;
+    const double lphi = log(phi);
+    double base = 0.0;
+    if (y) {
+      const double t = g0 + g1 * y;
+      const double sp = t > 0 ? t + log1p(exp(-t)) : log1p(exp(t));
+      base = -sp + lgamma(phi + y) - lgamma(1.0 + y) - lgamma(phi);
+    }
+    for (int k = 0; k < K; ++k) {
+      const double eta = an + e.beta[(int64_t)k * G + g];
+      const double mu = exp(eta);
+      const double lq = log(mu + phi);
+      double logp = eta - lq, log1mp = lphi - lq;
+      if (logp < -250.0) logp = -250.0;
+      if (log1mp < -250.0) log1mp = -250.0;
+      if (y) acc[k] += base + y * logp + phi * log1mp;
+      else acc[k] += bic_zero_term(mu, logp, log1mp, (float)phi, (float)g0, (float)g1);
+    }
+  }
+  for (int k = 0; k < K; ++k) {
+    const double v = warp_sum(acc[k]);
+    if (lane == 0) sh[warp * MAX_K + k] = v;
+  }
+  __syncthreads();
+  if (tid < K) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w * MAX_K + tid];
+    ll_ik[(int64_t)tid * s.N + i] = t;
+  }
+}
+
+__global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double* out) {
+  __shared__ double sh[32];
+  const int K = s.K;
+  double acc = 0.0;
+  for (int64_t i = threadIdx.x; i < s.N; i += blockDim.x) {
+    const int b = s.batch_of[i];
+    double mx = ll_ik[i];
+    for (int k = 1; k < K; ++k) mx = fmax(mx, ll_ik[(int64_t)k * s.N + i]);
+    double sum = 0.0;
+    for (int k = 0; k < K; ++k) sum += e.pi[b * K + k] * exp(ll_ik[(int64_t)k * s.N + i] - mx);
+    acc += mx + log(sum);
+  }
+  double v[1] = {acc};
+  block_sum<1>(v, sh);
+  if (threadIdx.x == 0) {
+    const double B = s.B, G = (double)s.G, N = (double)s.N;
+    const double nparam = (B + G) * K + 2 * B + G * (B * 2 - 1) + N - B;
+    out[0] = -2.0 * v[0] + log(G * N) * nparam;
+    out[1] = v[0];
+  }
+}
+
+}  // namespace bq

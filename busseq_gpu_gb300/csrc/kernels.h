@@ -1,0 +1,27 @@
+// Kernel entry points (defined in sweep_kernels.cu and init_kernels.cu).
+#pragma once
+#include "busseq_dev.h"
+
+namespace bq {
+
+__global__ void k_propose(DevState s, int mask);
+__global__ void k_zx_alpha(DevState s);
+__global__ void k_beta_nu(DevState s);
+__global__ void k_delta(DevState s);
+__global__ void k_phi(DevState s);
+__global__ void k_w_mh(DevState s);
+__global__ void k_w_gibbs(DevState s);
+__global__ void k_sort_pi(DevState s, int do_pi, int advance);
+__global__ void k_posterior(DevState s, int advance);
+int64_t propose_count(const DevState& s);
+
+__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax);
+__global__ void k_init_hist(DevState s, int32_t* hist);
+__global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell);
+__global__ void k_init_raw(DevState s);
+__global__ void k_init_finish(DevState s, int fresh);
+__global__ void k_finalize(DevState s, Estimates e, int n_kept);
+__global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik);
+__global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double* out);
+
+}  // namespace bq

@@ -1,0 +1,81 @@
+// Device helpers shared by the sweep, initialisation and summary kernels.
+#pragma once
+#include "busseq_dev.h"
+#include "rng.h"
+
+namespace bq {
+
+// The idx-th uniform (idx < 4) of stream (sid, entity) at sweep `iter`.
+// Matches the idx-th call of Stream::uniform() on a fresh stream.
+__device__ __forceinline__ float uniform_at(uint64_t seed, uint32_t sid, uint64_t ent, uint32_t iter, int idx) {
+  const U32x4 r = philox4x32_10(
+      U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (sid << 16), 0u, iter}, (uint32_t)seed,
+      (uint32_t)(seed >> 32));
+  const uint32_t v = idx == 0 ? r.x : idx == 1 ? r.y : idx == 2 ? r.z : r.w;
+  return u32_to_unit(v);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of NV doubles per thread; result valid in thread 0.
+// `sh` must hold (blockDim.x / 32) * NV doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = warp_sum(v[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) sh[warp * NV + j] = v[j];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += sh[w * NV + j];
+      v[j] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Completion counter: every CTA of a group calls this once after its global
+// writes; it returns true in exactly one CTA (the last to arrive), which then
+// sees every other CTA's writes.  The last CTA resets the counter.
+__device__ __forceinline__ bool arrive_last(unsigned* counter, unsigned total, int* sh_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(counter, 1u);
+    *sh_flag = (prev == total - 1u);
+    if (*sh_flag) *counter = 0u;
+  }
+  __syncthreads();
+  const bool last = *sh_flag != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+// Compensated (Kahan) float accumulator: float-pipe throughput with an error
+// that does not grow with the number of terms.
+struct KahanF {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// log-likelihood shift of one NB entry when eta moves by eps, without the
+// linear eps * X part:   (phi + X) * log1p(c * p),  c = expm1(eps), p = mu / (phi + mu)
+__device__ __forceinline__ float nb_shift_log(float w, float c, float p) { return w * log1pf(c * p); }
+
+}  // namespace bq

@@ -1,0 +1,235 @@
+/*
+ * busseq_gb300.h -- C ABI of the GB300-native BUSseq Gibbs sampler.
+ *
+ * The reference (Anguscgm/BUSseq_gpu, a single CUDA C program) exposes no
+ * library: its boundary is the executable's command line and its text files.
+ * This header is the drop-in boundary of that path as a shared library
+ * (libbusseq_gb300.so); the `busseq` executable built on top of it keeps the
+ * reference's command line and output files.  Each entry point names the
+ * reference code it replaces (BUSseq_gpu.cu:line).
+ *
+ * Conventions: plain C types, caller-owned host buffers, an opaque handle per
+ * chain, one GPU, not thread-safe per handle.  Every function returns 0
+ * (BUSSEQ_OK) or a negative error code; busseq_last_error() then describes the
+ * failure.  Arrays use the reference's layouts: counts row-major [cell][gene]
+ * with cells grouped batch by batch; beta/L [k*G+g]; nu/phi [b*G+g];
+ * gamma [0/1*B+b]; pi [b*K+k].
+ */
+#ifndef BUSSEQ_GB300_H
+#define BUSSEQ_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BUSSEQ_OK 0
+#define BUSSEQ_ERR_ARG (-1)      /* invalid argument or input data            */
+#define BUSSEQ_ERR_CUDA (-2)     /* CUDA runtime error                        */
+#define BUSSEQ_ERR_NOMEM (-3)    /* device or host allocation failed          */
+#define BUSSEQ_ERR_STATE (-4)    /* call out of order (e.g. no run begun)     */
+#define BUSSEQ_ERR_SAMPLER (-5)  /* a device rejection sampler hit its cap    */
+#define BUSSEQ_ERR_IO (-6)       /* file could not be read or written         */
+
+#define BUSSEQ_MAX_BATCHES 128   /* BUSseq_gpu.cu:9-10 (__constant__ d_n_b[128]) */
+#define BUSSEQ_MAX_TYPES 64
+
+/* W update: the reference's Metropolis move with a uniform proposal
+ * (BUSseq_gpu.cu:820-854), or a K-way categorical draw from the same full
+ * conditional. */
+#define BUSSEQ_W_MH 0
+#define BUSSEQ_W_GIBBS 1
+
+/* Stage ids for busseq_run_stage: contiguous groups of the reference's sweep
+ * order (BUSseq_gpu.cu:1267-1398). */
+#define BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L 0 /* Z/X, gamma0, gamma1, alpha, L, p/tau0 */
+#define BUSSEQ_STAGE_BETA_NU 1          /* beta, nu                            */
+#define BUSSEQ_STAGE_DELTA 2
+#define BUSSEQ_STAGE_PHI 3
+#define BUSSEQ_STAGE_W 4
+#define BUSSEQ_STAGE_PI 5               /* pi, then the new cell order         */
+
+typedef struct busseq_handle busseq_handle;
+
+typedef struct busseq_dims {
+  int32_t B;            /* batches (2..128), reference -B                      */
+  int32_t K;            /* cell types (1..64), reference -K                    */
+  int64_t G;            /* genes, reference -G                                 */
+  const int32_t* n_b;   /* [B] cells per batch, reference -N file               */
+} busseq_dims;
+
+typedef struct busseq_options {
+  uint64_t seed;        /* key of every random draw (reference -s)             */
+  double p0;            /* initial p; the reference uses rand()*0.5/RAND_MAX    */
+  int32_t w_update;     /* BUSSEQ_W_MH (default) or BUSSEQ_W_GIBBS             */
+  int32_t keep_draws;   /* store every kept draw (needed for reference -p)      */
+  int32_t device;       /* CUDA device ordinal                                 */
+  int32_t chunk_cells;  /* cells per gene-pass chunk; 0 = default (256)         */
+  int32_t reserved[8];
+} busseq_options;
+
+/* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
+ * caller-owned host buffer of the stated length, or NULL to skip it. */
+typedef struct busseq_estimates {
+  int32_t* Z;       /* [N*G] last sweep's dropout indicators (_post_Z)       */
+  int32_t* X;       /* [N*G] last sweep's underlying counts (_post_X)        */
+  double* gamma;    /* [2B]  posterior means (_post_gamma)                  */
+  double* alpha;    /* [G]                                                  */
+  double* L;        /* [(K-1)*G] posterior P(L=1), k >= 1 (_post_L)          */
+  double* beta;     /* [K*G] posterior means, row k=0 is 0 (_post_beta)     */
+  double* p_tau0;   /* [2]  posterior means of p and tau0 (_post_p)         */
+  double* nu;       /* [B*G] row b=0 is 0 (_post_nu)                         */
+  double* delta;    /* [N]                                                  */
+  double* phi;      /* [B*G]                                                */
+  int32_t* W;       /* [N]  posterior mode, 0-based (_post_W)               */
+  double* pi;       /* [B*K]                                                */
+} busseq_estimates;
+
+/* Kept draws in the reference's file layout: one row per scalar, one column
+ * per kept sweep (BUSseq_gpu.cu:1845-2018).  NULL pointers are skipped. */
+typedef struct busseq_preserved {
+  double* gamma;    /* [2B][n_kept]        */
+  double* alpha;    /* [G][n_kept]         */
+  int32_t* L;       /* [(K-1)G][n_kept]    */
+  double* beta;     /* [(K-1)G][n_kept]    */
+  double* p_tau0;   /* [2][n_kept]         */
+  double* nu;       /* [(B-1)G][n_kept]    */
+  double* delta;    /* [N][n_kept]         */
+  double* phi;      /* [BG][n_kept]        */
+  int32_t* W;       /* [N][n_kept]         */
+  double* pi;       /* [BK][n_kept]        */
+} busseq_preserved;
+
+/* Full sampler state in single precision (the kernels' working precision).
+ * Used by tests and by callers that checkpoint a chain. */
+typedef struct busseq_state {
+  int32_t* X;       /* [N*G] */
+  uint8_t* Z;       /* [N*G] */
+  int32_t* W;       /* [N]   */
+  int8_t* L;        /* [K*G] */
+  float* alpha;     /* [G]   */
+  float* mu_alpha;  /* [G]   */
+  float* beta;      /* [K*G] */
+  float* nu;        /* [B*G] */
+  float* mu_nu;     /* [B]   */
+  float* delta;     /* [N]   */
+  float* mu_delta;  /* [N]   */
+  float* phi;       /* [B*G] */
+  float* gamma;     /* [2B]  */
+  float* pi;        /* [B*K] */
+  float* p_tau0;    /* [2]   */
+} busseq_state;
+
+/* Log acceptance ratios (likelihood + prior) computed by the last sweep or
+ * stage, for diagnostics and parity tests.  NULL pointers are skipped. */
+typedef struct busseq_log_ratios {
+  double* gamma;    /* [2B]  */
+  double* alpha;    /* [G]   */
+  double* beta;     /* [K*G] (k >= 1) */
+  double* nu;       /* [B*G] (b >= 1) */
+  double* delta;    /* [N]   */
+  double* phi;      /* [B*G] */
+  double* W;        /* [N]   (MH only) */
+} busseq_log_ratios;
+
+/* ---- lifecycle ------------------------------------------------------------ */
+
+/* Uploads the N x G counts (host or device pointer, row-major, rows of G
+ * int32) and initialises the chain.  Replaces reading the count file's
+ * contents into device memory and the initialisation of BUSseq_gpu.cu:1143-1244. */
+int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, const busseq_options* opt,
+                  busseq_handle** out);
+
+/* Releases all device memory of the chain.  Safe with NULL. */
+void busseq_destroy(busseq_handle* h);
+
+/* Runs n_iter sweeps (n_burnin of burn-in), with p and tau0 held for the
+ * first n_unchanged sweeps, then computes the posterior summaries.
+ * Replaces BUSseq_gpu.cu:1246-1608. */
+int busseq_run(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_unchanged);
+
+/* Incremental form of busseq_run: busseq_begin fixes the run's lengths and
+ * resets the sweep counter; busseq_sweeps enqueues `count` sweeps (CUDA graphs,
+ * asynchronous); busseq_finish waits and computes the posterior summaries. */
+int busseq_begin(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_unchanged);
+int busseq_sweeps(busseq_handle* h, int32_t count);
+int busseq_finish(busseq_handle* h);
+int busseq_synchronize(busseq_handle* h);
+
+/* Copies the posterior estimates into host buffers (BUSseq_gpu.cu:1557-1813). */
+int busseq_get_estimates(busseq_handle* h, busseq_estimates* out);
+
+/* Copies the kept draws (requires keep_draws; BUSseq_gpu.cu:1845-2018). */
+int busseq_get_preserved(busseq_handle* h, busseq_preserved* out);
+
+/* BIC of the posterior estimates, marginalising dropouts and cell types
+ * (BUSseq_gpu.cu:967-1024 and :1815-1843). */
+int busseq_bic(busseq_handle* h, double* bic);
+
+/* ---- state access, single stages, diagnostics ----------------------------- */
+
+int busseq_get_state(busseq_handle* h, busseq_state* out);
+/* Replaces the whole state; derived data (exp(delta), exp(alpha+beta+nu), the
+ * cell order) is recomputed on the device. */
+int busseq_set_state(busseq_handle* h, const busseq_state* in);
+
+/* Runs one stage of the sweep at sweep index `iter` (p and tau0 are redrawn in
+ * stage 0 when iter >= n_unchanged). */
+int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_unchanged);
+
+int busseq_get_log_ratios(busseq_handle* h, busseq_log_ratios* out);
+
+/* Makes the chain launch its work on `cuda_stream` (a cudaStream_t) instead of
+ * its own stream.  Pass NULL to go back to the chain's own stream. */
+int busseq_set_stream(busseq_handle* h, void* cuda_stream);
+
+/* Times each kernel of `n_sweeps` sweeps with CUDA events on the chain's
+ * stream (sweeps launched one kernel at a time, outside graphs).  Writes up to
+ * `cap` average durations in milliseconds and returns the number of kernels
+ * through *n_out; busseq_kernel_name(i) names kernel i. */
+int busseq_profile(busseq_handle* h, int32_t n_sweeps, double* ms_avg, int32_t cap, int32_t* n_out);
+const char* busseq_kernel_name(int32_t i);
+
+/* Algorithmic HBM bytes of one launch of kernel i at this chain's size. */
+double busseq_kernel_bytes(busseq_handle* h, int32_t i);
+
+/* Number of kernel launches one sweep makes (burn-in and kept sweeps). */
+int busseq_launches_per_sweep(busseq_handle* h, int32_t kept);
+
+/* ---- files (the reference's formats) -------------------------------------- */
+
+/* Parses a whitespace-separated N x G integer count file (BUSseq_gpu.cu:1143-1161)
+ * with all host threads. */
+int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out);
+
+/* Writes the _post_*, _BIC and (print_preserved) _preserved_* files with the
+ * reference's names and formats (BUSseq_gpu.cu:1610-2018). */
+int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved);
+
+/* ---- synthetic data (the BUSseq generative model) ------------------------- */
+
+typedef struct busseq_sim_params {
+  double alpha_lo, alpha_hi;      /* alpha_g ~ U(lo, hi)                       */
+  double de_frac;                 /* fraction of genes with beta_gk != 0, k>=1 */
+  double beta_lo, beta_hi;        /* |beta_gk| ~ U(lo, hi), random sign        */
+  double nu_step, nu_sd;          /* nu_bg ~ N(nu_step*(b-1), nu_sd^2), b>=1   */
+  double delta_sd;                /* delta_bi ~ N(0, sd^2), first cell 0       */
+  double phi_lo, phi_hi;          /* phi_bg ~ U(lo, hi)                        */
+  double pi_conc;                 /* pi_b ~ Dirichlet(conc * 1_K)              */
+  double gamma0, gamma1;          /* Z ~ Bernoulli(logistic(g0 + g1 X))        */
+} busseq_sim_params;
+
+/* Draws Y [N*G] and the true W [N] (and optionally the true X) from the
+ * model, deterministically from `seed`, with all host threads. */
+int busseq_simulate(const busseq_dims* dims, const busseq_sim_params* prm, uint64_t seed, int32_t* Y,
+                    int32_t* W_true, int32_t* X_true);
+
+const char* busseq_last_error(void);
+const char* busseq_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BUSSEQ_GB300_H */

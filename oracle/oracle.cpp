@@ -275,7 +275,10 @@ typedef struct orc_debug {
   double* mg_pi;      // [B*K]
 } orc_debug;
 
-enum { ORC_STAGE_ZX_GAMMA_ALPHA_L = 0, ORC_STAGE_PTAU_BETA_NU = 1, ORC_STAGE_DELTA = 2,
+// Stages group the reference's sweep order (BUSseq_gpu.cu:1267-1398) the way
+// the kernels do: [Z/X, gamma0, gamma1, alpha, L, p+tau0], [beta, nu], [delta],
+// [phi], [W], [pi].
+enum { ORC_STAGE_ZX_GAMMA_ALPHA_L = 0, ORC_STAGE_BETA_NU = 1, ORC_STAGE_DELTA = 2,
        ORC_STAGE_PHI = 3, ORC_STAGE_W = 4, ORC_STAGE_PI = 5 };
 
 static inline std::vector<int64_t> batch_offsets(const orc_state* st) {
@@ -673,9 +676,9 @@ int orc_stage(orc_state* st, int stage, int iter, int n_unchanged, int w_update,
       stage_gamma(st, iter, dbg);
       stage_alpha(st, iter, dbg);
       stage_L(st, iter, dbg);
-      return 0;
-    case ORC_STAGE_PTAU_BETA_NU:
       if (iter >= n_unchanged) stage_ptau(st, iter, dbg);
+      return 0;
+    case ORC_STAGE_BETA_NU:
       stage_beta(st, iter, dbg);
       stage_nu(st, iter, dbg);
       return 0;

@@ -13,7 +13,7 @@ import numpy as np
 from . import build as _build
 
 STAGE_ZX_GAMMA_ALPHA_L = 0
-STAGE_PTAU_BETA_NU = 1
+STAGE_BETA_NU = 1
 STAGE_DELTA = 2
 STAGE_PHI = 3
 STAGE_W = 4
