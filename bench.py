@@ -1,0 +1,317 @@
+"""Benchmark: BUSseq Gibbs sweeps per second on one GB300 (config 1).
+
+Workload (the configuration the headline metric is quoted on): B = 4 batches
+of 2500 cells (N = 10^4), G = 10^4 genes, K = 8 cell types, synthetic counts
+drawn from the BUSseq generative model (20% differential genes), plain sampler
+(the reference's random-walk MH moves and MH cell-type move).
+
+A step is one full Gibbs sweep.  Reported:
+  value      sweeps/s with the counts already in HBM, CUDA events on the
+             sampler's stream around K graph-launched sweeps (half burn-in, half
+             kept, as in the reference's runs); X and Y are 400 MB each, larger
+             than L2, so no flush is needed between sweeps.
+  e2e        sweeps/s through the public C ABI from pinned host counts: upload,
+             initialisation, K sweeps, posterior summaries and the copy of every
+             estimate (including the N x G X and Z) back to the host.
+  roofline   the dominant kernel's algorithmic bytes per launch over its mean
+             CUDA-event duration, against the measured HBM copy bandwidth.
+  cpu_baseline the FP64 OpenMP oracle (the CPU restatement of the same sweep)
+             on the host cores, on a bounded sample of the same data.
+
+--impl reference runs the CPU arm only (the reference program has no CPU
+implementation of the sweep, so its CPU stand-in is the oracle port).
+Multi-GPU (--gpus N under torchrun): N independent chains, one per GPU
+(replicas: a BUSseq chain has no data-parallel split that avoids an
+all-reduce per sweep).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
+METRIC = "gibbs_iters_per_s"
+UNIT = "sweeps/s"
+
+
+def _peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_config1.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_data(seed):
+    import busseq_gpu_gb300 as bq
+    return bq.simulate(CFG1["n_b"], CFG1["G"], CFG1["K"], seed)
+
+
+def cpu_oracle_rate(Y, n_b, K, seed, cells_per_batch: int, sweeps: int):
+    """FP64 oracle sweeps/s on the first `cells_per_batch` cells of every batch,
+    scaled to the full cell count (the oracle's cost is linear in cells)."""
+    from oracle import pyoracle as po
+    off = np.concatenate([[0], np.cumsum(n_b)])
+    rows = np.concatenate([np.arange(off[b], off[b] + cells_per_batch) for b in range(len(n_b))])
+    Ys = np.ascontiguousarray(Y[rows])
+    st = po.State(Ys, [cells_per_batch] * len(n_b), K, seed)
+    st.init(0.25)
+    st.sweep(0, 1 << 30)  # warm caches / page in
+    t0 = time.perf_counter()
+    for it in range(1, sweeps + 1):
+        st.sweep(it, 0)
+    dt = time.perf_counter() - t0
+    frac = len(rows) / float(sum(n_b))
+    return sweeps / dt * frac, po.num_threads(), dt
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    n_b, K = CFG1["n_b"], CFG1["K"]
+    Y, _, _ = make_data(CFG1["seed"])
+    from oracle import pyoracle as po
+    off = np.concatenate([[0], np.cumsum(n_b)])
+    cpb = 100  # cells per batch in each step's sample
+    rows = np.concatenate([np.arange(off[b], off[b] + cpb) for b in range(len(n_b))])
+    st = po.State(np.ascontiguousarray(Y[rows]), [cpb] * len(n_b), K, CFG1["seed"])
+    st.init(0.25)
+    for it in range(args.warmup):
+        st.sweep(it, 0)
+    t0 = time.perf_counter()
+    for it in range(args.warmup, args.warmup + args.steps):
+        st.sweep(it, 0)
+    dt = time.perf_counter() - t0
+    frac = len(rows) / float(sum(n_b))
+    value = args.steps / dt * frac
+    sample = ("per step: one full FP64 oracle sweep over %d cells (first %d of each batch) x %d genes of the "
+              "config-1 data; sweeps/s scaled by %d/%d cells" % (len(rows), cpb, CFG1["G"], len(rows), sum(n_b)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (BUSseq generative model)",
+        "config": _config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference program has no CPU implementation of the sweep; this arm times the FP64 CPU "
+                "restatement of it (oracle/oracle.cpp) with all host threads",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _config():
+    return {"workload": "config1: B=4 x 2500 cells (N=10000), G=10000, K=8, plain MH sampler",
+            "B": 4, "N": 10000, "G": 10000, "K": 8, "w_update": "mh", "parallelism": "replicas (one chain per GPU)",
+            "l2": "no flush: X and Y are 400 MB each, larger than L2",
+            "precision": "f32 likelihood terms, f64 acceptance sums"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=30)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    import busseq_gpu_gb300 as bq
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    n_b, G, K = CFG1["n_b"], CFG1["G"], CFG1["K"]
+    seed = CFG1["seed"]
+    Y, W_true, _ = make_data(seed)
+    N = int(sum(n_b))
+
+    # ---- value: counts resident in HBM, graph-launched sweeps ---------------
+    Yd = torch.from_numpy(Y).to(f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local)
+    s.set_stream(stream.cuda_stream)
+    total = args.warmup + args.steps
+    s.begin(total, args.warmup + args.steps // 2, args.warmup)
+    s.sweeps(args.warmup)
+    s.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        s.sweeps(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    s.finish()
+    ms_t = torch.tensor([ms], device=f"cuda:{local}")
+    if dist is not None:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = args.steps * world / (ms_max / 1000.0)
+    launches = (args.steps // 2) * s.launches_per_sweep(False) + (args.steps - args.steps // 2) * s.launches_per_sweep(True)
+
+    # ---- per-kernel durations for the roofline (events on the same stream) --
+    prof = s.profile(20)
+    big = {k: v for k, v in prof.items() if k in ("k_zx_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w")}
+    dom = max(big, key=big.get)
+    idx = bq.lib()
+    kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(8)].index(dom)
+    alg_bytes = s.kernel_bytes(kid)
+    achieved = alg_bytes / (prof[dom] / 1000.0) / 1e9
+    peak, peak_kind = _peak_hbm()
+    traffic = _traffic(dom)
+    s.close()
+    del Yd
+    torch.cuda.empty_cache()
+
+    # ---- e2e: pinned host counts through the C ABI ---------------------------
+    Yp = torch.from_numpy(Y).pin_memory()
+    Yh = Yp.numpy()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    s2 = bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank, device=local)
+    s2.run(args.steps, args.steps // 2, min(args.warmup, args.steps))
+    est = s2.estimates(with_XZ=True)
+    t1 = time.perf_counter()
+    s2.close()
+    e2e_s = t1 - t0
+    e2e_t = torch.tensor([e2e_s], device=f"cuda:{local}")
+    if dist is not None:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = args.steps * world / float(e2e_t.item())
+    h2d = Y.nbytes
+    d2h = sum(v.nbytes for v in est.values())
+
+    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpb = 250
+        rate, cores, secs = cpu_oracle_rate(Y, n_b, K, seed, cpb, 2)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "2 FP64 oracle sweeps over the first %d cells of each batch (%d cells x %d genes, %.1f s), "
+                         "scaled to N=%d cells" % (cpb, cpb * len(n_b), G, secs, N)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (BUSseq generative model, seed %d)" % seed,
+            "config": _config(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps,
+                    "note": "one job per run: pinned-host upload, init, %d sweeps, posterior, all estimates to host"
+                            % args.steps},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "alg_bytes_per_launch": alg_bytes, "ms_per_launch": prof[dom]},
+            "kernels_ms": prof,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

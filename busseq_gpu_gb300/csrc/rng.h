@@ -247,10 +247,18 @@ BQ_HD float softplus_diff(float t, float dlt) {
   return softplusf(t + dlt) - softplusf(t);
 }
 
-// lgamma(z + dlt) - lgamma(z) for z > 0, z + dlt > 0, without cancellation.
-// For z, z + dlt >= 8 it uses the difference of Stirling's series
+// log(a / b) for a, b > 0 with d = a - b: log1p(d / b) while a and b are
+// within a factor of about two (then d carries no cancellation error),
+// otherwise the difference of the two logarithms, which stays accurate when
+// a << b (where 1 + d / b would cancel).
+BQ_HD float log_ratio(float a, float b, float d) {
+  return fabsf(d) < 0.5f * b ? log1pf(d / b) : logf(a) - logf(b);
+}
+
+// lgamma(zp) - lgamma(z) for z, zp > 0, dlt = zp - z, without cancellation.
+// For z, zp >= 8 it uses the difference of Stirling's series
 //   lgamma(z) = (z - 1/2) log z - z + log(2 pi)/2 + 1/(12z) - 1/(360z^3) + 1/(1260z^5) - ...
-// rearranged as (z' - 1/2) log1p(dlt/z) + dlt (log z - 1) + S(z') - S(z);
+// rearranged as (zp - 1/2) log(zp / z) + dlt (log z - 1) + S(zp) - S(z);
 // smaller arguments are shifted up with lgamma(x+1) = lgamma(x) + log x.
 BQ_HD float stirling_tail(float z) {
   const float r = 1.0f / z;
@@ -258,16 +266,16 @@ BQ_HD float stirling_tail(float z) {
   return r * (1.0f / 12.0f - r2 * (1.0f / 360.0f - r2 * (1.0f / 1260.0f)));
 }
 
-BQ_HD float lgamma_diff(float z, float dlt) {
+BQ_HD float lgamma_diff(float z, float zp, float dlt) {
   float acc = 0.0f;
-  float zz = z;
-  for (int j = 0; j < 8 && (zz < 8.0f || zz + dlt < 8.0f); ++j) {
-    acc -= log1pf(dlt / zz);
+  float zz = z, zq = zp;
+  for (int j = 0; j < 8 && (zz < 8.0f || zq < 8.0f); ++j) {
+    acc -= log_ratio(zq, zz, dlt);
     zz += 1.0f;
+    zq += 1.0f;
   }
-  const float zp = zz + dlt;
-  return acc + (zp - 0.5f) * log1pf(dlt / zz) + dlt * (logf(zz) - 1.0f) +
-         (stirling_tail(zp) - stirling_tail(zz));
+  return acc + (zq - 0.5f) * log_ratio(zq, zz, dlt) + dlt * (logf(zz) - 1.0f) +
+         (stirling_tail(zq) - stirling_tail(zz));
 }
 
 }  // namespace bq

@@ -494,7 +494,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
     float h = 0.0f;
     tab[0][tid] = 0.0f;
     for (int x = 1; x < PHI_TAB; ++x) {
-      h += log1pf(dl / (ph + (float)(x - 1)));
+      const float j = (float)(x - 1);
+      h += log_ratio(pp + j, ph + j, dl);
       tab[x][tid] = h;
     }
     int64_t nbig = 0;
@@ -509,11 +510,11 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
         if ((unsigned)x < (unsigned)PHI_TAB) {
           s1f += tab[x][tid];
         } else {
-          s1f += lgamma_diff(ph + (float)x, dl);
+          s1f += lgamma_diff(ph + (float)x, pp + (float)x, dl);
           ++nbig;
         }
         const float q = ph + mu;
-        s2f += (pp + (float)x) * log1pf(dl / q);
+        s2f += (pp + (float)x) * log_ratio(pp + mu, q, dl);
         s3f += logf(q);
       }
       s1 += s1f;
@@ -545,8 +546,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
     const float ph = s.phi[pos], pp = s.phi_p[pos];
     const float dl = pp - ph;
     const double nb = (double)(s.batch_off[bb + 1] - s.batch_off[bb]);
-    const double lgd0 = (double)lgamma_diff(ph, dl);        // lgamma(pp) - lgamma(ph)
-    const double l1 = (double)log1pf(dl / ph);              // log(pp / ph)
+    const double lgd0 = (double)lgamma_diff(ph, pp, dl);    // lgamma(pp) - lgamma(ph)
+    const double l1 = (double)log_ratio(pp, ph, dl);        // log(pp / ph)
     const double lph = (double)logf(ph);
     const double c1 = (double)pp * l1 + (double)dl * lph;   // pp log pp - ph log ph
     const double lr = (S1 - NB * lgd0) + nb * c1 - S2 - (double)dl * S3;
