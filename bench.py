@@ -221,8 +221,11 @@ def main():
 
     # ---- value: counts resident in HBM, graph-launched sweeps ---------------
     Yd = torch.from_numpy(Y).to(f"cuda:{local}")
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by the sampler and the events
+    stream = torch.cuda.Stream(device=local)
+    torch.cuda.set_stream(stream)
     s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local)
+    assert stream.cuda_stream != 0
     s.set_stream(stream.cuda_stream)
     total = args.warmup + args.steps
     s.begin(total, args.warmup + args.steps // 2, args.warmup)

@@ -232,10 +232,25 @@ __device__ void zx_global_tail(const DevState& s, uint32_t iter, double* sh) {
 
 // ---------------------------------------------------------------------------
 // Pass 1: Z/X + gamma statistics + alpha sums; tails: alpha, L, gamma, p, tau0
+//
+// The CTA walks its chunk ZX_ROWS cells at a time.  Entries with Y == 0 (the
+// only ones whose Z/X change) are first gathered into a shared-memory queue,
+// so the expensive negative-binomial draws run on all lanes instead of on the
+// scattered ~1/6 of lanes that hold a zero; the per-entry alpha terms then run
+// densely over the whole tile.
 // ---------------------------------------------------------------------------
+constexpr int ZX_ROWS = 8;
+
 __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
   __shared__ double sh[(GENE_TILE / 32) * 9];
   __shared__ int sh_flag;
+  __shared__ int xs[ZX_ROWS][GENE_TILE];             // X of the current cells, updated in place
+  __shared__ unsigned char zs[ZX_ROWS][GENE_TILE];   // bit 0: Z, bit 1: X changed
+  __shared__ unsigned short queue[ZX_ROWS * GENE_TILE];
+  __shared__ int qlen;
+  __shared__ int gi[ZX_ROWS];
+  __shared__ float gD[ZX_ROWS];
+  __shared__ float sM[GENE_TILE], sPh[GENE_TILE];
   const int tid = threadIdx.x, lane = tid & 31;
   const uint32_t iter = (uint32_t)*s.iter;
   const int tile = blockIdx.x;
@@ -258,59 +273,93 @@ __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
     const float M = valid ? s.E[((int64_t)b * s.K + k) * Gp + g] : 0.0f;
     const float ph = valid ? s.phi[(int64_t)b * Gp + g] : 1.0f;
     const float ca = valid ? expm1f(s.alpha_p[g] - s.alpha[g]) : 0.0f;
+    sM[tid] = M;
+    sPh[tid] = ph;
     const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
     const float g0p = s.gamma_p[b], dg0 = g0p - g0, dg1 = s.gamma_p[s.B + b] - g1;
+    const uint64_t G64 = (uint64_t)s.G;
+    const uint64_t gbase = (uint64_t)tile * GENE_TILE;
     int64_t sx = 0, xz = 0;
     int nz = 0, n0 = 0;
-    double la = 0.0, d0 = 0.0, d1a = 0.0, d1b = 0.0;
-    for (int j0 = 0; j0 < len; j0 += 32) {
-      const int jn = min(32, len - j0);
-      float laf = 0.0f, d0f = 0.0f, d1af = 0.0f, d1bf = 0.0f;
-      for (int jj = 0; jj < jn; ++jj) {
-        const int i = s.perm[start + j0 + jj];
-        const float D = s.Dexp[i];
-        const int64_t ro = (int64_t)i * Gp;
+    KahanF la, d0, d1a, d1b;
+    for (int j0 = 0; j0 < len; j0 += ZX_ROWS) {
+      const int rn = min(ZX_ROWS, len - j0);
+      if (tid < rn) {
+        const int i = s.perm[start + j0 + tid];
+        gi[tid] = i;
+        gD[tid] = s.Dexp[i];
+      }
+      if (tid == 0) qlen = 0;
+      __syncthreads();
+      // gather: X of the group into shared memory, Y == 0 entries into the queue
+      for (int r = 0; r < rn; ++r) {
+        const int i = gi[r];
+        xs[r][tid] = valid ? s.X[(int64_t)i * Gp + g] : 0;
+        zs[r][tid] = 0;
         const uint32_t ymw = s.y0m[(int64_t)i * Gw + (g >> 5)];
-        int x = valid ? s.X[ro + g] : 0;
         const bool y0 = valid && ((ymw >> lane) & 1u);
-        const float mu = M * D;
-        int z = 0;
-        bool changed = false;
-        if (y0) {
-          const int xo = x;
-          zx_entry(s.seed, (uint64_t)i * (uint64_t)s.G + (uint64_t)g, iter, mu, ph, g0, g1, x, z, s.err);
-          changed = x != xo;
-          nz += z;
-          xz += (int64_t)x * z;
-          if (x == 0) {
-            ++n0;
-          } else {
-            const float xf = (float)x;
-            const float t = fmaf(g1, xf, g0);
-            const float d1 = dg1 * xf;
-            d0f += softplus_diff(t, dg0);
-            d1af += softplus_diff(t, d1);
-            d1bf += softplus_diff(fmaf(g1, xf, g0p), d1);
-          }
+        const unsigned m = __ballot_sync(0xffffffffu, y0);
+        if (m) {
+          int base = 0;
+          if (lane == 0) base = atomicAdd(&qlen, __popc(m));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (y0) queue[base + __popc(m & ((1u << lane) - 1u))] = (unsigned short)((r << 8) | tid);
         }
-        const unsigned zb = __ballot_sync(0xffffffffu, z);
+      }
+      __syncthreads();
+      // dense Z/X updates of the queued entries (BUSseq_gpu.cu:484-512)
+      const int Q = qlen;
+      float d0f = 0.0f, d1af = 0.0f, d1bf = 0.0f;
+      for (int q = tid; q < Q; q += GENE_TILE) {
+        const int item = queue[q];
+        const int r = item >> 8, t = item & 0xFF;
+        const int i = gi[r];
+        int x = xs[r][t], z = 0;
+        const int xo = x;
+        zx_entry(s.seed, (uint64_t)i * G64 + gbase + (uint64_t)t, iter, sM[t] * gD[r], sPh[t], g0, g1, x, z,
+                 s.err);
+        xs[r][t] = x;
+        zs[r][t] = (unsigned char)(z | (x != xo ? 2 : 0));
+        nz += z;
+        xz += (int64_t)x * z;
+        if (x == 0) {
+          ++n0;
+        } else {
+          const float xf = (float)x;
+          const float tt = fmaf(g1, xf, g0);
+          const float d1 = dg1 * xf;
+          d0f += softplus_diff(tt, dg0);
+          d1af += softplus_diff(tt, d1);
+          d1bf += softplus_diff(fmaf(g1, xf, g0p), d1);
+        }
+      }
+      d0.add(d0f);
+      d1a.add(d1af);
+      d1b.add(d1bf);
+      __syncthreads();
+      // write back X and the Z bits; alpha terms over the whole tile
+      float laf = 0.0f;
+      for (int r = 0; r < rn; ++r) {
+        const int i = gi[r];
+        const int x = xs[r][tid];
+        const int zz = zs[r][tid];
+        const unsigned zb = __ballot_sync(0xffffffffu, zz & 1);
         if (lane == 0) s.zm[(int64_t)i * Gw + (g >> 5)] = zb;
-        if (__any_sync(0xffffffffu, changed) && valid) s.X[ro + g] = x;
+        if (__any_sync(0xffffffffu, zz & 2) && valid) s.X[(int64_t)i * Gp + g] = x;
         if (valid) {
+          const float mu = M * gD[r];
           sx += x;
           laf += nb_shift_log(ph + (float)x, ca, mu / (ph + mu));
         }
       }
-      la += laf;
-      d0 += d0f;
-      d1a += d1af;
-      d1b += d1bf;
+      la.add(laf);
+      __syncthreads();
     }
     if (valid) {
       s.part[((int64_t)row * NSLOT + 0) * Gp + g] = (double)sx;
-      s.part[((int64_t)row * NSLOT + 1) * Gp + g] = la;
+      s.part[((int64_t)row * NSLOT + 1) * Gp + g] = la.value();
     }
-    double v[6] = {(double)nz, (double)xz, (double)n0, d0, d1a, d1b};
+    double v[6] = {(double)nz, (double)xz, (double)n0, d0.value(), d1a.value(), d1b.value()};
     block_sum<6>(v, sh);
     if (tid == 0) {
       double* gp = s.gpart + ((int64_t)row * s.n_tiles + tile) * GSLOT;
@@ -490,7 +539,12 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
     const float pp = s.phi_p[(int64_t)b * Gp + g];
     const float dl = pp - ph;
     const float M = s.E[((int64_t)b * s.K + k) * Gp + g];
-    // H(x) = lgamma(pp + x) - lgamma(pp) - lgamma(ph + x) + lgamma(ph) for x < PHI_TAB
+    const float iph = 1.0f / ph;
+    // Per entry (BUSseq_gpu.cu:799-802, regrouped so that no large terms cancel):
+    //   t = [lgamma(pp+x) - lgamma(pp)] - [lgamma(ph+x) - lgamma(ph)]
+    //       - (pp + x) log((pp + mu) / (ph + mu)) + pp log(pp / ph) - dl log(1 + mu / ph)
+    const float lgd0 = lgamma_diff(ph, pp, dl);
+    const float c1 = pp * log_ratio(pp, ph, dl);
     float h = 0.0f;
     tab[0][tid] = 0.0f;
     for (int x = 1; x < PHI_TAB; ++x) {
@@ -498,63 +552,44 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
       h += log_ratio(pp + j, ph + j, dl);
       tab[x][tid] = h;
     }
-    int64_t nbig = 0;
-    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    for (int j0 = 0; j0 < len; j0 += 32) {
-      const int jn = min(32, len - j0);
-      float s1f = 0.0f, s2f = 0.0f, s3f = 0.0f;
+    KahanF acc;
+    for (int j0 = 0; j0 < len; j0 += 8) {
+      const int jn = min(8, len - j0);
+      float f = 0.0f;
       for (int jj = 0; jj < jn; ++jj) {
         const int i = s.perm[start + j0 + jj];
         const float mu = M * s.Dexp[i];
         const int x = s.X[(int64_t)i * Gp + g];
-        if ((unsigned)x < (unsigned)PHI_TAB) {
-          s1f += tab[x][tid];
-        } else {
-          s1f += lgamma_diff(ph + (float)x, pp + (float)x, dl);
-          ++nbig;
-        }
-        const float q = ph + mu;
-        s2f += (pp + (float)x) * log_ratio(pp + mu, q, dl);
-        s3f += logf(q);
+        const float xf = (float)x;
+        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff(ph + xf, pp + xf, dl) - lgd0;
+        f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1pf(mu * iph);
       }
-      s1 += s1f;
-      s2 += s2f;
-      s3 += s3f;
+      acc.add(f);
     }
-    double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
-    pr[0] = s1;
-    pr[Gp] = (double)nbig;
-    pr[2 * Gp] = s2;
-    pr[3 * Gp] = s3;
+    s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
   }
 
   if (!arrive_last(&s.cnt_tile[tile], (unsigned)s.cap_g, &sh_flag)) return;
   if (!valid) return;
 
   for (int bb = 0; bb < s.B; ++bb) {
-    double S1 = 0.0, NB = 0.0, S2 = 0.0, S3 = 0.0;
+    double S = 0.0;
     for (int c = 0; c < s.cap_g; ++c) {
       const int4 cc = s.gchunk[c];
       if (cc.w == 0 || cc.x != bb) continue;
-      const double* pr = s.part + (int64_t)c * NSLOT * Gp + g;
-      S1 += __ldcg(pr);
-      NB += __ldcg(pr + Gp);
-      S2 += __ldcg(pr + 2 * Gp);
-      S3 += __ldcg(pr + 3 * Gp);
+      S += __ldcg(s.part + (int64_t)c * NSLOT * Gp + g);
     }
     const int64_t pos = (int64_t)bb * Gp + g;
     const float ph = s.phi[pos], pp = s.phi_p[pos];
     const float dl = pp - ph;
-    const double nb = (double)(s.batch_off[bb + 1] - s.batch_off[bb]);
     const double lgd0 = (double)lgamma_diff(ph, pp, dl);    // lgamma(pp) - lgamma(ph)
     const double l1 = (double)log_ratio(pp, ph, dl);        // log(pp / ph)
     const double lph = (double)logf(ph);
-    const double c1 = (double)pp * l1 + (double)dl * lph;   // pp log pp - ph log ph
-    const double lr = (S1 - NB * lgd0) + nb * c1 - S2 - (double)dl * S3;
+    // Gamma(1, rate 0.1) prior and Gamma(phi, 1) proposal (BUSseq_gpu.cu:811-814)
     const double prior = (1.0 - (double)ph) * l1 + (double)dl * lph + (1.0 - TAU_PHI) * (double)dl - lgd0;
     const float u = uniform_at(s.seed, SID_PHI_ACC, (uint64_t)bb * (uint64_t)s.G + (uint64_t)g, iter, 0);
-    s.lr_phi[(int64_t)bb * s.G + g] = lr + prior;
-    if ((double)logf(u) <= lr + prior) s.phi[pos] = pp;
+    s.lr_phi[(int64_t)bb * s.G + g] = S + prior;
+    if ((double)logf(u) <= S + prior) s.phi[pos] = pp;
   }
 }
 
