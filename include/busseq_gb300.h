@@ -167,6 +167,27 @@ int busseq_get_preserved(busseq_handle* h, busseq_preserved* out);
  * (BUSseq_gpu.cu:967-1024 and :1815-1843). */
 int busseq_bic(busseq_handle* h, double* bic);
 
+/* BIC without any device allocation.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc -- code whose device memory is all
+ * owned by a framework's pool or arena, or that must not grow its footprint
+ * after start-up.  The caller passes device pointers: Y [N*G] int32 (row
+ * stride G), the estimates in busseq_estimates' layouts (double), and out_dev
+ * [2] = {BIC, log-likelihood}.  Work is enqueued on cuda_stream (NULL = the
+ * default stream); synchronise it before reading out_dev.
+ * Scratch: a fixed static __device__ array of BUSSEQ_NOALLOC_BIC_MAX_TYPES_X_CELLS
+ * doubles (8 MB) plus BUSSEQ_NOALLOC_BIC_MAX_CELLS ints (1 MB), held by every
+ * GPU that loads the library until the process exits.  Larger problems are
+ * rejected (BUSSEQ_ERR_ARG).  All calls share that array: calls that overlap
+ * on the GPU (other streams, other host threads) race.  The first call on a
+ * device looks up the array's device address; make that first call before any
+ * stream capture. */
+#define BUSSEQ_NOALLOC_BIC_MAX_TYPES_X_CELLS (1 << 20)
+#define BUSSEQ_NOALLOC_BIC_MAX_CELLS (1 << 18)
+int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev, const double* alpha_dev,
+                       const double* beta_dev, const double* nu_dev, const double* delta_dev,
+                       const double* phi_dev, const double* gamma_dev, const double* pi_dev, double* out_dev,
+                       void* cuda_stream);
+
 /* ---- state access, single stages, diagnostics ----------------------------- */
 
 int busseq_get_state(busseq_handle* h, busseq_state* out);

@@ -1,0 +1,67 @@
+"""The allocation-free BIC entry point (busseq_bic_noalloc) against busseq_bic.
+
+busseq_bic_noalloc is for callers that cannot call cudaMalloc (all device
+memory owned by a pool or arena they do not control, or a footprint fixed
+after start-up): it takes device pointers from the caller and keeps its
+per-(cell, type) scratch in a fixed static device array.  This file is named
+so that pytest collects it last.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import busseq_gpu_gb300 as bq
+
+pytestmark = pytest.mark.gpu
+
+BIC_RTOL = 2e-6  # the tolerance of the other BIC tests
+
+
+def _noalloc_fn():
+    f = bq.lib().busseq_bic_noalloc
+    f.argtypes = [C.POINTER(bq.Dims)] + [C.c_void_p] * 10
+    f.restype = C.c_int
+    return f
+
+
+def _case(n_b, G, K, seed):
+    Y, _, _ = bq.simulate(n_b, G, K, seed)
+    s = bq.Sampler(Y, n_b, K, seed=seed)
+    s.run(24, 12, 6)
+    est = s.estimates(with_XZ=False)
+    want = s.bic()
+    s.close()
+    return Y, est, want
+
+
+def test_bic_noalloc_matches_busseq_bic_twice():
+    torch = pytest.importorskip("torch")
+    fn = _noalloc_fn()
+    cases = [([40, 30, 30], 150, 3, 5), ([25, 35], 90, 2, 6)]
+    for n_b, G, K, seed in cases:  # two calls in a row share the static scratch
+        Y, est, want = _case(n_b, G, K, seed)
+        dev = torch.device("cuda", 0)
+        t = {k: torch.from_numpy(np.ascontiguousarray(est[k], dtype=np.float64)).to(dev)
+             for k in ("alpha", "beta", "nu", "delta", "phi", "gamma", "pi")}
+        Yd = torch.from_numpy(Y).to(dev)
+        out = torch.full((2,), float("nan"), dtype=torch.float64, device=dev)
+        nb = np.array(n_b, np.int32)
+        dims = bq.Dims(len(n_b), K, G, nb.ctypes.data_as(C.POINTER(C.c_int32)))
+        torch.cuda.synchronize()
+        rc = fn(C.byref(dims), Yd.data_ptr(), t["alpha"].data_ptr(), t["beta"].data_ptr(), t["nu"].data_ptr(),
+                t["delta"].data_ptr(), t["phi"].data_ptr(), t["gamma"].data_ptr(), t["pi"].data_ptr(),
+                out.data_ptr(), None)
+        assert rc == 0, bq.lib().busseq_last_error().decode()
+        torch.cuda.synchronize()
+        got = float(out[0].item())
+        assert abs(got - want) <= BIC_RTOL * abs(want), (got, want)
+
+
+def test_bic_noalloc_rejects_oversize():
+    fn = _noalloc_fn()
+    nb = np.array([1 << 17, 1 << 17, 1 << 17], np.int32)  # N above the static limit
+    dims = bq.Dims(3, 2, 10, nb.ctypes.data_as(C.POINTER(C.c_int32)))
+    rc = fn(C.byref(dims), *([C.c_void_p(16)] * 9), None)
+    assert rc == bq.BusseqError(-1, "").code
+    assert "exceed the fixed scratch" in bq.lib().busseq_last_error().decode()
