@@ -192,6 +192,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=0,
+                    help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
+    ap.add_argument("--only-value", action="store_true",
+                    help="measure only the device-resident sweep rate (the short run used under ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -216,7 +220,11 @@ def main():
 
     n_b, G, K = CFG1["n_b"], CFG1["G"], CFG1["K"]
     seed = CFG1["seed"]
-    Y, W_true, _ = make_data(seed)
+    if args.cells > 0:
+        n_b = [args.cells] * len(n_b)
+        Y, W_true, _ = bq.simulate(n_b, G, K, seed)
+    else:
+        Y, W_true, _ = make_data(seed)
     N = int(sum(n_b))
 
     # ---- value: counts resident in HBM, graph-launched sweeps ---------------
@@ -249,6 +257,14 @@ def main():
     ms_max = float(ms_t.item())
     value = args.steps * world / (ms_max / 1000.0)
     launches = (args.steps // 2) * s.launches_per_sweep(False) + (args.steps - args.steps // 2) * s.launches_per_sweep(True)
+
+    if args.only_value:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(),
+                              "note": "device-resident sweep rate only (--only-value)"}))
+        s.close()
+        return 0
 
     # ---- per-kernel durations for the roofline (events on the same stream) --
     prof = s.profile(20)

@@ -177,4 +177,19 @@ struct Estimates {
 // rounds it identically.
 __device__ __forceinline__ float eta3(float a, float b, float n) { return (a + b) + n; }
 
+// exp(a + b + c) with the sum carried as a float pair (TwoSum), so the result
+// has the error of one expf and one product instead of that of a rounded eta
+// (about 1e-6 relative for eta near 8, systematic across the cells of a gene).
+__device__ __forceinline__ float exp_sum3(float a, float b, float c) {
+  const float s1 = a + b;
+  const float bb = s1 - a;
+  const float e1 = (a - (s1 - bb)) + (b - bb);
+  const float s2 = s1 + c;
+  const float cc = s2 - s1;
+  const float e2 = (s1 - (s2 - cc)) + (c - cc);
+  const float lo = e1 + e2;
+  const float hi = expf(s2);
+  return fmaf(hi, lo, hi);
+}
+
 }  // namespace bq

@@ -202,7 +202,7 @@ __global__ void k_init_finish(DevState s, int fresh) {
     for (int b = 0; b < B; ++b) {
       const float nv = s.nu[(int64_t)b * Gp + t];
       for (int k = 0; k < K; ++k)
-        s.E[((int64_t)b * K + k) * Gp + t] = t < G ? expf(eta3(a, s.beta[(int64_t)k * Gp + t], nv)) : 1.0f;
+        s.E[((int64_t)b * K + k) * Gp + t] = t < G ? exp_sum3(a, s.beta[(int64_t)k * Gp + t], nv) : 1.0f;
     }
   }
 }

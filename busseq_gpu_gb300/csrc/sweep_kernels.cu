@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
 
   if (len > 0 && valid && (k > 0 || b > 0)) {
     const float bt = s.beta[(int64_t)k * Gp + g];
-    const float M = expf(eta3(s.alpha[g], bt, s.nu[(int64_t)b * Gp + g]));
+    const float M = exp_sum3(s.alpha[g], bt, s.nu[(int64_t)b * Gp + g]);
     const float ph = s.phi[(int64_t)b * Gp + g];
     const float eb = k > 0 ? s.beta_p[(int64_t)k * Gp + g] - bt : 0.0f;
     const float cb = expm1f(eb), fb = expf(eb);
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   for (int bb = 0; bb < s.B; ++bb) {
     const float nv = s.nu[(int64_t)bb * Gp + g];
     for (int kk = 0; kk < s.K; ++kk)
-      s.E[((int64_t)bb * s.K + kk) * Gp + g] = expf(eta3(a, s.beta[(int64_t)kk * Gp + g], nv));
+      s.E[((int64_t)bb * s.K + kk) * Gp + g] = exp_sum3(a, s.beta[(int64_t)kk * Gp + g], nv);
   }
 }
 
