@@ -44,6 +44,7 @@ constexpr float RW_STEP = 0.1f;  // random-walk proposal s.d. of alpha, beta, nu
 
 // ---- launch geometry -------------------------------------------------------
 constexpr int GENE_TILE = 128;     // genes per gene-pass CTA (one per thread)
+constexpr int MAX_CG = 256;        // largest gene-pass chunk (cells staged in shared memory)
 constexpr int CELL_TILE = 8;       // cells per cell-pass CTA
 constexpr int CELL_THREADS = 256;  // threads of a cell-pass CTA (4 genes each per step)
 constexpr int MAX_B = 128;

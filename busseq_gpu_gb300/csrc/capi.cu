@@ -269,7 +269,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.Gp = round_up(G, bq::GENE_TILE);
     s.Gw = s.Gp / 32;
     s.n_tiles = (int)((G + bq::GENE_TILE - 1) / bq::GENE_TILE);
-    s.CG = opt.chunk_cells > 0 ? opt.chunk_cells : 256;
+    s.CG = opt.chunk_cells > 0 ? std::min(opt.chunk_cells, bq::MAX_CG) : bq::MAX_CG;
     s.cap_g = 0;
     s.cap_c = 0;
     for (int b = 0; b < B; ++b) {

@@ -145,6 +145,61 @@ BQ_HD float bq_lgammaf(float x) {
 #endif
 }
 
+BQ_HD float fast_div(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// log(1 + y) for y > -1.  For |y| < 1/2 it sums log1p(y) = 2 atanh(s),
+// s = y / (2 + y) (so |s| <= 1/3), as s (2 + t (2/3 + t (2/5 + ... + t 2/13)))
+// with t = s^2; the first omitted term is below 2e-8 relative.  Otherwise
+// log(1 + y), whose argument is exact for y in (-1, -1/2] and relatively
+// accurate for y >= 1/2.
+BQ_HD float log1p_fast(float y) {
+  if (fabsf(y) < 0.5f) {
+    const float s = fast_div(y, 2.0f + y);
+    const float t = s * s;
+    float p = 2.0f / 13.0f;
+    p = fmaf(p, t, 2.0f / 11.0f);
+    p = fmaf(p, t, 2.0f / 9.0f);
+    p = fmaf(p, t, 2.0f / 7.0f);
+    p = fmaf(p, t, 2.0f / 5.0f);
+    p = fmaf(p, t, 2.0f / 3.0f);
+    p = fmaf(p, t, 2.0f);
+    return s * p;
+  }
+  return logf(1.0f + y);
+}
+
+// log(k!) for integer-valued k >= 0: exact values below 16, Stirling's series
+// (x - 1/2) log x - x + log(2 pi)/2 + 1/(12x) - 1/(360x^3), x = k + 1 >= 17,
+// above (truncation error below 1e-9).
+BQ_HD float log_factorial(float k) {
+  if (k < 16.0f) {
+    // log(k!) for k = 0..15, chosen by a branch-free binary select
+    const int i = (int)k;
+    const float t0[8] = {0.000000000e+00f, 0.000000000e+00f, 6.931471806e-01f, 1.791759469e+00f,
+                         3.178053830e+00f, 4.787491743e+00f, 6.579251212e+00f, 8.525161361e+00f};
+    const float t1[8] = {1.060460290e+01f, 1.280182748e+01f, 1.510441257e+01f, 1.750230785e+01f,
+                         1.998721450e+01f, 2.255216385e+01f, 2.519122118e+01f, 2.789927138e+01f};
+    float v = 0.0f;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int j = 0; j < 8; ++j) {
+      v = (i == j) ? t0[j] : v;
+      v = (i == j + 8) ? t1[j] : v;
+    }
+    return v;
+  }
+  const float x = k + 1.0f;
+  const float r = 1.0f / x;
+  return (x - 0.5f) * logf(x) - x + 0.918938533204672742f + r * (1.0f / 12.0f - (r * r) * (1.0f / 360.0f));
+}
+
 // ---------------------------------------------------------------------------
 // Samplers
 // ---------------------------------------------------------------------------
@@ -217,7 +272,7 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
     if (us >= 0.07f && V <= vr) return (int)kf;
     if (kf < 0.0f || (us < 0.013f && V > us)) continue;
     const float lhs = logf(V) + logf(invalpha) - logf(a / (us * us) + b);
-    const float rhs = -lam + kf * loglam - bq_lgammaf(kf + 1.0f);
+    const float rhs = -lam + kf * loglam - log_factorial(kf);
     if (lhs <= rhs) return (int)kf;
   }
   *err |= ERR_POISSON_CAP;
@@ -252,7 +307,7 @@ BQ_HD float softplus_diff(float t, float dlt) {
 // otherwise the difference of the two logarithms, which stays accurate when
 // a << b (where 1 + d / b would cancel).
 BQ_HD float log_ratio(float a, float b, float d) {
-  return fabsf(d) < 0.5f * b ? log1pf(d / b) : logf(a) - logf(b);
+  return fabsf(d) < 0.5f * b ? log1p_fast(fast_div(d, b)) : logf(a) - logf(b);
 }
 
 // lgamma(zp) - lgamma(z) for z, zp > 0, dlt = zp - z, without cancellation.

@@ -241,15 +241,24 @@ __device__ void zx_global_tail(const DevState& s, uint32_t iter, double* sh) {
 // ---------------------------------------------------------------------------
 constexpr int ZX_ROWS = 8;
 
+// Copies the chunk's cell indices and exp(delta) into shared memory.
+__device__ __forceinline__ void stage_chunk(const DevState& s, int start, int len, int* s_i, float* s_D) {
+  for (int j = threadIdx.x; j < len; j += blockDim.x) {
+    const int i = s.perm[start + j];
+    s_i[j] = i;
+    s_D[j] = s.Dexp[i];
+  }
+}
+
 __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
   __shared__ double sh[(GENE_TILE / 32) * 9];
   __shared__ int sh_flag;
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
   __shared__ int xs[ZX_ROWS][GENE_TILE];             // X of the current cells, updated in place
   __shared__ unsigned char zs[ZX_ROWS][GENE_TILE];   // bit 0: Z, bit 1: X changed
-  __shared__ unsigned short queue[ZX_ROWS * GENE_TILE];
-  __shared__ int qlen;
-  __shared__ int gi[ZX_ROWS];
-  __shared__ float gD[ZX_ROWS];
+  __shared__ unsigned short q1[ZX_ROWS * GENE_TILE], q2[ZX_ROWS * GENE_TILE];
+  __shared__ int q1n, q2n;
   __shared__ float sM[GENE_TILE], sPh[GENE_TILE];
   const int tid = threadIdx.x, lane = tid & 31;
   const uint32_t iter = (uint32_t)*s.iter;
@@ -275,53 +284,85 @@ __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
     const float ca = valid ? expm1f(s.alpha_p[g] - s.alpha[g]) : 0.0f;
     sM[tid] = M;
     sPh[tid] = ph;
+    stage_chunk(s, start, len, s_i, s_D);
+    if (tid == 0) { q1n = 0; q2n = 0; }
     const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
     const float g0p = s.gamma_p[b], dg0 = g0p - g0, dg1 = s.gamma_p[s.B + b] - g1;
+    const float zthr = 1.0f / (1.0f + expf(g0));
     const uint64_t G64 = (uint64_t)s.G;
     const uint64_t gbase = (uint64_t)tile * GENE_TILE;
     int64_t sx = 0, xz = 0;
     int nz = 0, n0 = 0;
     KahanF la, d0, d1a, d1b;
+    __syncthreads();
     for (int j0 = 0; j0 < len; j0 += ZX_ROWS) {
       const int rn = min(ZX_ROWS, len - j0);
-      if (tid < rn) {
-        const int i = s.perm[start + j0 + tid];
-        gi[tid] = i;
-        gD[tid] = s.Dexp[i];
+      // gather X and the Y == 0 bits of the group (independent loads first)
+      int xr[ZX_ROWS];
+      uint32_t mw[ZX_ROWS];
+#pragma unroll
+      for (int r = 0; r < ZX_ROWS; ++r) {
+        xr[r] = 0;
+        mw[r] = 0u;
+        if (r < rn) {
+          const int64_t i = s_i[j0 + r];
+          if (valid) xr[r] = s.X[i * Gp + g];
+          mw[r] = s.y0m[i * Gw + (g >> 5)];
+        }
       }
-      if (tid == 0) qlen = 0;
-      __syncthreads();
-      // gather: X of the group into shared memory, Y == 0 entries into the queue
-      for (int r = 0; r < rn; ++r) {
-        const int i = gi[r];
-        xs[r][tid] = valid ? s.X[(int64_t)i * Gp + g] : 0;
-        zs[r][tid] = 0;
-        const uint32_t ymw = s.y0m[(int64_t)i * Gw + (g >> 5)];
-        const bool y0 = valid && ((ymw >> lane) & 1u);
-        const unsigned m = __ballot_sync(0xffffffffu, y0);
-        if (m) {
-          int base = 0;
-          if (lane == 0) base = atomicAdd(&qlen, __popc(m));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (y0) queue[base + __popc(m & ((1u << lane) - 1u))] = (unsigned short)((r << 8) | tid);
+#pragma unroll
+      for (int r = 0; r < ZX_ROWS; ++r) {
+        if (r < rn) {
+          xs[r][tid] = xr[r];
+          zs[r][tid] = 0;
+          const bool y0 = valid && ((mw[r] >> lane) & 1u);
+          const unsigned m = __ballot_sync(0xffffffffu, y0);
+          if (m) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&q1n, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (y0) q1[base + __popc(m & ((1u << lane) - 1u))] = (unsigned short)((r << 8) | tid);
+          }
         }
       }
       __syncthreads();
-      // dense Z/X updates of the queued entries (BUSseq_gpu.cu:484-512)
-      const int Q = qlen;
-      float d0f = 0.0f, d1af = 0.0f, d1bf = 0.0f;
-      for (int q = tid; q < Q; q += GENE_TILE) {
-        const int item = queue[q];
+      // Z for the Y == 0 entries; those with Z = 1 go on to the NB queue
+      const int Q1 = q1n;
+      for (int q = tid; q < Q1; q += GENE_TILE) {
+        const int item = q1[q];
         const int r = item >> 8, t = item & 0xFF;
-        const int i = gi[r];
-        int x = xs[r][t], z = 0;
-        const int xo = x;
-        zx_entry(s.seed, (uint64_t)i * G64 + gbase + (uint64_t)t, iter, sM[t] * gD[r], sPh[t], g0, g1, x, z,
-                 s.err);
+        int z = 1;
+        if (xs[r][t] == 0) {
+          const uint64_t ent = (uint64_t)s_i[j0 + r] * G64 + gbase + (uint64_t)t;
+          z = uniform_at(s.seed, SID_ZX, ent, iter, 0) > zthr;
+        }
+        if (z) {
+          q2[atomicAdd(&q2n, 1)] = (unsigned short)item;
+        } else {
+          ++n0;  // Z = 0 and X stays 0
+        }
+      }
+      __syncthreads();
+      // imputation X ~ NB independence MH for the entries with Z = 1 (BUSseq_gpu.cu:497-506)
+      const int Q2 = q2n;
+      float d0f = 0.0f, d1af = 0.0f, d1bf = 0.0f;
+      for (int q = tid; q < Q2; q += GENE_TILE) {
+        const int item = q2[q];
+        const int r = item >> 8, t = item & 0xFF;
+        const int xo = xs[r][t];
+        const uint64_t ent = (uint64_t)s_i[j0 + r] * G64 + gbase + (uint64_t)t;
+        Stream st(s.seed, SID_ZX, ent, iter);
+        if (xo == 0) st.next_u32();  // the uniform of the Z draw
+        int err = 0;
+        const int xn = negbin(st, sM[t] * s_D[j0 + r], sPh[t], &err);
+        const float u = st.uniform();
+        const float lr = softplusf(-g0 - g1 * (float)xo) - softplusf(-g0 - g1 * (float)xn);
+        const int x = logf(u) <= lr ? xn : xo;
+        if (err) atomicOr(s.err, err);
         xs[r][t] = x;
-        zs[r][t] = (unsigned char)(z | (x != xo ? 2 : 0));
-        nz += z;
-        xz += (int64_t)x * z;
+        zs[r][t] = (unsigned char)(1 | (x != xo ? 2 : 0));
+        ++nz;
+        xz += x;
         if (x == 0) {
           ++n0;
         } else {
@@ -339,20 +380,24 @@ __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
       __syncthreads();
       // write back X and the Z bits; alpha terms over the whole tile
       float laf = 0.0f;
-      for (int r = 0; r < rn; ++r) {
-        const int i = gi[r];
-        const int x = xs[r][tid];
-        const int zz = zs[r][tid];
-        const unsigned zb = __ballot_sync(0xffffffffu, zz & 1);
-        if (lane == 0) s.zm[(int64_t)i * Gw + (g >> 5)] = zb;
-        if (__any_sync(0xffffffffu, zz & 2) && valid) s.X[(int64_t)i * Gp + g] = x;
-        if (valid) {
-          const float mu = M * gD[r];
-          sx += x;
-          laf += nb_shift_log(ph + (float)x, ca, mu / (ph + mu));
+#pragma unroll
+      for (int r = 0; r < ZX_ROWS; ++r) {
+        if (r < rn) {
+          const int64_t i = s_i[j0 + r];
+          const int x = xs[r][tid];
+          const int zz = zs[r][tid];
+          const unsigned zb = __ballot_sync(0xffffffffu, zz & 1);
+          if (lane == 0) s.zm[i * Gw + (g >> 5)] = zb;
+          if (__any_sync(0xffffffffu, zz & 2) && valid) s.X[i * Gp + g] = x;
+          if (valid) {
+            const float mu = M * s_D[j0 + r];
+            sx += x;
+            laf += (ph + (float)x) * log1p_fast(ca * fast_div(mu, ph + mu));
+          }
         }
       }
       la.add(laf);
+      if (tid == 0) { q1n = 0; q2n = 0; }
       __syncthreads();
     }
     if (valid) {
@@ -414,6 +459,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_zx_alpha(DevState s) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   __shared__ int sh_flag;
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
   const int tid = threadIdx.x;
   const uint32_t iter = (uint32_t)*s.iter;
   const int tile = blockIdx.x, row = blockIdx.y;
@@ -422,8 +469,11 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   const bool valid = g < s.G;
+  const bool work = len > 0 && (k > 0 || b > 0);
 
-  if (len > 0 && valid && (k > 0 || b > 0)) {
+  if (work) stage_chunk(s, start, len, s_i, s_D);
+  __syncthreads();
+  if (work && valid) {
     const float bt = s.beta[(int64_t)k * Gp + g];
     const float M = exp_sum3(s.alpha[g], bt, s.nu[(int64_t)b * Gp + g]);
     const float ph = s.phi[(int64_t)b * Gp + g];
@@ -432,36 +482,39 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
     const float en = b > 0 ? s.nu_p[(int64_t)b * Gp + g] - s.nu[(int64_t)b * Gp + g] : 0.0f;
     const float cn = expm1f(en);
     int64_t sx = 0;
-    double lb = 0.0, ln0 = 0.0, ln1 = 0.0;
-    for (int j0 = 0; j0 < len; j0 += 32) {
-      const int jn = min(32, len - j0);
+    KahanF lb, ln0, ln1;
+    for (int j0 = 0; j0 < len; j0 += 8) {
+      int xr[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) xr[u] = j0 + u < len ? s.X[(int64_t)s_i[j0 + u] * Gp + g] : 0;
       float lbf = 0.0f, ln0f = 0.0f, ln1f = 0.0f;
-      for (int jj = 0; jj < jn; ++jj) {
-        const int i = s.perm[start + j0 + jj];
-        const float D = s.Dexp[i];
-        const int x = s.X[(int64_t)i * Gp + g];
-        const float mu = M * D;
-        const float w = ph + (float)x;
-        const float p = mu / (ph + mu);
-        sx += x;
-        if (k > 0) lbf += nb_shift_log(w, cb, p);
-        if (b > 0) {
-          ln0f += nb_shift_log(w, cn, p);
-          if (k > 0) {
-            const float mu1 = mu * fb;
-            ln1f += nb_shift_log(w, cn, mu1 / (ph + mu1));
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (j0 + u < len) {
+          const int x = xr[u];
+          const float mu = M * s_D[j0 + u];
+          const float w = ph + (float)x;
+          const float p = fast_div(mu, ph + mu);
+          sx += x;
+          if (k > 0) lbf += w * log1p_fast(cb * p);
+          if (b > 0) {
+            ln0f += w * log1p_fast(cn * p);
+            if (k > 0) {
+              const float mu1 = mu * fb;
+              ln1f += w * log1p_fast(cn * fast_div(mu1, ph + mu1));
+            }
           }
         }
       }
-      lb += lbf;
-      ln0 += ln0f;
-      ln1 += ln1f;
+      lb.add(lbf);
+      ln0.add(ln0f);
+      ln1.add(ln1f);
     }
     double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
     pr[0] = (double)sx;
-    pr[Gp] = lb;
-    pr[2 * Gp] = ln0;
-    pr[3 * Gp] = ln1;
+    pr[Gp] = lb.value();
+    pr[2 * Gp] = ln0.value();
+    pr[3 * Gp] = ln1.value();
   }
 
   if (!arrive_last(&s.cnt_tile[tile], (unsigned)s.cap_g, &sh_flag)) return;
@@ -525,6 +578,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
 __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   __shared__ float tab[PHI_TAB][GENE_TILE];
   __shared__ int sh_flag;
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
   const int tid = threadIdx.x;
   const uint32_t iter = (uint32_t)*s.iter;
   const int tile = blockIdx.x, row = blockIdx.y;
@@ -534,6 +589,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   const bool valid = g < s.G;
 
+  if (len > 0) stage_chunk(s, start, len, s_i, s_D);
+  __syncthreads();
   if (len > 0 && valid) {
     const float ph = s.phi[(int64_t)b * Gp + g];
     const float pp = s.phi_p[(int64_t)b * Gp + g];
@@ -554,15 +611,19 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
     }
     KahanF acc;
     for (int j0 = 0; j0 < len; j0 += 8) {
-      const int jn = min(8, len - j0);
+      int xr[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) xr[u] = j0 + u < len ? s.X[(int64_t)s_i[j0 + u] * Gp + g] : 0;
       float f = 0.0f;
-      for (int jj = 0; jj < jn; ++jj) {
-        const int i = s.perm[start + j0 + jj];
-        const float mu = M * s.Dexp[i];
-        const int x = s.X[(int64_t)i * Gp + g];
-        const float xf = (float)x;
-        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff(ph + xf, pp + xf, dl) - lgd0;
-        f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1pf(mu * iph);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (j0 + u < len) {
+          const int x = xr[u];
+          const float mu = M * s_D[j0 + u];
+          const float xf = (float)x;
+          const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff(ph + xf, pp + xf, dl) - lgd0;
+          f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
+        }
       }
       acc.add(f);
     }
@@ -651,7 +712,7 @@ __global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
         for (int q = 0; q < 4; ++q) {
           if (g4 + q < G) {
             const float mu = ev[q] * sh_D[r];
-            a += nb_shift_log(pv[q] + (float)xs[q], sh_c[r], mu / (pv[q] + mu));
+            a += (pv[q] + (float)xs[q]) * log1p_fast(sh_c[r] * fast_div(mu, pv[q] + mu));
             sxi[r] += xs[q];
           }
         }
@@ -686,7 +747,7 @@ __global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
 // eps:  eps x - (phi + x) log[(phi + mu e^eps) / (phi + mu)].
 __device__ __forceinline__ float type_shift_term(float eps, float mu, float ph, int x) {
   float lg;
-  if (fabsf(eps) < 0.5f) lg = log1pf(expm1f(eps) * (mu / (ph + mu)));
+  if (fabsf(eps) < 0.5f) lg = log1p_fast(expm1f(eps) * fast_div(mu, ph + mu));
   else lg = logf(ph + mu * expf(eps)) - logf(ph + mu);
   return eps * (float)x - (ph + (float)x) * lg;
 }
