@@ -268,10 +268,9 @@ def main():
 
     # ---- per-kernel durations for the roofline (events on the same stream) --
     prof = s.profile(20)
-    big = {k: v for k, v in prof.items() if k in ("k_zx_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w")}
+    big = {k: v for k, v in prof.items() if k in ("k_zx", "k_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w")}
     dom = max(big, key=big.get)
-    idx = bq.lib()
-    kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(8)].index(dom)
+    kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(16)].index(dom)
     alg_bytes = s.kernel_bytes(kid)
     achieved = alg_bytes / (prof[dom] / 1000.0) / 1e9
     peak, peak_kind = _peak_hbm()

@@ -14,6 +14,8 @@
 //                                of <= CG cells of one (batch, type) segment
 //   ctile       int4 [cap_c]     cell-pass work list: runs of <= CELL_TILE cells
 //   part        f64 [cap_g][4][Gp] per-chunk partial sums of the gene passes
+//   zij, zval   int2 / uint8 [nz0]   the entries with Y == 0 ({cell, gene},
+//                                row-major order; Y never changes) and their Z
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
@@ -52,6 +54,8 @@ constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
 constexpr int PHI_TAB = 16;        // small-count table of lgamma differences
+constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
+constexpr int ZX_PER_CTA = 1024;   // zero entries per Z/X CTA
 
 // ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
 enum Stage : int {
@@ -122,10 +126,21 @@ struct DevState {
   int4* gchunk;
   int4* ctile;
   int32_t* seg_cnt;  // [B][K]
+  int2* seg_chunk;   // [B][K] {first chunk, number of chunks} of each (batch, type) segment
+
+  // the entries with Y == 0 and their Z/X work units
+  const int2* zij;          // [nz0] {cell, gene}
+  uint8_t* zval;            // [nz0] Z
+  int64_t nz0;
+  const int2* zcta;         // [n_zcta] {first entry, count}, each run inside one batch
+  const int32_t* zcta_batch;
+  const int32_t* zfirst;    // [B+1] first run of each batch
+  int n_zcta;
+  uint8_t* beta_acc;        // [K][Gp] accepted beta of the current sweep
 
   // scratch (partial sums and completion counters)
   double* part;    // [cap_g][NSLOT][Gp]
-  double* gpart;   // [cap_g * n_tiles][GSLOT]
+  double* gpart;   // [n_zcta][GSLOT]
   double* gstat;   // [n_static][4]
   double* tpart;   // [n_tiles][2]
   unsigned* cnt_tile;  // [n_tiles]

@@ -43,9 +43,11 @@ int fail(int code, const char* fmt, ...) {
 int64_t round_up(int64_t a, int64_t m) { return (a + m - 1) / m * m; }
 unsigned blocks_for(int64_t n, int t) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
-const char* const kKernelNames[] = {"k_propose", "k_zx_alpha", "k_beta_nu", "k_delta",
-                                    "k_phi",     "k_w",        "k_sort_pi", "k_posterior"};
-constexpr int kNumKernels = 8;
+const char* const kKernelNames[] = {"k_propose",     "k_zx",      "k_alpha",   "k_decide_alpha", "k_beta_nu",
+                                    "k_decide_beta", "k_decide_nu_E", "k_delta", "k_phi",          "k_decide_phi",
+                                    "k_w",           "k_sort_pi", "k_posterior"};
+constexpr int kNumKernels = 13;
+constexpr int kBurnLaunches = 12;  // kernels 0..11; kept sweeps add k_posterior
 
 }  // namespace
 
@@ -57,7 +59,6 @@ struct busseq_handle {
   busseq_options opt{};
   std::vector<int32_t> n_b, off;
   std::vector<void*> allocs;
-  int static_rows = 0;
   // run
   bool begun = false, finished = false;
   int n_iter = 0, n_burnin = 0, n_unchanged = 0, iter_host = 0, n_kept = 0;
@@ -109,8 +110,8 @@ int check_device_error(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
-// Enqueue the launches of one sweep on `st` (used for graph capture, for
-// profiling and for direct launches).
+// Enqueue kernel `which` of a sweep on `st` (used for graph capture, for
+// profiling and for single stages).
 int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const bq::DevState& s) {
   using namespace bq;
   const dim3 gene_grid(s.n_tiles, s.cap_g);
@@ -120,31 +121,51 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_propose");
       break;
     case 1:
-      k_zx_alpha<<<dim3(s.n_tiles, s.cap_g + h->static_rows), GENE_TILE, 0, st>>>(s);
-      LAUNCH_CHECK("k_zx_alpha");
+      k_zx<<<(unsigned)(s.n_zcta + s.n_static) > 0 ? (unsigned)(s.n_zcta + s.n_static) : 1u, ZX_THREADS, 0, st>>>(s);
+      LAUNCH_CHECK("k_zx");
       break;
     case 2:
+      k_alpha<<<gene_grid, GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_alpha");
+      break;
+    case 3:
+      k_decide_alpha<<<s.n_tiles + s.B, GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_decide_alpha");
+      break;
+    case 4:
       k_beta_nu<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_beta_nu");
       break;
-    case 3:
+    case 5:
+      k_decide_beta<<<blocks_for((int64_t)std::max(1, s.K - 1) * s.G, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_decide_beta");
+      break;
+    case 6:
+      k_decide_nu_E<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_decide_nu_E");
+      break;
+    case 7:
       k_delta<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
       LAUNCH_CHECK("k_delta");
       break;
-    case 4:
+    case 8:
       k_phi<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_phi");
       break;
-    case 5:
+    case 9:
+      k_decide_phi<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_decide_phi");
+      break;
+    case 10:
       if (s.w_update == BUSSEQ_W_GIBBS) k_w_gibbs<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
       else k_w_mh<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
       LAUNCH_CHECK("k_w");
       break;
-    case 6:
+    case 11:
       k_sort_pi<<<s.B, 1024, 0, st>>>(s, 1, kept ? 0 : 1);
       LAUNCH_CHECK("k_sort_pi");
       break;
-    case 7: {
+    case 12: {
       const unsigned nb = (unsigned)std::min<int64_t>(blocks_for((int64_t)s.K * s.G, 256), 152 * 8);
       k_posterior<<<nb, 256, 0, st>>>(s, 1);
       LAUNCH_CHECK("k_posterior");
@@ -157,8 +178,20 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
 }
 
 int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
-  const int n = kept ? 8 : 7;
+  const int n = kept ? kNumKernels : kBurnLaunches;
   for (int k = 0; k < n; ++k) TRY(launch_kernel(h, k, st, kept, h->s));
+  return BUSSEQ_OK;
+}
+
+// Z as a bit mask [N][Gw] in s.zm, from the per-entry zval (for transfers).
+int zmask_from_zval(busseq_handle* h) {
+  const bq::DevState& s = h->s;
+  CUDA_TRY(cudaMemsetAsync(s.zm, 0, (size_t)s.N * s.Gw * sizeof(uint32_t), h->stream));
+  if (s.nz0 > 0) {
+    bq::k_zmask_from_zval<<<blocks_for(s.nz0, 256), 256, 0, h->stream>>>(s);
+    LAUNCH_CHECK("k_zmask_from_zval");
+  }
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return BUSSEQ_OK;
 }
 
@@ -320,7 +353,6 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&s.ctile, s.cap_c));
     TRY(h->alloc(&s.seg_cnt, B * K));
     TRY(h->alloc(&s.part, (int64_t)s.cap_g * bq::NSLOT * Gp));
-    TRY(h->alloc(&s.gpart, (int64_t)s.cap_g * s.n_tiles * bq::GSLOT));
     TRY(h->alloc(&s.tpart, (int64_t)s.n_tiles * bq::MAX_B));
     TRY(h->alloc(&s.cnt_tile, s.n_tiles));
     TRY(h->alloc(&s.cnt_glob, 8));
@@ -337,9 +369,13 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&h->bic_out, 2));
     int64_t* libsize;
     int *ymax_d, *bad;
+    int32_t* rowcnt;
     TRY(h->alloc(&libsize, N));
     TRY(h->alloc(&ymax_d, 1));
     TRY(h->alloc(&bad, 1));
+    TRY(h->alloc(&rowcnt, N));
+    TRY(h->alloc(&s.seg_chunk, (int64_t)B * K));
+    TRY(h->alloc(&s.beta_acc, (int64_t)K * Gp));
 
     // ---- upload ----------------------------------------------------------
     CUDA_TRY(cudaMemcpy2DAsync(Yd, Gp * sizeof(int32_t), Y, G * sizeof(int32_t), G * sizeof(int32_t), N,
@@ -355,20 +391,60 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     CUDA_TRY(cudaMemcpyAsync(bad, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
 
     // ---- initialisation (BUSseq_gpu.cu:1163-1244) --------------------------
-    bq::k_init_scan<<<(unsigned)N, 256, 0, h->stream>>>(s, libsize, ymax_d);
+    bq::k_init_scan<<<(unsigned)N, 256, 0, h->stream>>>(s, libsize, ymax_d, rowcnt);
     LAUNCH_CHECK("k_init_scan");
     int ymax = 0;
+    std::vector<int32_t> rowcnt_h(N);
     CUDA_TRY(cudaMemcpyAsync(&ymax, ymax_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(rowcnt_h.data(), rowcnt, N * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     if (ymax < 0) return fail(BUSSEQ_ERR_ARG, "counts must be non-negative");
     if (ymax > (1 << 26)) return fail(BUSSEQ_ERR_ARG, "counts above 2^26 are not supported");
     s.ymax = std::max(ymax, 1);
-    s.n_static = B * ((s.ymax + bq::GENE_TILE - 1) / bq::GENE_TILE);
-    h->static_rows = (s.n_static + s.n_tiles - 1) / s.n_tiles;
+    s.n_static = B * ((s.ymax + bq::ZX_THREADS - 1) / bq::ZX_THREADS);
     int32_t* hist;
     TRY(h->alloc(&hist, (int64_t)B * (s.ymax + 1)));
     s.yhist = hist;
     TRY(h->alloc(&s.gstat, (int64_t)s.n_static * 4));
+    // the entries with Y == 0 (row-major) and their Z/X work units, one batch per unit
+    std::vector<int64_t> rowoff_h(N + 1, 0);
+    for (int64_t i = 0; i < N; ++i) rowoff_h[i + 1] = rowoff_h[i] + rowcnt_h[i];
+    s.nz0 = rowoff_h[N];
+    std::vector<int2> zcta_h;
+    std::vector<int32_t> zbatch_h, zfirst_h(B + 1, 0);
+    for (int b = 0; b < B; ++b) {
+      zfirst_h[b] = (int32_t)zcta_h.size();
+      const int64_t lo = rowoff_h[h->off[b]], hi = rowoff_h[h->off[b + 1]];
+      for (int64_t e = lo; e < hi; e += bq::ZX_PER_CTA) {
+        if (e > INT_MAX) return fail(BUSSEQ_ERR_ARG, "too many zero counts (more than 2^31)");
+        zcta_h.push_back(make_int2((int)e, (int)std::min<int64_t>(bq::ZX_PER_CTA, hi - e)));
+        zbatch_h.push_back(b);
+      }
+    }
+    zfirst_h[B] = (int32_t)zcta_h.size();
+    s.n_zcta = (int)zcta_h.size();
+    int64_t* rowoff;
+    int2 *zij, *zcta;
+    int32_t *zbatch, *zfirst;
+    TRY(h->alloc(&rowoff, N + 1));
+    TRY(h->alloc(&zij, std::max<int64_t>(1, s.nz0)));
+    TRY(h->alloc(&s.zval, std::max<int64_t>(1, s.nz0)));
+    TRY(h->alloc(&zcta, std::max(1, s.n_zcta)));
+    TRY(h->alloc(&zbatch, std::max(1, s.n_zcta)));
+    TRY(h->alloc(&zfirst, B + 1));
+    TRY(h->alloc(&s.gpart, (int64_t)std::max(1, s.n_zcta) * bq::GSLOT));
+    CUDA_TRY(cudaMemcpyAsync(rowoff, rowoff_h.data(), (N + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    if (s.n_zcta) {
+      CUDA_TRY(cudaMemcpyAsync(zcta, zcta_h.data(), zcta_h.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
+      CUDA_TRY(cudaMemcpyAsync(zbatch, zbatch_h.data(), zbatch_h.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+    CUDA_TRY(cudaMemcpyAsync(zfirst, zfirst_h.data(), (B + 1) * 4, cudaMemcpyHostToDevice, h->stream));
+    s.zij = zij;
+    s.zcta = zcta;
+    s.zcta_batch = zbatch;
+    s.zfirst = zfirst;
+    bq::k_zlist_fill<<<blocks_for(N, 8), 256, 0, h->stream>>>(s, rowoff, zij);
+    LAUNCH_CHECK("k_zlist_fill");
     bq::k_init_hist<<<(unsigned)N, 256, 0, h->stream>>>(s, hist);
     LAUNCH_CHECK("k_init_hist");
     bq::k_init_w_delta<<<blocks_for(N, 256), 256, 0, h->stream>>>(s, libsize, bad);
@@ -386,6 +462,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     LAUNCH_CHECK("k_init_finish");
     CUDA_TRY(cudaMemcpyAsync(s.X, s.Y, (size_t)N * Gp * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
     CUDA_TRY(cudaMemsetAsync(s.zm, 0, (size_t)N * s.Gw * sizeof(uint32_t), h->stream));
+    CUDA_TRY(cudaMemsetAsync(s.zval, 0, (size_t)std::max<int64_t>(1, s.nz0), h->stream));
     CUDA_TRY(cudaMemsetAsync(s.iter, 0, sizeof(int), h->stream));
     return check_device_error(h);
   }();
@@ -522,6 +599,7 @@ int busseq_get_estimates(busseq_handle* h, busseq_estimates* o) {
   TRY(cp(o->pi, e.pi, B * K * sizeof(double)));
   if (o->X) CUDA_TRY(cudaMemcpy2D(o->X, G * 4, s.X, s.Gp * 4, G * 4, N, cudaMemcpyDeviceToHost));
   if (o->Z) {
+    TRY(zmask_from_zval(h));
     std::vector<uint32_t> zm((size_t)N * s.Gw);
     CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
     for (int64_t i = 0; i < N; ++i)
@@ -602,6 +680,7 @@ int busseq_get_state(busseq_handle* h, busseq_state* o) {
   };
   TRY(rows(o->X, s.X, 4, N));
   if (o->Z) {
+    TRY(zmask_from_zval(h));
     std::vector<uint32_t> zm((size_t)N * s.Gw);
     CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
     for (int64_t i = 0; i < N; ++i)
@@ -649,6 +728,10 @@ int busseq_set_state(busseq_handle* h, const busseq_state* in) {
       for (int64_t g = 0; g < G; ++g)
         if (in->Z[i * G + g]) zm[i * s.Gw + (g >> 5)] |= 1u << (g & 31);
     CUDA_TRY(cudaMemcpy(s.zm, zm.data(), zm.size() * 4, cudaMemcpyHostToDevice));
+    if (s.nz0 > 0) {
+      bq::k_zval_from_mask<<<blocks_for(s.nz0, 256), 256, 0, h->stream>>>(s);
+      LAUNCH_CHECK("k_zval_from_mask");
+    }
   }
   TRY(flat(s.W, in->W, N * 4));
   TRY(rows(s.L, in->L, 1, K));
@@ -682,29 +765,33 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
   s.n_unchanged = n_unchanged;
   cudaStream_t st = h->stream;
   const unsigned pb = blocks_for(propose_count(s), 256);
+  auto run = [&](std::initializer_list<int> ks) -> int {
+    for (int k : ks) TRY(launch_kernel(h, k, st, 0, s));
+    return BUSSEQ_OK;
+  };
   switch (stage) {
     case BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA);
       LAUNCH_CHECK("k_propose");
-      TRY(launch_kernel(h, 1, st, 0, s));
+      TRY(run({1, 2, 3}));
       break;
     case BUSSEQ_STAGE_BETA_NU:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU);
       LAUNCH_CHECK("k_propose");
-      TRY(launch_kernel(h, 2, st, 0, s));
+      TRY(run({4, 5, 6}));
       break;
     case BUSSEQ_STAGE_DELTA:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_DELTA);
       LAUNCH_CHECK("k_propose");
-      TRY(launch_kernel(h, 3, st, 0, s));
+      TRY(run({7}));
       break;
     case BUSSEQ_STAGE_PHI:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_PHI);
       LAUNCH_CHECK("k_propose");
-      TRY(launch_kernel(h, 4, st, 0, s));
+      TRY(run({8, 9}));
       break;
     case BUSSEQ_STAGE_W:
-      TRY(launch_kernel(h, 5, st, 0, s));
+      TRY(run({10}));
       break;
     case BUSSEQ_STAGE_PI:
       k_sort_pi<<<s.B, 1024, 0, st>>>(s, 1, 0);
@@ -747,7 +834,7 @@ int busseq_profile(busseq_handle* h, int32_t n_sweeps, double* ms_avg, int32_t c
   if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
   if (n_sweeps <= 0) return fail(BUSSEQ_ERR_ARG, "n_sweeps must be positive");
   CUDA_TRY(cudaSetDevice(h->device));
-  const int nk = 7;  // one burn-in sweep: every kernel but the posterior accumulation
+  const int nk = kBurnLaunches;  // one burn-in sweep: every kernel but the posterior accumulation
   std::vector<cudaEvent_t> ev((size_t)nk * 2 * n_sweeps);
   for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
   int r = BUSSEQ_OK;
@@ -776,24 +863,31 @@ int busseq_profile(busseq_handle* h, int32_t n_sweeps, double* ms_avg, int32_t c
 
 double busseq_kernel_bytes(busseq_handle* h, int32_t i) {
   if (!h) return 0.0;
-  const double E = (double)h->s.N * (double)h->s.G;
-  const double params = 8.0 * ((double)h->s.K * h->s.G + 2.0 * h->s.B * h->s.G + h->s.N);
+  const bq::DevState& s = h->s;
+  const double E = (double)s.N * (double)s.G;
+  const double params = 8.0 * ((double)s.K * s.G + 2.0 * s.B * s.G + s.N);
+  const double part = 8.0 * (double)s.cap_g * s.Gp;  // one slot of the per-chunk partials
   switch (i) {
-    case 0: return params;                   // proposals
-    case 1: return 8.25 * E;                 // read X, write X, Y==0 mask in, Z mask out
-    case 2: return 4.0 * E;                  // read X
-    case 3: return 4.0 * E;
+    case 0: return params;                          // proposals
+    case 1: return 17.0 * (double)s.nz0;            // per zero entry: {cell, gene}, X in + out, Z out
+    case 2: return 4.0 * E;                         // read X
+    case 3: return 2.0 * part + params;             // alpha partials
     case 4: return 4.0 * E;
-    case 5: return 4.0 * E;
-    case 6: return 8.0 * h->s.N;             // W in, cell order out
-    case 7: return params;
+    case 5: return 2.0 * part + params;
+    case 6: return 2.0 * part + 4.0 * s.B * s.K * s.G;  // nu partials, E table out
+    case 7: return 4.0 * E;
+    case 8: return 4.0 * E;
+    case 9: return part + params;
+    case 10: return 4.0 * E;
+    case 11: return 8.0 * s.N;                      // W in, cell order out
+    case 12: return params;
     default: return 0.0;
   }
 }
 
 int busseq_launches_per_sweep(busseq_handle* h, int32_t kept) {
   (void)h;
-  return kept ? 8 : 7;
+  return kept ? kNumKernels : kBurnLaunches;
 }
 
 }  // extern "C"

@@ -1,0 +1,583 @@
+// Gene-side kernels of a sweep: proposals, the Z/X imputation, and the
+// per-gene Metropolis updates alpha, beta, nu, phi with their decisions.
+//
+//   k_propose       every random-walk / Gamma proposal of the sweep
+//   k_zx            Z/X update (BUSseq_gpu.cu:484-512), one thread per entry of
+//                   the static list of Y == 0 entries, with the per-batch
+//                   sufficient statistics of the gamma updates (:514-600); extra
+//                   CTAs evaluate the gamma terms of the Y > 0 entries from the
+//                   histogram of Y
+//   k_alpha         alpha sums (:602-623)
+//   k_decide_alpha  alpha decisions, L redraw (:634-648), p and tau0 (:650-668)
+//                   in the last gene CTA, gamma0 / gamma1 decisions in one CTA per
+//                   batch
+//   k_beta_nu       beta sums (:676-694) and the nu sums (:715-728) under both
+//                   outcomes of the beta of the cell's type
+//   k_decide_beta   beta decisions (:696-707)
+//   k_decide_nu_E   nu decisions (:730-737) and the table E = exp(alpha+beta+nu)
+//   k_phi           phi sums (:789-804)
+//   k_decide_phi    phi decisions (:806-818)
+//
+// Gene passes: a CTA owns GENE_TILE consecutive genes (one per thread) and one
+// chunk of <= CG cells that share batch b and type k (the cell order is
+// rebuilt after every W update), so every per-gene parameter of the chunk
+// lives in registers and X is read as coalesced 512-byte row segments.  The
+// chunk's cell indices and exp(delta) are staged in shared memory and eight
+// rows are loaded at a time.  Per-chunk partial sums (Kahan-compensated float
+// per thread, then double) go to `part`; the decision kernels reduce them in a
+// fixed order, so a sweep is bit-reproducible.
+#include "kernels_common.cuh"
+
+namespace bq {
+
+// ---------------------------------------------------------------------------
+// Proposals (all families of one sweep; `mask` selects families)
+// ---------------------------------------------------------------------------
+__global__ void k_propose(DevState s, int mask) {
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int64_t G = s.G, Gp = s.Gp;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // [0,B) gamma | [.., +G) alpha | (K-1)G beta | (B-1)G nu | N delta | B G phi
+  if (t < s.B) {
+    if (mask & PROP_GAMMA) {
+      const int b = (int)t;
+      Stream st(s.seed, SID_GAMMA, (uint64_t)b, iter);
+      const float z = normal(st);
+      s.gamma_p[b] = __fmaf_rn(RW_STEP, z, s.gamma[b]);
+      Stream sg(s.seed, SID_GAMMA1_PROP, (uint64_t)b, iter);
+      int err = 0;
+      const float g1 = s.gamma[s.B + b];
+      float gn = -(gamma_mt(sg, -10.0f * g1, &err) * 0.1f);
+      if (!(gn < 0.0f)) gn = -1.0e-30f;  // a Gamma draw that underflowed to 0
+      s.gamma_p[s.B + b] = gn;
+      if (err) atomicOr(s.err, err);
+    }
+    return;
+  }
+  t -= s.B;
+  if (t < G) {
+    if (mask & PROP_ALPHA) {
+      Stream st(s.seed, SID_ALPHA, (uint64_t)t, iter);
+      s.alpha_p[t] = __fmaf_rn(RW_STEP, normal(st), s.alpha[t]);
+    }
+    return;
+  }
+  t -= G;
+  if (t < (int64_t)(s.K - 1) * G) {
+    if (mask & PROP_BETA) {
+      const int k = 1 + (int)(t / G);
+      const int64_t g = t % G;
+      Stream st(s.seed, SID_BETA, (uint64_t)t, iter);
+      s.beta_p[k * Gp + g] = __fmaf_rn(RW_STEP, normal(st), s.beta[k * Gp + g]);
+    }
+    return;
+  }
+  t -= (int64_t)(s.K - 1) * G;
+  if (t < (int64_t)(s.B - 1) * G) {
+    if (mask & PROP_NU) {
+      const int b = 1 + (int)(t / G);
+      const int64_t g = t % G;
+      Stream st(s.seed, SID_NU, (uint64_t)t, iter);
+      s.nu_p[b * Gp + g] = __fmaf_rn(RW_STEP, normal(st), s.nu[b * Gp + g]);
+    }
+    return;
+  }
+  t -= (int64_t)(s.B - 1) * G;
+  if (t < s.N) {
+    if (mask & PROP_DELTA) {
+      Stream st(s.seed, SID_DELTA, (uint64_t)t, iter);
+      s.delta_p[t] = __fmaf_rn(RW_STEP, normal(st), s.delta[t]);
+    }
+    return;
+  }
+  t -= s.N;
+  if (t < (int64_t)s.B * G) {
+    if (mask & PROP_PHI) {
+      const int b = (int)(t / G);
+      const int64_t g = t % G;
+      Stream st(s.seed, SID_PHI_PROP, (uint64_t)t, iter);
+      int err = 0;
+      float pn = gamma_mt(st, s.phi[b * Gp + g], &err);
+      if (!(pn > 0.0f)) pn = 1.0e-30f;
+      s.phi_p[b * Gp + g] = pn;
+      if (err) atomicOr(s.err, err);
+    }
+  }
+}
+
+int64_t propose_count(const DevState& s) {
+  return (int64_t)s.B + s.G + (int64_t)(s.K - 1) * s.G + (int64_t)(s.B - 1) * s.G + s.N + (int64_t)s.B * s.G;
+}
+
+// ---------------------------------------------------------------------------
+// Z / X of the entries with Y == 0 (BUSseq_gpu.cu:484-512)
+// ---------------------------------------------------------------------------
+// Static part of the gamma statistics: entries with Y > 0 keep X = Y and
+// Z = 0, so their terms only depend on the histogram of Y per batch.
+__device__ void gamma_static_cta(const DevState& s, int sidx, double* sh) {
+  const int slices = (s.ymax + ZX_THREADS - 1) / ZX_THREADS;
+  double v[3] = {0.0, 0.0, 0.0};
+  int b = -1;
+  if (sidx < s.n_static) {
+    b = sidx / slices;
+    const int y = (sidx % slices) * ZX_THREADS + (int)threadIdx.x + 1;
+    if (y <= s.ymax) {
+      const int cnt = s.yhist[(int64_t)b * (s.ymax + 1) + y];
+      if (cnt) {
+        const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
+        const float g0p = s.gamma_p[b], g1p = s.gamma_p[s.B + b];
+        const float yf = (float)y;
+        const float t = fmaf(g1, yf, g0);
+        const float d1 = (g1p - g1) * yf;
+        v[0] = (double)cnt * (double)softplus_diff(t, g0p - g0);
+        v[1] = (double)cnt * (double)softplus_diff(t, d1);
+        v[2] = (double)cnt * (double)softplus_diff(fmaf(g1, yf, g0p), d1);
+      }
+    }
+  }
+  block_sum<3>(v, sh);
+  if (threadIdx.x == 0 && sidx < s.n_static) {
+    s.gstat[(int64_t)sidx * 4 + 0] = v[0];
+    s.gstat[(int64_t)sidx * 4 + 1] = v[1];
+    s.gstat[(int64_t)sidx * 4 + 2] = v[2];
+    s.gstat[(int64_t)sidx * 4 + 3] = (double)b;
+  }
+}
+
+// One entry: x is replaced by the new X, z receives the new Z.
+__device__ __forceinline__ void zx_entry(uint64_t seed, uint64_t ent, uint32_t iter, float mu, float phi, float g0,
+                                         float g1, float zthr, int& x, int& z, int* errp) {
+  Stream st(seed, SID_ZX, ent, iter);
+  z = x == 0 ? (st.uniform() > zthr) : 1;
+  if (z) {
+    int err = 0;
+    const int xn = negbin(st, mu, phi, &err);
+    const float u = st.uniform();
+    // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
+    const float lr = softplusf(-g0 - g1 * (float)x) - softplusf(-g0 - g1 * (float)xn);
+    if (logf(u) <= lr) x = xn;
+    if (err) atomicOr(errp, err);
+  } else {
+    x = 0;
+  }
+}
+
+// Work unit: a run of <= ZX_PER_CTA list entries of one batch (built at
+// initialisation); CTAs past n_zcta evaluate the static gamma terms.
+__global__ void __launch_bounds__(ZX_THREADS) k_zx(DevState s) {
+  __shared__ double sh[(ZX_THREADS / 32) * 6];
+  const int c = blockIdx.x;
+  if (c >= s.n_zcta) {
+    gamma_static_cta(s, c - s.n_zcta, sh);
+    return;
+  }
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int2 run = s.zcta[c];
+  const int b = s.zcta_batch[c];
+  const int64_t Gp = s.Gp;
+  const uint64_t G64 = (uint64_t)s.G;
+  const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
+  const float g0p = s.gamma_p[b], dg0 = g0p - g0, dg1 = s.gamma_p[s.B + b] - g1;
+  const float zthr = 1.0f / (1.0f + expf(g0));
+  int nz = 0, n0 = 0;
+  int64_t xz = 0;
+  float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
+  for (int e = threadIdx.x; e < run.y; e += ZX_THREADS) {
+    const int64_t j = (int64_t)run.x + e;
+    const int2 ig = s.zij[j];
+    const int64_t i = ig.x, g = ig.y;
+    const int k = s.W[i];
+    const float mu = s.E[((int64_t)b * s.K + k) * Gp + g] * s.Dexp[i];
+    const float ph = s.phi[(int64_t)b * Gp + g];
+    const int64_t pos = i * Gp + g;
+    const int xo = s.X[pos];
+    int x = xo, z = 0;
+    zx_entry(s.seed, (uint64_t)i * G64 + (uint64_t)g, iter, mu, ph, g0, g1, zthr, x, z, s.err);
+    if (x != xo) s.X[pos] = x;
+    s.zval[j] = (uint8_t)z;
+    nz += z;
+    xz += (int64_t)x * z;
+    if (x == 0) {
+      ++n0;
+    } else {
+      const float xf = (float)x;
+      const float tt = fmaf(g1, xf, g0);
+      const float d1 = dg1 * xf;
+      d0 += softplus_diff(tt, dg0);
+      d1a += softplus_diff(tt, d1);
+      d1b += softplus_diff(fmaf(g1, xf, g0p), d1);
+    }
+  }
+  double v[6] = {(double)nz, (double)xz, (double)n0, (double)d0, (double)d1a, (double)d1b};
+  block_sum<6>(v, sh);
+  if (threadIdx.x == 0) {
+    double* gp = s.gpart + (int64_t)c * GSLOT;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) gp[q] = v[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gene passes
+// ---------------------------------------------------------------------------
+// Copies the chunk's cell indices and exp(delta) into shared memory.
+__device__ __forceinline__ void stage_chunk(const DevState& s, int start, int len, int* s_i, float* s_D) {
+  for (int j = threadIdx.x; j < len; j += blockDim.x) {
+    const int i = s.perm[start + j];
+    s_i[j] = i;
+    s_D[j] = s.Dexp[i];
+  }
+}
+
+// Loads X of eight consecutive chunk cells for gene g.
+__device__ __forceinline__ void load8(const DevState& s, const int* s_i, int j0, int len, int64_t g, int (&xr)[8]) {
+#pragma unroll
+  for (int u = 0; u < 8; ++u) xr[u] = j0 + u < len ? s.X[(int64_t)s_i[j0 + u] * s.Gp + g] : 0;
+}
+
+// alpha: sum of x and of (phi + x) log1p(expm1(alpha' - alpha) p) over the chunk
+__global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int4 ch = s.gchunk[row];
+  const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + threadIdx.x;
+  if (len == 0) return;
+  stage_chunk(s, start, len, s_i, s_D);
+  __syncthreads();
+  if (g >= s.G) return;
+  const float M = s.E[((int64_t)b * s.K + k) * Gp + g];
+  const float ph = s.phi[(int64_t)b * Gp + g];
+  const float ca = expm1f(s.alpha_p[g] - s.alpha[g]);
+  int64_t sx = 0;
+  KahanF la;
+  for (int j0 = 0; j0 < len; j0 += 8) {
+    int xr[8];
+    load8(s, s_i, j0, len, g, xr);
+    float f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (j0 + u < len) {
+        const float mu = M * s_D[j0 + u];
+        sx += xr[u];
+        f += (ph + (float)xr[u]) * log1p_fast(ca * fast_div(mu, ph + mu));
+      }
+    }
+    la.add(f);
+  }
+  double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
+  pr[0] = (double)sx;
+  pr[Gp] = la.value();
+}
+
+__global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int4 ch = s.gchunk[row];
+  const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + threadIdx.x;
+  if (len == 0 || (k == 0 && b == 0)) return;
+  stage_chunk(s, start, len, s_i, s_D);
+  __syncthreads();
+  if (g >= s.G) return;
+  const float bt = s.beta[(int64_t)k * Gp + g];
+  const float M = exp_sum3(s.alpha[g], bt, s.nu[(int64_t)b * Gp + g]);
+  const float ph = s.phi[(int64_t)b * Gp + g];
+  const float eb = k > 0 ? s.beta_p[(int64_t)k * Gp + g] - bt : 0.0f;
+  const float cb = expm1f(eb), fb = expf(eb);
+  const float en = b > 0 ? s.nu_p[(int64_t)b * Gp + g] - s.nu[(int64_t)b * Gp + g] : 0.0f;
+  const float cn = expm1f(en);
+  int64_t sx = 0;
+  KahanF lb, ln0, ln1;
+  for (int j0 = 0; j0 < len; j0 += 8) {
+    int xr[8];
+    load8(s, s_i, j0, len, g, xr);
+    float lbf = 0.0f, ln0f = 0.0f, ln1f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (j0 + u < len) {
+        const int x = xr[u];
+        const float mu = M * s_D[j0 + u];
+        const float w = ph + (float)x;
+        const float p = fast_div(mu, ph + mu);
+        sx += x;
+        if (k > 0) lbf += w * log1p_fast(cb * p);
+        if (b > 0) {
+          ln0f += w * log1p_fast(cn * p);
+          if (k > 0) {
+            const float mu1 = mu * fb;
+            ln1f += w * log1p_fast(cn * fast_div(mu1, ph + mu1));
+          }
+        }
+      }
+    }
+    lb.add(lbf);
+    ln0.add(ln0f);
+    ln1.add(ln1f);
+  }
+  double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
+  pr[0] = (double)sx;
+  pr[Gp] = lb.value();
+  pr[2 * Gp] = ln0.value();
+  pr[3 * Gp] = ln1.value();
+}
+
+__global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
+  __shared__ float tab[PHI_TAB][GENE_TILE];
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_D[MAX_CG];
+  const int tid = threadIdx.x;
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int4 ch = s.gchunk[row];
+  const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + tid;
+  if (len == 0) return;
+  stage_chunk(s, start, len, s_i, s_D);
+  __syncthreads();
+  if (g >= s.G) return;
+  const float ph = s.phi[(int64_t)b * Gp + g];
+  const float pp = s.phi_p[(int64_t)b * Gp + g];
+  const float dl = pp - ph;
+  const float M = s.E[((int64_t)b * s.K + k) * Gp + g];
+  const float iph = 1.0f / ph;
+  // Per entry (BUSseq_gpu.cu:799-802, regrouped so that no large terms cancel):
+  //   t = [lgamma(pp+x) - lgamma(pp)] - [lgamma(ph+x) - lgamma(ph)]
+  //       - (pp + x) log((pp + mu) / (ph + mu)) + pp log(pp / ph) - dl log(1 + mu / ph)
+  const float lgd0 = lgamma_diff(ph, pp, dl);
+  const float c1 = pp * log_ratio(pp, ph, dl);
+  float h = 0.0f;
+  tab[0][tid] = 0.0f;
+  for (int x = 1; x < PHI_TAB; ++x) {
+    const float j = (float)(x - 1);
+    h += log_ratio(pp + j, ph + j, dl);
+    tab[x][tid] = h;
+  }
+  KahanF acc;
+  for (int j0 = 0; j0 < len; j0 += 8) {
+    int xr[8];
+    load8(s, s_i, j0, len, g, xr);
+    float f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (j0 + u < len) {
+        const int x = xr[u];
+        const float mu = M * s_D[j0 + u];
+        const float xf = (float)x;
+        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff(ph + xf, pp + xf, dl) - lgd0;
+        f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
+      }
+    }
+    acc.add(f);
+  }
+  s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
+}
+
+// ---------------------------------------------------------------------------
+// Decisions
+// ---------------------------------------------------------------------------
+// Sum of part slot `slot` of gene g over the chunks of segment (b, k).
+__device__ __forceinline__ double seg_sum(const DevState& s, int b, int k, int slot, int64_t g) {
+  const int2 r = s.seg_chunk[b * s.K + k];
+  double acc = 0.0;
+  for (int c = r.x; c < r.x + r.y; ++c) acc += __ldg(&s.part[((int64_t)c * NSLOT + slot) * s.Gp + g]);
+  return acc;
+}
+
+// gamma0 then gamma1 of batch b, one CTA (BUSseq_gpu.cu:514-600).
+__device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double* sh) {
+  double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = s.zfirst[b] + threadIdx.x; c < s.zfirst[b + 1]; c += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) v[q] += s.gpart[(int64_t)c * GSLOT + q];
+  }
+  const int slices = (s.ymax + ZX_THREADS - 1) / ZX_THREADS;
+  for (int c = b * slices + threadIdx.x; c < (b + 1) * slices && c < s.n_static; c += blockDim.x) {
+    v[6] += s.gstat[(int64_t)c * 4 + 0];
+    v[7] += s.gstat[(int64_t)c * 4 + 1];
+    v[8] += s.gstat[(int64_t)c * 4 + 2];
+  }
+  block_sum<9>(v, sh);
+  if (threadIdx.x != 0) return;
+  const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
+  const float g0p = s.gamma_p[b], g1p = s.gamma_p[s.B + b];
+  const double nZ = v[0], XZ = v[1], n0 = v[2];
+  // entries with Y == 0 and X == 0 all contribute softplus(g0p) - softplus(g0)
+  const double c0 = (double)softplus_diff(g0, g0p - g0);
+  const double lr0 = (double)(g0p - g0) * nZ - (v[3] + n0 * c0 + v[6]);
+  const double prior0 = ((double)g0 * g0 - (double)g0p * g0p) / (2.0 * SIGMA2_GAMMA0);
+  const float u0 = uniform_at(s.seed, SID_GAMMA, (uint64_t)b, iter, 2);
+  const bool acc0 = (double)logf(u0) <= lr0 + prior0;
+  s.lr_gamma[b] = lr0 + prior0;
+  if (acc0) s.gamma[b] = g0p;
+  const double lr1 = (double)(g1p - g1) * XZ - (acc0 ? (v[5] + v[8]) : (v[4] + v[7]));
+  // -gamma1 ~ Gamma(kappa, rate tau) prior, -10 gamma1 Gamma proposal (BUSseq_gpu.cu:588-600)
+  const double pv = -(double)g1, nv = -(double)g1p;
+  const double prior1 = (KAPPA_GAMMA1 - 1.0) * (log(nv) - log(pv)) + TAU_GAMMA1 * (pv - nv) - lgamma(10.0 * nv) +
+                        (10.0 * nv - 1.0) * log(pv) + 10.0 * nv * (log(10.0) + 1.0) + lgamma(10.0 * pv) -
+                        (10.0 * pv - 1.0) * log(nv) - 10.0 * pv * (log(10.0) + 1.0);
+  const float u1 = uniform_at(s.seed, SID_GAMMA, (uint64_t)b, iter, 3);
+  s.lr_gamma[s.B + b] = lr1 + prior1;
+  if ((double)logf(u1) <= lr1 + prior1) s.gamma[s.B + b] = g1p;
+}
+
+// Gene CTAs (blockIdx.x < n_tiles): alpha decisions and L; the last of them
+// draws p and tau0.  CTAs n_tiles .. n_tiles + B - 1: gamma of one batch.
+__global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
+  __shared__ double sh[(GENE_TILE / 32) * 9];
+  __shared__ int sh_flag;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int tid = threadIdx.x;
+  if ((int)blockIdx.x >= s.n_tiles) {
+    gamma_decide_cta(s, blockIdx.x - s.n_tiles, iter, sh);
+    return;
+  }
+  const int tile = blockIdx.x;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + tid;
+  double lv[2] = {0.0, 0.0};
+  if (g < s.G) {
+    double Sx = 0.0, La = 0.0;
+    for (int c = 0; c < s.cap_g; ++c) {
+      const bool used = s.gchunk[c].w > 0;
+      const double a0 = __ldg(&s.part[((int64_t)c * NSLOT + 0) * Gp + g]);
+      const double a1 = __ldg(&s.part[((int64_t)c * NSLOT + 1) * Gp + g]);
+      Sx += used ? a0 : 0.0;
+      La += used ? a1 : 0.0;
+    }
+    const float a = s.alpha[g], ap = s.alpha_p[g];
+    const double ma = s.mu_alpha[g];
+    const double lr = (double)(ap - a) * Sx - La;
+    const double prior = (((double)a - ma) * ((double)a - ma) - ((double)ap - ma) * ((double)ap - ma)) /
+                         (2.0 * SIGMA2_ALPHA);
+    const float ua = uniform_at(s.seed, SID_ALPHA, (uint64_t)g, iter, 2);
+    s.lr_alpha[g] = lr + prior;
+    if ((double)logf(ua) <= lr + prior) s.alpha[g] = ap;
+    // L from the current beta, p and tau0 (BUSseq_gpu.cu:634-648)
+    const float p = s.p_tau0[0], tau0 = s.p_tau0[1];
+    const float base = logf(p) - logf(1.0f - p) - (logf((float)TAU1) - logf(tau0)) * 0.5f;
+    const float qd = 1.0f / (2.0f * tau0) - 1.0f / (2.0f * (float)TAU1);
+    for (int kk = 1; kk < s.K; ++kk) {
+      const float bt = s.beta[(int64_t)kk * Gp + g];
+      const float lo = base + bt * bt * qd;
+      const float u = uniform_at(s.seed, SID_L, (uint64_t)(kk - 1) * (uint64_t)s.G + (uint64_t)g, iter, 0);
+      const int Lk = u > 1.0f / (1.0f + expf(lo)) ? 1 : 0;
+      s.L[(int64_t)kk * Gp + g] = (int8_t)Lk;
+      lv[0] += Lk;
+      if (!Lk) lv[1] += (double)bt * (double)bt;
+    }
+  }
+  block_sum<2>(lv, sh);
+  if (tid == 0) {
+    s.tpart[2 * tile] = lv[0];
+    s.tpart[2 * tile + 1] = lv[1];
+  }
+  if (!arrive_last(&s.cnt_glob[0], (unsigned)s.n_tiles, &sh_flag)) return;
+  if ((int)iter < s.n_unchanged) return;
+  // p ~ Beta(sum L + 1, G(K-1) - sum L + 3), tau0 = 1 / Gamma(...) (BUSseq_gpu.cu:650-668)
+  double v[2] = {0.0, 0.0};
+  for (int t = tid; t < s.n_tiles; t += blockDim.x) {
+    v[0] += __ldcg(&s.tpart[2 * t]);
+    v[1] += __ldcg(&s.tpart[2 * t + 1]);
+  }
+  block_sum<2>(v, sh);
+  if (tid == 0) {
+    const double cnt = v[0], bsq = v[1];
+    const double tot = (double)s.G * (double)(s.K - 1);
+    int err = 0;
+    Stream sp(s.seed, SID_P, 0, iter);
+    const float ga = gamma_mt(sp, (float)(cnt + A_P), &err);
+    const float gb = gamma_mt(sp, (float)(tot - cnt + B_P), &err);
+    s.p_tau0[0] = ga / (ga + gb);
+    Stream stt(s.seed, SID_TAU0, 0, iter);
+    const double shape = A_TAU0 + (tot - cnt) / 2.0;
+    const double rate = B_TAU0 + bsq / 2.0;
+    const float gt = gamma_mt(stt, (float)shape, &err);
+    s.p_tau0[1] = (float)(1.0 / ((double)gt * (1.0 / rate)));
+    if (err) atomicOr(s.err, err);
+  }
+}
+
+// beta_gk for k >= 1: one thread per (k, g) (BUSseq_gpu.cu:696-707).
+__global__ void k_decide_beta(DevState s) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = s.G, Gp = s.Gp;
+  if (t >= (int64_t)(s.K - 1) * G) return;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int k = 1 + (int)(t / G);
+  const int64_t g = t % G;
+  double Sx = 0.0, Lb = 0.0;
+  for (int b = 0; b < s.B; ++b) {
+    Sx += seg_sum(s, b, k, 0, g);
+    Lb += seg_sum(s, b, k, 1, g);
+  }
+  const int64_t pos = (int64_t)k * Gp + g;
+  const float bo = s.beta[pos], bn = s.beta_p[pos];
+  const double var = s.L[pos] == 1 ? TAU1 : (double)s.p_tau0[1];
+  const double lr = (double)(bn - bo) * Sx - Lb;
+  const double prior = ((double)bo * bo - (double)bn * bn) / (2.0 * var);
+  const float u = uniform_at(s.seed, SID_BETA, (uint64_t)t, iter, 2);
+  s.lr_beta[(int64_t)k * G + g] = lr + prior;
+  const bool acc = (double)logf(u) <= lr + prior;
+  if (acc) s.beta[pos] = bn;
+  s.beta_acc[pos] = acc ? 1 : 0;
+}
+
+// nu_bg for b >= 1 (BUSseq_gpu.cu:730-737), then E[b][.][g] for every b.
+__global__ void k_decide_nu_E(DevState s) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = s.G, Gp = s.Gp;
+  if (t >= (int64_t)s.B * G) return;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int b = (int)(t / G);
+  const int64_t g = t % G;
+  const int64_t pos = (int64_t)b * Gp + g;
+  if (b > 0) {
+    double Sx = 0.0, Ln = 0.0;
+    for (int k = 0; k < s.K; ++k) {
+      Sx += seg_sum(s, b, k, 0, g);
+      const bool bacc = k > 0 && s.beta_acc[(int64_t)k * Gp + g];
+      Ln += seg_sum(s, b, k, bacc ? 3 : 2, g);
+    }
+    const float vo = s.nu[pos], vn = s.nu_p[pos];
+    const double mn = s.mu_nu[b];
+    const double lr = (double)(vn - vo) * Sx - Ln;
+    const double prior = (((double)vo - mn) * ((double)vo - mn) - ((double)vn - mn) * ((double)vn - mn)) /
+                         (2.0 * SIGMA2_NU);
+    const float u = uniform_at(s.seed, SID_NU, (uint64_t)(b - 1) * (uint64_t)G + (uint64_t)g, iter, 2);
+    s.lr_nu[(int64_t)b * G + g] = lr + prior;
+    if ((double)logf(u) <= lr + prior) s.nu[pos] = vn;
+  }
+  const float a = s.alpha[g], nv = s.nu[pos];
+  for (int k = 0; k < s.K; ++k)
+    s.E[((int64_t)b * s.K + k) * Gp + g] = exp_sum3(a, s.beta[(int64_t)k * Gp + g], nv);
+}
+
+// phi_bg (BUSseq_gpu.cu:806-818).
+__global__ void k_decide_phi(DevState s) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = s.G, Gp = s.Gp;
+  if (t >= (int64_t)s.B * G) return;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int b = (int)(t / G);
+  const int64_t g = t % G;
+  double S = 0.0;
+  for (int k = 0; k < s.K; ++k) S += seg_sum(s, b, k, 0, g);
+  const int64_t pos = (int64_t)b * Gp + g;
+  const float ph = s.phi[pos], pp = s.phi_p[pos];
+  const float dl = pp - ph;
+  const double lgd0 = (double)lgamma_diff(ph, pp, dl);  // lgamma(pp) - lgamma(ph)
+  const double l1 = (double)log_ratio(pp, ph, dl);      // log(pp / ph)
+  const double lph = (double)logf(ph);
+  // Gamma(1, rate 0.1) prior and Gamma(phi, 1) proposal (BUSseq_gpu.cu:811-814)
+  const double prior = (1.0 - (double)ph) * l1 + (double)dl * lph + (1.0 - TAU_PHI) * (double)dl - lgd0;
+  const float u = uniform_at(s.seed, SID_PHI_ACC, (uint64_t)t, iter, 0);
+  s.lr_phi[(int64_t)b * G + g] = S + prior;
+  if ((double)logf(u) <= S + prior) s.phi[pos] = pp;
+}
+
+}  // namespace bq

@@ -15,18 +15,22 @@
 
 namespace bq {
 
-__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax) {
+__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax, int32_t* rowcnt) {
   const int64_t i = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __shared__ long long sh_sum[32];
   __shared__ int sh_max[32];
+  __shared__ int sh_cnt[32];
   long long sum = 0;
-  int mx = 0;
+  int mx = 0, nzero = 0;
   for (int64_t w = warp; w < s.Gw; w += nw) {
     const int64_t g = w * 32 + lane;
     const int y = g < s.G ? s.Y[i * s.Gp + g] : 1;
     const unsigned m = __ballot_sync(0xffffffffu, y == 0);
-    if (lane == 0) const_cast<uint32_t*>(s.y0m)[i * s.Gw + w] = m;
+    if (lane == 0) {
+      const_cast<uint32_t*>(s.y0m)[i * s.Gw + w] = m;
+      nzero += __popc(m);
+    }
     if (g < s.G) {
       sum += y;
       mx = max(mx, y);
@@ -36,15 +40,61 @@ __global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax) {
     sum += __shfl_down_sync(0xffffffffu, sum, o);
     mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
   }
-  if (lane == 0) { sh_sum[warp] = sum; sh_max[warp] = mx; }
+  if (lane == 0) { sh_sum[warp] = sum; sh_max[warp] = mx; sh_cnt[warp] = nzero; }
   __syncthreads();
   if (threadIdx.x == 0) {
     long long t = 0;
-    int m = 0;
-    for (int w = 0; w < nw; ++w) { t += sh_sum[w]; m = max(m, sh_max[w]); }
+    int m = 0, c = 0;
+    for (int w = 0; w < nw; ++w) { t += sh_sum[w]; m = max(m, sh_max[w]); c += sh_cnt[w]; }
     libsize[i] = t;
+    rowcnt[i] = c;
     atomicMax(ymax, m);
   }
+}
+
+// The list of entries with Y == 0, row by row: one warp per cell, 32 mask
+// words at a time, positions from a warp prefix sum of the words' popcounts.
+__global__ void k_zlist_fill(DevState s, const int64_t* rowoff, int2* zij) {
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= s.N) return;
+  const int lane = threadIdx.x & 31;
+  int64_t base = rowoff[i];
+  for (int64_t w0 = 0; w0 < s.Gw; w0 += 32) {
+    const int64_t w = w0 + lane;
+    const uint32_t m = w < s.Gw ? s.y0m[i * s.Gw + w] : 0u;
+    const int c = __popc(m);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int64_t pos = base + incl - c;
+    uint32_t mm = m;
+    while (mm) {
+      const int bit = __ffs(mm) - 1;
+      mm &= mm - 1u;
+      zij[pos++] = make_int2((int)i, (int)(w * 32 + bit));
+    }
+    base += __shfl_sync(0xffffffffu, incl, 31);
+  }
+}
+
+// zval[j] = Z bit of entry j from the bit mask (after a state upload).
+__global__ void k_zval_from_mask(DevState s) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= s.nz0) return;
+  const int2 ig = s.zij[j];
+  s.zval[j] = (uint8_t)((s.zm[(int64_t)ig.x * s.Gw + (ig.y >> 5)] >> (ig.y & 31)) & 1u);
+}
+
+// Bit mask from zval (the mask must be cleared first).
+__global__ void k_zmask_from_zval(DevState s) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= s.nz0) return;
+  if (!s.zval[j]) return;
+  const int2 ig = s.zij[j];
+  atomicOr(&s.zm[(int64_t)ig.x * s.Gw + (ig.y >> 5)], 1u << (ig.y & 31));
 }
 
 // Histogram of Y > 0 per batch; warp-aggregated so that repeated small values

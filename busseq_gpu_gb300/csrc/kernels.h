@@ -1,22 +1,31 @@
-// Kernel entry points (defined in sweep_kernels.cu and init_kernels.cu).
+// Kernel entry points (defined in gene_kernels.cu, cell_kernels.cu and
+// init_kernels.cu).
 #pragma once
 #include "busseq_dev.h"
 
 namespace bq {
 
 __global__ void k_propose(DevState s, int mask);
-__global__ void k_zx_alpha(DevState s);
+__global__ void k_zx(DevState s);
+__global__ void k_alpha(DevState s);
+__global__ void k_decide_alpha(DevState s);
 __global__ void k_beta_nu(DevState s);
-__global__ void k_delta(DevState s);
+__global__ void k_decide_beta(DevState s);
+__global__ void k_decide_nu_E(DevState s);
 __global__ void k_phi(DevState s);
+__global__ void k_decide_phi(DevState s);
+__global__ void k_delta(DevState s);
 __global__ void k_w_mh(DevState s);
 __global__ void k_w_gibbs(DevState s);
 __global__ void k_sort_pi(DevState s, int do_pi, int advance);
 __global__ void k_posterior(DevState s, int advance);
 int64_t propose_count(const DevState& s);
 
-__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax);
+__global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax, int32_t* rowcnt);
 __global__ void k_init_hist(DevState s, int32_t* hist);
+__global__ void k_zlist_fill(DevState s, const int64_t* rowoff, int2* zij);
+__global__ void k_zval_from_mask(DevState s);
+__global__ void k_zmask_from_zval(DevState s);
 __global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell);
 __global__ void k_init_raw(DevState s);
 __global__ void k_init_finish(DevState s, int fresh);
