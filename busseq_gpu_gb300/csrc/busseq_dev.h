@@ -53,7 +53,7 @@ constexpr int MAX_B = 128;
 constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
-constexpr int PHI_TAB = 16;        // small-count table of lgamma differences
+constexpr int PHI_TAB = 32;        // small-count table of lgamma differences
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
 constexpr int ZX_PER_CTA = 1024;   // zero entries per Z/X CTA
 

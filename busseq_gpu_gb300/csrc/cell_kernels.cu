@@ -11,26 +11,46 @@ namespace bq {
 // ---------------------------------------------------------------------------
 // Cell passes: one CTA per tile of <= CELL_TILE cells of one (batch, type)
 // ---------------------------------------------------------------------------
-// Sums over the CTA of CELL_TILE per-thread doubles; results in sh_out[r].
-__device__ __forceinline__ void cell_reduce(double (&acc)[CELL_TILE], double* sh, double* sh_out) {
+// Sums over the CTA of CELL_TILE per-thread float-float values; results in
+// sh_out[r].  `sh` holds (blockDim.x / 32) * CELL_TILE pairs.
+__device__ __forceinline__ void cell_reduce(FF (&acc)[CELL_TILE], FF* sh, FF* sh_out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int r = 0; r < CELL_TILE; ++r) {
-    const double v = warp_sum(acc[r]);
+    const FF v = ff_warp_sum(acc[r]);
     if (lane == 0) sh[warp * CELL_TILE + r] = v;
   }
   __syncthreads();
   if (threadIdx.x < CELL_TILE) {
-    double t = 0.0;
+    FF t = sh[threadIdx.x];
+    for (int w = 1; w < nw; ++w) t = ff_add(t, sh[w * CELL_TILE + threadIdx.x]);
+    sh_out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// Integer version of cell_reduce.
+__device__ __forceinline__ void cell_reduce_i(long long (&acc)[CELL_TILE], long long* sh, long long* sh_out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int r = 0; r < CELL_TILE; ++r) {
+    const long long v = i64_warp_sum(acc[r]);
+    if (lane == 0) sh[warp * CELL_TILE + r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < CELL_TILE) {
+    long long t = 0;
     for (int w = 0; w < nw; ++w) t += sh[w * CELL_TILE + threadIdx.x];
     sh_out[threadIdx.x] = t;
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
-  __shared__ double sh[(CELL_THREADS / 32) * CELL_TILE];
-  __shared__ double sh_l[CELL_TILE], sh_x[CELL_TILE];
+__global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
+  __shared__ FF sh[(CELL_THREADS / 32) * CELL_TILE];
+  __shared__ long long shi[(CELL_THREADS / 32) * CELL_TILE];
+  __shared__ FF sh_l[CELL_TILE];
+  __shared__ long long sh_x[CELL_TILE];
   __shared__ int sh_i[CELL_TILE];
   __shared__ float sh_D[CELL_TILE], sh_c[CELL_TILE];
   const int4 t = s.ctile[blockIdx.x];
@@ -46,7 +66,9 @@ __global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
     sh_c[tid] = tid < len ? expm1f(s.delta_p[i] - s.delta[i]) : 0.0f;
   }
   __syncthreads();
-  KahanF acc[CELL_TILE];
+  float acc[CELL_TILE];
+#pragma unroll
+  for (int r = 0; r < CELL_TILE; ++r) acc[r] = 0.0f;
   int sxi[CELL_TILE];
 #pragma unroll
   for (int r = 0; r < CELL_TILE; ++r) sxi[r] = 0;
@@ -70,21 +92,22 @@ __global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
             sxi[r] += xs[q];
           }
         }
-        acc[r].add(a);
+        acc[r] += a;
       }
     }
   }
-  double al[CELL_TILE], ax[CELL_TILE];
+  FF al[CELL_TILE];
+  long long ax[CELL_TILE];
 #pragma unroll
-  for (int r = 0; r < CELL_TILE; ++r) { al[r] = acc[r].value(); ax[r] = (double)sxi[r]; }
+  for (int r = 0; r < CELL_TILE; ++r) { al[r] = FF{acc[r], 0.0f}; ax[r] = sxi[r]; }
   cell_reduce(al, sh, sh_l);
-  cell_reduce(ax, sh, sh_x);
+  cell_reduce_i(ax, shi, sh_x);
   if (tid < len) {
     const int i = sh_i[tid];
     if (i != s.batch_off[b]) {  // the first cell of each batch keeps delta = 0
       const float d = s.delta[i], dp = s.delta_p[i];
       const double md = s.mu_delta[i];
-      const double lr = (double)(dp - d) * sh_x[tid] - sh_l[tid];
+      const double lr = (double)(dp - d) * (double)sh_x[tid] - ff_value(sh_l[tid]);
       const double prior = (((double)d - md) * ((double)d - md) - ((double)dp - md) * ((double)dp - md)) /
                            (2.0 * SIGMA2_DELTA);
       const float u = uniform_at(s.seed, SID_DELTA, (uint64_t)i, iter, 2);
@@ -98,18 +121,17 @@ __global__ void __launch_bounds__(CELL_THREADS) k_delta(DevState s) {
 }
 
 // Log-likelihood change of one entry when its type moves and beta changes by
-// eps:  eps x - (phi + x) log[(phi + mu e^eps) / (phi + mu)].
-__device__ __forceinline__ float type_shift_term(float eps, float mu, float ph, int x) {
-  float lg;
-  if (fabsf(eps) < 0.5f) lg = log1p_fast(expm1f(eps) * fast_div(mu, ph + mu));
-  else lg = logf(ph + mu * expf(eps)) - logf(ph + mu);
-  return eps * (float)x - (ph + (float)x) * lg;
+// eps = beta' - beta:  eps x - (phi + x) log[(phi + mu') / (phi + mu)], with
+// mu' = mu e^eps read from the table exp(alpha + beta + nu) of the new type.
+__device__ __forceinline__ float type_shift_term(float eps, float mu, float mup, float ph, int x) {
+  const float xf = (float)x;
+  return fmaf(eps, xf, -(ph + xf) * log_ratio(ph + mup, ph + mu, mup - mu));
 }
 
 // W by Metropolis-Hastings with a uniform proposal (the reference's move).
-__global__ void __launch_bounds__(CELL_THREADS) k_w_mh(DevState s) {
-  __shared__ double sh[(CELL_THREADS / 32) * CELL_TILE];
-  __shared__ double sh_l[CELL_TILE];
+__global__ void __launch_bounds__(CELL_THREADS, 4) k_w_mh(DevState s) {
+  __shared__ FF sh[(CELL_THREADS / 32) * CELL_TILE];
+  __shared__ FF sh_l[CELL_TILE];
   __shared__ int sh_i[CELL_TILE], sh_kp[CELL_TILE];
   __shared__ float sh_D[CELL_TILE], sh_u[CELL_TILE];
   const int4 t = s.ctile[blockIdx.x];
@@ -128,37 +150,41 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_mh(DevState s) {
     sh_u[tid] = st.uniform();
   }
   __syncthreads();
-  KahanF acc[CELL_TILE];
-  const float* Er = s.E + ((int64_t)b * s.K + k) * Gp;
+  float acc[CELL_TILE];
+#pragma unroll
+  for (int r = 0; r < CELL_TILE; ++r) acc[r] = 0.0f;
+  const float* Eb = s.E + (int64_t)b * s.K * Gp;
+  const float* Er = Eb + (int64_t)k * Gp;
   const float* Pr = s.phi + (int64_t)b * Gp;
   const float* Bk = s.beta + (int64_t)k * Gp;
-  for (int64_t g4 = (int64_t)tid * 4; g4 < Gp; g4 += (int64_t)CELL_THREADS * 4) {
-    const float4 e = *reinterpret_cast<const float4*>(Er + g4);
-    const float4 ph = *reinterpret_cast<const float4*>(Pr + g4);
-    const float4 bk = *reinterpret_cast<const float4*>(Bk + g4);
-    const float ev[4] = {e.x, e.y, e.z, e.w}, pv[4] = {ph.x, ph.y, ph.z, ph.w}, bv[4] = {bk.x, bk.y, bk.z, bk.w};
-#pragma unroll
+  // two genes per thread and step (64-bit loads) keep the eight cells' loads
+  // within the register budget of three CTAs per SM
+  for (int64_t g2 = (int64_t)tid * 2; g2 < Gp; g2 += (int64_t)CELL_THREADS * 2) {
+    const float2 e = *reinterpret_cast<const float2*>(Er + g2);
+    const float2 ph = *reinterpret_cast<const float2*>(Pr + g2);
+    const float2 bk = *reinterpret_cast<const float2*>(Bk + g2);
+    const bool two = g2 + 1 < G;
+#pragma unroll 4
     for (int r = 0; r < CELL_TILE; ++r) {
-      if (r < len && sh_kp[r] != k) {
-        const float4 bp = *reinterpret_cast<const float4*>(s.beta + (int64_t)sh_kp[r] * Gp + g4);
-        const int4 xv = *reinterpret_cast<const int4*>(s.X + (int64_t)sh_i[r] * Gp + g4);
-        const float bpv[4] = {bp.x, bp.y, bp.z, bp.w};
-        const int xs[4] = {xv.x, xv.y, xv.z, xv.w};
-        float a = 0.0f;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (g4 + q < G) a += type_shift_term(bpv[q] - bv[q], ev[q] * sh_D[r], pv[q], xs[q]);
-        acc[r].add(a);
+      if (r < len && sh_kp[r] != k && g2 < G) {
+        const int64_t kp_off = (int64_t)sh_kp[r] * Gp + g2;
+        const float2 bp = *reinterpret_cast<const float2*>(s.beta + kp_off);
+        const float2 ep = *reinterpret_cast<const float2*>(Eb + kp_off);
+        const int2 xv = *reinterpret_cast<const int2*>(s.X + (int64_t)sh_i[r] * Gp + g2);
+        const float D = sh_D[r];
+        float a = type_shift_term(bp.x - bk.x, e.x * D, ep.x * D, ph.x, xv.x);
+        if (two) a += type_shift_term(bp.y - bk.y, e.y * D, ep.y * D, ph.y, xv.y);
+        acc[r] += a;
       }
     }
   }
-  double al[CELL_TILE];
+  FF al[CELL_TILE];
 #pragma unroll
-  for (int r = 0; r < CELL_TILE; ++r) al[r] = acc[r].value();
+  for (int r = 0; r < CELL_TILE; ++r) al[r] = FF{acc[r], 0.0f};
   cell_reduce(al, sh, sh_l);
   if (tid < len) {
     const int i = sh_i[tid], kp = sh_kp[tid];
-    const double rhs = (double)logf(s.pi[b * s.K + kp]) - (double)logf(s.pi[b * s.K + k]) + sh_l[tid];
+    const double rhs = (double)logf(s.pi[b * s.K + kp]) - (double)logf(s.pi[b * s.K + k]) + ff_value(sh_l[tid]);
     s.lr_W[i] = rhs;
     if ((double)logf(sh_u[tid]) <= rhs) s.W[i] = kp;
   }
@@ -170,7 +196,7 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_mh(DevState s) {
 constexpr int GIBBS_CELLS = 2;
 constexpr int GIBBS_TYPES = 8;
 __global__ void __launch_bounds__(CELL_THREADS) k_w_gibbs(DevState s) {
-  __shared__ double sh_red[(CELL_THREADS / 32) * GIBBS_CELLS * GIBBS_TYPES];
+  __shared__ FF sh_red[(CELL_THREADS / 32) * GIBBS_CELLS * GIBBS_TYPES];
   __shared__ double sh_lp[CELL_TILE][MAX_K];
   __shared__ int sh_i[CELL_TILE];
   __shared__ float sh_D[CELL_TILE];
@@ -187,7 +213,8 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_gibbs(DevState s) {
     sh_D[tid] = s.Dexp[i];
   }
   __syncthreads();
-  const float* Er = s.E + ((int64_t)b * K + k) * Gp;
+  const float* Eb = s.E + (int64_t)b * K * Gp;
+  const float* Er = Eb + (int64_t)k * Gp;
   const float* Pr = s.phi + (int64_t)b * Gp;
   const float* Bk = s.beta + (int64_t)k * Gp;
   for (int r0 = 0; r0 < len; r0 += GIBBS_CELLS) {
@@ -195,17 +222,21 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_gibbs(DevState s) {
       KahanF acc[GIBBS_CELLS][GIBBS_TYPES];
       for (int64_t g = tid; g < G; g += CELL_THREADS) {
         const float e = Er[g], ph = Pr[g], bk = Bk[g];
-        float bt[GIBBS_TYPES];
+        float bt[GIBBS_TYPES], et[GIBBS_TYPES];
 #pragma unroll
-        for (int kk = 0; kk < GIBBS_TYPES; ++kk) bt[kk] = (k0 + kk < K) ? s.beta[(int64_t)(k0 + kk) * Gp + g] : bk;
+        for (int kk = 0; kk < GIBBS_TYPES; ++kk) {
+          bt[kk] = (k0 + kk < K) ? s.beta[(int64_t)(k0 + kk) * Gp + g] : bk;
+          et[kk] = (k0 + kk < K) ? Eb[(int64_t)(k0 + kk) * Gp + g] : e;
+        }
 #pragma unroll
         for (int r = 0; r < GIBBS_CELLS; ++r) {
           if (r0 + r < len) {
             const int x = s.X[(int64_t)sh_i[r0 + r] * Gp + g];
-            const float mu = e * sh_D[r0 + r];
+            const float D = sh_D[r0 + r];
+            const float mu = e * D;
 #pragma unroll
             for (int kk = 0; kk < GIBBS_TYPES; ++kk)
-              if (k0 + kk < K && k0 + kk != k) acc[r][kk].add(type_shift_term(bt[kk] - bk, mu, ph, x));
+              if (k0 + kk < K && k0 + kk != k) acc[r][kk].add(type_shift_term(bt[kk] - bk, mu, et[kk] * D, ph, x));
           }
         }
       }
@@ -213,15 +244,15 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_gibbs(DevState s) {
       for (int r = 0; r < GIBBS_CELLS; ++r)
 #pragma unroll
         for (int kk = 0; kk < GIBBS_TYPES; ++kk) {
-          const double v = warp_sum(acc[r][kk].value());
+          const FF v = ff_warp_sum(acc[r][kk].ff());
           if (lane == 0) sh_red[(warp * GIBBS_CELLS + r) * GIBBS_TYPES + kk] = v;
         }
       __syncthreads();
       if (tid < GIBBS_CELLS * GIBBS_TYPES) {
         const int r = tid / GIBBS_TYPES, kk = tid % GIBBS_TYPES;
-        double tsum = 0.0;
-        for (int w = 0; w < nw; ++w) tsum += sh_red[(w * GIBBS_CELLS + r) * GIBBS_TYPES + kk];
-        if (r0 + r < len && k0 + kk < K) sh_lp[r0 + r][k0 + kk] = tsum;
+        FF tsum = sh_red[r * GIBBS_TYPES + kk];
+        for (int w = 1; w < nw; ++w) tsum = ff_add(tsum, sh_red[(w * GIBBS_CELLS + r) * GIBBS_TYPES + kk]);
+        if (r0 + r < len && k0 + kk < K) sh_lp[r0 + r][k0 + kk] = ff_value(tsum);
       }
       __syncthreads();
     }

@@ -144,76 +144,180 @@ __device__ void gamma_static_cta(const DevState& s, int sidx, double* sh) {
   }
 }
 
-// One entry: x is replaced by the new X, z receives the new Z.
-__device__ __forceinline__ void zx_entry(uint64_t seed, uint64_t ent, uint32_t iter, float mu, float phi, float g0,
-                                         float g1, float zthr, int& x, int& z, int* errp) {
-  Stream st(seed, SID_ZX, ent, iter);
-  z = x == 0 ? (st.uniform() > zthr) : 1;
-  if (z) {
-    int err = 0;
-    const int xn = negbin(st, mu, phi, &err);
-    const float u = st.uniform();
-    // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
-    const float lr = softplusf(-g0 - g1 * (float)x) - softplusf(-g0 - g1 * (float)xn);
-    if (logf(u) <= lr) x = xn;
-    if (err) atomicOr(errp, err);
-  } else {
-    x = 0;
+// The three gamma-statistic terms of one entry with X = x > 0 (BUSseq_gpu.cu:
+// 514-600): softplus(t + dg0) - softplus(t), softplus(t + d1) - softplus(t)
+// and softplus(tp + d1) - softplus(tp), t = g0 + g1 x, tp = g0' + g1 x,
+// d1 = (g1' - g1) x.
+struct GammaTerms {
+  float g0, g1, g0p, dg0, dg1;
+  __device__ __forceinline__ void add(int x, float w, float& d0, float& d1a, float& d1b) const {
+    const float xf = (float)x;
+    const float tt = fmaf(g1, xf, g0);
+    const float d1 = dg1 * xf;
+    d0 = fmaf(w, softplus_diff(tt, dg0), d0);
+    d1a = fmaf(w, softplus_diff(tt, d1), d1a);
+    d1b = fmaf(w, softplus_diff(fmaf(g1, xf, g0p), d1), d1b);
   }
-}
+};
 
 // Work unit: a run of <= ZX_PER_CTA list entries of one batch (built at
 // initialisation); CTAs past n_zcta evaluate the static gamma terms.
+//
+// Each warp takes 128 entries, draws Z for them, and packs the entries that
+// need a negative-binomial proposal into a warp-private shared-memory queue
+// (inversion draws from the front, Gamma-Poisson draws from the back, slots
+// from ballot prefix counts, so the order is deterministic).  The queued draws
+// then run on every lane.  The Philox block opened for the Z uniform is passed
+// along, so the NB draw continues the same stream without recomputing it.
+//
+// The gamma terms depend on the entry only through x, so values below ZX_HIST
+// are counted in a shared histogram and each bin's terms are evaluated once;
+// the MH ratio reads softplus(-g0 - g1 x) from a table for the same range.
+constexpr int ZX_WARPS = ZX_THREADS / 32;
+constexpr int ZX_PER_WARP = ZX_PER_CTA / ZX_WARPS;
+constexpr int ZX_PER_LANE = ZX_PER_WARP / 32;
+constexpr int ZX_HIST = 128;
+static_assert(ZX_HIST <= ZX_THREADS, "one thread per histogram bin");
+
 __global__ void __launch_bounds__(ZX_THREADS) k_zx(DevState s) {
   __shared__ double sh[(ZX_THREADS / 32) * 6];
+  __shared__ FF shf[ZX_WARPS * 3];
+  __shared__ long long shn[ZX_WARPS * 3];
+  __shared__ float q_mu[ZX_WARPS][ZX_PER_WARP], q_ph[ZX_WARPS][ZX_PER_WARP];
+  __shared__ int q_xo[ZX_WARPS][ZX_PER_WARP], q_e[ZX_WARPS][ZX_PER_WARP];
+  __shared__ uint32_t q_w[3][ZX_WARPS][ZX_PER_WARP];
+  __shared__ float sp_tab[ZX_HIST];
+  __shared__ int xhist[ZX_HIST];
   const int c = blockIdx.x;
   if (c >= s.n_zcta) {
     gamma_static_cta(s, c - s.n_zcta, sh);
     return;
   }
   const uint32_t iter = (uint32_t)*s.iter;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int2 run = s.zcta[c];
   const int b = s.zcta_batch[c];
   const int64_t Gp = s.Gp;
   const uint64_t G64 = (uint64_t)s.G;
-  const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
-  const float g0p = s.gamma_p[b], dg0 = g0p - g0, dg1 = s.gamma_p[s.B + b] - g1;
+  GammaTerms gt;
+  gt.g0 = s.gamma[b];
+  gt.g1 = s.gamma[s.B + b];
+  gt.g0p = s.gamma_p[b];
+  gt.dg0 = gt.g0p - gt.g0;
+  gt.dg1 = s.gamma_p[s.B + b] - gt.g1;
+  const float g0 = gt.g0, g1 = gt.g1;
   const float zthr = 1.0f / (1.0f + expf(g0));
-  int nz = 0, n0 = 0;
-  int64_t xz = 0;
+  const uint32_t k0 = (uint32_t)s.seed, k1 = (uint32_t)(s.seed >> 32);
+  if (tid < ZX_HIST) {
+    sp_tab[tid] = softplusf(-g0 - g1 * (float)tid);
+    xhist[tid] = 0;
+  }
+
+  // ---- Z for the warp's entries; queue the ones that need an NB draw -------
+  int n_inv = 0, n_gp = 0;
+  long long n0 = 0;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int u = 0; u < ZX_PER_LANE; ++u) {
+    const int e = warp * ZX_PER_WARP + u * 32 + lane;
+    bool need = false, inv = false;
+    float mu = 0.0f, ph = 1.0f;
+    int xo = 0;
+    uint32_t w1 = 0, w2 = 0, w3 = 0;
+    if (e < run.y) {
+      const int64_t j = (int64_t)run.x + e;
+      const int2 ig = s.zij[j];
+      const int64_t i = ig.x, g = ig.y;
+      mu = s.E[((int64_t)b * s.K + s.W[i]) * Gp + g] * s.Dexp[i];
+      ph = s.phi[(int64_t)b * Gp + g];
+      xo = s.X[i * Gp + g];
+      int z = 1;
+      if (xo == 0) {
+        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+        const U32x4 r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter},
+                                      k0, k1);
+        z = u32_to_unit(r.x) > zthr;
+        w1 = r.y;
+        w2 = r.z;
+        w3 = r.w;
+      }
+      if (z) {
+        need = true;
+        inv = negbin_use_inversion(mu, ph);
+      } else {
+        s.zval[j] = 0;  // Z = 0 and X stays 0
+        ++n0;
+      }
+    }
+    const unsigned mi = __ballot_sync(0xffffffffu, need && inv);
+    const unsigned mg = __ballot_sync(0xffffffffu, need && !inv);
+    if (need) {
+      const int slot = inv ? n_inv + __popc(mi & lt) : ZX_PER_WARP - 1 - (n_gp + __popc(mg & lt));
+      q_mu[warp][slot] = mu;
+      q_ph[warp][slot] = ph;
+      q_xo[warp][slot] = xo;
+      q_e[warp][slot] = e;
+      q_w[0][warp][slot] = w1;
+      q_w[1][warp][slot] = w2;
+      q_w[2][warp][slot] = w3;
+    }
+    n_inv += __popc(mi);
+    n_gp += __popc(mg);
+  }
+  __syncthreads();  // queues, sp_tab and xhist ready
+
+  // ---- the queued imputations: X ~ NB independence MH (BUSseq_gpu.cu:497-506)
+  const int nq = n_inv + n_gp;
+  long long nz = 0, xz = 0;
   float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-  for (int e = threadIdx.x; e < run.y; e += ZX_THREADS) {
+  for (int q = lane; q < nq; q += 32) {
+    const bool is_inv = q < n_inv;
+    const int slot = is_inv ? q : ZX_PER_WARP - 1 - (q - n_inv);
+    const int e = q_e[warp][slot];
+    const int xo = q_xo[warp][slot];
     const int64_t j = (int64_t)run.x + e;
     const int2 ig = s.zij[j];
-    const int64_t i = ig.x, g = ig.y;
-    const int k = s.W[i];
-    const float mu = s.E[((int64_t)b * s.K + k) * Gp + g] * s.Dexp[i];
-    const float ph = s.phi[(int64_t)b * Gp + g];
-    const int64_t pos = i * Gp + g;
-    const int xo = s.X[pos];
-    int x = xo, z = 0;
-    zx_entry(s.seed, (uint64_t)i * G64 + (uint64_t)g, iter, mu, ph, g0, g1, zthr, x, z, s.err);
-    if (x != xo) s.X[pos] = x;
-    s.zval[j] = (uint8_t)z;
-    nz += z;
-    xz += (int64_t)x * z;
+    const uint64_t ent = (uint64_t)ig.x * G64 + (uint64_t)ig.y;
+    Stream st = xo == 0 ? Stream::resume1(s.seed, SID_ZX, ent, iter, q_w[0][warp][slot], q_w[1][warp][slot],
+                                          q_w[2][warp][slot])
+                        : Stream(s.seed, SID_ZX, ent, iter);
+    int err = 0;
+    const float mu = q_mu[warp][slot], ph = q_ph[warp][slot];
+    const int xn = is_inv ? negbin_inversion(st, mu, ph, &err) : negbin_gamma_poisson(st, mu, ph, &err);
+    const float ua = st.uniform();
+    // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
+    const float spo = (unsigned)xo < (unsigned)ZX_HIST ? sp_tab[xo] : softplusf(-g0 - g1 * (float)xo);
+    const float spn = (unsigned)xn < (unsigned)ZX_HIST ? sp_tab[xn] : softplusf(-g0 - g1 * (float)xn);
+    const int x = log_fast(ua) <= spo - spn ? xn : xo;
+    if (err) atomicOr(s.err, err);
+    if (x != xo) s.X[(int64_t)ig.x * Gp + ig.y] = x;
+    s.zval[j] = 1;
+    ++nz;
+    xz += x;
     if (x == 0) {
       ++n0;
+    } else if (x < ZX_HIST) {
+      atomicAdd(&xhist[x], 1);
     } else {
-      const float xf = (float)x;
-      const float tt = fmaf(g1, xf, g0);
-      const float d1 = dg1 * xf;
-      d0 += softplus_diff(tt, dg0);
-      d1a += softplus_diff(tt, d1);
-      d1b += softplus_diff(fmaf(g1, xf, g0p), d1);
+      gt.add(x, 1.0f, d0, d1a, d1b);
     }
   }
-  double v[6] = {(double)nz, (double)xz, (double)n0, (double)d0, (double)d1a, (double)d1b};
-  block_sum<6>(v, sh);
-  if (threadIdx.x == 0) {
+  __syncthreads();  // histogram complete
+  if (tid > 0 && tid < ZX_HIST) {
+    const int cnt = xhist[tid];
+    if (cnt) gt.add(tid, (float)cnt, d0, d1a, d1b);
+  }
+  FF f[3] = {FF{d0, 0.0f}, FF{d1a, 0.0f}, FF{d1b, 0.0f}};
+  long long n[3] = {nz, xz, n0};
+  block_sum_ff<3, 3>(f, n, shf, shn);
+  if (tid == 0) {
     double* gp = s.gpart + (int64_t)c * GSLOT;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) gp[q] = v[q];
+    gp[0] = (double)n[0];
+    gp[1] = (double)n[1];
+    gp[2] = (double)n[2];
+    gp[3] = ff_value(f[0]);
+    gp[4] = ff_value(f[1]);
+    gp[5] = ff_value(f[2]);
   }
 }
 
@@ -368,7 +472,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
         const int x = xr[u];
         const float mu = M * s_D[j0 + u];
         const float xf = (float)x;
-        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff(ph + xf, pp + xf, dl) - lgd0;
+        // x >= PHI_TAB >= 8: both arguments are past the shift range
+        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
         f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
       }
     }

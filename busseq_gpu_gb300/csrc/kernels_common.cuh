@@ -44,6 +44,77 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Float-float sums.  GB300 runs FP64 at a small fraction of the FP32 rate, so
+// the sweep kernels reduce in unevaluated pairs hi + lo of floats (about 48
+// significant bits): Knuth's TwoSum gives the exact rounding error of hi + hi',
+// which is folded into lo, and a final Fast2Sum renormalises the pair.  The
+// reduction trees have a fixed shape, so the sums are bit-reproducible.
+// ---------------------------------------------------------------------------
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  const float e = (a.hi - (s - v)) + (b.hi - v);
+  const float t = e + (a.lo + b.lo);
+  const float hi = s + t;
+  return FF{hi, t - (hi - s)};
+}
+
+__device__ __forceinline__ double ff_value(FF v) { return (double)v.hi + (double)v.lo; }
+
+__device__ __forceinline__ FF ff_warp_sum(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const FF w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    v = ff_add(v, w);
+  }
+  return v;
+}
+
+__device__ __forceinline__ long long i64_warp_sum(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// CTA sums of NF float-float and NI integer values per thread; results valid
+// in thread 0.  `shf` holds (blockDim.x / 32) * NF pairs, `shn`
+// (blockDim.x / 32) * NI integers.
+template <int NF, int NI>
+__device__ __forceinline__ void block_sum_ff(FF (&f)[NF], long long (&n)[NI], FF* shf, long long* shn) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NF; ++j) f[j] = ff_warp_sum(f[j]);
+#pragma unroll
+  for (int j = 0; j < NI; ++j) n[j] = i64_warp_sum(n[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < NF; ++j) shf[warp * NF + j] = f[j];
+#pragma unroll
+    for (int j = 0; j < NI; ++j) shn[warp * NI + j] = n[j];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NF; ++j) {
+      FF t = shf[j];
+      for (int w = 1; w < nw; ++w) t = ff_add(t, shf[w * NF + j]);
+      f[j] = t;
+    }
+#pragma unroll
+    for (int j = 0; j < NI; ++j) {
+      long long t = shn[j];
+      for (int w = 1; w < nw; ++w) t += shn[w * NI + j];
+      n[j] = t;
+    }
+  }
+  __syncthreads();
+}
+
 // Completion counter: every CTA of a group calls this once after its global
 // writes; it returns true in exactly one CTA (the last to arrive), which then
 // sees every other CTA's writes.  The last CTA resets the counter.
@@ -72,6 +143,7 @@ struct KahanF {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ FF ff() const { return FF{s, -c}; }
 };
 
 // log-likelihood shift of one NB entry when eta moves by eps, without the

@@ -25,6 +25,7 @@
 #pragma once
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define BQ_HD __host__ __device__ __forceinline__
@@ -124,6 +125,17 @@ struct Stream {
     return v;
   }
   BQ_HD float uniform() { return u32_to_unit(next_u32()); }
+  // The stream after its first uniform, given the other three words of block 0.
+  BQ_HD static Stream resume1(uint64_t seed, uint32_t sid, uint64_t entity, uint32_t iter, uint32_t w1, uint32_t w2,
+                              uint32_t w3) {
+    Stream s(seed, sid, entity, iter);
+    s.blk = 1;
+    s.b0 = w1;
+    s.b1 = w2;
+    s.b2 = w3;
+    s.n = 3;
+    return s;
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -153,25 +165,80 @@ BQ_HD float fast_div(float a, float b) {
 #endif
 }
 
-// log(1 + y) for y > -1.  For |y| < 1/2 it sums log1p(y) = 2 atanh(s),
-// s = y / (2 + y) (so |s| <= 1/3), as s (2 + t (2/3 + t (2/5 + ... + t 2/13)))
-// with t = s^2; the first omitted term is below 2e-8 relative.  Otherwise
-// log(1 + y), whose argument is exact for y in (-1, -1/2] and relatively
-// accurate for y >= 1/2.
+BQ_HD int float_bits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_int(x);
+#else
+  int i;
+  memcpy(&i, &x, sizeof i);
+  return i;
+#endif
+}
+
+BQ_HD float bits_float(int i) {
+#if defined(__CUDA_ARCH__)
+  return __int_as_float(i);
+#else
+  float x;
+  memcpy(&x, &i, sizeof x);
+  return x;
+#endif
+}
+
+// Logarithms without branches or library calls.  A positive normal float is
+// split as x = 2^e m with m in [sqrt(1/2), sqrt(2)) by integer arithmetic on
+// its bits (0x3F3504F3 is sqrt(1/2)); then
+//   log x = e log 2 + log m,   log m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...),
+//   s = (m - 1) / (m + 1),  |s| <= 0.1716,
+// summed to s^9 (the first omitted term is below 3e-9 relative), with log 2
+// split into a 16-bit head and a tail so that e log 2 carries no rounding.
+// log_mant takes f = m - 1, which callers may supply exactly.
+constexpr float LN2_HI = 0.693145751953125f;
+constexpr float LN2_LO = 1.42860682030941723212e-06f;
+constexpr int SQRT_HALF_BITS = 0x3F3504F3;
+
+BQ_HD float log_mant(float f, int e) {
+  const float s = fast_div(f, 2.0f + f);
+  const float t = s * s;
+  float p = 2.0f / 9.0f;
+  p = fmaf(p, t, 2.0f / 7.0f);
+  p = fmaf(p, t, 2.0f / 5.0f);
+  p = fmaf(p, t, 2.0f / 3.0f);
+  const float lm = fmaf(s * t, p, 2.0f * s);
+  const float ef = (float)e;
+  return fmaf(ef, LN2_HI, fmaf(ef, LN2_LO, lm));
+}
+
+BQ_HD int log_exponent(int bits) { return (bits - SQRT_HALF_BITS) >> 23; }
+
+// log x for a positive normal float x.
+BQ_HD float log_fast(float x) {
+  const int bits = float_bits(x);
+  const int e = log_exponent(bits);
+  return log_mant(bits_float(bits - (e << 23)) - 1.0f, e);
+}
+
+// log(1 + y) for y > -1.  While 1 + y lies in [sqrt(1/2), sqrt(2)) the
+// exponent is 0 and f = y is used as given, so small y loses nothing to the
+// rounding of 1 + y; outside that range |log(1 + y)| > 0.34 and the rounding
+// of 1 + y (2^-24 relative) is immaterial.
 BQ_HD float log1p_fast(float y) {
-  if (fabsf(y) < 0.5f) {
-    const float s = fast_div(y, 2.0f + y);
-    const float t = s * s;
-    float p = 2.0f / 13.0f;
-    p = fmaf(p, t, 2.0f / 11.0f);
-    p = fmaf(p, t, 2.0f / 9.0f);
-    p = fmaf(p, t, 2.0f / 7.0f);
-    p = fmaf(p, t, 2.0f / 5.0f);
-    p = fmaf(p, t, 2.0f / 3.0f);
-    p = fmaf(p, t, 2.0f);
-    return s * p;
-  }
-  return logf(1.0f + y);
+  const int bits = float_bits(1.0f + y);
+  const int e = log_exponent(bits);
+  const float f = e == 0 ? y : bits_float(bits - (e << 23)) - 1.0f;
+  return log_mant(f, e);
+}
+
+// log(a / b) for a, b > 0 given d = a - b.  With r = a / b: while r lies in
+// [sqrt(1/2), sqrt(2)) the mantissa argument is d / b (no cancellation for
+// a close to b); otherwise |log r| > 0.34 and r itself is relatively
+// accurate, including a << b.  One reciprocal serves both quotients.
+BQ_HD float log_ratio(float a, float b, float d) {
+  const float rb = fast_div(1.0f, b);
+  const int bits = float_bits(a * rb);
+  const int e = log_exponent(bits);
+  const float f = e == 0 ? d * rb : bits_float(bits - (e << 23)) - 1.0f;
+  return log_mant(f, e);
 }
 
 // log(k!) for integer-valued k >= 0: exact values below 16, Stirling's series
@@ -196,8 +263,8 @@ BQ_HD float log_factorial(float k) {
     return v;
   }
   const float x = k + 1.0f;
-  const float r = 1.0f / x;
-  return (x - 0.5f) * logf(x) - x + 0.918938533204672742f + r * (1.0f / 12.0f - (r * r) * (1.0f / 360.0f));
+  const float r = fast_div(1.0f, x);
+  return (x - 0.5f) * log_fast(x) - x + 0.918938533204672742f + r * (1.0f / 12.0f - (r * r) * (1.0f / 360.0f));
 }
 
 // ---------------------------------------------------------------------------
@@ -207,7 +274,7 @@ BQ_HD float log_factorial(float k) {
 BQ_HD float normal(Stream& s) {
   const float u1 = s.uniform();
   const float u2 = s.uniform();
-  return sqrtf(-2.0f * logf(u1)) * cospi2f(u2);
+  return sqrtf(-2.0f * log_fast(u1)) * cospi2f(u2);
 }
 
 // Gamma(shape a, scale 1), Marsaglia and Tsang (2000).  Each try consumes a
@@ -229,12 +296,12 @@ BQ_HD float gamma_mt(Stream& s, float a, int* err) {
     const float u = s.uniform();
     const float z2 = z * z;
     if (u < 1.0f - 0.0331f * (z2 * z2)) { x = d * v; break; }
-    if (logf(u) < 0.5f * z2 + d * (1.0f - v + logf(v))) { x = d * v; break; }
+    if (log_fast(u) < 0.5f * z2 + d * (1.0f - v + log_fast(v))) { x = d * v; break; }
   }
   if (it == GAMMA_MAX_ITER) *err |= ERR_GAMMA_CAP;
   if (boost) {
     const float u = s.uniform();
-    x = x * expf(logf(u) / a);
+    x = x * expf(fast_div(log_fast(u), a));
   }
   return x;
 }
@@ -251,7 +318,7 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
     int k = 0;
     while (u > F && k < POISSON_INV_MAX_K) {
       ++k;
-      p = p * (lam / (float)k);
+      p = p * fast_div(lam, (float)k);
       const float Fn = F + p;
       if (Fn == F) break;  // the cumulative sum stopped growing
       F = Fn;
@@ -259,7 +326,7 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
     return k;
   }
   const float slam = sqrtf(lam);
-  const float loglam = logf(lam);
+  const float loglam = log_fast(lam);
   const float b = 0.931f + 2.53f * slam;
   const float a = -0.059f + 0.02483f * b;
   const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
@@ -268,10 +335,10 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
     const float U = s.uniform() - 0.5f;
     const float V = s.uniform();
     const float us = 0.5f - fabsf(U);
-    const float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+    const float kf = floorf((fast_div(2.0f * a, us) + b) * U + lam + 0.43f);
     if (us >= 0.07f && V <= vr) return (int)kf;
     if (kf < 0.0f || (us < 0.013f && V > us)) continue;
-    const float lhs = logf(V) + logf(invalpha) - logf(a / (us * us) + b);
+    const float lhs = log_fast(fast_div(V * invalpha, fast_div(a, us * us) + b));
     const float rhs = -lam + kf * loglam - log_factorial(kf);
     if (lhs <= rhs) return (int)kf;
   }
@@ -279,48 +346,89 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
   return (int)lam;
 }
 
-// Negative binomial with mean mu and size phi, as Gamma(phi, mu/phi) then
-// Poisson (the reference's rnbinom, BUSseq_gpu.cu:199-210).
-BQ_HD int negbin(Stream& s, float mu, float phi, int* err) {
+// Negative binomial with mean mu and size phi.
+//  * mu < NB_INV_MU and phi >= 1: inversion of the NB distribution function
+//    with one uniform, P(0) = (phi / (phi + mu))^phi and
+//    P(x+1) = P(x) (phi + x) / (x + 1) * mu / (phi + mu);
+//  * otherwise Gamma(phi, mu/phi) then Poisson, as the reference's rnbinom
+//    (BUSseq_gpu.cu:199-210).
+// Both draw exactly from NB(mu, phi); the switch keeps the common small-mean
+// draws to one uniform and a short loop.
+constexpr float NB_INV_MU = 16.0f;
+constexpr int NB_INV_MAX_K = 1024;
+enum : int { ERR_NB_INV_CAP = 4 };
+
+BQ_HD bool negbin_use_inversion(float mu, float phi) { return mu < NB_INV_MU && phi >= 1.0f; }
+
+BQ_HD int negbin_inversion(Stream& s, float mu, float phi, int* err) {
+  const float q = mu / (phi + mu);
+  float p = expf(phi * log1p_fast(-q));
+  float F = p;
+  const float u = s.uniform();
+  int k = 0;
+  while (u > F) {
+    if (k >= NB_INV_MAX_K) { *err |= ERR_NB_INV_CAP; break; }
+    p = p * (q * fast_div(phi + (float)k, (float)(k + 1)));
+    ++k;
+    const float Fn = F + p;
+    if (Fn == F) break;  // the distribution function stopped growing
+    F = Fn;
+  }
+  return k;
+}
+
+BQ_HD int negbin_gamma_poisson(Stream& s, float mu, float phi, int* err) {
   const float g = gamma_mt(s, phi, err);
   return poisson(s, g * (mu / phi), err);
+}
+
+BQ_HD int negbin(Stream& s, float mu, float phi, int* err) {
+  return negbin_use_inversion(mu, phi) ? negbin_inversion(s, mu, phi, err) : negbin_gamma_poisson(s, mu, phi, err);
 }
 
 // ---------------------------------------------------------------------------
 // Numerically stable differences used by every Metropolis ratio
 // ---------------------------------------------------------------------------
 BQ_HD float softplusf(float t) {
-  return t > 0.0f ? t + log1pf(expf(-t)) : log1pf(expf(t));
+  return t > 0.0f ? t + log1p_fast(expf(-t)) : log1p_fast(expf(t));
 }
 
 // softplus(t + dlt) - softplus(t) without cancellation.
 BQ_HD float softplus_diff(float t, float dlt) {
   if (fabsf(dlt) < 0.5f) {
     const float sig = 1.0f / (1.0f + expf(-t));
-    return log1pf(sig * expm1f(dlt));
+    return log1p_fast(sig * expm1f(dlt));
   }
   return softplusf(t + dlt) - softplusf(t);
 }
 
-// log(a / b) for a, b > 0 with d = a - b: log1p(d / b) while a and b are
-// within a factor of about two (then d carries no cancellation error),
-// otherwise the difference of the two logarithms, which stays accurate when
-// a << b (where 1 + d / b would cancel).
-BQ_HD float log_ratio(float a, float b, float d) {
-  return fabsf(d) < 0.5f * b ? log1p_fast(fast_div(d, b)) : logf(a) - logf(b);
+// log(a / b) as log_ratio, given rb = 1 / b.
+BQ_HD float log_ratio_rcp(float a, float rb, float d) {
+  const int bits = float_bits(a * rb);
+  const int e = log_exponent(bits);
+  const float f = e == 0 ? d * rb : bits_float(bits - (e << 23)) - 1.0f;
+  return log_mant(f, e);
 }
 
-// lgamma(zp) - lgamma(z) for z, zp > 0, dlt = zp - z, without cancellation.
-// For z, zp >= 8 it uses the difference of Stirling's series
-//   lgamma(z) = (z - 1/2) log z - z + log(2 pi)/2 + 1/(12z) - 1/(360z^3) + 1/(1260z^5) - ...
-// rearranged as (zp - 1/2) log(zp / z) + dlt (log z - 1) + S(zp) - S(z);
-// smaller arguments are shifted up with lgamma(x+1) = lgamma(x) + log x.
-BQ_HD float stirling_tail(float z) {
-  const float r = 1.0f / z;
-  const float r2 = r * r;
-  return r * (1.0f / 12.0f - r2 * (1.0f / 360.0f - r2 * (1.0f / 1260.0f)));
+// lgamma(zq) - lgamma(zz) for zz, zq >= 8, dlt = zq - zz, from the
+// difference of Stirling's series
+//   lgamma(z) = (z - 1/2) log z - z + log(2 pi)/2 + S(z),
+//   S(z) = 1/(12z) - 1/(360z^3) + 1/(1260z^5) - ...   (next term < 1e-9 at z = 8)
+// rearranged as (zq - 1/2) log(zq / zz) + dlt (log zz - 1) + S(zq) - S(zz).
+// With w = 1/(zq zz): 1/zq - 1/zz = -dlt w, and S(zq) - S(zz) factors as
+// -dlt w [1/12 - (q + w)/360 + (q^2 + w q - w^2)/1260], q = 1/zq^2 + 1/zz^2,
+// so no difference of nearly equal numbers is formed.
+BQ_HD float lgamma_diff_large(float zz, float zq, float dlt) {
+  const float w = fast_div(1.0f, zz * zq);
+  const float rz = zq * w, rq = zz * w;
+  const float q = fmaf(rq, rq, rz * rz);
+  const float poly = (1.0f / 12.0f) - (q + w) * (1.0f / 360.0f) + fmaf(q, q, w * (q - w)) * (1.0f / 1260.0f);
+  const float tail = -dlt * w * poly;
+  return fmaf(zq - 0.5f, log_ratio_rcp(zq, rz, dlt), fmaf(dlt, log_fast(zz) - 1.0f, tail));
 }
 
+// lgamma(zp) - lgamma(z) for z, zp > 0, dlt = zp - z, without cancellation:
+// arguments below 8 are shifted up with lgamma(x+1) = lgamma(x) + log x.
 BQ_HD float lgamma_diff(float z, float zp, float dlt) {
   float acc = 0.0f;
   float zz = z, zq = zp;
@@ -329,8 +437,7 @@ BQ_HD float lgamma_diff(float z, float zp, float dlt) {
     zz += 1.0f;
     zq += 1.0f;
   }
-  return acc + (zq - 0.5f) * log_ratio(zq, zz, dlt) + dlt * (logf(zz) - 1.0f) +
-         (stirling_tail(zq) - stirling_tail(zz));
+  return acc + lgamma_diff_large(zz, zq, dlt);
 }
 
 }  // namespace bq

@@ -206,7 +206,29 @@ static int poisson(Stream& s, double lam, double* mg) {
   return (int)lam;
 }
 
+// NB(mu, phi): inversion of the distribution function when mu < 16 and
+// phi >= 1 (one uniform), Gamma-Poisson otherwise; the same method switch as
+// the kernels, so both consume the same uniforms.
 static int negbin(Stream& s, double mu, double phi, double* mg) {
+  mark(mg, mu - 16.0, 16.0);
+  mark(mg, phi - 1.0, 1.0);
+  if (mu < 16.0 && phi >= 1.0) {
+    const double q = mu / (phi + mu);
+    double p = exp(phi * log1p(-q));
+    double F = p;
+    const double u = s.unif();
+    int k = 0;
+    for (;;) {
+      mark(mg, u - F, 1.0);
+      if (!(u > F) || k >= 1024) break;
+      p = p * (q * ((phi + (double)k) / (double)(k + 1)));
+      ++k;
+      const double Fn = F + p;
+      if (Fn == F) break;
+      F = Fn;
+    }
+    return k;
+  }
   const double g = gamma_mt(s, phi, mg);
   return poisson(s, g * (mu / phi), mg);
 }

@@ -4,7 +4,12 @@ Tolerances (single-precision kernels against a double-precision oracle that
 consumes the same uniforms):
   * float parameters where both sides took the same decision: rtol 1e-5,
     atol 1e-6 (the kernels store parameters in float);
-  * log acceptance ratios: |lr_gpu - lr_orc| <= 2e-3 + 2e-5 |lr_orc|;
+  * log acceptance ratios: |lr_gpu - lr_orc| <= 5e-3 + 5e-5 |lr_orc|.  The
+    kernels evaluate each entry's term in float; its pieces can be ten times
+    the term itself, so float rounding of about 1e-6 |step| per entry adds up
+    to ~1e-3 over a few hundred cells.  A formula error (for instance the
+    cancellation of log1p(d/b) when a Gamma proposal lands far below phi) shows
+    up as 0.1 to 2 nats and fails this bound;
   * a Metropolis decision may differ only where log(u) lies between the two
     log ratios, i.e. the oracle's margin |log u - lr_orc| <= |lr_gpu - lr_orc|;
   * integer draws (X, Z, L, W, ...) must be bit-exact except where the oracle
@@ -19,8 +24,8 @@ from oracle import pyoracle as po
 
 RTOL = 1e-5
 ATOL = 1e-6
-LR_ATOL = 2e-3
-LR_RTOL = 2e-5
+LR_ATOL = 5e-3
+LR_RTOL = 5e-5
 TIE_TOL = 3e-5
 
 

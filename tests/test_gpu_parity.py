@@ -11,7 +11,7 @@ import pytest
 
 import busseq_gpu_gb300 as bq
 from oracle import pyoracle as po
-from tests.parity_util import check_discrete, check_mh, oracle_state
+from tests.parity_util import LR_ATOL, LR_RTOL, check_discrete, check_mh, oracle_state
 
 pytestmark = pytest.mark.gpu
 
@@ -143,7 +143,7 @@ def test_stage_W_mh(case):
     d = po.Debug(o)
     o.step("W", it, w_update=0, debug=d)
     dlr = np.abs(lr["W"] - d.lr_W)
-    assert np.all(dlr <= 2e-3 + 2e-5 * np.abs(d.lr_W)), dlr.max()
+    assert np.all(dlr <= LR_ATOL + LR_RTOL * np.abs(d.lr_W)), dlr.max()
     flip = g["W"] != o.W
     assert np.all(d.mg_W[flip] <= dlr[flip] + 1e-6), (np.flatnonzero(flip), d.mg_W[flip], dlr[flip])
     print(c["name"], "W moved", int((g["W"] != st0["W"]).sum()), "flips", int(flip.sum()), "max dlr", dlr.max())
