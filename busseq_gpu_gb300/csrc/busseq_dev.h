@@ -49,6 +49,13 @@ constexpr int GENE_TILE = 128;     // genes per gene-pass CTA (one per thread)
 constexpr int MAX_CG = 256;        // largest gene-pass chunk (cells staged in shared memory)
 constexpr int CELL_TILE = 8;       // cells per cell-pass CTA
 constexpr int CELL_THREADS = 256;  // threads of a cell-pass CTA (4 genes each per step)
+// Cell passes stream the tile's X rows through shared memory in X_STAGES
+// stages of DELTA_WIDTH (delta) or W_WIDTH (W) genes.
+constexpr int X_STAGES = 2;
+constexpr int DELTA_WIDTH = 4 * CELL_THREADS;
+constexpr int W_WIDTH = 2 * CELL_THREADS;
+constexpr int DELTA_SMEM = X_STAGES * CELL_TILE * DELTA_WIDTH * (int)sizeof(int);
+constexpr int W_SMEM = X_STAGES * CELL_TILE * W_WIDTH * (int)sizeof(int);
 constexpr int MAX_B = 128;
 constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)

@@ -105,7 +105,10 @@ int check_device_error(busseq_handle* h) {
   int err = 0;
   CUDA_TRY(cudaMemcpy(&err, h->s.err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
-    return fail(BUSSEQ_ERR_SAMPLER, "a device rejection sampler reached its iteration cap (flags 0x%x)", err);
+    return fail(BUSSEQ_ERR_SAMPLER,
+                "a device-side bound was reached (flags 0x%x: 1 Gamma, 2 Poisson and 4 NB sampler caps, "
+                "8 shared-memory copy wait)",
+                err);
   }
   return BUSSEQ_OK;
 }
@@ -145,7 +148,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_decide_nu_E");
       break;
     case 7:
-      k_delta<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
+      k_delta<<<s.cap_c, CELL_THREADS, DELTA_SMEM, st>>>(s);
       LAUNCH_CHECK("k_delta");
       break;
     case 8:
@@ -158,7 +161,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       break;
     case 10:
       if (s.w_update == BUSSEQ_W_GIBBS) k_w_gibbs<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
-      else k_w_mh<<<s.cap_c, CELL_THREADS, 0, st>>>(s);
+      else k_w_mh<<<s.cap_c, CELL_THREADS, W_SMEM, st>>>(s);
       LAUNCH_CHECK("k_w");
       break;
     case 11:
@@ -281,6 +284,9 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
   else opt.p0 = 0.25;
   if (!(opt.p0 > 0.0 && opt.p0 < 1.0)) return fail(BUSSEQ_ERR_ARG, "p0 must be in (0, 1)");
   CUDA_TRY(cudaSetDevice(opt.device));
+  // the delta pass stages 64 KB of X rows per CTA (above the 48 KB default)
+  CUDA_TRY(cudaFuncSetAttribute(bq::k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, bq::DELTA_SMEM));
+  CUDA_TRY(cudaFuncSetAttribute(bq::k_w_mh, cudaFuncAttributeMaxDynamicSharedMemorySize, bq::W_SMEM));
 
   busseq_handle* h = new busseq_handle();
   h->device = opt.device;

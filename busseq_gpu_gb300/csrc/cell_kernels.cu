@@ -46,7 +46,68 @@ __device__ __forceinline__ void cell_reduce_i(long long (&acc)[CELL_TILE], long 
   __syncthreads();
 }
 
+// X rows of a cell tile, streamed through shared memory: a ring of NST stages,
+// each holding the tile's rows over WIDTH consecutive genes, filled by bulk
+// asynchronous copies that thread 0 issues NST stages ahead of the compute.
+// Row starts are 16-byte aligned (Gp is a multiple of GENE_TILE) and every
+// copy is a multiple of 16 bytes.
+template <int WIDTH, int NST>
+struct XRowRing {
+  int* buf;       // [NST][CELL_TILE][WIDTH]
+  uint64_t* bar;  // [NST]
+  const int* X;
+  const int* rows;  // the tile's cell indices (shared memory)
+  int64_t Gp;
+  int len, n_steps;
+
+  static constexpr int bytes() { return NST * CELL_TILE * WIDTH * (int)sizeof(int); }
+
+  __device__ void init(int tid) {
+    if (tid == 0) {
+      for (int q = 0; q < NST; ++q) mbar_init(&bar[q], 1);
+      mbar_init_fence();
+    }
+  }
+  __device__ void issue(int step) const {
+    const int st = step % NST;
+    const int64_t g0 = (int64_t)step * WIDTH;
+    const uint32_t nb = (uint32_t)((Gp - g0 < WIDTH ? Gp - g0 : WIDTH) * (int64_t)sizeof(int));
+    mbar_arrive_expect_tx(&bar[st], nb * (uint32_t)len);
+    for (int r = 0; r < len; ++r)
+      bulk_copy_g2s(buf + (st * CELL_TILE + r) * WIDTH, X + (int64_t)rows[r] * Gp + g0, nb, &bar[st]);
+  }
+  __device__ void prologue(int tid) const {
+    if (tid == 0)
+      for (int q = 0; q < NST && q < n_steps; ++q) issue(q);
+  }
+  __device__ bool wait(int step) { return mbar_wait(&bar[step % NST], (uint32_t)((step / NST) & 1)); }
+  __device__ const int* row(int step, int r) const { return buf + ((step % NST) * CELL_TILE + r) * WIDTH; }
+  // After every thread finished reading stage `step`: refill it.
+  __device__ void advance(int tid, int step) const {
+    if (tid == 0 && step + NST < n_steps) {
+      fence_proxy_async_smem();
+      issue(step + NST);
+    }
+  }
+  // Failure at `step`: flag it and let the copies in flight land before the
+  // CTA exits (bounded waits).
+  __device__ void abandon(int tid, int step, int* err) {
+    if (tid == 0) {
+      atomicOr(err, ERR_COPY_TIMEOUT);
+      const int issued = step + NST < n_steps ? step + NST : n_steps;
+      for (int q = step; q < issued; ++q) wait(q);
+    }
+    __syncthreads();
+  }
+};
+
+using DeltaRing = XRowRing<DELTA_WIDTH, X_STAGES>;
+using WRing = XRowRing<W_WIDTH, X_STAGES>;
+static_assert(DeltaRing::bytes() == DELTA_SMEM && WRing::bytes() == W_SMEM, "ring sizes");
+
 __global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
+  extern __shared__ __align__(128) int xbuf[];
+  __shared__ __align__(8) uint64_t bar[X_STAGES];
   __shared__ FF sh[(CELL_THREADS / 32) * CELL_TILE];
   __shared__ long long shi[(CELL_THREADS / 32) * CELL_TILE];
   __shared__ FF sh_l[CELL_TILE];
@@ -59,6 +120,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
   const int tid = threadIdx.x;
   const uint32_t iter = (uint32_t)*s.iter;
   const int64_t Gp = s.Gp, G = s.G;
+  DeltaRing ring{xbuf, bar, s.X, sh_i, Gp, len, (int)((Gp + DELTA_WIDTH - 1) / DELTA_WIDTH)};
+  ring.init(tid);
   if (tid < CELL_TILE) {
     const int i = s.perm[start + (tid < len ? tid : 0)];
     sh_i[tid] = i;
@@ -66,6 +129,7 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
     sh_c[tid] = tid < len ? expm1f(s.delta_p[i] - s.delta[i]) : 0.0f;
   }
   __syncthreads();
+  ring.prologue(tid);
   float acc[CELL_TILE];
 #pragma unroll
   for (int r = 0; r < CELL_TILE; ++r) acc[r] = 0.0f;
@@ -74,27 +138,40 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
   for (int r = 0; r < CELL_TILE; ++r) sxi[r] = 0;
   const float* Er = s.E + ((int64_t)b * s.K + k) * Gp;
   const float* Pr = s.phi + (int64_t)b * Gp;
-  for (int64_t g4 = (int64_t)tid * 4; g4 < Gp; g4 += (int64_t)CELL_THREADS * 4) {
-    const float4 e = *reinterpret_cast<const float4*>(Er + g4);
-    const float4 ph = *reinterpret_cast<const float4*>(Pr + g4);
-    const float ev[4] = {e.x, e.y, e.z, e.w}, pv[4] = {ph.x, ph.y, ph.z, ph.w};
+  for (int step = 0; step < ring.n_steps; ++step) {
+    const int64_t g4 = (int64_t)step * DELTA_WIDTH + tid * 4;
+    const bool in = g4 < Gp;
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f), ph = e;
+    if (in) {
+      e = *reinterpret_cast<const float4*>(Er + g4);
+      ph = *reinterpret_cast<const float4*>(Pr + g4);
+    }
+    const bool ok = ring.wait(step);
+    if (in) {
+      const float ev[4] = {e.x, e.y, e.z, e.w}, pv[4] = {ph.x, ph.y, ph.z, ph.w};
 #pragma unroll
-    for (int r = 0; r < CELL_TILE; ++r) {
-      if (r < len) {
-        const int4 xv = *reinterpret_cast<const int4*>(s.X + (int64_t)sh_i[r] * Gp + g4);
-        const int xs[4] = {xv.x, xv.y, xv.z, xv.w};
-        float a = 0.0f;
+      for (int r = 0; r < CELL_TILE; ++r) {
+        if (r < len) {
+          const int4 xv = *reinterpret_cast<const int4*>(ring.row(step, r) + tid * 4);
+          const int xs[4] = {xv.x, xv.y, xv.z, xv.w};
+          float a = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (g4 + q < G) {
-            const float mu = ev[q] * sh_D[r];
-            a += (pv[q] + (float)xs[q]) * log1p_fast(sh_c[r] * fast_div(mu, pv[q] + mu));
-            sxi[r] += xs[q];
+          for (int q = 0; q < 4; ++q) {
+            if (g4 + q < G) {
+              const float mu = ev[q] * sh_D[r];
+              a += (pv[q] + (float)xs[q]) * log1p_near0(sh_c[r] * fast_div(mu, pv[q] + mu));
+              sxi[r] += xs[q];
+            }
           }
+          acc[r] += a;
         }
-        acc[r] += a;
       }
     }
+    if (!__syncthreads_and(ok)) {
+      ring.abandon(tid, step, s.err);
+      return;
+    }
+    ring.advance(tid, step);
   }
   FF al[CELL_TILE];
   long long ax[CELL_TILE];
@@ -130,9 +207,11 @@ __device__ __forceinline__ float type_shift_term(float eps, float mu, float mup,
 
 // W by Metropolis-Hastings with a uniform proposal (the reference's move).
 __global__ void __launch_bounds__(CELL_THREADS, 4) k_w_mh(DevState s) {
+  extern __shared__ __align__(128) int xbuf[];
+  __shared__ __align__(8) uint64_t bar[X_STAGES];
   __shared__ FF sh[(CELL_THREADS / 32) * CELL_TILE];
   __shared__ FF sh_l[CELL_TILE];
-  __shared__ int sh_i[CELL_TILE], sh_kp[CELL_TILE];
+  __shared__ int sh_i[CELL_TILE], sh_kp[CELL_TILE], sh_ai[CELL_TILE], sh_ar[CELL_TILE], sh_na;
   __shared__ float sh_D[CELL_TILE], sh_u[CELL_TILE];
   const int4 t = s.ctile[blockIdx.x];
   const int b = t.x, k = t.y, start = t.z, len = t.w;
@@ -150,6 +229,24 @@ __global__ void __launch_bounds__(CELL_THREADS, 4) k_w_mh(DevState s) {
     sh_u[tid] = st.uniform();
   }
   __syncthreads();
+  // cells whose proposed type differs from the current one; only their X rows
+  // are read
+  if (tid == 0) {
+    int na = 0;
+    for (int r = 0; r < len; ++r)
+      if (sh_kp[r] != k) {
+        sh_ai[na] = sh_i[r];
+        sh_ar[na] = r;
+        ++na;
+      }
+    sh_na = na;
+  }
+  WRing ring{xbuf, bar, s.X, sh_ai, Gp, 0, (int)((Gp + W_WIDTH - 1) / W_WIDTH)};
+  ring.init(tid);
+  __syncthreads();
+  const int na = sh_na;
+  ring.len = na;
+  if (na > 0) ring.prologue(tid);
   float acc[CELL_TILE];
 #pragma unroll
   for (int r = 0; r < CELL_TILE; ++r) acc[r] = 0.0f;
@@ -157,34 +254,50 @@ __global__ void __launch_bounds__(CELL_THREADS, 4) k_w_mh(DevState s) {
   const float* Er = Eb + (int64_t)k * Gp;
   const float* Pr = s.phi + (int64_t)b * Gp;
   const float* Bk = s.beta + (int64_t)k * Gp;
-  // two genes per thread and step (64-bit loads) keep the eight cells' loads
-  // within the register budget of three CTAs per SM
-  for (int64_t g2 = (int64_t)tid * 2; g2 < Gp; g2 += (int64_t)CELL_THREADS * 2) {
-    const float2 e = *reinterpret_cast<const float2*>(Er + g2);
-    const float2 ph = *reinterpret_cast<const float2*>(Pr + g2);
-    const float2 bk = *reinterpret_cast<const float2*>(Bk + g2);
+  for (int step = 0; na > 0 && step < ring.n_steps; ++step) {
+    const int64_t g2 = (int64_t)step * W_WIDTH + tid * 2;
+    const bool in = g2 < G;
+    float2 e = make_float2(0.f, 0.f), ph = e, bk = e;
+    if (in) {
+      e = *reinterpret_cast<const float2*>(Er + g2);
+      ph = *reinterpret_cast<const float2*>(Pr + g2);
+      bk = *reinterpret_cast<const float2*>(Bk + g2);
+    }
     const bool two = g2 + 1 < G;
-#pragma unroll 4
-    for (int r = 0; r < CELL_TILE; ++r) {
-      if (r < len && sh_kp[r] != k && g2 < G) {
-        const int64_t kp_off = (int64_t)sh_kp[r] * Gp + g2;
-        const float2 bp = *reinterpret_cast<const float2*>(s.beta + kp_off);
-        const float2 ep = *reinterpret_cast<const float2*>(Eb + kp_off);
-        const int2 xv = *reinterpret_cast<const int2*>(s.X + (int64_t)sh_i[r] * Gp + g2);
-        const float D = sh_D[r];
-        float a = type_shift_term(bp.x - bk.x, e.x * D, ep.x * D, ph.x, xv.x);
-        if (two) a += type_shift_term(bp.y - bk.y, e.y * D, ep.y * D, ph.y, xv.y);
-        acc[r] += a;
+    const bool ok = ring.wait(step);
+    if (in) {
+#pragma unroll
+      for (int a = 0; a < CELL_TILE; ++a) {
+        if (a < na) {
+          const int r = sh_ar[a];
+          const int64_t kp_off = (int64_t)sh_kp[r] * Gp + g2;
+          const float2 bp = *reinterpret_cast<const float2*>(s.beta + kp_off);
+          const float2 ep = *reinterpret_cast<const float2*>(Eb + kp_off);
+          const int2 xv = *reinterpret_cast<const int2*>(ring.row(step, a) + tid * 2);
+          const float D = sh_D[r];
+          float v = type_shift_term(bp.x - bk.x, e.x * D, ep.x * D, ph.x, xv.x);
+          if (two) v += type_shift_term(bp.y - bk.y, e.y * D, ep.y * D, ph.y, xv.y);
+          acc[a] += v;
+        }
       }
     }
+    if (!__syncthreads_and(ok)) {
+      ring.abandon(tid, step, s.err);
+      return;
+    }
+    ring.advance(tid, step);
   }
   FF al[CELL_TILE];
 #pragma unroll
-  for (int r = 0; r < CELL_TILE; ++r) al[r] = FF{acc[r], 0.0f};
-  cell_reduce(al, sh, sh_l);
+  for (int a = 0; a < CELL_TILE; ++a) al[a] = FF{acc[a], 0.0f};
+  cell_reduce(al, sh, sh_l);  // sh_l[a]: active slot a
   if (tid < len) {
     const int i = sh_i[tid], kp = sh_kp[tid];
-    const double rhs = (double)logf(s.pi[b * s.K + kp]) - (double)logf(s.pi[b * s.K + k]) + ff_value(sh_l[tid]);
+    int a = -1;
+    for (int q = 0; q < na; ++q)
+      if (sh_ar[q] == tid) a = q;
+    const double ll = a >= 0 ? ff_value(sh_l[a]) : 0.0;
+    const double rhs = (double)logf(s.pi[b * s.K + kp]) - (double)logf(s.pi[b * s.K + k]) + ll;
     s.lr_W[i] = rhs;
     if ((double)logf(sh_u[tid]) <= rhs) s.W[i] = kp;
   }

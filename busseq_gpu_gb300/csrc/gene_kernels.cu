@@ -163,12 +163,19 @@ struct GammaTerms {
 // Work unit: a run of <= ZX_PER_CTA list entries of one batch (built at
 // initialisation); CTAs past n_zcta evaluate the static gamma terms.
 //
-// Each warp takes 128 entries, draws Z for them, and packs the entries that
-// need a negative-binomial proposal into a warp-private shared-memory queue
-// (inversion draws from the front, Gamma-Poisson draws from the back, slots
-// from ballot prefix counts, so the order is deterministic).  The queued draws
-// then run on every lane.  The Philox block opened for the Z uniform is passed
-// along, so the NB draw continues the same stream without recomputing it.
+// Phase 1 (each warp, 128 entries, all lanes busy): the entry's loads, block 0
+// of its Philox stream (an entry with X = 0 reads its Z uniform there, and
+// every NB proposal starts there) and the Z draw.  Entries that need an NB
+// proposal are staged in shared memory with their block 0 and a cost class:
+// class 0 for Gamma-Poisson draws, classes 1..16 for CDF inversions ordered
+// by the expected length of the search, mu (-log(1 - u)) with u the uniform
+// the inversion will use, longest first.
+// Phase 2: a counting sort over (class, warp, rank) - all counts come from
+// ballots and match masks, so the order is deterministic - lays the staged
+// entries out as one CTA-wide queue, and thread t takes queue positions
+// t, t + 256, ...  The rare, expensive Gamma-Poisson draws thus share a few
+// warps instead of idling most lanes of every warp, and lanes of one warp run
+// inversion searches of similar length.
 //
 // The gamma terms depend on the entry only through x, so values below ZX_HIST
 // are counted in a shared histogram and each bin's terms are evaluated once;
@@ -177,15 +184,28 @@ constexpr int ZX_WARPS = ZX_THREADS / 32;
 constexpr int ZX_PER_WARP = ZX_PER_CTA / ZX_WARPS;
 constexpr int ZX_PER_LANE = ZX_PER_WARP / 32;
 constexpr int ZX_HIST = 128;
+constexpr int ZX_NCLS = 17;
 static_assert(ZX_HIST <= ZX_THREADS, "one thread per histogram bin");
+static_assert(ZX_NCLS <= 32 && ZX_PER_WARP <= 128 && ZX_WARPS <= 8, "queue index packing");
 
-__global__ void __launch_bounds__(ZX_THREADS) k_zx(DevState s) {
+__device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
+  if (!inv) return 0;
+  const float key = mu * -log_fast(1.0f - u_nb);  // 1 - u is exact for u = (2m+1) 2^-24
+  const int bin = key < 30.0f ? (int)(key * 0.5f) : 15;
+  return 16 - bin;
+}
+
+__global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
   __shared__ double sh[(ZX_THREADS / 32) * 6];
   __shared__ FF shf[ZX_WARPS * 3];
   __shared__ long long shn[ZX_WARPS * 3];
   __shared__ float q_mu[ZX_WARPS][ZX_PER_WARP], q_ph[ZX_WARPS][ZX_PER_WARP];
-  __shared__ int q_xo[ZX_WARPS][ZX_PER_WARP], q_e[ZX_WARPS][ZX_PER_WARP];
-  __shared__ uint32_t q_w[3][ZX_WARPS][ZX_PER_WARP];
+  __shared__ int q_xo[ZX_WARPS][ZX_PER_WARP], q_kr[ZX_WARPS][ZX_PER_WARP];
+  __shared__ uint16_t q_e[ZX_WARPS][ZX_PER_WARP];
+  __shared__ uint32_t q_w[4][ZX_WARPS][ZX_PER_WARP];
+  __shared__ uint16_t perm[ZX_PER_CTA];
+  __shared__ int cnt_w[ZX_WARPS][ZX_NCLS], off[ZX_NCLS][ZX_WARPS], n_need_w[ZX_WARPS];
+  __shared__ int n_queue;
   __shared__ float sp_tab[ZX_HIST];
   __shared__ int xhist[ZX_HIST];
   const int c = blockIdx.x;
@@ -212,18 +232,21 @@ __global__ void __launch_bounds__(ZX_THREADS) k_zx(DevState s) {
     sp_tab[tid] = softplusf(-g0 - g1 * (float)tid);
     xhist[tid] = 0;
   }
+  if (lane < ZX_NCLS) cnt_w[warp][lane] = 0;
+  __syncthreads();
 
-  // ---- Z for the warp's entries; queue the ones that need an NB draw -------
-  int n_inv = 0, n_gp = 0;
+  // ---- phase 1: Z for the warp's entries; stage the ones that need NB -------
+  int n_need = 0;
   long long n0 = 0;
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
   for (int u = 0; u < ZX_PER_LANE; ++u) {
     const int e = warp * ZX_PER_WARP + u * 32 + lane;
-    bool need = false, inv = false;
+    bool need = false;
+    int cls = -1;
     float mu = 0.0f, ph = 1.0f;
     int xo = 0;
-    uint32_t w1 = 0, w2 = 0, w3 = 0;
+    U32x4 r{0u, 0u, 0u, 0u};
     if (e < run.y) {
       const int64_t j = (int64_t)run.x + e;
       const int2 ig = s.zij[j];
@@ -231,58 +254,85 @@ __global__ void __launch_bounds__(ZX_THREADS) k_zx(DevState s) {
       mu = s.E[((int64_t)b * s.K + s.W[i]) * Gp + g] * s.Dexp[i];
       ph = s.phi[(int64_t)b * Gp + g];
       xo = s.X[i * Gp + g];
-      int z = 1;
-      if (xo == 0) {
-        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
-        const U32x4 r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter},
-                                      k0, k1);
-        z = u32_to_unit(r.x) > zthr;
-        w1 = r.y;
-        w2 = r.z;
-        w3 = r.w;
-      }
+      const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+      r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0, k1);
+      const bool z = xo != 0 || u32_to_unit(r.x) > zthr;
       if (z) {
         need = true;
-        inv = negbin_use_inversion(mu, ph);
+        cls = zx_class(negbin_use_inversion(mu, ph), mu, u32_to_unit(xo == 0 ? r.y : r.x));
       } else {
         s.zval[j] = 0;  // Z = 0 and X stays 0
         ++n0;
       }
     }
-    const unsigned mi = __ballot_sync(0xffffffffu, need && inv);
-    const unsigned mg = __ballot_sync(0xffffffffu, need && !inv);
+    const unsigned nm = __ballot_sync(0xffffffffu, need);
+    const unsigned grp = __match_any_sync(0xffffffffu, cls);
     if (need) {
-      const int slot = inv ? n_inv + __popc(mi & lt) : ZX_PER_WARP - 1 - (n_gp + __popc(mg & lt));
+      const int slot = n_need + __popc(nm & lt);
+      const int rank = cnt_w[warp][cls] + __popc(grp & lt);
       q_mu[warp][slot] = mu;
       q_ph[warp][slot] = ph;
       q_xo[warp][slot] = xo;
-      q_e[warp][slot] = e;
-      q_w[0][warp][slot] = w1;
-      q_w[1][warp][slot] = w2;
-      q_w[2][warp][slot] = w3;
+      q_e[warp][slot] = (uint16_t)e;
+      q_kr[warp][slot] = (cls << 16) | rank;
+      q_w[0][warp][slot] = r.x;
+      q_w[1][warp][slot] = r.y;
+      q_w[2][warp][slot] = r.z;
+      q_w[3][warp][slot] = r.w;
     }
-    n_inv += __popc(mi);
-    n_gp += __popc(mg);
+    __syncwarp();
+    if (need && (grp & lt) == 0) cnt_w[warp][cls] += __popc(grp);  // the class group's first lane
+    __syncwarp();
+    n_need += __popc(nm);
   }
-  __syncthreads();  // queues, sp_tab and xhist ready
+  if (lane == 0) n_need_w[warp] = n_need;
+  __syncthreads();
 
-  // ---- the queued imputations: X ~ NB independence MH (BUSseq_gpu.cu:497-506)
-  const int nq = n_inv + n_gp;
+  // ---- phase 2: queue offsets per (class, warp), then the CTA-wide order ---
+  if (warp == 0) {
+    int tot = 0;
+    if (lane < ZX_NCLS)
+      for (int w = 0; w < ZX_WARPS; ++w) tot += cnt_w[w][lane];
+    int incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane < ZX_NCLS) {
+      int base = incl - tot;
+      for (int w = 0; w < ZX_WARPS; ++w) {
+        off[lane][w] = base;
+        base += cnt_w[w][lane];
+      }
+    }
+    if (lane == ZX_NCLS - 1) n_queue = incl;
+  }
+  __syncthreads();
+  for (int q = lane; q < n_need_w[warp]; q += 32) {
+    const int kr = q_kr[warp][q];
+    perm[off[kr >> 16][warp] + (kr & 0xFFFF)] = (uint16_t)((warp << 7) | q);
+  }
+  __syncthreads();
+
+  // ---- phase 3: the queued imputations, X ~ NB independence MH
+  //      (BUSseq_gpu.cu:497-506)
+  const int nq = n_queue;
   long long nz = 0, xz = 0;
   float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-  for (int q = lane; q < nq; q += 32) {
-    const bool is_inv = q < n_inv;
-    const int slot = is_inv ? q : ZX_PER_WARP - 1 - (q - n_inv);
-    const int e = q_e[warp][slot];
-    const int xo = q_xo[warp][slot];
+  for (int q = tid; q < nq; q += ZX_THREADS) {
+    const int ws = perm[q];
+    const int qw = ws >> 7, slot = ws & 127;
+    const bool is_inv = (q_kr[qw][slot] >> 16) != 0;
+    const int e = q_e[qw][slot];
+    const int xo = q_xo[qw][slot];
     const int64_t j = (int64_t)run.x + e;
     const int2 ig = s.zij[j];
     const uint64_t ent = (uint64_t)ig.x * G64 + (uint64_t)ig.y;
-    Stream st = xo == 0 ? Stream::resume1(s.seed, SID_ZX, ent, iter, q_w[0][warp][slot], q_w[1][warp][slot],
-                                          q_w[2][warp][slot])
-                        : Stream(s.seed, SID_ZX, ent, iter);
+    Stream st = Stream::resume(s.seed, SID_ZX, ent, iter, q_w[0][qw][slot], q_w[1][qw][slot], q_w[2][qw][slot],
+                               q_w[3][qw][slot], xo == 0);
     int err = 0;
-    const float mu = q_mu[warp][slot], ph = q_ph[warp][slot];
+    const float mu = q_mu[qw][slot], ph = q_ph[qw][slot];
     const int xn = is_inv ? negbin_inversion(st, mu, ph, &err) : negbin_gamma_poisson(st, mu, ph, &err);
     const float ua = st.uniform();
     // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
@@ -366,7 +416,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
       if (j0 + u < len) {
         const float mu = M * s_D[j0 + u];
         sx += xr[u];
-        f += (ph + (float)xr[u]) * log1p_fast(ca * fast_div(mu, ph + mu));
+        f += (ph + (float)xr[u]) * log1p_near0(ca * fast_div(mu, ph + mu));
       }
     }
     la.add(f);
@@ -409,12 +459,12 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
         const float w = ph + (float)x;
         const float p = fast_div(mu, ph + mu);
         sx += x;
-        if (k > 0) lbf += w * log1p_fast(cb * p);
+        if (k > 0) lbf += w * log1p_near0(cb * p);
         if (b > 0) {
-          ln0f += w * log1p_fast(cn * p);
+          ln0f += w * log1p_near0(cn * p);
           if (k > 0) {
             const float mu1 = mu * fb;
-            ln1f += w * log1p_fast(cn * fast_div(mu1, ph + mu1));
+            ln1f += w * log1p_near0(cn * fast_div(mu1, ph + mu1));
           }
         }
       }

@@ -125,15 +125,17 @@ struct Stream {
     return v;
   }
   BQ_HD float uniform() { return u32_to_unit(next_u32()); }
-  // The stream after its first uniform, given the other three words of block 0.
-  BQ_HD static Stream resume1(uint64_t seed, uint32_t sid, uint64_t entity, uint32_t iter, uint32_t w1, uint32_t w2,
-                              uint32_t w3) {
+  // The stream with block 0 = (w0, w1, w2, w3) already generated; when
+  // `skip_first` is set the first word counts as consumed.
+  BQ_HD static Stream resume(uint64_t seed, uint32_t sid, uint64_t entity, uint32_t iter, uint32_t w0, uint32_t w1,
+                             uint32_t w2, uint32_t w3, bool skip_first) {
     Stream s(seed, sid, entity, iter);
     s.blk = 1;
-    s.b0 = w1;
-    s.b1 = w2;
-    s.b2 = w3;
-    s.n = 3;
+    s.b0 = skip_first ? w1 : w0;
+    s.b1 = skip_first ? w2 : w1;
+    s.b2 = skip_first ? w3 : w2;
+    s.b3 = w3;
+    s.n = skip_first ? 3 : 4;
     return s;
   }
 };
@@ -227,6 +229,15 @@ BQ_HD float log1p_fast(float y) {
   const int e = log_exponent(bits);
   const float f = e == 0 ? y : bits_float(bits - (e << 23)) - 1.0f;
   return log_mant(f, e);
+}
+
+// log1p for arguments that are nearly always inside (-0.29, 0.41), where the
+// exponent is 0 and log_mant applies directly; others take log1p_fast.  The
+// branch is taken uniformly by a warp in the Metropolis sums, whose arguments
+// are expm1(step) * p with p in (0, 1).
+BQ_HD float log1p_near0(float y) {
+  if (y > -0.29f && y < 0.41f) return log_mant(y, 0);
+  return log1p_fast(y);
 }
 
 // log(a / b) for a, b > 0 given d = a - b.  With r = a / b: while r lies in

@@ -29,7 +29,7 @@ extern "C" {
 #define BUSSEQ_ERR_CUDA (-2)     /* CUDA runtime error                        */
 #define BUSSEQ_ERR_NOMEM (-3)    /* device or host allocation failed          */
 #define BUSSEQ_ERR_STATE (-4)    /* call out of order (e.g. no run begun)     */
-#define BUSSEQ_ERR_SAMPLER (-5)  /* a device rejection sampler hit its cap    */
+#define BUSSEQ_ERR_SAMPLER (-5)  /* a device sampler cap or copy wait bound   */
 #define BUSSEQ_ERR_IO (-6)       /* file could not be read or written         */
 
 #define BUSSEQ_MAX_BATCHES 128   /* BUSseq_gpu.cu:9-10 (__constant__ d_n_b[128]) */
