@@ -51,8 +51,8 @@ constexpr int CELL_TILE = 8;       // cells per cell-pass CTA
 constexpr int CELL_THREADS = 256;  // threads of a cell-pass CTA (4 genes each per step)
 // Cell passes stream the tile's X rows through shared memory in X_STAGES
 // stages of DELTA_WIDTH (delta) or W_WIDTH (W) genes.
-constexpr int X_STAGES = 2;
-constexpr int DELTA_WIDTH = 4 * CELL_THREADS;
+constexpr int X_STAGES = 3;
+constexpr int DELTA_WIDTH = 2 * CELL_THREADS;
 constexpr int W_WIDTH = 2 * CELL_THREADS;
 constexpr int DELTA_SMEM = X_STAGES * CELL_TILE * DELTA_WIDTH * (int)sizeof(int);
 constexpr int W_SMEM = X_STAGES * CELL_TILE * W_WIDTH * (int)sizeof(int);
@@ -60,7 +60,7 @@ constexpr int MAX_B = 128;
 constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
-constexpr int PHI_TAB = 32;        // small-count table of lgamma differences
+constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
 constexpr int ZX_PER_CTA = 1024;   // zero entries per Z/X CTA
 
@@ -126,6 +126,8 @@ struct DevState {
   float* nu_p;     // [B][Gp]
   float* delta_p;  // [N]
   float* phi_p;    // [B][Gp]
+  float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
+  float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   float* gamma_p;  // [2][B]
 
   // cell order and work lists

@@ -284,7 +284,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
   else opt.p0 = 0.25;
   if (!(opt.p0 > 0.0 && opt.p0 < 1.0)) return fail(BUSSEQ_ERR_ARG, "p0 must be in (0, 1)");
   CUDA_TRY(cudaSetDevice(opt.device));
-  // the delta pass stages 64 KB of X rows per CTA (above the 48 KB default)
+  // the cell passes stage 48 KB of X rows per CTA (with their static shared
+  // memory, above the 48 KB default)
   CUDA_TRY(cudaFuncSetAttribute(bq::k_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, bq::DELTA_SMEM));
   CUDA_TRY(cudaFuncSetAttribute(bq::k_w_mh, cudaFuncAttributeMaxDynamicSharedMemorySize, bq::W_SMEM));
 
@@ -323,7 +324,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     int32_t* Yd;
     TRY(h->alloc(&Yd, N * Gp));
     s.Y = Yd;
-    TRY(h->alloc(&s.X, N * Gp));
+    // one extra all-zero row: the gene passes pad their cell chunks with it
+    TRY(h->alloc(&s.X, (N + 1) * Gp));
     uint32_t* y0m;
     TRY(h->alloc(&y0m, N * s.Gw));
     s.y0m = y0m;
@@ -353,6 +355,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&s.nu_p, B * Gp));
     TRY(h->alloc(&s.delta_p, N));
     TRY(h->alloc(&s.phi_p, B * Gp));
+    TRY(h->alloc(&s.phi_tab, (int64_t)B * bq::PHI_TAB * Gp));
+    TRY(h->alloc(&s.phi_lgd0, B * Gp));
     TRY(h->alloc(&s.gamma_p, 2 * B));
     TRY(h->alloc(&s.perm, N));
     TRY(h->alloc(&s.gchunk, s.cap_g));

@@ -105,7 +105,7 @@ using DeltaRing = XRowRing<DELTA_WIDTH, X_STAGES>;
 using WRing = XRowRing<W_WIDTH, X_STAGES>;
 static_assert(DeltaRing::bytes() == DELTA_SMEM && WRing::bytes() == W_SMEM, "ring sizes");
 
-__global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
+__global__ void __launch_bounds__(CELL_THREADS, 4) k_delta(DevState s) {
   extern __shared__ __align__(128) int xbuf[];
   __shared__ __align__(8) uint64_t bar[X_STAGES];
   __shared__ FF sh[(CELL_THREADS / 32) * CELL_TILE];
@@ -139,30 +139,29 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_delta(DevState s) {
   const float* Er = s.E + ((int64_t)b * s.K + k) * Gp;
   const float* Pr = s.phi + (int64_t)b * Gp;
   for (int step = 0; step < ring.n_steps; ++step) {
-    const int64_t g4 = (int64_t)step * DELTA_WIDTH + tid * 4;
-    const bool in = g4 < Gp;
-    float4 e = make_float4(0.f, 0.f, 0.f, 0.f), ph = e;
+    const int64_t g2 = (int64_t)step * DELTA_WIDTH + tid * 2;
+    const bool in = g2 < G;
+    float2 e = make_float2(0.f, 0.f), ph = e;
     if (in) {
-      e = *reinterpret_cast<const float4*>(Er + g4);
-      ph = *reinterpret_cast<const float4*>(Pr + g4);
+      e = *reinterpret_cast<const float2*>(Er + g2);
+      ph = *reinterpret_cast<const float2*>(Pr + g2);
     }
+    const bool two = g2 + 1 < G;
     const bool ok = ring.wait(step);
     if (in) {
-      const float ev[4] = {e.x, e.y, e.z, e.w}, pv[4] = {ph.x, ph.y, ph.z, ph.w};
 #pragma unroll
       for (int r = 0; r < CELL_TILE; ++r) {
         if (r < len) {
-          const int4 xv = *reinterpret_cast<const int4*>(ring.row(step, r) + tid * 4);
-          const int xs[4] = {xv.x, xv.y, xv.z, xv.w};
-          float a = 0.0f;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (g4 + q < G) {
-              const float mu = ev[q] * sh_D[r];
-              a += (pv[q] + (float)xs[q]) * log1p_near0(sh_c[r] * fast_div(mu, pv[q] + mu));
-              sxi[r] += xs[q];
-            }
+          const int2 xv = *reinterpret_cast<const int2*>(ring.row(step, r) + tid * 2);
+          const float D = sh_D[r], c = sh_c[r];
+          const float mu0 = e.x * D, mu1 = e.y * D;
+          float a = (ph.x + (float)xv.x) * log1p_near0(c * fast_div(mu0, ph.x + mu0));
+          int sxv = xv.x;
+          if (two) {
+            a += (ph.y + (float)xv.y) * log1p_near0(c * fast_div(mu1, ph.y + mu1));
+            sxv += xv.y;
           }
+          sxi[r] += sxv;
           acc[r] += a;
         }
       }

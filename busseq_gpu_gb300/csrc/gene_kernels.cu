@@ -97,10 +97,23 @@ __global__ void k_propose(DevState s, int mask) {
       const int64_t g = t % G;
       Stream st(s.seed, SID_PHI_PROP, (uint64_t)t, iter);
       int err = 0;
-      float pn = gamma_mt(st, s.phi[b * Gp + g], &err);
+      const float ph = s.phi[b * Gp + g];
+      float pn = gamma_mt(st, ph, &err);
       if (!(pn > 0.0f)) pn = 1.0e-30f;
       s.phi_p[b * Gp + g] = pn;
       if (err) atomicOr(s.err, err);
+      // lgamma differences of the phi update: h(x) = sum_{j<x} log((pn + j) / (ph + j))
+      // for x < PHI_TAB, and lgamma(pn) - lgamma(ph)
+      const float dl = pn - ph;
+      float* tab = s.phi_tab + (int64_t)b * PHI_TAB * Gp + g;
+      float h = 0.0f;
+      tab[0] = 0.0f;
+      for (int x = 1; x < PHI_TAB; ++x) {
+        const float j = (float)(x - 1);
+        h += log_ratio(pn + j, ph + j, dl);
+        tab[(int64_t)x * Gp] = h;
+      }
+      s.phi_lgd0[b * Gp + g] = lgamma_diff(ph, pn, dl);
     }
   }
 }
@@ -374,51 +387,70 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
 // ---------------------------------------------------------------------------
 // Gene passes
 // ---------------------------------------------------------------------------
-// Copies the chunk's cell indices and exp(delta) into shared memory.
-__device__ __forceinline__ void stage_chunk(const DevState& s, int start, int len, int* s_i, float* s_D) {
-  for (int j = threadIdx.x; j < len; j += blockDim.x) {
-    const int i = s.perm[start + j];
+// Copies the chunk's cell indices and exp(delta) into shared memory and pads
+// the chunk to a multiple of 8 cells with the all-zero row N of X and
+// exp(delta) = 0: a padding entry has x = 0 and mu = 0, and every per-entry
+// term below is then exactly zero, so the inner loops need no bounds tests.
+// Returns the padded length.
+__device__ __forceinline__ int stage_chunk(const DevState& s, int start, int len, int* s_i, float* s_D) {
+  const int len8 = (len + 7) & ~7;
+  for (int j = threadIdx.x; j < len8; j += blockDim.x) {
+    const bool in = j < len;
+    const int i = in ? s.perm[start + j] : (int)s.N;
     s_i[j] = i;
-    s_D[j] = s.Dexp[i];
+    s_D[j] = in ? s.Dexp[i] : 0.0f;
   }
+  return len8;
 }
 
-// Loads X of eight consecutive chunk cells for gene g.
-__device__ __forceinline__ void load8(const DevState& s, const int* s_i, int j0, int len, int64_t g, int (&xr)[8]) {
+// X and exp(delta) of chunk cells j0..j0+7 for the gene whose column starts
+// at Xg (128-bit shared loads; row offsets by one 32x32->64-bit multiply-add).
+__device__ __forceinline__ void load8(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D, int j0,
+                                      int (&xr)[8], float (&dv)[8]) {
+  const int4 ia = *reinterpret_cast<const int4*>(s_i + j0);
+  const int4 ib = *reinterpret_cast<const int4*>(s_i + j0 + 4);
+  const float4 da = *reinterpret_cast<const float4*>(s_D + j0);
+  const float4 db = *reinterpret_cast<const float4*>(s_D + j0 + 4);
+  const int iv[8] = {ia.x, ia.y, ia.z, ia.w, ib.x, ib.y, ib.z, ib.w};
 #pragma unroll
-  for (int u = 0; u < 8; ++u) xr[u] = j0 + u < len ? s.X[(int64_t)s_i[j0 + u] * s.Gp + g] : 0;
+  for (int u = 0; u < 8; ++u) xr[u] = *reinterpret_cast<const int*>(Xg + (uint64_t)(uint32_t)iv[u] * row_bytes);
+  dv[0] = da.x; dv[1] = da.y; dv[2] = da.z; dv[3] = da.w;
+  dv[4] = db.x; dv[5] = db.y; dv[6] = db.z; dv[7] = db.w;
 }
 
 // alpha: sum of x and of (phi + x) log1p(expm1(alpha' - alpha) p) over the chunk
 __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
-  __shared__ int s_i[MAX_CG];
-  __shared__ float s_D[MAX_CG];
+  __shared__ __align__(16) int s_i[MAX_CG];
+  __shared__ __align__(16) float s_D[MAX_CG];
   const int tile = blockIdx.x, row = blockIdx.y;
   const int4 ch = s.gchunk[row];
   const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + threadIdx.x;
   if (len == 0) return;
-  stage_chunk(s, start, len, s_i, s_D);
+  const int len8 = stage_chunk(s, start, len, s_i, s_D);
   __syncthreads();
   if (g >= s.G) return;
+  const char* Xg = reinterpret_cast<const char*>(s.X + g);
+  const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
   const float M = s.E[((int64_t)b * s.K + k) * Gp + g];
   const float ph = s.phi[(int64_t)b * Gp + g];
   const float ca = expm1f(s.alpha_p[g] - s.alpha[g]);
   int64_t sx = 0;
   KahanF la;
-  for (int j0 = 0; j0 < len; j0 += 8) {
+  for (int j0 = 0; j0 < len8; j0 += 8) {
     int xr[8];
-    load8(s, s_i, j0, len, g, xr);
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
     float f = 0.0f;
+    int s8 = 0;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      if (j0 + u < len) {
-        const float mu = M * s_D[j0 + u];
-        sx += xr[u];
-        f += (ph + (float)xr[u]) * log1p_near0(ca * fast_div(mu, ph + mu));
-      }
+      const float mu = M * dv[u];
+      s8 += xr[u];
+      f += (ph + (float)xr[u]) * log1p_near0(ca * fast_div(mu, ph + mu));
     }
+    sx += s8;
     la.add(f);
   }
   double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
@@ -426,18 +458,55 @@ __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
   pr[Gp] = la.value();
 }
 
+// Chunk sums of k_beta_nu for one CTA-uniform case: HB = the chunk's type
+// has a beta (k > 0), HN = its batch has a nu (b > 0).
+template <bool HB, bool HN>
+__device__ __forceinline__ void beta_nu_sums(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D,
+                                             int len8, float M, float ph, float cb, float fb, float cn, int64_t& sx,
+                                             KahanF& lb, KahanF& ln0, KahanF& ln1) {
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    float lbf = 0.0f, ln0f = 0.0f, ln1f = 0.0f;
+    int s8 = 0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int x = xr[u];
+      const float mu = M * dv[u];
+      const float w = ph + (float)x;
+      const float p = fast_div(mu, ph + mu);
+      s8 += x;
+      if (HB) lbf += w * log1p_near0(cb * p);
+      if (HN) {
+        ln0f += w * log1p_near0(cn * p);
+        if (HB) {
+          const float mu1 = mu * fb;
+          ln1f += w * log1p_near0(cn * fast_div(mu1, ph + mu1));
+        }
+      }
+    }
+    sx += s8;
+    if (HB) lb.add(lbf);
+    if (HN) ln0.add(ln0f);
+    if (HB && HN) ln1.add(ln1f);
+  }
+}
+
 __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
-  __shared__ int s_i[MAX_CG];
-  __shared__ float s_D[MAX_CG];
+  __shared__ __align__(16) int s_i[MAX_CG];
+  __shared__ __align__(16) float s_D[MAX_CG];
   const int tile = blockIdx.x, row = blockIdx.y;
   const int4 ch = s.gchunk[row];
   const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + threadIdx.x;
   if (len == 0 || (k == 0 && b == 0)) return;
-  stage_chunk(s, start, len, s_i, s_D);
+  const int len8 = stage_chunk(s, start, len, s_i, s_D);
   __syncthreads();
   if (g >= s.G) return;
+  const char* Xg = reinterpret_cast<const char*>(s.X + g);
+  const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
   const float bt = s.beta[(int64_t)k * Gp + g];
   const float M = exp_sum3(s.alpha[g], bt, s.nu[(int64_t)b * Gp + g]);
   const float ph = s.phi[(int64_t)b * Gp + g];
@@ -447,32 +516,9 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   const float cn = expm1f(en);
   int64_t sx = 0;
   KahanF lb, ln0, ln1;
-  for (int j0 = 0; j0 < len; j0 += 8) {
-    int xr[8];
-    load8(s, s_i, j0, len, g, xr);
-    float lbf = 0.0f, ln0f = 0.0f, ln1f = 0.0f;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      if (j0 + u < len) {
-        const int x = xr[u];
-        const float mu = M * s_D[j0 + u];
-        const float w = ph + (float)x;
-        const float p = fast_div(mu, ph + mu);
-        sx += x;
-        if (k > 0) lbf += w * log1p_near0(cb * p);
-        if (b > 0) {
-          ln0f += w * log1p_near0(cn * p);
-          if (k > 0) {
-            const float mu1 = mu * fb;
-            ln1f += w * log1p_near0(cn * fast_div(mu1, ph + mu1));
-          }
-        }
-      }
-    }
-    lb.add(lbf);
-    ln0.add(ln0f);
-    ln1.add(ln1f);
-  }
+  if (k > 0 && b > 0) beta_nu_sums<true, true>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  else if (k > 0) beta_nu_sums<true, false>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  else beta_nu_sums<false, true>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
   double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
   pr[0] = (double)sx;
   pr[Gp] = lb.value();
@@ -482,8 +528,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
 
 __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   __shared__ float tab[PHI_TAB][GENE_TILE];
-  __shared__ int s_i[MAX_CG];
-  __shared__ float s_D[MAX_CG];
+  __shared__ __align__(16) int s_i[MAX_CG];
+  __shared__ __align__(16) float s_D[MAX_CG];
   const int tid = threadIdx.x;
   const int tile = blockIdx.x, row = blockIdx.y;
   const int4 ch = s.gchunk[row];
@@ -491,7 +537,11 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   if (len == 0) return;
-  stage_chunk(s, start, len, s_i, s_D);
+  const int len8 = stage_chunk(s, start, len, s_i, s_D);
+  // the proposal's table of lgamma differences, built by k_propose
+  const float* tg = s.phi_tab + (int64_t)b * PHI_TAB * Gp + g;
+#pragma unroll 8
+  for (int x = 0; x < PHI_TAB; ++x) tab[x][tid] = tg[(int64_t)x * Gp];
   __syncthreads();
   if (g >= s.G) return;
   const float ph = s.phi[(int64_t)b * Gp + g];
@@ -502,30 +552,24 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   // Per entry (BUSseq_gpu.cu:799-802, regrouped so that no large terms cancel):
   //   t = [lgamma(pp+x) - lgamma(pp)] - [lgamma(ph+x) - lgamma(ph)]
   //       - (pp + x) log((pp + mu) / (ph + mu)) + pp log(pp / ph) - dl log(1 + mu / ph)
-  const float lgd0 = lgamma_diff(ph, pp, dl);
+  const float lgd0 = s.phi_lgd0[(int64_t)b * Gp + g];
   const float c1 = pp * log_ratio(pp, ph, dl);
-  float h = 0.0f;
-  tab[0][tid] = 0.0f;
-  for (int x = 1; x < PHI_TAB; ++x) {
-    const float j = (float)(x - 1);
-    h += log_ratio(pp + j, ph + j, dl);
-    tab[x][tid] = h;
-  }
+  const char* Xg = reinterpret_cast<const char*>(s.X + g);
+  const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
   KahanF acc;
-  for (int j0 = 0; j0 < len; j0 += 8) {
+  for (int j0 = 0; j0 < len8; j0 += 8) {
     int xr[8];
-    load8(s, s_i, j0, len, g, xr);
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
     float f = 0.0f;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      if (j0 + u < len) {
-        const int x = xr[u];
-        const float mu = M * s_D[j0 + u];
-        const float xf = (float)x;
-        // x >= PHI_TAB >= 8: both arguments are past the shift range
-        const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
-        f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
-      }
+      const int x = xr[u];
+      const float mu = M * dv[u];
+      const float xf = (float)x;
+      // x >= PHI_TAB >= 8: both arguments are past the shift range
+      const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
+      f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
     }
     acc.add(f);
   }

@@ -159,9 +159,22 @@ BQ_HD float bq_lgammaf(float x) {
 #endif
 }
 
+// 1 / b from the hardware reciprocal approximation (rcp.approx.ftz.f32, about
+// 1 ulp) and a / b as a times that; b is a positive normal number wherever
+// these are used.
+BQ_HD float fast_rcp(float b) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return r;
+#else
+  return 1.0f / b;
+#endif
+}
+
 BQ_HD float fast_div(float a, float b) {
 #if defined(__CUDA_ARCH__)
-  return __fdividef(a, b);
+  return a * fast_rcp(b);
 #else
   return a / b;
 #endif
@@ -231,12 +244,12 @@ BQ_HD float log1p_fast(float y) {
   return log_mant(f, e);
 }
 
-// log1p for arguments that are nearly always inside (-0.29, 0.41), where the
+// log1p for arguments that are nearly always inside (-0.29, 0.29), where the
 // exponent is 0 and log_mant applies directly; others take log1p_fast.  The
 // branch is taken uniformly by a warp in the Metropolis sums, whose arguments
 // are expm1(step) * p with p in (0, 1).
 BQ_HD float log1p_near0(float y) {
-  if (y > -0.29f && y < 0.41f) return log_mant(y, 0);
+  if (fabsf(y) < 0.29f) return log_mant(y, 0);
   return log1p_fast(y);
 }
 
@@ -245,7 +258,7 @@ BQ_HD float log1p_near0(float y) {
 // a close to b); otherwise |log r| > 0.34 and r itself is relatively
 // accurate, including a << b.  One reciprocal serves both quotients.
 BQ_HD float log_ratio(float a, float b, float d) {
-  const float rb = fast_div(1.0f, b);
+  const float rb = fast_rcp(b);
   const int bits = float_bits(a * rb);
   const int e = log_exponent(bits);
   const float f = e == 0 ? d * rb : bits_float(bits - (e << 23)) - 1.0f;
@@ -274,7 +287,7 @@ BQ_HD float log_factorial(float k) {
     return v;
   }
   const float x = k + 1.0f;
-  const float r = fast_div(1.0f, x);
+  const float r = fast_rcp(x);
   return (x - 0.5f) * log_fast(x) - x + 0.918938533204672742f + r * (1.0f / 12.0f - (r * r) * (1.0f / 360.0f));
 }
 
@@ -430,7 +443,7 @@ BQ_HD float log_ratio_rcp(float a, float rb, float d) {
 // -dlt w [1/12 - (q + w)/360 + (q^2 + w q - w^2)/1260], q = 1/zq^2 + 1/zz^2,
 // so no difference of nearly equal numbers is formed.
 BQ_HD float lgamma_diff_large(float zz, float zq, float dlt) {
-  const float w = fast_div(1.0f, zz * zq);
+  const float w = fast_rcp(zz * zq);
   const float rz = zq * w, rq = zz * w;
   const float q = fmaf(rq, rq, rz * rz);
   const float poly = (1.0f / 12.0f) - (q + w) * (1.0f / 360.0f) + fmaf(q, q, w * (q - w)) * (1.0f / 1260.0f);
