@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
   __shared__ float q_mu[ZX_WARPS][ZX_PER_WARP], q_ph[ZX_WARPS][ZX_PER_WARP];
   __shared__ int q_xo[ZX_WARPS][ZX_PER_WARP], q_kr[ZX_WARPS][ZX_PER_WARP];
   __shared__ uint16_t q_e[ZX_WARPS][ZX_PER_WARP];
+  __shared__ int q_i[ZX_WARPS][ZX_PER_WARP], q_g[ZX_WARPS][ZX_PER_WARP];
   __shared__ uint32_t q_w[4][ZX_WARPS][ZX_PER_WARP];
   __shared__ uint16_t perm[ZX_PER_CTA];
   __shared__ int cnt_w[ZX_WARPS][ZX_NCLS], off[ZX_NCLS][ZX_WARPS], n_need_w[ZX_WARPS];
@@ -249,6 +250,38 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
   __syncthreads();
 
   // ---- phase 1: Z for the warp's entries; stage the ones that need NB -------
+  // All loads of the warp's four rounds are issued before any of the
+  // ballot / match bookkeeping, so their latencies overlap.
+  int ei[ZX_PER_LANE], eg[ZX_PER_LANE], exo[ZX_PER_LANE];
+  float emu[ZX_PER_LANE], eph[ZX_PER_LANE];
+#pragma unroll
+  for (int u = 0; u < ZX_PER_LANE; ++u) {
+    const int e = warp * ZX_PER_WARP + u * 32 + lane;
+    const int2 ig = e < run.y ? s.zij[(int64_t)run.x + e] : make_int2(-1, 0);
+    ei[u] = ig.x;
+    eg[u] = ig.y;
+  }
+  int ew[ZX_PER_LANE];
+  float eD[ZX_PER_LANE];
+#pragma unroll
+  for (int u = 0; u < ZX_PER_LANE; ++u) {
+    if (ei[u] >= 0) {
+      const int64_t i = ei[u], g = eg[u];
+      ew[u] = s.W[i];
+      eD[u] = s.Dexp[i];
+      eph[u] = s.phi[(int64_t)b * Gp + g];
+      exo[u] = s.X[i * Gp + g];
+    } else {
+      ew[u] = 0;
+      eD[u] = 0.0f;
+      eph[u] = 1.0f;
+      exo[u] = 0;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < ZX_PER_LANE; ++u)
+    emu[u] = ei[u] >= 0 ? s.E[((int64_t)b * s.K + ew[u]) * Gp + eg[u]] * eD[u] : 0.0f;
+
   int n_need = 0;
   long long n0 = 0;
   const unsigned lt = (1u << lane) - 1u;
@@ -257,24 +290,18 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
     const int e = warp * ZX_PER_WARP + u * 32 + lane;
     bool need = false;
     int cls = -1;
-    float mu = 0.0f, ph = 1.0f;
-    int xo = 0;
+    const float mu = emu[u], ph = eph[u];
+    const int xo = exo[u];
     U32x4 r{0u, 0u, 0u, 0u};
-    if (e < run.y) {
-      const int64_t j = (int64_t)run.x + e;
-      const int2 ig = s.zij[j];
-      const int64_t i = ig.x, g = ig.y;
-      mu = s.E[((int64_t)b * s.K + s.W[i]) * Gp + g] * s.Dexp[i];
-      ph = s.phi[(int64_t)b * Gp + g];
-      xo = s.X[i * Gp + g];
-      const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+    if (ei[u] >= 0) {
+      const uint64_t ent = (uint64_t)ei[u] * G64 + (uint64_t)eg[u];
       r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0, k1);
       const bool z = xo != 0 || u32_to_unit(r.x) > zthr;
       if (z) {
         need = true;
         cls = zx_class(negbin_use_inversion(mu, ph), mu, u32_to_unit(xo == 0 ? r.y : r.x));
       } else {
-        s.zval[j] = 0;  // Z = 0 and X stays 0
+        s.zval[(int64_t)run.x + e] = 0;  // Z = 0 and X stays 0
         ++n0;
       }
     }
@@ -287,6 +314,8 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
       q_ph[warp][slot] = ph;
       q_xo[warp][slot] = xo;
       q_e[warp][slot] = (uint16_t)e;
+      q_i[warp][slot] = ei[u];
+      q_g[warp][slot] = eg[u];
       q_kr[warp][slot] = (cls << 16) | rank;
       q_w[0][warp][slot] = r.x;
       q_w[1][warp][slot] = r.y;
@@ -340,7 +369,7 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
     const int e = q_e[qw][slot];
     const int xo = q_xo[qw][slot];
     const int64_t j = (int64_t)run.x + e;
-    const int2 ig = s.zij[j];
+    const int2 ig = make_int2(q_i[qw][slot], q_g[qw][slot]);
     const uint64_t ent = (uint64_t)ig.x * G64 + (uint64_t)ig.y;
     Stream st = Stream::resume(s.seed, SID_ZX, ent, iter, q_w[0][qw][slot], q_w[1][qw][slot], q_w[2][qw][slot],
                                q_w[3][qw][slot], xo == 0);
