@@ -7,6 +7,8 @@
 * ``ref_harness``  -- oracle/ref_harness.cpp, a CUDA-driver-API loader that runs
   the reference's deterministic kernels from that cubin (needs libcuda, so it
   is built where a driver is installed, i.e. on the GPU machine).
+* ``ref_sweep_timer`` -- oracle/ref_sweep_timer.cpp, which replays the
+  reference's per-sweep launch sequence from that cubin to time it.
 
 Nothing in the product package imports this module.
 """
@@ -26,6 +28,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ORACLE_SO = os.path.join(LIB_DIR, "liborc.so")
 REF_CUBIN = os.path.join(REF_DIR, "busseq_ref.cubin")
 HARNESS_BIN = os.path.join(LIB_DIR, "ref_harness")
+TIMER_BIN = os.path.join(LIB_DIR, "ref_sweep_timer")
 
 
 def _run(cmd: list[str]) -> None:
@@ -83,10 +86,28 @@ def build_harness(force: bool = False) -> str | None:
     return HARNESS_BIN
 
 
+def build_ref_timer(force: bool = False) -> str | None:
+    """Build the reference sweep timer (driver API; needs libcuda, like the harness)."""
+    src = os.path.join(HERE, "ref_sweep_timer.cpp")
+    os.makedirs(LIB_DIR, exist_ok=True)
+    if not force and not _stale(TIMER_BIN, [src]):
+        return TIMER_BIN
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(CUDA_HOME, "include"), "-o", TIMER_BIN, src]
+    for d in (os.path.join(CUDA_HOME, "lib64"), os.path.join(CUDA_HOME, "lib64", "stubs")):
+        cmd += ["-L", d]
+    cmd += ["-lcuda"]
+    try:
+        _run(cmd)
+    except RuntimeError:
+        return None
+    return TIMER_BIN
+
+
 def build_all(force: bool = False) -> dict:
     out = {"oracle": build_oracle(force), "ref_cubin": build_ref_cubin(force)}
     if shutil.which("g++"):
         out["harness"] = build_harness(force)
+        out["ref_timer"] = build_ref_timer(force)
     return out
 
 
