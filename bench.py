@@ -185,6 +185,35 @@ def _config():
             "precision": "f32 likelihood terms, f64 acceptance sums"}
 
 
+def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000):
+    """One whole job with kept draws: ESS (Geyer, initial monotone sequence) of
+    every beta (k >= 1) and nu (b >= 1) coordinate, ESS/s over the wall time of
+    the whole job (upload, init, burn-in, kept sweeps, estimates), and the ARI
+    of the posterior W against the simulated types."""
+    import busseq_gpu_gb300 as bq
+    from busseq_gpu_gb300.diagnostics import adjusted_rand_index, ess_geyer
+
+    t0 = time.perf_counter()
+    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True)
+    s.run(n_iter, n_burnin, min(500, n_burnin))
+    est = s.estimates(with_XZ=False)
+    wall = time.perf_counter() - t0
+    pres = s.preserved()
+    s.close()
+    out = {"sweeps": n_iter, "burnin": n_burnin, "kept": n_iter - n_burnin, "wall_s": wall,
+           "ari_W": adjusted_rand_index(est["W"], W_true), "estimator": "Geyer initial monotone sequence"}
+    for name in ("beta", "nu"):
+        e = ess_geyer(pres[name].astype(np.float64))
+        moving = np.isfinite(e)
+        ev = e[moving]
+        out[name] = {"coords": int(e.size), "moving": int(moving.sum()),
+                     "ess_median": float(np.median(ev)) if ev.size else None,
+                     "ess_min": float(ev.min()) if ev.size else None,
+                     "ess_per_s_median": float(np.median(ev)) / wall if ev.size else None,
+                     "ess_per_s_min": float(ev.min()) / wall if ev.size else None}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,6 +223,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cells", type=int, default=0,
                     help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
+    ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     args = ap.parse_args()
@@ -298,6 +328,11 @@ def main():
     h2d = Y.nbytes
     d2h = sum(v.nbytes for v in est.values())
 
+    # ---- mixing and recovery: ESS of beta and nu, ARI of W (rank 0) -------
+    quality = None
+    if rank == 0 and not args.no_ess:
+        quality = ess_run(Y, W_true, n_b, K, seed)
+
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -324,6 +359,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "quality": quality,
         }
         print(json.dumps(line))
     if dist is not None:
