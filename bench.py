@@ -40,6 +40,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
+# the large uneven workload: 6 batches, 15 % differential genes, phi ~ U(2, 30)
+CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide")
+WORKLOADS = {"config1": CFG1, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
 UNIT = "sweeps/s"
 
@@ -53,9 +56,10 @@ def _peak_hbm():
         return 6800.0, "fallback"
 
 
-def _traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic_config1.txt")
+def _traffic(kernel: str, workload: str = "config1"):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of this
+    workload, or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_%s.txt" % workload)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -120,9 +124,10 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_data(seed):
+def make_data(seed, cfg=CFG1, n_b=None):
     import busseq_gpu_gb300 as bq
-    return bq.simulate(CFG1["n_b"], CFG1["G"], CFG1["K"], seed)
+    prm = bq.CONFIG_SIM[cfg.get("sim", "default")]
+    return bq.simulate(n_b if n_b is not None else cfg["n_b"], cfg["G"], cfg["K"], seed, **prm)
 
 
 def cpu_oracle_rate(Y, n_b, K, seed, cells_per_batch: int, sweeps: int):
@@ -146,13 +151,14 @@ def cpu_oracle_rate(Y, n_b, K, seed, cells_per_batch: int, sweeps: int):
 def run_reference(args, rank):
     if rank != 0:
         return 0
-    n_b, K = CFG1["n_b"], CFG1["K"]
-    Y, _, _ = make_data(CFG1["seed"])
+    cfg = WORKLOADS[args.workload]
+    n_b, K = list(cfg["n_b"]), cfg["K"]
+    Y, _, _ = make_data(cfg["seed"], cfg)
     from oracle import pyoracle as po
     off = np.concatenate([[0], np.cumsum(n_b)])
     cpb = 100  # cells per batch in each step's sample
     rows = np.concatenate([np.arange(off[b], off[b] + cpb) for b in range(len(n_b))])
-    st = po.State(np.ascontiguousarray(Y[rows]), [cpb] * len(n_b), K, CFG1["seed"])
+    st = po.State(np.ascontiguousarray(Y[rows]), [cpb] * len(n_b), K, cfg["seed"])
     st.init(0.25)
     for it in range(args.warmup):
         st.sweep(it, 0)
@@ -163,12 +169,13 @@ def run_reference(args, rank):
     frac = len(rows) / float(sum(n_b))
     value = args.steps / dt * frac
     sample = ("per step: one full FP64 oracle sweep over %d cells (first %d of each batch) x %d genes of the "
-              "config-1 data; sweeps/s scaled by %d/%d cells" % (len(rows), cpb, CFG1["G"], len(rows), sum(n_b)))
+              "%s data; sweeps/s scaled by %d/%d cells" % (len(rows), cpb, cfg["G"], args.workload, len(rows),
+                                                          sum(n_b)))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (BUSseq generative model)",
-        "config": _config(),
+        "config": _config(args.workload, n_b),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference program has no CPU implementation of the sweep; this arm times the FP64 CPU "
@@ -178,10 +185,16 @@ def run_reference(args, rank):
     return 0
 
 
-def _config():
-    return {"workload": "config1: B=4 x 2500 cells (N=10000), G=10000, K=8, plain MH sampler",
-            "B": 4, "N": 10000, "G": 10000, "K": 8, "w_update": "mh", "parallelism": "replicas (one chain per GPU)",
-            "l2": "no flush: X and Y are 400 MB each, larger than L2",
+def _config(name="config1", n_b=None):
+    cfg = WORKLOADS[name]
+    n_b = list(n_b if n_b is not None else cfg["n_b"])
+    N, G, K = int(sum(n_b)), cfg["G"], cfg["K"]
+    mb = N * G * 4 / 1e6
+    desc = "%s: B=%d batches of %s cells (N=%d), G=%d, K=%d, plain MH sampler" % (
+        name, len(n_b), "/".join(str(n) for n in n_b), N, G, K)
+    return {"workload": desc, "B": len(n_b), "N": N, "G": G, "K": K, "w_update": "mh",
+            "parallelism": "replicas (one chain per GPU)",
+            "l2": "no flush: X and Y are %.0f MB each, larger than L2" % mb,
             "precision": "f32 likelihood terms, f64 acceptance sums"}
 
 
@@ -224,6 +237,8 @@ def main():
     ap.add_argument("--cells", type=int, default=0,
                     help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
+    ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
+                    help="config1 (the headline, default) or config4 (N=50000, G=20000, K=12, uneven batches)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     args = ap.parse_args()
@@ -248,13 +263,12 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    n_b, G, K = CFG1["n_b"], CFG1["G"], CFG1["K"]
-    seed = CFG1["seed"]
+    cfg = WORKLOADS[args.workload]
+    n_b, G, K = list(cfg["n_b"]), cfg["G"], cfg["K"]
+    seed = cfg["seed"]
     if args.cells > 0:
         n_b = [args.cells] * len(n_b)
-        Y, W_true, _ = bq.simulate(n_b, G, K, seed)
-    else:
-        Y, W_true, _ = make_data(seed)
+    Y, W_true, _ = make_data(seed, cfg, n_b)
     N = int(sum(n_b))
 
     # ---- value: counts resident in HBM, graph-launched sweeps ---------------
@@ -291,7 +305,7 @@ def main():
     if args.only_value:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                              "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(),
+                              "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(args.workload, n_b),
                               "note": "device-resident sweep rate only (--only-value)"}))
         s.close()
         return 0
@@ -304,7 +318,7 @@ def main():
     alg_bytes = s.kernel_bytes(kid)
     achieved = alg_bytes / (prof[dom] / 1000.0) / 1e9
     peak, peak_kind = _peak_hbm()
-    traffic = _traffic(dom)
+    traffic = _traffic(dom, args.workload) if args.cells <= 0 else None
     s.close()
     del Yd
     torch.cuda.empty_cache()
@@ -347,7 +361,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (BUSseq generative model, seed %d)" % seed,
-            "config": _config(),
+            "config": _config(args.workload, n_b),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "note": "one job per run: pinned-host upload, init, %d sweeps, posterior, all estimates to host"
