@@ -111,6 +111,8 @@ def lib():
         "busseq_run_stage": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
         "busseq_get_log_ratios": ([H, C.POINTER(LogRatios)], C.c_int),
         "busseq_set_stream": ([H, C.c_void_p], C.c_int),
+        "busseq_checkpoint_save": ([H, C.c_char_p], C.c_int),
+        "busseq_checkpoint_load": ([H, C.c_char_p], C.c_int),
         "busseq_profile": ([H, C.c_int32, _PD, C.c_int32, _PI32], C.c_int),
         "busseq_kernel_name": ([C.c_int32], C.c_char_p),
         "busseq_kernel_bytes": ([H, C.c_int32], C.c_double),
@@ -262,6 +264,28 @@ class Sampler:
             setattr(p, k, _p(v, _PI32 if v.dtype == np.int32 else _PD))
         _check(lib().busseq_get_preserved(self._h, C.byref(p)))
         return o
+
+    def checkpoint_save(self, path: str):
+        """Writes the chain and the run in progress to `path` (busseq_checkpoint_save)."""
+        _check(lib().busseq_checkpoint_save(self._h, os.fsencode(path)))
+
+    def checkpoint_load(self, path: str):
+        """Restores a checkpoint written for the same counts, dimensions, seed and
+        options; a run in progress continues with sweeps() / finish()."""
+        _check(lib().busseq_checkpoint_load(self._h, os.fsencode(path)))
+        kept = self._read_run_lengths(path)  # the Python side mirrors the restored run's length
+        if kept is not None:
+            self.n_kept = kept
+
+    @staticmethod
+    def _read_run_lengths(path: str):
+        import struct
+        with open(path, "rb") as f:
+            head = f.read(8 + 4 + 4 * 11)
+        if len(head) < 56 or head[:8] != b"BUSSEQCK":
+            return None
+        (_ver, _B, _K, _wu, _kd, begun, _fin, n_iter, n_burnin, _nu, _ih, _idev) = struct.unpack("<I11i", head[8:56])
+        return (n_iter - n_burnin) if begun else None
 
     def bic(self) -> float:
         v = C.c_double()

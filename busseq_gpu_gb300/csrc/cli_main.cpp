@@ -16,6 +16,7 @@
 #include <sys/time.h>
 
 #include <chrono>
+#include <string>
 #include <vector>
 
 namespace {
@@ -44,11 +45,16 @@ int main(int argc, char** argv) {
   char output_file[4096] = "demo_output";
   char n_file[4096] = "";
   int n_file_flag = 0, burnin_flag = 1, unchanged_flag = 1, seed_flag = 1;
-  int w_update = BUSSEQ_W_MH, device = 0, stats = 0;
+  int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0;
+  std::string ck_path, resume_path;
 
   static struct option longopts[] = {{"w-update", required_argument, nullptr, 1000},
                                      {"device", required_argument, nullptr, 1001},
                                      {"stats", no_argument, nullptr, 1002},
+                                     {"checkpoint", required_argument, nullptr, 1003},
+                                     {"checkpoint-every", required_argument, nullptr, 1004},
+                                     {"resume", required_argument, nullptr, 1005},
+                                     {"stop-after", required_argument, nullptr, 1006},
                                      {nullptr, 0, nullptr, 0}};
   int opt;
   while ((opt = getopt_long(argc, argv, "B:N:G:K:s:c:i:b:u:po:", longopts, nullptr)) != -1) {
@@ -71,6 +77,10 @@ int main(int argc, char** argv) {
         break;
       case 1001: device = atoi(optarg); break;
       case 1002: stats = 1; break;
+      case 1003: ck_path = optarg; break;
+      case 1004: ck_every = atoi(optarg); break;
+      case 1005: resume_path = optarg; break;
+      case 1006: stop_after = atoi(optarg); break;
       default:
         printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
                "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
@@ -142,11 +152,51 @@ int main(int argc, char** argv) {
 
   printf("Start MCMC.\n");
   fflush(stdout);
-  if (busseq_begin(h, n_iter, n_burnin, n_unchanged) != BUSSEQ_OK) die_lib("starting the run");
-  if (busseq_sweeps(h, n_burnin) != BUSSEQ_OK || busseq_synchronize(h) != BUSSEQ_OK) die_lib("burn-in");
+  int done = 0;
+  if (!resume_path.empty()) {
+    // --resume: the run's lengths come from the checkpoint
+    if (busseq_checkpoint_load(h, resume_path.c_str()) != BUSSEQ_OK) die_lib("resuming");
+    if (busseq_get_progress(h, &done, &n_iter, &n_burnin) != BUSSEQ_OK) die_lib("resuming");
+    if (n_iter == 0) {
+      fprintf(stderr, "%s holds no run in progress\n", resume_path.c_str());
+      return 1;
+    }
+    fprintf(stderr, "resumed from %s at sweep %d of %d\n", resume_path.c_str(), done, n_iter);
+  } else if (busseq_begin(h, n_iter, n_burnin, n_unchanged) != BUSSEQ_OK) {
+    die_lib("starting the run");
+  }
+  // sweeps up to `target`, with a checkpoint every ck_every sweeps and at the
+  // end of each phase when --checkpoint is given
+  if (stop_after > 0 && ck_path.empty()) {
+    fprintf(stderr, "--stop-after needs --checkpoint\n");
+    return 1;
+  }
+  auto advance_to = [&](int target, const char* what) {
+    if (stop_after > 0 && target > stop_after) target = stop_after;
+    while (done < target) {
+      int step = target - done;
+      if (ck_every > 0 && step > ck_every - done % ck_every) step = ck_every - done % ck_every;
+      if (busseq_sweeps(h, step) != BUSSEQ_OK) die_lib(what);
+      done += step;
+      if (!ck_path.empty() && (done == target || (ck_every > 0 && done % ck_every == 0)))
+        if (busseq_synchronize(h) != BUSSEQ_OK || busseq_checkpoint_save(h, ck_path.c_str()) != BUSSEQ_OK)
+          die_lib("writing the checkpoint");
+    }
+    if (busseq_synchronize(h) != BUSSEQ_OK) die_lib(what);
+  };
+  auto stop_here = [&]() {
+    if (stop_after > 0 && done >= stop_after && done < n_iter) {
+      fprintf(stderr, "stopped after sweep %d of %d; checkpoint in %s\n", done, n_iter, ck_path.c_str());
+      busseq_destroy(h);
+      exit(0);
+    }
+  };
+  advance_to(n_burnin, "burn-in");
+  stop_here();
   printf("Burnin completed. Start recording iterations.\n");
   fflush(stdout);
-  if (busseq_sweeps(h, n_iter - n_burnin) != BUSSEQ_OK || busseq_synchronize(h) != BUSSEQ_OK) die_lib("sampling");
+  advance_to(n_iter, "sampling");
+  stop_here();
   double t3 = now_s();
 
   printf("Start posterior inference.\n");

@@ -97,6 +97,44 @@ __global__ void k_zmask_from_zval(DevState s) {
   atomicOr(&s.zm[(int64_t)ig.x * s.Gw + (ig.y >> 5)], 1u << (ig.y & 31));
 }
 
+// X at the Y == 0 entries, in list order (checkpoint files store only these:
+// X equals Y everywhere else).
+__global__ void k_zlist_gather_x(DevState s, int32_t* out) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= s.nz0) return;
+  const int2 ig = s.zij[j];
+  out[j] = s.X[(int64_t)ig.x * s.Gp + ig.y];
+}
+
+__global__ void k_zlist_scatter_x(DevState s, const int32_t* in) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= s.nz0) return;
+  const int2 ig = s.zij[j];
+  s.X[(int64_t)ig.x * s.Gp + ig.y] = in[j];
+}
+
+// Order-independent 64-bit fingerprint of Y: sum over entries of
+// (Y + 1) * mix(entry index + 0x9E3779B97F4A7C15) mod 2^64, mix = the
+// SplitMix64 finaliser (the offset keeps every entry's weight nonzero: the
+// finaliser maps 0 to 0).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_y_fingerprint(DevState s, unsigned long long* out) {
+  const int64_t total = s.N * s.G;
+  uint64_t acc = 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / s.G, g = e - i * s.G;
+    acc += (uint64_t)(s.Y[i * s.Gp + g] + 1) * mix64((uint64_t)e + 0x9E3779B97F4A7C15ull);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, (unsigned long long)acc);
+}
+
 // Histogram of Y > 0 per batch; warp-aggregated so that repeated small values
 // cost one atomic per distinct value per warp.
 __global__ void k_init_hist(DevState s, int32_t* hist) {

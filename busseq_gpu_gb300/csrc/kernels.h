@@ -26,6 +26,9 @@ __global__ void k_init_hist(DevState s, int32_t* hist);
 __global__ void k_zlist_fill(DevState s, const int64_t* rowoff, int2* zij);
 __global__ void k_zval_from_mask(DevState s);
 __global__ void k_zmask_from_zval(DevState s);
+__global__ void k_zlist_gather_x(DevState s, int32_t* out);
+__global__ void k_zlist_scatter_x(DevState s, const int32_t* in);
+__global__ void k_y_fingerprint(DevState s, unsigned long long* out);
 __global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell);
 __global__ void k_init_raw(DevState s);
 __global__ void k_init_finish(DevState s, int fresh);

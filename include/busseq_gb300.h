@@ -195,6 +195,22 @@ int busseq_get_state(busseq_handle* h, busseq_state* out);
  * cell order) is recomputed on the device. */
 int busseq_set_state(busseq_handle* h, const busseq_state* in);
 
+/* Checkpoint and resume (no reference equivalent: the reference program can
+ * neither stop nor continue a run).  busseq_checkpoint_save writes the chain
+ * state (X and Z of the Y == 0 entries, W, L and every parameter), and, when a
+ * run has begun, its lengths, sweep counters, posterior accumulators and kept
+ * draws, to `path` (through `path`.tmp and a rename).  busseq_checkpoint_load
+ * restores them into a handle created from the same counts (checked by a
+ * fingerprint), dimensions, seed, W move and keep_draws setting; the run then
+ * continues with busseq_sweeps / busseq_finish.  Draws are keyed by the sweep
+ * index, so a resumed run reproduces an uninterrupted one bit for bit. */
+int busseq_checkpoint_save(busseq_handle* h, const char* path);
+int busseq_checkpoint_load(busseq_handle* h, const char* path);
+
+/* Position of the current run: sweeps launched so far, run length and burn-in
+ * length (all 0 before busseq_begin).  NULL pointers are skipped. */
+int busseq_get_progress(busseq_handle* h, int32_t* n_done, int32_t* n_iter, int32_t* n_burnin);
+
 /* Runs one stage of the sweep at sweep index `iter` (p and tau0 are redrawn in
  * stage 0 when iter >= n_unchanged). */
 int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_unchanged);
