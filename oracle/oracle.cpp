@@ -941,6 +941,154 @@ double orc_term_gamma1(double g0, double g1o, double g1n, int X, int Z) {
   return (g1n * X * Z - softplus(g0 + g1n * X)) - (g1o * X * Z - softplus(g0 + g1o * X));
 }
 
+// ---------------------------------------------------------------------------
+// Gradient-based block update (Hamiltonian Monte Carlo).  Not in the
+// reference: its alpha, beta, nu, delta and phi steps are random-walk
+// Metropolis (BUSseq_gpu.cu:602-818).  The target is the same conditional
+// density those steps leave invariant, taken jointly over
+//   theta = (alpha_g, beta_gk (k >= 1), nu_bg (b >= 1), delta_i (not the first
+//            cell of a batch), psi_bg = log phi_bg)
+// given X, W, L, p and tau0:
+//   log p = sum_{i,g} [lgamma(x + phi) - lgamma(phi) + phi log phi
+//                      - (phi + x) log(phi + mu) + x eta]      (eta = log mu)
+//         - (alpha - mu_alpha)^2 / (2 sigma2_alpha) - beta^2 / (2 v(L))
+//         - (nu - mu_nu)^2 / (2 sigma2_nu) - (delta - mu_delta)^2 / (2 sigma2_delta)
+//         + kappa psi - tau_phi e^psi          (Gamma(kappa, rate tau) prior on phi
+//                                               and the Jacobian of psi = log phi)
+// with v(L) = tau1 if L = 1 else tau0, exactly the priors of the MH steps
+// (:625-632, :696-707, :730-737, :763-778, :806-818).  Terms constant in theta
+// (lgamma(x + 1)) are dropped.
+// ---------------------------------------------------------------------------
+double orc_hmc_logpost(const orc_state* st) {
+  const int64_t G = st->G, N = st->N;
+  const int B = st->B, K = st->K;
+  auto off = batch_offsets(st);
+  double ll = 0.0;
+#pragma omp parallel for reduction(+ : ll) schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    double acc = 0.0;
+    for (int64_t g = 0; g < G; ++g) {
+      const double x = st->X[i * G + g];
+      const double ph = st->phi[b * G + g];
+      const double eta = st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->nu[b * G + g] + st->delta[i];
+      const double mu = exp(eta);
+      acc += lgamma(x + ph) - lgamma(ph) + ph * log(ph) - (ph + x) * log(ph + mu) + x * eta;
+    }
+    ll += acc;
+  }
+  double pr = 0.0;
+  const double tau0 = st->p_tau0[1];
+  for (int64_t g = 0; g < G; ++g) {
+    const double da = st->alpha[g] - st->mu_alpha[g];
+    pr -= da * da / (2.0 * SIGMA2_ALPHA);
+    for (int k = 1; k < K; ++k) {
+      const double bt = st->beta[k * G + g];
+      pr -= bt * bt / (2.0 * (st->L[k * G + g] == 1 ? TAU1 : tau0));
+    }
+    for (int b = 1; b < B; ++b) {
+      const double dn = st->nu[b * G + g] - st->mu_nu[b];
+      pr -= dn * dn / (2.0 * SIGMA2_NU);
+    }
+    for (int b = 0; b < B; ++b) {
+      const double ph = st->phi[b * G + g];
+      pr += KAPPA_PHI * log(ph) - TAU_PHI * ph;
+    }
+  }
+  for (int b = 0; b < B; ++b)
+    for (int64_t i = off[b] + 1; i < off[b + 1]; ++i) {
+      const double dd = st->delta[i] - st->mu_delta[i];
+      pr -= dd * dd / (2.0 * SIGMA2_DELTA);
+    }
+  return ll + pr;
+}
+
+// Gradient of orc_hmc_logpost with respect to theta (psi = log phi), and the
+// diagonal metric used by the kernels: the Fisher information of the
+// eta-coordinates, sum phi mu / (phi + mu) over the coordinate's entries, and
+// the observed information of psi, each plus the prior's curvature.  Fixed
+// coordinates (beta_0, nu_0, the first cell of each batch) get gradient 0 and
+// metric 1.  Any output pointer may be NULL.
+int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double* gd, double* gp, double* ma,
+                 double* mb, double* mn, double* md, double* mp) {
+  const int64_t G = st->G, N = st->N;
+  const int B = st->B, K = st->K;
+  auto off = batch_offsets(st);
+  std::vector<double> sa(G, 0.0), sb((size_t)K * G, 0.0), sn((size_t)B * G, 0.0), sp((size_t)B * G, 0.0);
+  std::vector<double> wa(G, 0.0), wb((size_t)K * G, 0.0), wn((size_t)B * G, 0.0), ip((size_t)B * G, 0.0);
+  std::vector<double> sd(N, 0.0), wd(N, 0.0);
+  // per cell: delta sums; per gene: the rest (cells of a batch in order)
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    for (int b = 0; b < B; ++b) {
+      const double ph = st->phi[b * G + g];
+      for (int64_t i = off[b]; i < off[b + 1]; ++i) {
+        const int k = st->W[i];
+        const double x = st->X[i * G + g];
+        const double mu = exp(st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g] + st->delta[i]);
+        const double r = ph * (x - mu) / (ph + mu);
+        const double w = ph * mu / (ph + mu);
+        sa[g] += r;
+        wa[g] += w;
+        sb[(size_t)k * G + g] += r;
+        wb[(size_t)k * G + g] += w;
+        sn[(size_t)b * G + g] += r;
+        wn[(size_t)b * G + g] += w;
+        double dg = 0.0, tg = 0.0;  // psi(x + phi) - psi(phi), psi'(phi) - psi'(x + phi)
+        for (int j = 0; j < (int)x; ++j) {
+          dg += 1.0 / (ph + j);
+          tg += 1.0 / ((ph + j) * (ph + j));
+        }
+        const double d1 = dg + log(ph) - log(ph + mu) + (mu - x) / (ph + mu);           // d ll / d phi
+        const double d2 = -tg + 1.0 / ph - 2.0 / (ph + mu) + (ph + x) / ((ph + mu) * (ph + mu));  // d2 ll / d phi2
+        sp[(size_t)b * G + g] += ph * d1;
+        ip[(size_t)b * G + g] -= ph * d1 + ph * ph * d2;
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    const int k = st->W[i];
+    double s = 0.0, w = 0.0;
+    for (int64_t g = 0; g < G; ++g) {
+      const double ph = st->phi[b * G + g];
+      const double x = st->X[i * G + g];
+      const double mu = exp(st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g] + st->delta[i]);
+      s += ph * (x - mu) / (ph + mu);
+      w += ph * mu / (ph + mu);
+    }
+    sd[i] = s;
+    wd[i] = w;
+  }
+  const double tau0 = st->p_tau0[1];
+  for (int64_t g = 0; g < G; ++g) {
+    if (ga) ga[g] = sa[g] - (st->alpha[g] - st->mu_alpha[g]) / SIGMA2_ALPHA;
+    if (ma) ma[g] = wa[g] + 1.0 / SIGMA2_ALPHA;
+    for (int k = 0; k < K; ++k) {
+      const int64_t pos = (int64_t)k * G + g;
+      const double v = st->L[pos] == 1 ? TAU1 : tau0;
+      if (gb) gb[pos] = k == 0 ? 0.0 : sb[pos] - st->beta[pos] / v;
+      if (mb) mb[pos] = k == 0 ? 1.0 : wb[pos] + 1.0 / v;
+    }
+    for (int b = 0; b < B; ++b) {
+      const int64_t pos = (int64_t)b * G + g;
+      if (gn) gn[pos] = b == 0 ? 0.0 : sn[pos] - (st->nu[pos] - st->mu_nu[b]) / SIGMA2_NU;
+      if (mn) mn[pos] = b == 0 ? 1.0 : wn[pos] + 1.0 / SIGMA2_NU;
+      const double ph = st->phi[pos];
+      if (gp) gp[pos] = sp[pos] + KAPPA_PHI - TAU_PHI * ph;
+      if (mp) mp[pos] = ip[pos] + TAU_PHI * ph;
+    }
+  }
+  for (int b = 0; b < B; ++b)
+    for (int64_t i = off[b]; i < off[b + 1]; ++i) {
+      const bool first = i == off[b];
+      if (gd) gd[i] = first ? 0.0 : sd[i] - (st->delta[i] - st->mu_delta[i]) / SIGMA2_DELTA;
+      if (md) md[i] = first ? 1.0 : wd[i] + 1.0 / SIGMA2_DELTA;
+    }
+  return 0;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

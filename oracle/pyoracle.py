@@ -74,6 +74,9 @@ def lib():
         L.orc_term_gamma0.restype = C.c_double
         L.orc_term_gamma1.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
         L.orc_term_gamma1.restype = C.c_double
+        L.orc_hmc_logpost.argtypes = [C.POINTER(OrcState)]
+        L.orc_hmc_logpost.restype = C.c_double
+        L.orc_hmc_grad.argtypes = [C.POINTER(OrcState)] + [_PD] * 10
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -164,6 +167,20 @@ class State:
 
     def sweep(self, it: int, n_unchanged: int, w_update: int = 0):
         lib().orc_sweep(C.byref(self.c()), it, n_unchanged, w_update)
+
+    def hmc_logpost(self) -> float:
+        """Log posterior of (alpha, beta, nu, delta, log phi) given the rest, up to a constant."""
+        return lib().orc_hmc_logpost(C.byref(self.c()))
+
+    def hmc_grad(self) -> dict:
+        """Gradient of hmc_logpost (psi = log phi) and the diagonal metric."""
+        G, K, B, N = self.G, self.K, self.B, self.N
+        o = {"alpha": np.zeros(G), "beta": np.zeros((K, G)), "nu": np.zeros((B, G)), "delta": np.zeros(N),
+             "psi": np.zeros((B, G))}
+        m = {k: np.zeros_like(v) for k, v in o.items()}
+        lib().orc_hmc_grad(C.byref(self.c()), *[_ptr(o[k], _PD) for k in ("alpha", "beta", "nu", "delta", "psi")],
+                           *[_ptr(m[k], _PD) for k in ("alpha", "beta", "nu", "delta", "psi")])
+        return {"grad": o, "metric": m}
 
     def bic(self):
         ll = np.zeros((self.K, self.N))
