@@ -44,7 +44,8 @@ class Dims(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
-                ("device", C.c_int32), ("chunk_cells", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("device", C.c_int32), ("chunk_cells", C.c_int32), ("hmc_leapfrog", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
 
 
 class Estimates(C.Structure):
@@ -113,6 +114,10 @@ def lib():
         "busseq_set_stream": ([H, C.c_void_p], C.c_int),
         "busseq_checkpoint_save": ([H, C.c_char_p], C.c_int),
         "busseq_checkpoint_load": ([H, C.c_char_p], C.c_int),
+        "busseq_get_progress": ([H, _PI32, _PI32, _PI32], C.c_int),
+        "busseq_hmc_stats": ([H, _PD], C.c_int),
+        "busseq_hmc_gradient": ([H, _PD, _PD], C.c_int),
+        "busseq_hmc_logpost_diff": ([H, C.POINTER(State), _PD], C.c_int),
         "busseq_profile": ([H, C.c_int32, _PD, C.c_int32, _PI32], C.c_int),
         "busseq_kernel_name": ([C.c_int32], C.c_char_p),
         "busseq_kernel_bytes": ([H, C.c_int32], C.c_double),
@@ -174,7 +179,7 @@ class Sampler:
     read counts -> initialise -> sweeps -> posterior -> files)."""
 
     def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
-                 keep_draws: bool = False, device: int = 0, chunk_cells: int = 0):
+                 keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
         self.B, self.K = len(self.n_b), int(K)
@@ -182,7 +187,8 @@ class Sampler:
         if isinstance(w_update, str):
             w_update = {"mh": W_MH, "gibbs": W_GIBBS}[w_update]
         opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
-                      keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells))
+                      keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells),
+                      hmc_leapfrog=int(hmc_leapfrog))
         on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
         if on_dev:
             assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2
@@ -318,7 +324,9 @@ class Sampler:
         _check(lib().busseq_get_state(self._h, C.byref(s)))
         return o
 
-    def set_state(self, st: dict):
+    def _state_struct(self, st: dict):
+        """A State structure pointing at (converted copies of) the arrays in `st`,
+        and the list that keeps those copies alive."""
         ref = self._state_arrays()
         s = State()
         keep = []
@@ -328,7 +336,12 @@ class Sampler:
             a = np.ascontiguousarray(st[k], dtype=v.dtype).reshape(v.shape)
             keep.append(a)
             setattr(s, k, _p(a, self._ptr_for(a)))
+        return s, keep
+
+    def set_state(self, st: dict):
+        s, keep = self._state_struct(st)
         _check(lib().busseq_set_state(self._h, C.byref(s)))
+        del keep
 
     def run_stage(self, stage, it: int, n_unchanged: int = 1 << 30):
         if isinstance(stage, str):
@@ -350,10 +363,46 @@ class Sampler:
         _check(lib().busseq_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
 
     def profile(self, n_sweeps: int) -> dict:
-        ms = np.zeros(16)
+        """Mean event-timed milliseconds per sweep of every kernel (summed over
+        its launches in a sweep); kernels the sampler does not launch read 0."""
+        ms = np.zeros(64)
         n = C.c_int32()
-        _check(lib().busseq_profile(self._h, n_sweeps, _p(ms, _PD), 16, C.byref(n)))
+        _check(lib().busseq_profile(self._h, n_sweeps, _p(ms, _PD), 64, C.byref(n)))
         return {lib().busseq_kernel_name(i).decode(): float(ms[i]) for i in range(n.value)}
+
+    # ---- gradient-based block update (hmc_leapfrog > 0) ----------------------
+    def _hmc_split(self, flat):
+        G, K, B, N = self.G, self.K, self.B, self.N
+        o, at = {}, 0
+        for name, shape in (("alpha", (G,)), ("beta", (K, G)), ("nu", (B, G)), ("psi", (B, G)), ("delta", (N,))):
+            n = int(np.prod(shape))
+            o[name] = flat[at:at + n].reshape(shape)
+            at += n
+        return o
+
+    def hmc_stats(self) -> dict:
+        out = np.zeros(4)
+        _check(lib().busseq_hmc_stats(self._h, _p(out, _PD)))
+        return {"step_size": out[0], "accept_rate_kept": out[1], "last_accept_prob": out[2], "last_dH": out[3]}
+
+    def hmc_gradient(self, with_metric: bool = True) -> dict:
+        """Gradient (and metric) of the block log posterior at the current state."""
+        n = self.G * (1 + self.K + 2 * self.B) + self.N
+        g = np.zeros(n)
+        m = np.zeros(n) if with_metric else None
+        _check(lib().busseq_hmc_gradient(self._h, _p(g, _PD), _p(m, _PD) if m is not None else None))
+        out = {"grad": self._hmc_split(g)}
+        if m is not None:
+            out["metric"] = self._hmc_split(m)
+        return out
+
+    def hmc_logpost_diff(self, from_state: dict) -> float:
+        """Block log posterior of the current state minus that of `from_state`."""
+        st, keep = self._state_struct(from_state)
+        out = C.c_double()
+        _check(lib().busseq_hmc_logpost_diff(self._h, C.byref(st), C.byref(out)))
+        del keep
+        return float(out.value)
 
     def kernel_bytes(self, i: int) -> float:
         return float(lib().busseq_kernel_bytes(self._h, i))

@@ -81,6 +81,29 @@ enum PropMask : int {
   PROP_ALL = 63
 };
 
+// Unevaluated sum hi + lo of two floats (a "float-float" value, ~48 bits).
+struct FF {
+  float hi, lo;
+};
+
+// Device scalars of the HMC block update (double [HS_COUNT]).
+enum HmcScalar : int {
+  HS_EPS = 0,         // step size (adapted during burn-in)
+  HS_HBAR = 1,        // dual-averaging statistic
+  HS_MU = 2,          // dual-averaging shrinkage point, log(10 eps0)
+  HS_M = 3,           // dual-averaging iteration count
+  HS_LOG_EPS_BAR = 4, // averaged log step size
+  HS_EPS_USED = 5,    // jittered step size of the current transition
+  HS_LAST_DH = 6,     // H(end) - H(start) of the last transition
+  HS_LAST_ACC = 7,    // min(1, exp(-dH)) of the last transition
+  HS_ACCEPTED = 8,    // 1 if the last transition was accepted
+  HS_N_KEPT = 9,      // transitions in kept sweeps
+  HS_ACC_KEPT = 10,   // accepted transitions in kept sweeps
+  HS_COUNT = 16
+};
+constexpr double HMC_TARGET_ACCEPT = 0.7;
+constexpr double HMC_EPS0 = 0.05;
+
 struct DevState {
   // dimensions and run configuration
   int B, K;
@@ -126,6 +149,22 @@ struct DevState {
   float* nu_p;     // [B][Gp]
   float* delta_p;  // [N]
   float* phi_p;    // [B][Gp]
+
+  // gradient-based block update (hmc_L > 0 selects it); flat layout
+  // alpha [Gp] | beta [K][Gp] | nu [B][Gp] | psi [B][Gp] | delta [N]
+  int hmc_L;
+  int64_t hmc_D;
+  float* psi;       // [B][Gp] log phi: the position of the phi block
+  float* hmc_mom;   // [D] momentum
+  float* hmc_mom0;  // [D] momentum at the start of the transition
+  float* hmc_grad;  // [D] gradient of the log posterior
+  float* hmc_mass;  // [D] diagonal metric
+  float* hmc_th0;   // [D] coordinates at the start of the transition
+  float* hmc_cpart; // [n_tiles][N] per-tile sums of d ll / d delta
+  float* hmc_cpartw;// [n_tiles][N] per-tile Fisher information of delta
+  FF* hmc_hpart;    // [n_tiles * cap_g] per-CTA log-likelihood change
+  FF* hmc_epart;    // [ceil(D / 256)] per-CTA kinetic minus prior change
+  double* hmc_sc;   // [HS_COUNT]
   float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   float* gamma_p;  // [2][B]

@@ -5,6 +5,7 @@
 #include "kernels.h"
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -43,11 +44,20 @@ int fail(int code, const char* fmt, ...) {
 int64_t round_up(int64_t a, int64_t m) { return (a + m - 1) / m * m; }
 unsigned blocks_for(int64_t n, int t) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
-const char* const kKernelNames[] = {"k_propose",     "k_zx",      "k_alpha",   "k_decide_alpha", "k_beta_nu",
-                                    "k_decide_beta", "k_decide_nu_E", "k_delta", "k_phi",          "k_decide_phi",
-                                    "k_w",           "k_sort_pi", "k_posterior"};
-constexpr int kNumKernels = 13;
-constexpr int kBurnLaunches = 12;  // kernels 0..11; kept sweeps add k_posterior
+const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha",      "k_decide_alpha",
+                                    "k_beta_nu",      "k_decide_beta",  "k_decide_nu_E", "k_delta",
+                                    "k_phi",          "k_decide_phi",   "k_w",          "k_sort_pi",
+                                    "k_posterior",    "k_hmc_grad",     "k_hmc_assemble", "k_hmc_start",
+                                    "k_hmc_leap0",    "k_hmc_leap",     "k_hmc_refresh_E", "k_hmc_dll",
+                                    "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish"};
+constexpr int kNumKernels = 23;
+enum : int {
+  KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
+  KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
+  KID_POSTERIOR = 12, KID_HMC_GRAD = 13, KID_HMC_ASSEMBLE = 14, KID_HMC_START = 15, KID_HMC_LEAP0 = 16,
+  KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
+  KID_HMC_FINISH = 22
+};
 
 }  // namespace
 
@@ -120,7 +130,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
   const dim3 gene_grid(s.n_tiles, s.cap_g);
   switch (which) {
     case 0:
-      k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(s, PROP_ALL);
+      k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(s, s.hmc_L > 0 ? (int)PROP_GAMMA : (int)PROP_ALL);
       LAUNCH_CHECK("k_propose");
       break;
     case 1:
@@ -174,15 +184,74 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_posterior");
       break;
     }
+    case KID_HMC_GRAD:
+      k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s, 0);
+      LAUNCH_CHECK("k_hmc_grad");
+      break;
+    case KID_HMC_ASSEMBLE:
+      k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, 0);
+      LAUNCH_CHECK("k_hmc_assemble");
+      break;
+    case KID_HMC_START:
+      k_hmc_start<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_start");
+      break;
+    case KID_HMC_LEAP0:
+    case KID_HMC_LEAP:
+      k_hmc_leap<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, which == KID_HMC_LEAP0 ? 1 : 0);
+      LAUNCH_CHECK("k_hmc_leap");
+      break;
+    case KID_HMC_E:
+      k_hmc_refresh_E<<<blocks_for((int64_t)s.B * s.K * s.Gp, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_refresh_E");
+      break;
+    case KID_HMC_DLL:
+      k_hmc_dll<<<gene_grid, GENE_TILE, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_dll");
+      break;
+    case KID_HMC_ENERGY:
+      k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, 1);
+      LAUNCH_CHECK("k_hmc_energy");
+      break;
+    case KID_HMC_ACCEPT:
+      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256), 0);
+      LAUNCH_CHECK("k_hmc_accept");
+      break;
+    case KID_HMC_FINISH:
+      k_hmc_finish<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_finish");
+      break;
     default:
       return fail(BUSSEQ_ERR_ARG, "no kernel %d", which);
   }
   return BUSSEQ_OK;
 }
 
+// The kernels of one sweep, in order.  Random-walk MH (the reference's sweep):
+// proposals, Z/X, alpha, L, p/tau0, gamma, beta, nu, delta, phi, W, pi.  HMC:
+// proposals of gamma, Z/X, L, p/tau0, gamma, one HMC transition of
+// (alpha, beta, nu, delta, log phi), W, pi.
+std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
+  std::vector<int> q;
+  if (h->s.hmc_L > 0) {
+    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD, KID_HMC_ASSEMBLE, KID_HMC_START};
+    for (int l = 0; l < h->s.hmc_L; ++l) {
+      q.push_back(l == 0 ? KID_HMC_LEAP0 : KID_HMC_LEAP);
+      q.push_back(KID_HMC_E);
+      q.push_back(KID_HMC_GRAD);
+      q.push_back(KID_HMC_ASSEMBLE);
+    }
+    const int tail[] = {KID_HMC_DLL, KID_HMC_ENERGY, KID_HMC_ACCEPT, KID_HMC_FINISH, KID_HMC_E, KID_W, KID_SORT_PI};
+    q.insert(q.end(), tail, tail + 7);
+  } else {
+    for (int k = 0; k <= KID_SORT_PI; ++k) q.push_back(k);
+  }
+  if (kept) q.push_back(KID_POSTERIOR);
+  return q;
+}
+
 int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
-  const int n = kept ? kNumKernels : kBurnLaunches;
-  for (int k = 0; k < n; ++k) TRY(launch_kernel(h, k, st, kept, h->s));
+  for (int k : sweep_sequence(h, kept)) TRY(launch_kernel(h, k, st, kept, h->s));
   return BUSSEQ_OK;
 }
 
@@ -363,6 +432,24 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&s.ctile, s.cap_c));
     TRY(h->alloc(&s.seg_cnt, B * K));
     TRY(h->alloc(&s.part, (int64_t)s.cap_g * bq::NSLOT * Gp));
+    // the gradient-based block update
+    s.hmc_L = std::max(0, opt.hmc_leapfrog);
+    s.hmc_D = Gp * (1 + K + 2 * B) + N;
+    if (s.hmc_L > 0) {
+      TRY(h->alloc(&s.psi, B * Gp));
+      TRY(h->alloc(&s.hmc_mom, s.hmc_D));
+      TRY(h->alloc(&s.hmc_mom0, s.hmc_D));
+      TRY(h->alloc(&s.hmc_grad, s.hmc_D));
+      TRY(h->alloc(&s.hmc_mass, s.hmc_D));
+      TRY(h->alloc(&s.hmc_th0, s.hmc_D));
+      TRY(h->alloc(&s.hmc_cpart, (int64_t)s.n_tiles * N));
+      TRY(h->alloc(&s.hmc_cpartw, (int64_t)s.n_tiles * N));
+      TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g));
+      TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
+      TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
+      bq::k_hmc_unit_mass<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s);
+      LAUNCH_CHECK("k_hmc_unit_mass");
+    }
     TRY(h->alloc(&s.tpart, (int64_t)s.n_tiles * bq::MAX_B));
     TRY(h->alloc(&s.cnt_tile, s.n_tiles));
     TRY(h->alloc(&s.cnt_glob, 8));
@@ -541,6 +628,12 @@ int busseq_begin(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_u
     TRY(h->alloc(&s.keep_phi, nk * B * G, true));
     TRY(h->alloc(&s.keep_W, nk * N, true));
     TRY(h->alloc(&s.keep_pi, nk * B * K, true));
+  }
+  if (s.hmc_L > 0) {  // step size and its adaptation start afresh with every run
+    double sc[bq::HS_COUNT] = {0.0};
+    sc[bq::HS_EPS] = bq::HMC_EPS0;
+    sc[bq::HS_MU] = log(10.0 * bq::HMC_EPS0);
+    CUDA_TRY(cudaMemcpyAsync(s.hmc_sc, sc, sizeof sc, cudaMemcpyHostToDevice, h->stream));
   }
   CUDA_TRY(cudaMemsetAsync(s.iter, 0, sizeof(int), h->stream));
   CUDA_TRY(cudaMemsetAsync(s.cnt_tile, 0, s.n_tiles * sizeof(unsigned), h->stream));
@@ -858,6 +951,11 @@ std::vector<DevBlock> run_blocks(const busseq_handle* h) {
         {s.keep_pi, nk * B * K * 4}};
     v.insert(v.end(), k.begin(), k.end());
   }
+  if (s.hmc_L > 0) {  // log phi as the chain holds it, the adapted metric and the step size
+    v.push_back({s.psi, (size_t)s.B * s.Gp * 4});
+    v.push_back({s.hmc_mass, (size_t)s.hmc_D * 4});
+    v.push_back({s.hmc_sc, (size_t)bq::HS_COUNT * 8});
+  }
   return v;
 }
 
@@ -1030,19 +1128,8 @@ int busseq_checkpoint_load(busseq_handle* h, const char* path) {
   for (int64_t j = 0; j < s.nz0; ++j)
     if (zx[j] < 0 || zval[j] > 1) return fail(BUSSEQ_ERR_IO, "%s: invalid X or Z value at entry %lld", path, (long long)j);
 
-  // the run first (busseq_begin resets the counters), then the state
-  if (hd.begun) {
-    if (hd.iter_host < 0 || hd.iter_host > hd.n_iter || hd.iter_dev != hd.iter_host)
-      return fail(BUSSEQ_ERR_IO, "%s: inconsistent sweep counters", path);
-    TRY(busseq_begin(h, hd.n_iter, hd.n_burnin, hd.n_unchanged));
-    for (const DevBlock& blk : run_blocks(h)) {
-      std::vector<uint8_t> buf(blk.bytes);
-      TRY(read_block(in.f, buf.data(), blk.bytes, path, "run accumulators"));
-      CUDA_TRY(cudaMemcpy(blk.p, buf.data(), blk.bytes, cudaMemcpyHostToDevice));
-    }
-    CUDA_TRY(cudaMemcpy(s.iter, &hd.iter_dev, sizeof(int), cudaMemcpyHostToDevice));
-    h->iter_host = hd.iter_host;
-  }
+  // the state first (busseq_set_state recomputes the derived arrays), then
+  // the run (busseq_begin resets its counters; the saved ones replace them)
   busseq_state st{};
   st.W = W.data();
   st.L = L.data();
@@ -1071,8 +1158,123 @@ int busseq_checkpoint_load(busseq_handle* h, const char* path) {
     cudaFree(d);
     if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "checkpoint scatter: %s", cudaGetErrorString(e));
   }
+  if (hd.begun) {
+    if (hd.iter_host < 0 || hd.iter_host > hd.n_iter || hd.iter_dev != hd.iter_host)
+      return fail(BUSSEQ_ERR_IO, "%s: inconsistent sweep counters", path);
+    TRY(busseq_begin(h, hd.n_iter, hd.n_burnin, hd.n_unchanged));
+    for (const DevBlock& blk : run_blocks(h)) {
+      std::vector<uint8_t> buf(blk.bytes);
+      TRY(read_block(in.f, buf.data(), blk.bytes, path, "run accumulators"));
+      CUDA_TRY(cudaMemcpy(blk.p, buf.data(), blk.bytes, cudaMemcpyHostToDevice));
+    }
+    CUDA_TRY(cudaMemcpy(s.iter, &hd.iter_dev, sizeof(int), cudaMemcpyHostToDevice));
+    h->iter_host = hd.iter_host;
+  }
   h->est_valid = false;
   if (hd.begun && hd.finished) TRY(busseq_finish(h));
+  return check_device_error(h);
+}
+
+// ---- gradient-based block update: statistics and test entry points --------
+}  // extern "C"
+
+namespace {
+
+// Flat padded layout (alpha [Gp] | beta [K][Gp] | nu [B][Gp] | psi [B][Gp] |
+// delta [N]) <-> the unpadded one of the ABI (alpha [G] | beta [K*G] |
+// nu [B*G] | psi [B*G] | delta [N]).
+template <typename S, typename D>
+void hmc_unpad(const bq::DevState& s, const S* src, D* dst) {
+  const int64_t G = s.G, Gp = s.Gp;
+  const int64_t rows = 1 + s.K + 2 * s.B;
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t g = 0; g < G; ++g) dst[r * G + g] = (D)src[r * Gp + g];
+  for (int64_t i = 0; i < s.N; ++i) dst[rows * G + i] = (D)src[rows * Gp + i];
+}
+
+int need_hmc(busseq_handle* h) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (h->s.hmc_L <= 0) return fail(BUSSEQ_ERR_STATE, "the chain was created without hmc_leapfrog");
+  return BUSSEQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int busseq_hmc_stats(busseq_handle* h, double out[4]) {
+  TRY(need_hmc(h));
+  if (!out) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  double sc[bq::HS_COUNT];
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(sc, h->s.hmc_sc, sizeof sc, cudaMemcpyDeviceToHost));
+  out[0] = sc[bq::HS_EPS];
+  out[1] = sc[bq::HS_N_KEPT] > 0 ? sc[bq::HS_ACC_KEPT] / sc[bq::HS_N_KEPT] : 0.0;
+  out[2] = sc[bq::HS_LAST_ACC];
+  out[3] = sc[bq::HS_LAST_DH];
+  return BUSSEQ_OK;
+}
+
+int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
+  TRY(need_hmc(h));
+  if (!grad) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const bq::DevState& s = h->s;
+  const dim3 gene_grid(s.n_tiles, s.cap_g);
+  // the adapted metric of the chain is kept: the call works on a copy
+  std::vector<float> mass_keep(s.hmc_D);
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
+  bq::k_hmc_grad<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 1);
+  LAUNCH_CHECK("k_hmc_grad");
+  bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 1);
+  LAUNCH_CHECK("k_hmc_assemble");
+  TRY(check_device_error(h));
+  std::vector<float> gf(s.hmc_D), mf(s.hmc_D);
+  CUDA_TRY(cudaMemcpy(gf.data(), s.hmc_grad, s.hmc_D * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(mf.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(s.hmc_mass, mass_keep.data(), s.hmc_D * 4, cudaMemcpyHostToDevice));
+  hmc_unpad(s, gf.data(), grad);
+  if (metric) hmc_unpad(s, mf.data(), metric);
+  return BUSSEQ_OK;
+}
+
+int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* out) {
+  TRY(need_hmc(h));
+  if (!from || !out || !from->alpha || !from->beta || !from->nu || !from->phi || !from->delta)
+    return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const bq::DevState& s = h->s;
+  const int64_t G = s.G, Gp = s.Gp, N = s.N;
+  const int B = s.B, K = s.K;
+  std::vector<float> th((size_t)s.hmc_D, 0.0f);
+  for (int64_t g = 0; g < G; ++g) {
+    th[g] = from->alpha[g];
+    for (int k = 0; k < K; ++k) th[Gp + k * Gp + g] = from->beta[k * G + g];
+    for (int b = 0; b < B; ++b) {
+      th[Gp * (1 + K) + b * Gp + g] = from->nu[b * G + g];
+      th[Gp * (1 + K + B) + b * Gp + g] = logf(from->phi[b * G + g]);
+    }
+  }
+  for (int64_t i = 0; i < N; ++i) th[Gp * (1 + K + 2 * B) + i] = from->delta[i];
+  float* d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, s.hmc_D * 4));
+  cudaError_t e = cudaMemcpyAsync(d, th.data(), s.hmc_D * 4, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) {
+    const dim3 gene_grid(s.n_tiles, s.cap_g);
+    bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
+    bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
+    bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
+    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256), 1);
+    e = cudaGetLastError();
+  }
+  double sc[bq::HS_COUNT];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sc, s.hmc_sc, sizeof sc, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "log posterior difference: %s", cudaGetErrorString(e));
+  *out = sc[bq::HS_LAST_DH];
   return check_device_error(h);
 }
 
@@ -1114,29 +1316,32 @@ int busseq_profile(busseq_handle* h, int32_t n_sweeps, double* ms_avg, int32_t c
   if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
   if (n_sweeps <= 0) return fail(BUSSEQ_ERR_ARG, "n_sweeps must be positive");
   CUDA_TRY(cudaSetDevice(h->device));
-  const int nk = kBurnLaunches;  // one burn-in sweep: every kernel but the posterior accumulation
-  std::vector<cudaEvent_t> ev((size_t)nk * 2 * n_sweeps);
+  // burn-in sweeps (every kernel but the posterior accumulation); time per
+  // kernel id, summed over its launches in a sweep
+  const std::vector<int> seq = sweep_sequence(h, 0);
+  const size_t nl = seq.size();
+  std::vector<cudaEvent_t> ev(nl * 2 * n_sweeps);
   for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
   int r = BUSSEQ_OK;
   for (int sw = 0; sw < n_sweeps && r == BUSSEQ_OK; ++sw)
-    for (int k = 0; k < nk && r == BUSSEQ_OK; ++k) {
-      cudaEventRecord(ev[((size_t)sw * nk + k) * 2], h->stream);
-      r = launch_kernel(h, k, h->stream, 0, h->s);
-      cudaEventRecord(ev[((size_t)sw * nk + k) * 2 + 1], h->stream);
+    for (size_t k = 0; k < nl && r == BUSSEQ_OK; ++k) {
+      cudaEventRecord(ev[((size_t)sw * nl + k) * 2], h->stream);
+      r = launch_kernel(h, seq[k], h->stream, 0, h->s);
+      cudaEventRecord(ev[((size_t)sw * nl + k) * 2 + 1], h->stream);
     }
   if (r == BUSSEQ_OK) r = check_device_error(h);
-  std::vector<double> tot(nk, 0.0);
+  std::vector<double> tot(kNumKernels, 0.0);
   if (r == BUSSEQ_OK)
     for (int sw = 0; sw < n_sweeps; ++sw)
-      for (int k = 0; k < nk; ++k) {
+      for (size_t k = 0; k < nl; ++k) {
         float ms = 0.0f;
-        cudaEventElapsedTime(&ms, ev[((size_t)sw * nk + k) * 2], ev[((size_t)sw * nk + k) * 2 + 1]);
-        tot[k] += ms;
+        cudaEventElapsedTime(&ms, ev[((size_t)sw * nl + k) * 2], ev[((size_t)sw * nl + k) * 2 + 1]);
+        tot[seq[k]] += ms;
       }
   for (auto& e : ev) cudaEventDestroy(e);
   if (r != BUSSEQ_OK) return r;
-  for (int k = 0; k < nk && k < cap; ++k) ms_avg[k] = tot[k] / n_sweeps;
-  if (n_out) *n_out = nk;
+  for (int k = 0; k < kNumKernels && k < cap; ++k) ms_avg[k] = tot[k] / n_sweeps;
+  if (n_out) *n_out = std::min<int>(kNumKernels, cap);
   h->est_valid = false;
   return BUSSEQ_OK;
 }
@@ -1161,13 +1366,15 @@ double busseq_kernel_bytes(busseq_handle* h, int32_t i) {
     case 10: return 4.0 * E;
     case 11: return 8.0 * s.N;                      // W in, cell order out
     case 12: return params;
+    case 13: return 4.0 * E;                        // HMC gradient pass: read X
+    case 19: return 4.0 * E;                        // HMC log-likelihood change: read X
     default: return 0.0;
   }
 }
 
 int busseq_launches_per_sweep(busseq_handle* h, int32_t kept) {
-  (void)h;
-  return kept ? kNumKernels : kBurnLaunches;
+  if (!h) return 0;
+  return (int)sweep_sequence(h, kept).size();
 }
 
 }  // extern "C"

@@ -432,21 +432,6 @@ __device__ __forceinline__ int stage_chunk(const DevState& s, int start, int len
   return len8;
 }
 
-// X and exp(delta) of chunk cells j0..j0+7 for the gene whose column starts
-// at Xg (128-bit shared loads; row offsets by one 32x32->64-bit multiply-add).
-__device__ __forceinline__ void load8(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D, int j0,
-                                      int (&xr)[8], float (&dv)[8]) {
-  const int4 ia = *reinterpret_cast<const int4*>(s_i + j0);
-  const int4 ib = *reinterpret_cast<const int4*>(s_i + j0 + 4);
-  const float4 da = *reinterpret_cast<const float4*>(s_D + j0);
-  const float4 db = *reinterpret_cast<const float4*>(s_D + j0 + 4);
-  const int iv[8] = {ia.x, ia.y, ia.z, ia.w, ib.x, ib.y, ib.z, ib.w};
-#pragma unroll
-  for (int u = 0; u < 8; ++u) xr[u] = *reinterpret_cast<const int*>(Xg + (uint64_t)(uint32_t)iv[u] * row_bytes);
-  dv[0] = da.x; dv[1] = da.y; dv[2] = da.z; dv[3] = da.w;
-  dv[4] = db.x; dv[5] = db.y; dv[6] = db.z; dv[7] = db.w;
-}
-
 // alpha: sum of x and of (phi + x) log1p(expm1(alpha' - alpha) p) over the chunk
 __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
   __shared__ __align__(16) int s_i[MAX_CG];
@@ -608,14 +593,6 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
 // ---------------------------------------------------------------------------
 // Decisions
 // ---------------------------------------------------------------------------
-// Sum of part slot `slot` of gene g over the chunks of segment (b, k).
-__device__ __forceinline__ double seg_sum(const DevState& s, int b, int k, int slot, int64_t g) {
-  const int2 r = s.seg_chunk[b * s.K + k];
-  double acc = 0.0;
-  for (int c = r.x; c < r.x + r.y; ++c) acc += __ldg(&s.part[((int64_t)c * NSLOT + slot) * s.Gp + g]);
-  return acc;
-}
-
 // gamma0 then gamma1 of batch b, one CTA (BUSseq_gpu.cu:514-600).
 __device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double* sh) {
   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -668,7 +645,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   double lv[2] = {0.0, 0.0};
-  if (g < s.G) {
+  if (g < s.G && s.hmc_L == 0) {  // alpha: random-walk MH (the HMC block updates it otherwise)
     double Sx = 0.0, La = 0.0;
     for (int c = 0; c < s.cap_g; ++c) {
       const bool used = s.gchunk[c].w > 0;
@@ -685,6 +662,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
     const float ua = uniform_at(s.seed, SID_ALPHA, (uint64_t)g, iter, 2);
     s.lr_alpha[g] = lr + prior;
     if ((double)logf(ua) <= lr + prior) s.alpha[g] = ap;
+  }
+  if (g < s.G) {
     // L from the current beta, p and tau0 (BUSseq_gpu.cu:634-648)
     const float p = s.p_tau0[0], tau0 = s.p_tau0[1];
     const float base = logf(p) - logf(1.0f - p) - (logf((float)TAU1) - logf(tau0)) * 0.5f;

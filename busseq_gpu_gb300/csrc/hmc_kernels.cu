@@ -1,0 +1,606 @@
+// Gradient-based block update (Hamiltonian Monte Carlo) of
+//   theta = (alpha_g, beta_gk (k >= 1), nu_bg (b >= 1), delta_i (not the first
+//            cell of a batch), psi_bg = log phi_bg)
+// given X, W, L, p and tau0.  This replaces the reference's five random-walk
+// Metropolis steps (BUSseq_gpu.cu:602-632, :670-818) with one transition that
+// leaves the same conditional density invariant:
+//   log p = sum_{i,g} [lgamma(x + phi) - lgamma(phi) + phi log phi
+//                      - (phi + x) log(phi + mu) + x eta]
+//         - (alpha - mu_alpha)^2 / (2 sigma2_alpha) - beta^2 / (2 v(L))
+//         - (nu - mu_nu)^2 / (2 sigma2_nu) - (delta - mu_delta)^2 / (2 sigma2_delta)
+//         + kappa psi - tau_phi e^psi,
+// the priors of the reference's MH steps, with v(L) = tau1 or tau0.
+//
+// Coordinates live in the parameter arrays themselves; momentum, gradient,
+// metric and the start of the trajectory use one flat layout of length
+//   D = Gp (1 + K + 2B) + N:  alpha [Gp] | beta [K][Gp] | nu [B][Gp] | psi [B][Gp] | delta [N]
+// (padding genes, beta_0, nu_0 and the first cell of each batch are fixed).
+//
+// One transition: gradient at theta0 (with the metric during its adaptation),
+// momentum p ~ N(0, M), L leapfrog steps (kick, drift, refresh of exp(.)
+// tables, gradient), a final half kick, the change of the Hamiltonian
+// (likelihood part from a cancellation-free per-entry pass, prior and kinetic
+// parts per coordinate), the Metropolis decision and, if rejected, a restore.
+// Step size: dual averaging (Hoffman and Gelman, JMLR 15, 2014, algorithm 5)
+// during burn-in with a random jitter of +-10 %; metric: the diagonal Fisher
+// information of the eta-coordinates and the observed information of psi,
+// recomputed at every transition of the first half of burn-in, then frozen.
+#include "kernels_common.cuh"
+
+namespace bq {
+
+// ---------------------------------------------------------------------------
+// Layout helpers
+// ---------------------------------------------------------------------------
+enum HmcKind : int { HK_ALPHA = 0, HK_BETA = 1, HK_NU = 2, HK_PSI = 3, HK_DELTA = 4 };
+
+struct HmcCoord {
+  int kind;     // HmcKind
+  int seg;      // k for beta, b for nu / psi, batch for delta
+  int64_t idx;  // gene g, or cell i
+  bool free;    // updated by the transition
+  float* pos;   // the parameter it lives in
+};
+
+__device__ __forceinline__ HmcCoord hmc_coord(const DevState& s, int64_t d) {
+  const int64_t Gp = s.Gp;
+  HmcCoord c{};
+  const int64_t nb = Gp, nk = Gp * s.K, nn = Gp * s.B;
+  if (d < nb) {
+    c.kind = HK_ALPHA;
+    c.idx = d;
+    c.free = d < s.G;
+    c.pos = s.alpha + d;
+    return c;
+  }
+  d -= nb;
+  if (d < nk) {
+    c.kind = HK_BETA;
+    c.seg = (int)(d / Gp);
+    c.idx = d % Gp;
+    c.free = c.seg > 0 && c.idx < s.G;
+    c.pos = s.beta + d;
+    return c;
+  }
+  d -= nk;
+  if (d < nn) {
+    c.kind = HK_NU;
+    c.seg = (int)(d / Gp);
+    c.idx = d % Gp;
+    c.free = c.seg > 0 && c.idx < s.G;
+    c.pos = s.nu + d;
+    return c;
+  }
+  d -= nn;
+  if (d < nn) {
+    c.kind = HK_PSI;
+    c.seg = (int)(d / Gp);
+    c.idx = d % Gp;
+    c.free = c.idx < s.G;
+    c.pos = s.psi + d;
+    return c;
+  }
+  d -= nn;
+  c.kind = HK_DELTA;
+  c.idx = d;
+  c.seg = s.batch_of[d];
+  c.free = d != s.batch_off[c.seg];
+  c.pos = s.delta + d;
+  return c;
+}
+
+__device__ __forceinline__ bool hmc_adapt_metric(const DevState& s, int iter) {
+  return iter == 0 || iter < s.n_burnin / 2;
+}
+
+// psi(z0 + x) - psi(z0 + 32)... differences of the digamma / trigamma
+// functions for arguments >= 32 from their asymptotic series
+//   psi(z)  = log z - 1/(2z) - 1/(12 z^2) + 1/(120 z^4) - 1/(252 z^6)
+//   psi'(z) = 1/z + 1/(2 z^2) + 1/(6 z^3) - 1/(30 z^5) + 1/(42 z^7)
+// (the first omitted terms are below 1e-12 at z = 32).
+__device__ __forceinline__ float digamma_tail(float z) {
+  const float r = fast_rcp(z), r2 = r * r;
+  return -0.5f * r - r2 * (1.0f / 12.0f - r2 * (1.0f / 120.0f - r2 * (1.0f / 252.0f)));
+}
+__device__ __forceinline__ float trigamma_asym(float z) {
+  const float r = fast_rcp(z), r2 = r * r;
+  return r * (1.0f + r * (0.5f + r * (1.0f / 6.0f - r2 * (1.0f / 30.0f - r2 * (1.0f / 42.0f)))));
+}
+
+constexpr int HMC_TAB = 32;  // digamma / trigamma differences tabulated for counts below this
+
+// Sums 8 per-lane values (v[u], one per chunk cell j0+u) over the warp: after
+// the exchange, lanes with lane % 4 == 0 hold the warp total of value
+// ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1).
+__device__ __forceinline__ float transpose_sum8(float (&v)[8], int lane) {
+  const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+  float a[4], b2[2];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float send = h16 ? v[q] : v[q + 4];
+    const float recv = __shfl_xor_sync(0xffffffffu, send, 16);
+    a[q] = (h16 ? v[q + 4] : v[q]) + recv;
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float send = h8 ? a[q] : a[q + 2];
+    const float recv = __shfl_xor_sync(0xffffffffu, send, 8);
+    b2[q] = (h8 ? a[q + 2] : a[q]) + recv;
+  }
+  float c = h4 ? b2[1] : b2[0];
+  c += __shfl_xor_sync(0xffffffffu, h4 ? b2[0] : b2[1], 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  return c;
+}
+
+__device__ __forceinline__ int transpose_slot(int lane) {
+  return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+
+// ---------------------------------------------------------------------------
+// Gradient pass (gene-pass layout: CTA = 128 genes x one chunk of cells of one
+// (batch, type)).  Per-gene partial sums go to part slots 0 (sum d ll / d eta),
+// 1 (sum d ll / d psi), and, while the metric adapts, 2 (Fisher information of
+// eta) and 3 (observed information of psi); per-cell sums over the CTA's genes
+// go to hmc_cpart[tile][cell] (and hmc_cpartw for the Fisher information).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int force_metric) {
+  __shared__ float tdg[HMC_TAB][GENE_TILE];
+  __shared__ float ttg[HMC_TAB][GENE_TILE];
+  __shared__ __align__(16) int s_i[MAX_CG];
+  __shared__ __align__(16) float s_D[MAX_CG];
+  __shared__ float s_cell[GENE_TILE / 32][MAX_CG];
+  __shared__ float s_cellw[GENE_TILE / 32][MAX_CG];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int4 ch = s.gchunk[row];
+  const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + tid;
+  if (len == 0) return;
+  const bool adapt = force_metric || hmc_adapt_metric(s, *s.iter);
+  const int len8 = (len + 7) & ~7;
+  for (int j = tid; j < len8; j += GENE_TILE) {
+    const bool in = j < len;
+    const int i = in ? s.perm[start + j] : (int)s.N;
+    s_i[j] = i;
+    s_D[j] = in ? s.Dexp[i] : 0.0f;
+  }
+  const bool gv = g < s.G;
+  const float ph = gv ? s.phi[(int64_t)b * Gp + g] : 1.0f;
+  const float M = gv ? s.E[((int64_t)b * s.K + k) * Gp + g] : 0.0f;
+  const float iph = fast_rcp(ph);
+  // sum_{j<x} 1/(ph + j) and 1/(ph + j)^2 for x < HMC_TAB
+  {
+    float dg = 0.0f, tg = 0.0f;
+    for (int x = 0; x < HMC_TAB; ++x) {
+      tdg[x][tid] = dg;
+      ttg[x][tid] = tg;
+      const float r = fast_rcp(ph + (float)x);
+      dg += r;
+      tg = fmaf(r, r, tg);
+    }
+  }
+  const float z32 = ph + (float)HMC_TAB;
+  const float dg32 = tdg[HMC_TAB - 1][tid] + fast_rcp(z32 - 1.0f);
+  const float tg32 = ttg[HMC_TAB - 1][tid] + fast_rcp((z32 - 1.0f) * (z32 - 1.0f));
+  const float dtail32 = digamma_tail(z32), tasym32 = trigamma_asym(z32);
+  __syncthreads();
+  const char* Xg = reinterpret_cast<const char*>(s.X + g);
+  const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
+  KahanF ar, ap, aw, ai;
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8], rv[8], wv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    float fr = 0.0f, fp = 0.0f, fw = 0.0f, fi = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int x = xr[u];
+      const float xf = (float)x;
+      const float mu = M * dv[u];
+      const float rc = fast_rcp(ph + mu);
+      const float r = ph * (xf - mu) * rc;
+      float dg;
+      if (x < HMC_TAB) dg = tdg[x][tid];
+      else dg = dg32 + log_ratio(ph + xf, z32, xf - (float)HMC_TAB) + (digamma_tail(ph + xf) - dtail32);
+      const float d1 = dg - log1p_fast(mu * iph) + (mu - xf) * rc;  // d ll / d phi
+      fr += r;
+      fp = fmaf(ph, d1, fp);
+      rv[u] = gv ? r : 0.0f;
+      if (adapt) {
+        const float w = ph * mu * rc;
+        const float tg = x < HMC_TAB ? ttg[x][tid] : tg32 + (tasym32 - trigamma_asym(ph + xf));
+        const float d2 = -tg + iph - 2.0f * rc + (ph + xf) * rc * rc;  // d2 ll / d phi2
+        fw += w;
+        fi -= ph * (d1 + ph * d2);
+        wv[u] = gv ? w : 0.0f;
+      }
+    }
+    ar.add(fr);
+    ap.add(fp);
+    const float cs = transpose_sum8(rv, lane);
+    if ((lane & 3) == 0) s_cell[warp][j0 + transpose_slot(lane)] = cs;
+    if (adapt) {
+      aw.add(fw);
+      ai.add(fi);
+      const float cw = transpose_sum8(wv, lane);
+      if ((lane & 3) == 0) s_cellw[warp][j0 + transpose_slot(lane)] = cw;
+    }
+  }
+  double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
+  pr[0] = gv ? ar.value() : 0.0;
+  pr[Gp] = gv ? ap.value() : 0.0;
+  if (adapt) {
+    pr[2 * Gp] = gv ? aw.value() : 0.0;
+    pr[3 * Gp] = gv ? ai.value() : 0.0;
+  }
+  __syncthreads();
+  for (int j = tid; j < len; j += GENE_TILE) {
+    float t = 0.0f, tw = 0.0f;
+#pragma unroll
+    for (int w = 0; w < GENE_TILE / 32; ++w) {
+      t += s_cell[w][j];
+      if (adapt) tw += s_cellw[w][j];
+    }
+    s.hmc_cpart[(int64_t)tile * s.N + s_i[j]] = t;
+    if (adapt) s.hmc_cpartw[(int64_t)tile * s.N + s_i[j]] = tw;
+  }
+}
+
+// Gradient (and metric) of every coordinate from the partial sums, plus the
+// priors (thread per coordinate).
+constexpr float HMC_MASS_FLOOR = 1e-2f;
+
+__global__ void k_hmc_assemble(DevState s, int force_metric) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= s.hmc_D) return;
+  const bool adapt = force_metric || hmc_adapt_metric(s, *s.iter);
+  const HmcCoord c = hmc_coord(s, d);
+  double gr = 0.0, m = 1.0;
+  if (c.free) {
+    const int64_t g = c.idx;
+    const int B = s.B, K = s.K;
+    switch (c.kind) {
+      case HK_ALPHA: {
+        double sr = 0.0, sw = 0.0;
+        for (int b = 0; b < B; ++b)
+          for (int k = 0; k < K; ++k) {
+            sr += seg_sum(s, b, k, 0, g);
+            if (adapt) sw += seg_sum(s, b, k, 2, g);
+          }
+        gr = sr - ((double)s.alpha[g] - (double)s.mu_alpha[g]) / SIGMA2_ALPHA;
+        m = sw + 1.0 / SIGMA2_ALPHA;
+        break;
+      }
+      case HK_BETA: {
+        double sr = 0.0, sw = 0.0;
+        for (int b = 0; b < B; ++b) {
+          sr += seg_sum(s, b, c.seg, 0, g);
+          if (adapt) sw += seg_sum(s, b, c.seg, 2, g);
+        }
+        const double v = s.L[(int64_t)c.seg * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1];
+        gr = sr - (double)*c.pos / v;
+        m = sw + 1.0 / v;
+        break;
+      }
+      case HK_NU: {
+        double sr = 0.0, sw = 0.0;
+        for (int k = 0; k < K; ++k) {
+          sr += seg_sum(s, c.seg, k, 0, g);
+          if (adapt) sw += seg_sum(s, c.seg, k, 2, g);
+        }
+        gr = sr - ((double)*c.pos - (double)s.mu_nu[c.seg]) / SIGMA2_NU;
+        m = sw + 1.0 / SIGMA2_NU;
+        break;
+      }
+      case HK_PSI: {
+        double sp = 0.0, si = 0.0;
+        for (int k = 0; k < K; ++k) {
+          sp += seg_sum(s, c.seg, k, 1, g);
+          if (adapt) si += seg_sum(s, c.seg, k, 3, g);
+        }
+        const double ph = s.phi[(int64_t)c.seg * s.Gp + g];
+        gr = sp + KAPPA_PHI - TAU_PHI * ph;
+        m = si + TAU_PHI * ph;
+        break;
+      }
+      default: {  // delta
+        double sr = 0.0, sw = 0.0;
+        for (int t = 0; t < s.n_tiles; ++t) {
+          sr += s.hmc_cpart[(int64_t)t * s.N + c.idx];
+          if (adapt) sw += s.hmc_cpartw[(int64_t)t * s.N + c.idx];
+        }
+        gr = sr - ((double)*c.pos - (double)s.mu_delta[c.idx]) / SIGMA2_DELTA;
+        m = sw + 1.0 / SIGMA2_DELTA;
+        break;
+      }
+    }
+  }
+  s.hmc_grad[d] = c.free ? (float)gr : 0.0f;
+  if (adapt) s.hmc_mass[d] = c.free ? fmaxf((float)m, HMC_MASS_FLOOR) : 1.0f;
+}
+
+// Momentum p ~ N(0, M) and the start of the trajectory; thread 0 draws the
+// transition's jittered step size.
+__global__ void k_hmc_start(DevState s) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t iter = (uint32_t)*s.iter;
+  if (d == 0) {
+    const float u = uniform_at(s.seed, SID_HMC_ACC, 0, iter, 1);
+    s.hmc_sc[HS_EPS_USED] = s.hmc_sc[HS_EPS] * (0.9 + 0.2 * (double)u);
+  }
+  if (d >= s.hmc_D) return;
+  const HmcCoord c = hmc_coord(s, d);
+  float p = 0.0f;
+  if (c.free) {
+    Stream st(s.seed, SID_HMC_MOM, (uint64_t)d, iter);
+    p = sqrtf(s.hmc_mass[d]) * normal(st);
+  }
+  s.hmc_mom[d] = p;
+  s.hmc_mom0[d] = p;
+  s.hmc_th0[d] = *c.pos;
+}
+
+// exp(.) of the coordinates that feed the per-entry means.
+__device__ __forceinline__ void hmc_derived(const DevState& s, const HmcCoord& c, float v) {
+  if (c.kind == HK_PSI) s.phi[(int64_t)c.seg * s.Gp + c.idx] = expf(v);
+  else if (c.kind == HK_DELTA) s.Dexp[c.idx] = expf(v);
+}
+
+// One leapfrog step: kick (half at the first step, full afterwards: the
+// previous step's closing half kick merged in), then drift.
+__global__ void k_hmc_leap(DevState s, int first) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= s.hmc_D) return;
+  const HmcCoord c = hmc_coord(s, d);
+  if (!c.free) return;
+  const float eps = (float)s.hmc_sc[HS_EPS_USED];
+  const float p = s.hmc_mom[d] + (first ? 0.5f : 1.0f) * eps * s.hmc_grad[d];
+  s.hmc_mom[d] = p;
+  const float v = *c.pos + eps * p / s.hmc_mass[d];
+  *c.pos = v;
+  hmc_derived(s, c, v);
+}
+
+// E = exp(alpha + beta + nu) after the coordinates moved.
+__global__ void k_hmc_refresh_E(DevState s) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t Gp = s.Gp;
+  if (t >= (int64_t)s.B * s.K * Gp) return;
+  const int64_t g = t % Gp;
+  const int64_t bk = t / Gp;
+  const int k = (int)(bk % s.K), b = (int)(bk / s.K);
+  s.E[t] = g < s.G ? exp_sum3(s.alpha[g], s.beta[(int64_t)k * Gp + g], s.nu[(int64_t)b * Gp + g]) : 1.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Change of the log likelihood between the start of the trajectory (th0) and
+// the current coordinates, per entry without cancellation:
+//   dl = H(x) + phi1 log(phi1/phi0) - (phi1 + x) log((phi1 + mu1) / (phi0 + mu0))
+//        - dphi log1p(mu0 / phi0) + x deta,
+//   H(x) = [lgamma(phi1 + x) - lgamma(phi1)] - [lgamma(phi0 + x) - lgamma(phi0)],
+//   mu1 - mu0 = mu0 expm1(deta), phi1 - phi0 = phi0 expm1(psi1 - psi0).
+// One float-float partial per CTA in hmc_hpart.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_dll(DevState s) {
+  __shared__ float tab[PHI_TAB][GENE_TILE];
+  __shared__ __align__(16) int s_i[MAX_CG];
+  __shared__ __align__(16) float s_D[MAX_CG];
+  __shared__ float s_dd[MAX_CG];
+  __shared__ FF shf[GENE_TILE / 32];
+  __shared__ long long shn[GENE_TILE / 32];
+  const int tid = threadIdx.x;
+  const int tile = blockIdx.x, row = blockIdx.y;
+  const int cta = row * gridDim.x + tile;
+  const int4 ch = s.gchunk[row];
+  const int b = ch.x, k = ch.y, start = ch.z, len = ch.w;
+  const int64_t Gp = s.Gp;
+  const int64_t g = (int64_t)tile * GENE_TILE + tid;
+  if (len == 0) {
+    if (tid == 0) s.hmc_hpart[cta] = FF{0.0f, 0.0f};
+    return;
+  }
+  const float* th0 = s.hmc_th0;
+  const int64_t o_beta = Gp, o_nu = Gp * (1 + s.K), o_psi = Gp * (1 + s.K + s.B), o_delta = Gp * (1 + s.K + 2 * s.B);
+  const int len8 = (len + 7) & ~7;
+  for (int j = tid; j < len8; j += GENE_TILE) {
+    const bool in = j < len;
+    const int i = in ? s.perm[start + j] : (int)s.N;
+    s_i[j] = i;
+    const float d0 = in ? th0[o_delta + i] : 0.0f;
+    s_D[j] = in ? expf(d0) : 0.0f;  // exp(delta0)
+    s_dd[j] = in ? s.delta[i] - d0 : 0.0f;
+  }
+  const bool gv = g < s.G;
+  float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f, n0 = 0.f, n1 = 0.f, p0 = 0.f, p1 = 0.f;
+  if (gv) {
+    a0 = th0[g];
+    a1 = s.alpha[g];
+    b0 = th0[o_beta + (int64_t)k * Gp + g];
+    b1 = s.beta[(int64_t)k * Gp + g];
+    n0 = th0[o_nu + (int64_t)b * Gp + g];
+    n1 = s.nu[(int64_t)b * Gp + g];
+    p0 = th0[o_psi + (int64_t)b * Gp + g];
+    p1 = s.psi[(int64_t)b * Gp + g];
+  }
+  const float M0 = gv ? exp_sum3(a0, b0, n0) : 0.0f;
+  const float dA = (a1 - a0) + (b1 - b0) + (n1 - n0);
+  const float ph0 = expf(p0);
+  const float dph = ph0 * expm1f(p1 - p0);
+  const float ph1 = ph0 + dph;
+  const float c1 = ph1 * log_ratio(ph1, ph0, dph);
+  const float lgd0 = lgamma_diff(ph0, ph1, dph);
+  {
+    float h = 0.0f;
+    for (int x = 0; x < PHI_TAB; ++x) {
+      tab[x][tid] = h;
+      const float j = (float)x;
+      h += log_ratio(ph1 + j, ph0 + j, dph);
+    }
+  }
+  __syncthreads();
+  const float iph0 = fast_rcp(ph0);
+  const char* Xg = reinterpret_cast<const char*>(s.X + g);
+  const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
+  KahanF acc;
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    float f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int x = xr[u];
+      const float xf = (float)x;
+      const float mu0 = M0 * dv[u];
+      const float de = dA + s_dd[j0 + u];
+      const float dmu = mu0 * expm1f(de);
+      const float hx = x < PHI_TAB ? tab[x][tid] : lgamma_diff_large(ph0 + xf, ph1 + xf, dph) - lgd0;
+      const float t = hx + c1 - (ph1 + xf) * log_ratio(ph1 + mu0 + dmu, ph0 + mu0, dph + dmu) -
+                      dph * log1p_fast(mu0 * iph0) + xf * de;
+      f += dv[u] > 0.0f ? t : 0.0f;  // padding cells contribute nothing
+    }
+    acc.add(f);
+  }
+  FF fsum[1] = {gv ? acc.ff() : FF{0.0f, 0.0f}};
+  long long nn[1] = {0};
+  block_sum_ff<1, 1>(fsum, nn, shf, shn);
+  if (tid == 0) s.hmc_hpart[cta] = fsum[0];
+}
+
+// Closing half kick, then per coordinate the kinetic change minus the prior
+// change (cancellation-free), summed per CTA into hmc_epart.
+__global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
+  __shared__ FF shf[8];
+  __shared__ long long shn[8];
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float e = 0.0f;
+  if (d < s.hmc_D) {
+    const HmcCoord c = hmc_coord(s, d);
+    if (c.free) {
+      float p = s.hmc_mom[d];
+      if (kick) {
+        p += 0.5f * (float)s.hmc_sc[HS_EPS_USED] * s.hmc_grad[d];
+        s.hmc_mom[d] = p;
+      }
+      const float p0 = s.hmc_mom0[d];
+      const float dK = p == p0 ? 0.0f : (p - p0) * (p + p0) * 0.5f / s.hmc_mass[d];
+      const float v1 = *c.pos, v0 = s.hmc_th0[d];
+      const float dv = v1 - v0;
+      float dprior;
+      switch (c.kind) {
+        case HK_ALPHA: {
+          const float m = s.mu_alpha[c.idx];
+          dprior = -dv * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_ALPHA);
+          break;
+        }
+        case HK_BETA: {
+          const double v = s.L[(int64_t)c.seg * s.Gp + c.idx] == 1 ? TAU1 : (double)s.p_tau0[1];
+          dprior = (float)(-(double)dv * ((double)v1 + (double)v0) * 0.5 / v);
+          break;
+        }
+        case HK_NU: {
+          const float m = s.mu_nu[c.seg];
+          dprior = -dv * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_NU);
+          break;
+        }
+        case HK_PSI:
+          dprior = (float)KAPPA_PHI * dv - (float)TAU_PHI * expf(v0) * expm1f(dv);
+          break;
+        default: {
+          const float m = s.mu_delta[c.idx];
+          dprior = -dv * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_DELTA);
+          break;
+        }
+      }
+      e = dK - dprior;
+    }
+  }
+  FF f[1] = {FF{e, 0.0f}};
+  long long n[1] = {0};
+  block_sum_ff<1, 1>(f, n, shf, shn);
+  if (threadIdx.x == 0) s.hmc_epart[blockIdx.x] = f[0];
+}
+
+// The Metropolis decision on H = -log p + K (one CTA), and the step-size
+// adaptation.  mode 1 only reports the change of the log posterior
+// (-(H1 - H0) with zero momenta) in HS_LAST_DH.
+__global__ void __launch_bounds__(256) k_hmc_accept(DevState s, int n_hpart, int n_epart, int mode) {
+  __shared__ FF shf[8 * 2];
+  __shared__ long long shn[8];
+  FF acc{0.0f, 0.0f}, ace{0.0f, 0.0f};
+  for (int t = threadIdx.x; t < n_hpart; t += blockDim.x) acc = ff_add(acc, s.hmc_hpart[t]);
+  for (int t = threadIdx.x; t < n_epart; t += blockDim.x) ace = ff_add(ace, s.hmc_epart[t]);
+  FF f[2] = {acc, ace};
+  long long n[1] = {0};
+  block_sum_ff<2, 1>(f, n, shf, shn);
+  if (threadIdx.x != 0) return;
+  const double dll = ff_value(f[0]);
+  const double dH = -dll + ff_value(f[1]);
+  double* sc = s.hmc_sc;
+  sc[HS_LAST_DH] = dH;
+  if (mode == 1) {
+    sc[HS_LAST_DH] = -dH;
+    return;
+  }
+  const int iter = *s.iter;
+  const double a = dH == dH ? fmin(1.0, exp(-dH)) : 0.0;
+  const float u = uniform_at(s.seed, SID_HMC_ACC, 0, (uint32_t)iter, 0);
+  const bool accept = dH == dH && (double)logf(u) < -dH;
+  sc[HS_ACCEPTED] = accept ? 1.0 : 0.0;
+  sc[HS_LAST_ACC] = a;
+  if (iter >= s.n_burnin) {
+    sc[HS_N_KEPT] += 1.0;
+    sc[HS_ACC_KEPT] += accept ? 1.0 : 0.0;
+  }
+  // dual averaging during burn-in, restarted when the metric freezes
+  if (iter < s.n_burnin) {
+    const int restart = s.n_burnin / 2;
+    if (iter == restart) {
+      sc[HS_HBAR] = 0.0;
+      sc[HS_M] = 0.0;
+      sc[HS_MU] = log(10.0 * sc[HS_EPS]);
+      sc[HS_LOG_EPS_BAR] = 0.0;
+    }
+    const double gam = 0.05, t0 = 10.0, kap = 0.75, target = HMC_TARGET_ACCEPT;
+    const double m = sc[HS_M] + 1.0;
+    sc[HS_M] = m;
+    sc[HS_HBAR] = (1.0 - 1.0 / (m + t0)) * sc[HS_HBAR] + (target - a) / (m + t0);
+    const double log_eps = sc[HS_MU] - sqrt(m) / gam * sc[HS_HBAR];
+    const double w = pow(m, -kap);
+    sc[HS_LOG_EPS_BAR] = w * log_eps + (1.0 - w) * sc[HS_LOG_EPS_BAR];
+    sc[HS_EPS] = exp(fmin(fmax(log_eps, -12.0), 2.0));
+    if (iter == s.n_burnin - 1) sc[HS_EPS] = exp(fmin(fmax(sc[HS_LOG_EPS_BAR], -12.0), 2.0));
+  }
+}
+
+// Restores the start of the trajectory when the transition was rejected.
+__global__ void k_hmc_finish(DevState s) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= s.hmc_D) return;
+  if (s.hmc_sc[HS_ACCEPTED] != 0.0) return;
+  const HmcCoord c = hmc_coord(s, d);
+  if (!c.free) return;
+  const float v = s.hmc_th0[d];
+  *c.pos = v;
+  hmc_derived(s, c, v);
+}
+
+// Unit metric before the first adaptation.
+__global__ void k_hmc_unit_mass(DevState s) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < s.hmc_D) s.hmc_mass[d] = 1.0f;
+}
+
+// Loads `src` (flat layout) into th0 for the log-posterior difference.
+__global__ void k_hmc_set_th0(DevState s, const float* src) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= s.hmc_D) return;
+  s.hmc_th0[d] = src[d];
+  s.hmc_mom[d] = 0.0f;
+  s.hmc_mom0[d] = 0.0f;
+}
+
+}  // namespace bq

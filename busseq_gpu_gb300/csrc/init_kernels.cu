@@ -277,6 +277,7 @@ __global__ void k_init_finish(DevState s, int fresh) {
     if (t == 0) s.p_tau0[1] = TAU0_INIT;
   }
   if (t < s.N) s.Dexp[t] = expf(s.delta[t]);
+  if (s.psi && t < (int64_t)B * Gp) s.psi[t] = logf(s.phi[t]);
   if (t < Gp && t >= G) {
     s.alpha[t] = 0.0f;
     for (int k = 0; k < K; ++k) s.beta[(int64_t)k * Gp + t] = 0.0f;

@@ -51,10 +51,6 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
 // which is folded into lo, and a final Fast2Sum renormalises the pair.  The
 // reduction trees have a fixed shape, so the sums are bit-reproducible.
 // ---------------------------------------------------------------------------
-struct FF {
-  float hi, lo;
-};
-
 __device__ __forceinline__ FF ff_add(FF a, FF b) {
   const float s = a.hi + b.hi;
   const float v = s - a.hi;
@@ -210,5 +206,28 @@ struct KahanF {
 // log-likelihood shift of one NB entry when eta moves by eps, without the
 // linear eps * X part:   (phi + X) * log1p(c * p),  c = expm1(eps), p = mu / (phi + mu)
 __device__ __forceinline__ float nb_shift_log(float w, float c, float p) { return w * log1pf(c * p); }
+
+// X and exp(delta) of chunk cells j0..j0+7 for the gene whose column starts
+// at Xg (128-bit shared loads; row offsets by one 32x32->64-bit multiply-add).
+__device__ __forceinline__ void load8(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D, int j0,
+                                      int (&xr)[8], float (&dv)[8]) {
+  const int4 ia = *reinterpret_cast<const int4*>(s_i + j0);
+  const int4 ib = *reinterpret_cast<const int4*>(s_i + j0 + 4);
+  const float4 da = *reinterpret_cast<const float4*>(s_D + j0);
+  const float4 db = *reinterpret_cast<const float4*>(s_D + j0 + 4);
+  const int iv[8] = {ia.x, ia.y, ia.z, ia.w, ib.x, ib.y, ib.z, ib.w};
+#pragma unroll
+  for (int u = 0; u < 8; ++u) xr[u] = *reinterpret_cast<const int*>(Xg + (uint64_t)(uint32_t)iv[u] * row_bytes);
+  dv[0] = da.x; dv[1] = da.y; dv[2] = da.z; dv[3] = da.w;
+  dv[4] = db.x; dv[5] = db.y; dv[6] = db.z; dv[7] = db.w;
+}
+
+// Sum of part slot `slot` of gene g over the chunks of segment (b, k).
+__device__ __forceinline__ double seg_sum(const DevState& s, int b, int k, int slot, int64_t g) {
+  const int2 r = s.seg_chunk[b * s.K + k];
+  double acc = 0.0;
+  for (int c = r.x; c < r.x + r.y; ++c) acc += __ldg(&s.part[((int64_t)c * NSLOT + slot) * s.Gp + g]);
+  return acc;
+}
 
 }  // namespace bq

@@ -53,6 +53,8 @@ enum StreamId : uint32_t {
   SID_PHI_ACC = 12,      // b*G+g       : accept (u0)
   SID_W = 13,            // cell i      : proposal / categorical (u0), accept (u1)
   SID_PI = 14,           // b*K+k       : Dirichlet component (Gamma draw)
+  SID_HMC_MOM = 15,      // coordinate d: momentum of the HMC block update
+  SID_HMC_ACC = 16,      // 0           : HMC accept (u0), step-size jitter (u1)
   SID_INIT_W = 20,       // cell i      : initial cell type
   SID_INIT_L = 21,       // k*G+g       : initial indicator L
   SID_SIM = 30           // synthetic-data generator (not used by the sampler)

@@ -66,7 +66,11 @@ typedef struct busseq_options {
   int32_t keep_draws;   /* store every kept draw (needed for reference -p)      */
   int32_t device;       /* CUDA device ordinal                                 */
   int32_t chunk_cells;  /* cells per gene-pass chunk; 0 = default (256)         */
-  int32_t reserved[8];
+  int32_t hmc_leapfrog; /* 0: random-walk MH for alpha, beta, nu, delta, phi (the
+                           reference's sampler); L > 0: one Hamiltonian Monte Carlo
+                           transition of that block per sweep with L leapfrog
+                           steps (not in the reference)                         */
+  int32_t reserved[7];
 } busseq_options;
 
 /* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
@@ -206,6 +210,21 @@ int busseq_set_state(busseq_handle* h, const busseq_state* in);
  * index, so a resumed run reproduces an uninterrupted one bit for bit. */
 int busseq_checkpoint_save(busseq_handle* h, const char* path);
 int busseq_checkpoint_load(busseq_handle* h, const char* path);
+
+/* Gradient-based block update (opt.hmc_leapfrog > 0).
+ * busseq_hmc_stats: out[0] step size, out[1] acceptance rate over the kept
+ * sweeps so far, out[2] acceptance probability of the last transition, out[3]
+ * its change of the Hamiltonian.
+ * busseq_hmc_gradient: the gradient of the block's log posterior at the
+ * current state, and (when `metric` is not NULL) the diagonal metric the
+ * transitions would adapt to there, in the flat layout
+ *   alpha [G] | beta [K*G] | nu [B*G] | log phi [B*G] | delta [N]
+ * (fixed coordinates: gradient 0, metric 1).
+ * busseq_hmc_logpost_diff: log posterior of the current state minus that of
+ * `from` (same conditioning: X, W, L, p, tau0 of the current state).  */
+int busseq_hmc_stats(busseq_handle* h, double out[4]);
+int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric);
+int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* out);
 
 /* Position of the current run: sweeps launched so far, run length and burn-in
  * length (all 0 before busseq_begin).  NULL pointers are skipped. */
