@@ -42,7 +42,9 @@ sys.path.insert(0, ROOT)
 CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
 # the large uneven workload: 6 batches, 15 % differential genes, phi ~ U(2, 30)
 CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide")
-WORKLOADS = {"config1": CFG1, "config4": CFG4}
+# config-1 data with the HMC block update (10 leapfrog steps) in place of the random-walk steps
+CFG2 = dict(CFG1, hmc=10)
+WORKLOADS = {"config1": CFG1, "config2": CFG2, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
 UNIT = "sweeps/s"
 
@@ -190,15 +192,17 @@ def _config(name="config1", n_b=None):
     n_b = list(n_b if n_b is not None else cfg["n_b"])
     N, G, K = int(sum(n_b)), cfg["G"], cfg["K"]
     mb = N * G * 4 / 1e6
-    desc = "%s: B=%d batches of %s cells (N=%d), G=%d, K=%d, plain MH sampler" % (
-        name, len(n_b), "/".join(str(n) for n in n_b), N, G, K)
+    sampler = ("HMC block update, %d leapfrog steps" % cfg["hmc"]) if cfg.get("hmc") else "plain MH sampler"
+    desc = "%s: B=%d batches of %s cells (N=%d), G=%d, K=%d, %s" % (
+        name, len(n_b), "/".join(str(n) for n in n_b), N, G, K, sampler)
     return {"workload": desc, "B": len(n_b), "N": N, "G": G, "K": K, "w_update": "mh",
+            "sampler": "hmc" if cfg.get("hmc") else "mh", "hmc_leapfrog": cfg.get("hmc", 0),
             "parallelism": "replicas (one chain per GPU)",
             "l2": "no flush: X and Y are %.0f MB each, larger than L2" % mb,
             "precision": "f32 likelihood terms, f64 acceptance sums"}
 
 
-def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000):
+def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
     """One whole job with kept draws: ESS (Geyer, initial monotone sequence) of
     every beta (k >= 1) and nu (b >= 1) coordinate, ESS/s over the wall time of
     the whole job (upload, init, burn-in, kept sweeps, estimates), and the ARI
@@ -207,14 +211,18 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000):
     from busseq_gpu_gb300.diagnostics import adjusted_rand_index, ess_geyer
 
     t0 = time.perf_counter()
-    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True)
+    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True, hmc_leapfrog=hmc)
     s.run(n_iter, n_burnin, min(500, n_burnin))
     est = s.estimates(with_XZ=False)
     wall = time.perf_counter() - t0
     pres = s.preserved()
+    hstats = s.hmc_stats() if hmc else None
     s.close()
     out = {"sweeps": n_iter, "burnin": n_burnin, "kept": n_iter - n_burnin, "wall_s": wall,
-           "ari_W": adjusted_rand_index(est["W"], W_true), "estimator": "Geyer initial monotone sequence"}
+           "ari_W": adjusted_rand_index(est["W"], W_true), "estimator": "Geyer initial monotone sequence",
+           "sampler": ("HMC, %d leapfrog steps" % hmc) if hmc else "random-walk MH (the reference's)"}
+    if hstats:
+        out["hmc"] = {k: float(v) for k, v in hstats.items()}
     for name in ("beta", "nu"):
         e = ess_geyer(pres[name].astype(np.float64))
         moving = np.isfinite(e)
@@ -238,7 +246,8 @@ def main():
                     help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
-                    help="config1 (the headline, default) or config4 (N=50000, G=20000, K=12, uneven batches)")
+                    help="config1 (the headline, default), config2 (config-1 data, HMC block update with 10 "
+                         "leapfrog steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     args = ap.parse_args()
@@ -276,7 +285,8 @@ def main():
     # a dedicated (non-default) stream shared by the sampler and the events
     stream = torch.cuda.Stream(device=local)
     torch.cuda.set_stream(stream)
-    s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local)
+    hmc = cfg.get("hmc", 0)
+    s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc)
     assert stream.cuda_stream != 0
     s.set_stream(stream.cuda_stream)
     total = args.warmup + args.steps
@@ -312,11 +322,14 @@ def main():
 
     # ---- per-kernel durations for the roofline (events on the same stream) --
     prof = s.profile(20)
-    big = {k: v for k, v in prof.items() if k in ("k_zx", "k_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w")}
+    big = {k: v for k, v in prof.items() if k in ("k_zx", "k_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w",
+                                                  "k_hmc_grad", "k_hmc_dll")}
     dom = max(big, key=big.get)
     kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(16)].index(dom)
     alg_bytes = s.kernel_bytes(kid)
-    achieved = alg_bytes / (prof[dom] / 1000.0) / 1e9
+    n_launch = hmc if dom == "k_hmc_grad" else 1  # launches of the kernel per sweep (one per leapfrog step)
+    ms_launch = prof[dom] / n_launch
+    achieved = alg_bytes / (ms_launch / 1000.0) / 1e9
     peak, peak_kind = _peak_hbm()
     traffic = _traffic(dom, args.workload) if args.cells <= 0 else None
     s.close()
@@ -329,7 +342,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    s2 = bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank, device=local)
+    s2 = bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc)
     s2.run(args.steps, args.steps // 2, min(args.warmup, args.steps))
     est = s2.estimates(with_XZ=True)
     t1 = time.perf_counter()
@@ -345,7 +358,7 @@ def main():
     # ---- mixing and recovery: ESS of beta and nu, ARI of W (rank 0) -------
     quality = None
     if rank == 0 and not args.no_ess:
-        quality = ess_run(Y, W_true, n_b, K, seed)
+        quality = ess_run(Y, W_true, n_b, K, seed, hmc=hmc)
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     cpu = None
@@ -368,7 +381,8 @@ def main():
                             % args.steps},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "alg_bytes_per_launch": alg_bytes, "ms_per_launch": prof[dom]},
+                         "alg_bytes_per_launch": alg_bytes, "ms_per_launch": ms_launch,
+                         "launches_per_sweep": n_launch},
             "kernels_ms": prof,
             "gpu_launches": launches,
             "clocks": clk.summary(),

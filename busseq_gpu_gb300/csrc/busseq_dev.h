@@ -102,6 +102,7 @@ enum HmcScalar : int {
   HS_COUNT = 16
 };
 constexpr double HMC_TARGET_ACCEPT = 0.7;
+constexpr int HMC_BLOCK_MAX = 24;  // largest K + B - 1 with a per-gene block metric
 constexpr double HMC_EPS0 = 0.05;
 
 struct DevState {
@@ -165,6 +166,17 @@ struct DevState {
   FF* hmc_hpart;    // [n_tiles * cap_g] per-CTA log-likelihood change
   FF* hmc_epart;    // [ceil(D / 256)] per-CTA kinetic minus prior change
   double* hmc_sc;   // [HS_COUNT]
+  // per-gene block metric over (alpha_g, beta_g1..g(K-1), nu_g1..g(B-1)):
+  // hmc_nb = K + B - 1 coordinates, Cholesky factor packed [nb (nb + 1) / 2][G]
+  // (0: diagonal metric everywhere)
+  int hmc_nb;
+  float* hmc_chol;
+  // frozen data of the metric: the information part of every diagonal mass
+  // (without the priors, which follow the current L and tau0) and the
+  // per-segment Fisher sums W_bkg of the blocks [B*K][G]
+  float* hmc_fis;
+  float* hmc_wbk;
+  FF* hmc_epart_b;  // [ceil(G / 256)] per-CTA kinetic minus prior change of the gene blocks
   float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   float* gamma_p;  // [2][B]

@@ -49,14 +49,19 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_phi",          "k_decide_phi",   "k_w",          "k_sort_pi",
                                     "k_posterior",    "k_hmc_grad",     "k_hmc_assemble", "k_hmc_start",
                                     "k_hmc_leap0",    "k_hmc_leap",     "k_hmc_refresh_E", "k_hmc_dll",
-                                    "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish"};
-constexpr int kNumKernels = 23;
+                                    "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish", "k_hmc_metric_blocks",
+                                    "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
+                                    "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
+                                    "k_hmc_assemble_start"};
+constexpr int kNumKernels = 31;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
   KID_POSTERIOR = 12, KID_HMC_GRAD = 13, KID_HMC_ASSEMBLE = 14, KID_HMC_START = 15, KID_HMC_LEAP0 = 16,
   KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
-  KID_HMC_FINISH = 22
+  KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
+  KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
+  KID_HMC_ASSEMBLE_START = 30
 };
 
 }  // namespace
@@ -185,11 +190,13 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       break;
     }
     case KID_HMC_GRAD:
-      k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s, 0);
+    case KID_HMC_GRAD_START:
+      k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s, which == KID_HMC_GRAD_START ? 1 : 0);
       LAUNCH_CHECK("k_hmc_grad");
       break;
     case KID_HMC_ASSEMBLE:
-      k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, 0);
+    case KID_HMC_ASSEMBLE_START:
+      k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, which == KID_HMC_ASSEMBLE_START ? 1 : 0);
       LAUNCH_CHECK("k_hmc_assemble");
       break;
     case KID_HMC_START:
@@ -214,8 +221,30 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_energy");
       break;
     case KID_HMC_ACCEPT:
-      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256), 0);
+      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
+                                      (int)blocks_for(s.G, 256), 0);
       LAUNCH_CHECK("k_hmc_accept");
+      break;
+    case KID_HMC_METRIC_BLOCKS:
+      k_hmc_metric_blocks<<<blocks_for(s.G, 128), 128, 0, st>>>(s, 1);
+      LAUNCH_CHECK("k_hmc_metric_blocks");
+      break;
+    case KID_HMC_START_BLOCKS:
+      k_hmc_start_blocks<<<blocks_for(s.G, 128), 128, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_start_blocks");
+      break;
+    case KID_HMC_LEAP_BLOCKS0:
+    case KID_HMC_LEAP_BLOCKS:
+      k_hmc_leap_blocks<<<blocks_for(s.G, 128), 128, 0, st>>>(s, which == KID_HMC_LEAP_BLOCKS0 ? 1 : 0);
+      LAUNCH_CHECK("k_hmc_leap_blocks");
+      break;
+    case KID_HMC_MASS:
+      k_hmc_mass<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_mass");
+      break;
+    case KID_HMC_ENERGY_BLOCKS:
+      k_hmc_energy_blocks<<<blocks_for(s.G, 256), 256, 0, st>>>(s, 1);
+      LAUNCH_CHECK("k_hmc_energy_blocks");
       break;
     case KID_HMC_FINISH:
       k_hmc_finish<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s);
@@ -234,15 +263,23 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
 std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
-    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD, KID_HMC_ASSEMBLE, KID_HMC_START};
+    const bool blocks = h->s.hmc_nb > 0;
+    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START, KID_HMC_MASS};
+    if (blocks) q.push_back(KID_HMC_METRIC_BLOCKS);
+    q.push_back(KID_HMC_START);
+    if (blocks) q.push_back(KID_HMC_START_BLOCKS);
     for (int l = 0; l < h->s.hmc_L; ++l) {
       q.push_back(l == 0 ? KID_HMC_LEAP0 : KID_HMC_LEAP);
+      if (blocks) q.push_back(l == 0 ? KID_HMC_LEAP_BLOCKS0 : KID_HMC_LEAP_BLOCKS);
       q.push_back(KID_HMC_E);
       q.push_back(KID_HMC_GRAD);
       q.push_back(KID_HMC_ASSEMBLE);
     }
-    const int tail[] = {KID_HMC_DLL, KID_HMC_ENERGY, KID_HMC_ACCEPT, KID_HMC_FINISH, KID_HMC_E, KID_W, KID_SORT_PI};
-    q.insert(q.end(), tail, tail + 7);
+    q.push_back(KID_HMC_DLL);
+    q.push_back(KID_HMC_ENERGY);
+    if (blocks) q.push_back(KID_HMC_ENERGY_BLOCKS);
+    const int tail[] = {KID_HMC_ACCEPT, KID_HMC_FINISH, KID_HMC_E, KID_W, KID_SORT_PI};
+    q.insert(q.end(), tail, tail + 5);
   } else {
     for (int k = 0; k <= KID_SORT_PI; ++k) q.push_back(k);
   }
@@ -447,6 +484,13 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g));
       TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
       TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
+      TRY(h->alloc(&s.hmc_fis, s.hmc_D));
+      s.hmc_nb = (K + B - 1 <= bq::HMC_BLOCK_MAX) ? K + B - 1 : 0;
+      if (s.hmc_nb > 0) {
+        TRY(h->alloc(&s.hmc_chol, (int64_t)s.hmc_nb * (s.hmc_nb + 1) / 2 * G));
+        TRY(h->alloc(&s.hmc_wbk, (int64_t)B * K * G));
+        TRY(h->alloc(&s.hmc_epart_b, (int64_t)blocks_for(G, 256)));
+      }
       bq::k_hmc_unit_mass<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s);
       LAUNCH_CHECK("k_hmc_unit_mass");
     }
@@ -955,6 +999,11 @@ std::vector<DevBlock> run_blocks(const busseq_handle* h) {
     v.push_back({s.psi, (size_t)s.B * s.Gp * 4});
     v.push_back({s.hmc_mass, (size_t)s.hmc_D * 4});
     v.push_back({s.hmc_sc, (size_t)bq::HS_COUNT * 8});
+    v.push_back({s.hmc_fis, (size_t)s.hmc_D * 4});
+    if (s.hmc_nb > 0) {
+      v.push_back({s.hmc_chol, (size_t)s.hmc_nb * (s.hmc_nb + 1) / 2 * s.G * 4});
+      v.push_back({s.hmc_wbk, (size_t)s.B * s.K * s.G * 4});
+    }
   }
   return v;
 }
@@ -1226,9 +1275,9 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   std::vector<float> mass_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
-  bq::k_hmc_grad<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 1);
+  bq::k_hmc_grad<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
-  bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 1);
+  bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_assemble");
   TRY(check_device_error(h));
   std::vector<float> gf(s.hmc_D), mf(s.hmc_D);
@@ -1266,7 +1315,9 @@ int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* 
     bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
     bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
     bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
-    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256), 1);
+    if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G, 256), 256, 0, h->stream>>>(s, 0);
+    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
+                                               (int)blocks_for(s.G, 256), 1);
     e = cudaGetLastError();
   }
   double sc[bq::HS_COUNT];
@@ -1368,6 +1419,7 @@ double busseq_kernel_bytes(busseq_handle* h, int32_t i) {
     case 12: return params;
     case 13: return 4.0 * E;                        // HMC gradient pass: read X
     case 19: return 4.0 * E;                        // HMC log-likelihood change: read X
+    case 29: return 4.0 * E;                        // HMC gradient at the start of a transition
     default: return 0.0;
   }
 }

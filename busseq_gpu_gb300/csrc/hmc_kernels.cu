@@ -89,8 +89,21 @@ __device__ __forceinline__ HmcCoord hmc_coord(const DevState& s, int64_t d) {
   return c;
 }
 
+// Coordinates of the per-gene blocks (alpha, beta, nu) are moved by the block
+// kernels when the block metric is on.
+__device__ __forceinline__ bool hmc_in_block(const DevState& s, const HmcCoord& c) {
+  return s.hmc_nb > 0 && c.kind <= HK_NU;
+}
+
 __device__ __forceinline__ bool hmc_adapt_metric(const DevState& s, int iter) {
   return iter == 0 || iter < s.n_burnin / 2;
+}
+
+// metric_mode 0: never (the gradients inside a trajectory: the metric must not
+// change along it), 1: while it adapts (the gradient at the start of a
+// transition), 2: always (the test entry point).
+__device__ __forceinline__ bool hmc_metric_now(const DevState& s, int metric_mode) {
+  return metric_mode == 2 || (metric_mode == 1 && hmc_adapt_metric(s, *s.iter));
 }
 
 // psi(z0 + x) - psi(z0 + 32)... differences of the digamma / trigamma
@@ -145,7 +158,7 @@ __device__ __forceinline__ int transpose_slot(int lane) {
 // eta) and 3 (observed information of psi); per-cell sums over the CTA's genes
 // go to hmc_cpart[tile][cell] (and hmc_cpartw for the Fisher information).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int force_metric) {
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_mode) {
   __shared__ float tdg[HMC_TAB][GENE_TILE];
   __shared__ float ttg[HMC_TAB][GENE_TILE];
   __shared__ __align__(16) int s_i[MAX_CG];
@@ -159,7 +172,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int force_me
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   if (len == 0) return;
-  const bool adapt = force_metric || hmc_adapt_metric(s, *s.iter);
+  const bool adapt = hmc_metric_now(s, metric_mode);
   const int len8 = (len + 7) & ~7;
   for (int j = tid; j < len8; j += GENE_TILE) {
     const bool in = j < len;
@@ -249,14 +262,26 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int force_me
   }
 }
 
+// Precision of a free coordinate's prior; psi's (tau_phi phi) stays in the
+// frozen part.
+__device__ __forceinline__ double hmc_prior_precision(const DevState& s, const HmcCoord& c) {
+  switch (c.kind) {
+    case HK_ALPHA: return 1.0 / SIGMA2_ALPHA;
+    case HK_BETA: return 1.0 / (s.L[(int64_t)c.seg * s.Gp + c.idx] == 1 ? TAU1 : (double)s.p_tau0[1]);
+    case HK_NU: return 1.0 / SIGMA2_NU;
+    case HK_PSI: return 0.0;
+    default: return 1.0 / SIGMA2_DELTA;
+  }
+}
+
 // Gradient (and metric) of every coordinate from the partial sums, plus the
 // priors (thread per coordinate).
 constexpr float HMC_MASS_FLOOR = 1e-2f;
 
-__global__ void k_hmc_assemble(DevState s, int force_metric) {
+__global__ void k_hmc_assemble(DevState s, int metric_mode) {
   const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= s.hmc_D) return;
-  const bool adapt = force_metric || hmc_adapt_metric(s, *s.iter);
+  const bool adapt = hmc_metric_now(s, metric_mode);
   const HmcCoord c = hmc_coord(s, d);
   double gr = 0.0, m = 1.0;
   if (c.free) {
@@ -319,7 +344,20 @@ __global__ void k_hmc_assemble(DevState s, int force_metric) {
     }
   }
   s.hmc_grad[d] = c.free ? (float)gr : 0.0f;
-  if (adapt) s.hmc_mass[d] = c.free ? fmaxf((float)m, HMC_MASS_FLOOR) : 1.0f;
+  if (adapt) {
+    s.hmc_mass[d] = c.free ? fmaxf((float)m, HMC_MASS_FLOOR) : 1.0f;
+    s.hmc_fis[d] = c.free ? (float)(m - hmc_prior_precision(s, c)) : 0.0f;
+  }
+}
+
+// The diagonal metric of the transition: the frozen information part plus the
+// priors' precisions under the current L and tau0 (L and tau0 are held fixed
+// within a transition, so the metric may follow them).
+__global__ void k_hmc_mass(DevState s) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= s.hmc_D) return;
+  const HmcCoord c = hmc_coord(s, d);
+  s.hmc_mass[d] = c.free ? fmaxf(s.hmc_fis[d] + (float)hmc_prior_precision(s, c), HMC_MASS_FLOOR) : 1.0f;
 }
 
 // Momentum p ~ N(0, M) and the start of the trajectory; thread 0 draws the
@@ -333,6 +371,7 @@ __global__ void k_hmc_start(DevState s) {
   }
   if (d >= s.hmc_D) return;
   const HmcCoord c = hmc_coord(s, d);
+  if (c.free && hmc_in_block(s, c)) return;  // k_hmc_start_blocks draws these
   float p = 0.0f;
   if (c.free) {
     Stream st(s.seed, SID_HMC_MOM, (uint64_t)d, iter);
@@ -355,7 +394,7 @@ __global__ void k_hmc_leap(DevState s, int first) {
   const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= s.hmc_D) return;
   const HmcCoord c = hmc_coord(s, d);
-  if (!c.free) return;
+  if (!c.free || hmc_in_block(s, c)) return;
   const float eps = (float)s.hmc_sc[HS_EPS_USED];
   const float p = s.hmc_mom[d] + (first ? 0.5f : 1.0f) * eps * s.hmc_grad[d];
   s.hmc_mom[d] = p;
@@ -479,7 +518,7 @@ __global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
   float e = 0.0f;
   if (d < s.hmc_D) {
     const HmcCoord c = hmc_coord(s, d);
-    if (c.free) {
+    if (c.free && !hmc_in_block(s, c)) {
       float p = s.hmc_mom[d];
       if (kick) {
         p += 0.5f * (float)s.hmc_sc[HS_EPS_USED] * s.hmc_grad[d];
@@ -527,12 +566,14 @@ __global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
 // The Metropolis decision on H = -log p + K (one CTA), and the step-size
 // adaptation.  mode 1 only reports the change of the log posterior
 // (-(H1 - H0) with zero momenta) in HS_LAST_DH.
-__global__ void __launch_bounds__(256) k_hmc_accept(DevState s, int n_hpart, int n_epart, int mode) {
+__global__ void __launch_bounds__(256) k_hmc_accept(DevState s, int n_hpart, int n_epart, int n_epart_b, int mode) {
   __shared__ FF shf[8 * 2];
   __shared__ long long shn[8];
   FF acc{0.0f, 0.0f}, ace{0.0f, 0.0f};
   for (int t = threadIdx.x; t < n_hpart; t += blockDim.x) acc = ff_add(acc, s.hmc_hpart[t]);
   for (int t = threadIdx.x; t < n_epart; t += blockDim.x) ace = ff_add(ace, s.hmc_epart[t]);
+  if (s.hmc_nb > 0)
+    for (int t = threadIdx.x; t < n_epart_b; t += blockDim.x) ace = ff_add(ace, s.hmc_epart_b[t]);
   FF f[2] = {acc, ace};
   long long n[1] = {0};
   block_sum_ff<2, 1>(f, n, shf, shn);
@@ -586,6 +627,189 @@ __global__ void k_hmc_finish(DevState s) {
   const float v = s.hmc_th0[d];
   *c.pos = v;
   hmc_derived(s, c, v);
+}
+
+// ---------------------------------------------------------------------------
+// Per-gene block metric.  Within gene g the coordinates
+//   u = (alpha_g, beta_g1 .. beta_g(K-1), nu_g1 .. nu_g(B-1))
+// enter every entry's eta through a_bk . u (a_bk: 1 for alpha, 1 for beta_k if
+// k >= 1, 1 for nu_b if b >= 1), so the Fisher information of u is
+//   F_g = sum_{b,k} W_bkg a_bk a_bk^T,   W_bkg = sum over the cells of (b, k) of
+//   phi mu / (phi + mu)  (part slot 2, per segment),
+// plus the priors' precisions on the diagonal.  Its Cholesky factor turns the
+// strong alpha-beta and alpha-nu correlations (alpha is informed only by
+// type-0 cells once the betas are free) into unit scale.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t hmc_block_pos(const DevState& s, int j, int64_t g) {
+  const int K = s.K;
+  if (j == 0) return g;                                              // alpha
+  if (j < K) return s.Gp + (int64_t)j * s.Gp + g;                    // beta_j
+  return s.Gp * (1 + K) + (int64_t)(j - K + 1) * s.Gp + g;           // nu_(j-K+1)
+}
+
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }  // j <= i
+
+__global__ void k_hmc_metric_blocks(DevState s, int metric_mode) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= s.G || s.hmc_nb == 0) return;
+  const bool adapt = hmc_metric_now(s, metric_mode);
+  const int K = s.K, B = s.B, nb = s.hmc_nb;
+  float F[HMC_BLOCK_MAX * (HMC_BLOCK_MAX + 1) / 2];
+  for (int t = 0; t < nb * (nb + 1) / 2; ++t) F[t] = 0.0f;
+  for (int b = 0; b < B; ++b)
+    for (int k = 0; k < K; ++k) {
+      float* wp = s.hmc_wbk + ((int64_t)b * K + k) * s.G + g;
+      if (adapt) *wp = (float)seg_sum(s, b, k, 2, g);
+      const float w = *wp;
+      // a_bk has ones at 0, k (k >= 1) and K - 1 + b (b >= 1)
+      int idx[3], n = 0;
+      idx[n++] = 0;
+      if (k >= 1) idx[n++] = k;
+      if (b >= 1) idx[n++] = K - 1 + b;
+      for (int p = 0; p < n; ++p)
+        for (int q = 0; q <= p; ++q) F[tri(idx[p], idx[q])] += w;
+    }
+  // the priors' precisions under the current L and tau0
+  F[tri(0, 0)] += (float)(1.0 / SIGMA2_ALPHA);
+  for (int k = 1; k < K; ++k)
+    F[tri(k, k)] += (float)(1.0 / (s.L[(int64_t)k * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1]));
+  for (int b = 1; b < B; ++b) F[tri(K - 1 + b, K - 1 + b)] += (float)(1.0 / SIGMA2_NU);
+  // in-place Cholesky F = L L^T (lower); a non-positive pivot falls back to
+  // the diagonal
+  bool ok = true;
+  for (int i = 0; i < nb && ok; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      float v = F[tri(i, j)];
+      for (int q = 0; q < j; ++q) v -= F[tri(i, q)] * F[tri(j, q)];
+      if (i == j) {
+        if (!(v > 0.0f)) {
+          ok = false;
+          break;
+        }
+        F[tri(i, i)] = sqrtf(v);
+      } else {
+        F[tri(i, j)] = v / F[tri(j, j)];
+      }
+    }
+  }
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j <= i; ++j) {
+      float v;
+      if (ok) v = F[tri(i, j)];
+      else v = i == j ? sqrtf(fmaxf(s.hmc_mass[hmc_block_pos(s, i, g)], HMC_MASS_FLOOR)) : 0.0f;
+      s.hmc_chol[(int64_t)tri(i, j) * s.G + g] = v;
+    }
+}
+
+// x = L^{-1} y (forward substitution) with the gene's packed factor.
+__device__ __forceinline__ void hmc_lsolve(const DevState& s, int64_t g, const float* y, float* x) {
+  const int nb = s.hmc_nb;
+  for (int i = 0; i < nb; ++i) {
+    float v = y[i];
+    for (int q = 0; q < i; ++q) v -= s.hmc_chol[(int64_t)tri(i, q) * s.G + g] * x[q];
+    x[i] = v / s.hmc_chol[(int64_t)tri(i, i) * s.G + g];
+  }
+}
+
+// x = L^{-T} y (back substitution).
+__device__ __forceinline__ void hmc_ltsolve(const DevState& s, int64_t g, const float* y, float* x) {
+  const int nb = s.hmc_nb;
+  for (int i = nb - 1; i >= 0; --i) {
+    float v = y[i];
+    for (int q = i + 1; q < nb; ++q) v -= s.hmc_chol[(int64_t)tri(q, i) * s.G + g] * x[q];
+    x[i] = v / s.hmc_chol[(int64_t)tri(i, i) * s.G + g];
+  }
+}
+
+// Momentum of the gene blocks: p = L z, z ~ N(0, I).
+__global__ void k_hmc_start_blocks(DevState s) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= s.G || s.hmc_nb == 0) return;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int nb = s.hmc_nb;
+  float z[HMC_BLOCK_MAX];
+  Stream st(s.seed, SID_HMC_MOM, (uint64_t)s.hmc_D + (uint64_t)g, iter);
+  for (int j = 0; j < nb; ++j) z[j] = normal(st);
+  for (int i = 0; i < nb; ++i) {
+    float p = 0.0f;
+    for (int q = 0; q <= i; ++q) p += s.hmc_chol[(int64_t)tri(i, q) * s.G + g] * z[q];
+    const int64_t d = hmc_block_pos(s, i, g);
+    s.hmc_mom[d] = p;
+    s.hmc_mom0[d] = p;
+    s.hmc_th0[d] = i == 0 ? s.alpha[g] : (i < s.K ? s.beta[(int64_t)i * s.Gp + g]
+                                                  : s.nu[(int64_t)(i - s.K + 1) * s.Gp + g]);
+  }
+}
+
+// Kick and drift of the gene blocks: p += c eps grad, u += eps M^{-1} p.
+__global__ void k_hmc_leap_blocks(DevState s, int first) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= s.G || s.hmc_nb == 0) return;
+  const int nb = s.hmc_nb;
+  const float eps = (float)s.hmc_sc[HS_EPS_USED];
+  const float c = first ? 0.5f : 1.0f;
+  float p[HMC_BLOCK_MAX], y[HMC_BLOCK_MAX], v[HMC_BLOCK_MAX];
+  for (int i = 0; i < nb; ++i) {
+    const int64_t d = hmc_block_pos(s, i, g);
+    p[i] = s.hmc_mom[d] + c * eps * s.hmc_grad[d];
+    s.hmc_mom[d] = p[i];
+  }
+  hmc_lsolve(s, g, p, y);
+  hmc_ltsolve(s, g, y, v);
+  s.alpha[g] += eps * v[0];
+  for (int k = 1; k < s.K; ++k) s.beta[(int64_t)k * s.Gp + g] += eps * v[k];
+  for (int b = 1; b < s.B; ++b) s.nu[(int64_t)b * s.Gp + g] += eps * v[s.K - 1 + b];
+}
+
+// Closing half kick of the gene blocks, then their kinetic change
+// (|L^{-1} p|^2 - |L^{-1} p0|^2) / 2 minus the prior change, per CTA.
+__global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick) {
+  __shared__ FF shf[8];
+  __shared__ long long shn[8];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float e = 0.0f;
+  if (g < s.G && s.hmc_nb > 0) {
+    const int nb = s.hmc_nb, K = s.K;
+    const float eps = (float)s.hmc_sc[HS_EPS_USED];
+    float p[HMC_BLOCK_MAX], p0[HMC_BLOCK_MAX], y[HMC_BLOCK_MAX], y0[HMC_BLOCK_MAX];
+    bool same = true;
+    for (int i = 0; i < nb; ++i) {
+      const int64_t d = hmc_block_pos(s, i, g);
+      p[i] = s.hmc_mom[d];
+      if (kick) {
+        p[i] += 0.5f * eps * s.hmc_grad[d];
+        s.hmc_mom[d] = p[i];
+      }
+      p0[i] = s.hmc_mom0[d];
+      same = same && p[i] == p0[i];
+    }
+    float dK = 0.0f;
+    if (!same) {
+      hmc_lsolve(s, g, p, y);
+      hmc_lsolve(s, g, p0, y0);
+      for (int i = 0; i < nb; ++i) dK += (y[i] - y0[i]) * (y[i] + y0[i]);
+      dK *= 0.5f;
+    }
+    // prior change of alpha, beta and nu (cancellation-free)
+    const float a1 = s.alpha[g], a0 = s.hmc_th0[g], ma = s.mu_alpha[g];
+    float dprior = -(a1 - a0) * ((a1 - ma) + (a0 - ma)) * (float)(0.5 / SIGMA2_ALPHA);
+    for (int k = 1; k < K; ++k) {
+      const int64_t d = hmc_block_pos(s, k, g);
+      const float v1 = s.beta[(int64_t)k * s.Gp + g], v0 = s.hmc_th0[d];
+      const double v = s.L[(int64_t)k * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1];
+      dprior += (float)(-(double)(v1 - v0) * ((double)v1 + (double)v0) * 0.5 / v);
+    }
+    for (int b = 1; b < s.B; ++b) {
+      const int64_t d = hmc_block_pos(s, K - 1 + b, g);
+      const float v1 = s.nu[(int64_t)b * s.Gp + g], v0 = s.hmc_th0[d], m = s.mu_nu[b];
+      dprior += -(v1 - v0) * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_NU);
+    }
+    e = dK - dprior;
+  }
+  FF f[1] = {FF{e, 0.0f}};
+  long long n[1] = {0};
+  block_sum_ff<1, 1>(f, n, shf, shn);
+  if (threadIdx.x == 0) s.hmc_epart_b[blockIdx.x] = f[0];
 }
 
 // Unit metric before the first adaptation.

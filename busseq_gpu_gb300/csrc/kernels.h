@@ -27,14 +27,19 @@ __global__ void k_zlist_fill(DevState s, const int64_t* rowoff, int2* zij);
 __global__ void k_zval_from_mask(DevState s);
 __global__ void k_zmask_from_zval(DevState s);
 __global__ void k_zlist_gather_x(DevState s, int32_t* out);
-__global__ void k_hmc_grad(DevState s, int force_metric);
-__global__ void k_hmc_assemble(DevState s, int force_metric);
+__global__ void k_hmc_grad(DevState s, int metric_mode);
+__global__ void k_hmc_assemble(DevState s, int metric_mode);
 __global__ void k_hmc_start(DevState s);
 __global__ void k_hmc_leap(DevState s, int first);
 __global__ void k_hmc_refresh_E(DevState s);
 __global__ void k_hmc_dll(DevState s);
 __global__ void k_hmc_energy(DevState s, int kick);
-__global__ void k_hmc_accept(DevState s, int n_hpart, int n_epart, int mode);
+__global__ void k_hmc_accept(DevState s, int n_hpart, int n_epart, int n_epart_b, int mode);
+__global__ void k_hmc_metric_blocks(DevState s, int metric_mode);
+__global__ void k_hmc_mass(DevState s);
+__global__ void k_hmc_start_blocks(DevState s);
+__global__ void k_hmc_leap_blocks(DevState s, int first);
+__global__ void k_hmc_energy_blocks(DevState s, int kick);
 __global__ void k_hmc_finish(DevState s);
 __global__ void k_hmc_set_th0(DevState s, const float* src);
 __global__ void k_hmc_unit_mass(DevState s);
