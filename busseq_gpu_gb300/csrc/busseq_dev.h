@@ -171,6 +171,7 @@ struct DevState {
   // (0: diagonal metric everywhere)
   int hmc_nb;
   float* hmc_chol;
+  float* hmc_minv;  // [nb * nb][G] inverse of each gene's block metric (velocity and kinetic energy)
   // frozen data of the metric: the information part of every diagonal mass
   // (without the priors, which follow the current L and tau0) and the
   // per-segment Fisher sums W_bkg of the blocks [B*K][G]

@@ -222,7 +222,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       break;
     case KID_HMC_ACCEPT:
       k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
-                                      (int)blocks_for(s.G, 256), 0);
+                                      (int)blocks_for(s.G * 32, 256), 0);
       LAUNCH_CHECK("k_hmc_accept");
       break;
     case KID_HMC_METRIC_BLOCKS:
@@ -230,12 +230,12 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_metric_blocks");
       break;
     case KID_HMC_START_BLOCKS:
-      k_hmc_start_blocks<<<blocks_for(s.G, 128), 128, 0, st>>>(s);
+      k_hmc_start_blocks<<<blocks_for(s.G * 32, 128), 128, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_start_blocks");
       break;
     case KID_HMC_LEAP_BLOCKS0:
     case KID_HMC_LEAP_BLOCKS:
-      k_hmc_leap_blocks<<<blocks_for(s.G, 128), 128, 0, st>>>(s, which == KID_HMC_LEAP_BLOCKS0 ? 1 : 0);
+      k_hmc_leap_blocks<<<blocks_for(s.G * 32, 128), 128, 0, st>>>(s, which == KID_HMC_LEAP_BLOCKS0 ? 1 : 0);
       LAUNCH_CHECK("k_hmc_leap_blocks");
       break;
     case KID_HMC_MASS:
@@ -243,7 +243,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_mass");
       break;
     case KID_HMC_ENERGY_BLOCKS:
-      k_hmc_energy_blocks<<<blocks_for(s.G, 256), 256, 0, st>>>(s, 1);
+      k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, st>>>(s, 1);
       LAUNCH_CHECK("k_hmc_energy_blocks");
       break;
     case KID_HMC_FINISH:
@@ -487,9 +487,10 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_fis, s.hmc_D));
       s.hmc_nb = (K + B - 1 <= bq::HMC_BLOCK_MAX) ? K + B - 1 : 0;
       if (s.hmc_nb > 0) {
-        TRY(h->alloc(&s.hmc_chol, (int64_t)s.hmc_nb * (s.hmc_nb + 1) / 2 * G));
+        TRY(h->alloc(&s.hmc_chol, (int64_t)bq::HMC_BLOCK_MAX * (bq::HMC_BLOCK_MAX + 1) / 2 * G));
         TRY(h->alloc(&s.hmc_wbk, (int64_t)B * K * G));
-        TRY(h->alloc(&s.hmc_epart_b, (int64_t)blocks_for(G, 256)));
+        TRY(h->alloc(&s.hmc_minv, (int64_t)bq::HMC_BLOCK_MAX * bq::HMC_BLOCK_MAX * G));
+        TRY(h->alloc(&s.hmc_epart_b, (int64_t)blocks_for(G * 32, 256)));
       }
       bq::k_hmc_unit_mass<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s);
       LAUNCH_CHECK("k_hmc_unit_mass");
@@ -1001,8 +1002,9 @@ std::vector<DevBlock> run_blocks(const busseq_handle* h) {
     v.push_back({s.hmc_sc, (size_t)bq::HS_COUNT * 8});
     v.push_back({s.hmc_fis, (size_t)s.hmc_D * 4});
     if (s.hmc_nb > 0) {
-      v.push_back({s.hmc_chol, (size_t)s.hmc_nb * (s.hmc_nb + 1) / 2 * s.G * 4});
+      v.push_back({s.hmc_chol, (size_t)bq::HMC_BLOCK_MAX * (bq::HMC_BLOCK_MAX + 1) / 2 * s.G * 4});
       v.push_back({s.hmc_wbk, (size_t)s.B * s.K * s.G * 4});
+      v.push_back({s.hmc_minv, (size_t)bq::HMC_BLOCK_MAX * bq::HMC_BLOCK_MAX * s.G * 4});
     }
   }
   return v;
@@ -1315,9 +1317,9 @@ int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* 
     bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
     bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
     bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
-    if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G, 256), 256, 0, h->stream>>>(s, 0);
+    if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0);
     bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
-                                               (int)blocks_for(s.G, 256), 1);
+                                               (int)blocks_for(s.G * 32, 256), 1);
     e = cudaGetLastError();
   }
   double sc[bq::HS_COUNT];

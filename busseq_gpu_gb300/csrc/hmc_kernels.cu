@@ -122,6 +122,16 @@ __device__ __forceinline__ float trigamma_asym(float z) {
 
 constexpr int HMC_TAB = 32;  // digamma / trigamma differences tabulated for counts below this
 
+// log x from the hardware base-2 logarithm (lg2.approx.f32, absolute error
+// about 2^-22).  Used only for gradients: their errors cost acceptance rate,
+// never correctness, since the decision uses the accurate change of the log
+// likelihood from k_hmc_dll.
+__device__ __forceinline__ float log_hw(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r * 0.6931471805599453f;
+}
+
 // Sums 8 per-lane values (v[u], one per chunk cell j0+u) over the warp: after
 // the exchange, lanes with lane % 4 == 0 hold the warp total of value
 // ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1).
@@ -197,8 +207,9 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
   }
   const float z32 = ph + (float)HMC_TAB;
   const float dg32 = tdg[HMC_TAB - 1][tid] + fast_rcp(z32 - 1.0f);
+  const float iz32h = fast_rcp(z32 - 0.5f);
   const float tg32 = ttg[HMC_TAB - 1][tid] + fast_rcp((z32 - 1.0f) * (z32 - 1.0f));
-  const float dtail32 = digamma_tail(z32), tasym32 = trigamma_asym(z32);
+  const float tasym32 = trigamma_asym(z32);
   __syncthreads();
   const char* Xg = reinterpret_cast<const char*>(s.X + g);
   const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
@@ -215,10 +226,16 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
       const float mu = M * dv[u];
       const float rc = fast_rcp(ph + mu);
       const float r = ph * (xf - mu) * rc;
+      // psi(ph + x) - psi(ph): table, or for x >= 32 the asymptotic series
+      // psi(z) = log(z - 1/2) + 1/(24 (z - 1/2)^2) + O((z - 1/2)^-4)
       float dg;
-      if (x < HMC_TAB) dg = tdg[x][tid];
-      else dg = dg32 + log_ratio(ph + xf, z32, xf - (float)HMC_TAB) + (digamma_tail(ph + xf) - dtail32);
-      const float d1 = dg - log1p_fast(mu * iph) + (mu - xf) * rc;  // d ll / d phi
+      if (x < HMC_TAB) {
+        dg = tdg[x][tid];
+      } else {
+        const float iz = fast_rcp(ph + xf - 0.5f);
+        dg = dg32 + log_hw((ph + xf - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f);
+      }
+      const float d1 = dg + log_hw(ph * rc) + (mu - xf) * rc;  // d ll / d phi
       fr += r;
       fp = fmaf(ph, d1, fp);
       rv[u] = gv ? r : 0.0f;
@@ -649,12 +666,16 @@ __device__ __forceinline__ int64_t hmc_block_pos(const DevState& s, int j, int64
 
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }  // j <= i
 
+// per-gene storage of the factor and the inverse (gene-major)
+constexpr int HMC_TRI = HMC_BLOCK_MAX * (HMC_BLOCK_MAX + 1) / 2;
+constexpr int HMC_SQ = HMC_BLOCK_MAX * HMC_BLOCK_MAX;
+
 __global__ void k_hmc_metric_blocks(DevState s, int metric_mode) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= s.G || s.hmc_nb == 0) return;
   const bool adapt = hmc_metric_now(s, metric_mode);
   const int K = s.K, B = s.B, nb = s.hmc_nb;
-  float F[HMC_BLOCK_MAX * (HMC_BLOCK_MAX + 1) / 2];
+  float F[HMC_TRI];
   for (int t = 0; t < nb * (nb + 1) / 2; ++t) F[t] = 0.0f;
   for (int b = 0; b < B; ++b)
     for (int k = 0; k < K; ++k) {
@@ -697,114 +718,133 @@ __global__ void k_hmc_metric_blocks(DevState s, int metric_mode) {
       float v;
       if (ok) v = F[tri(i, j)];
       else v = i == j ? sqrtf(fmaxf(s.hmc_mass[hmc_block_pos(s, i, g)], HMC_MASS_FLOOR)) : 0.0f;
-      s.hmc_chol[(int64_t)tri(i, j) * s.G + g] = v;
+      F[tri(i, j)] = v;
+      s.hmc_chol[g * HMC_TRI + tri(i, j)] = v;
+    }
+  // M^{-1} = L^{-T} L^{-1}: invert L in place (lower), then the product
+  for (int i = 0; i < nb; ++i) {
+    F[tri(i, i)] = 1.0f / F[tri(i, i)];
+    for (int j = 0; j < i; ++j) {
+      float v = 0.0f;
+      for (int q = j; q < i; ++q) v += F[tri(i, q)] * F[tri(q, j)];
+      F[tri(i, j)] = -v * F[tri(i, i)];
+    }
+  }
+  for (int i = 0; i < nb; ++i)
+    for (int j = 0; j <= i; ++j) {
+      float v = 0.0f;
+      for (int q = i; q < nb; ++q) v += F[tri(q, i)] * F[tri(q, j)];
+      s.hmc_minv[g * HMC_SQ + i * nb + j] = v;
+      s.hmc_minv[g * HMC_SQ + j * nb + i] = v;
     }
 }
 
-// x = L^{-1} y (forward substitution) with the gene's packed factor.
-__device__ __forceinline__ void hmc_lsolve(const DevState& s, int64_t g, const float* y, float* x) {
-  const int nb = s.hmc_nb;
-  for (int i = 0; i < nb; ++i) {
-    float v = y[i];
-    for (int q = 0; q < i; ++q) v -= s.hmc_chol[(int64_t)tri(i, q) * s.G + g] * x[q];
-    x[i] = v / s.hmc_chol[(int64_t)tri(i, i) * s.G + g];
-  }
+
+// The gene-block kernels run one warp per gene: lane i < nb holds block
+// coordinate i, and the products with the factor or the inverse gather the
+// other coordinates by shuffles.
+__device__ __forceinline__ float* hmc_block_ptr(const DevState& s, int i, int64_t g) {
+  if (i == 0) return s.alpha + g;
+  if (i < s.K) return s.beta + (int64_t)i * s.Gp + g;
+  return s.nu + (int64_t)(i - s.K + 1) * s.Gp + g;
 }
 
-// x = L^{-T} y (back substitution).
-__device__ __forceinline__ void hmc_ltsolve(const DevState& s, int64_t g, const float* y, float* x) {
-  const int nb = s.hmc_nb;
-  for (int i = nb - 1; i >= 0; --i) {
-    float v = y[i];
-    for (int q = i + 1; q < nb; ++q) v -= s.hmc_chol[(int64_t)tri(q, i) * s.G + g] * x[q];
-    x[i] = v / s.hmc_chol[(int64_t)tri(i, i) * s.G + g];
+// sum_j A[i][j] x_j over the warp's block (A row-major, nb x nb, at `a`).
+__device__ __forceinline__ float hmc_row_dot(const float* a, int nb, int lane, float x) {
+  float acc = 0.0f;
+  for (int j = 0; j < nb; ++j) {
+    const float xj = __shfl_sync(0xffffffffu, x, j);
+    if (lane < nb) acc = fmaf(a[lane * nb + j], xj, acc);
   }
+  return acc;
 }
 
 // Momentum of the gene blocks: p = L z, z ~ N(0, I).
-__global__ void k_hmc_start_blocks(DevState s) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= s.G || s.hmc_nb == 0) return;
-  const uint32_t iter = (uint32_t)*s.iter;
+__global__ void __launch_bounds__(128) k_hmc_start_blocks(DevState s) {
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= s.G || s.hmc_nb == 0) return;  // whole warps leave together
   const int nb = s.hmc_nb;
-  float z[HMC_BLOCK_MAX];
-  Stream st(s.seed, SID_HMC_MOM, (uint64_t)s.hmc_D + (uint64_t)g, iter);
-  for (int j = 0; j < nb; ++j) z[j] = normal(st);
-  for (int i = 0; i < nb; ++i) {
-    float p = 0.0f;
-    for (int q = 0; q <= i; ++q) p += s.hmc_chol[(int64_t)tri(i, q) * s.G + g] * z[q];
-    const int64_t d = hmc_block_pos(s, i, g);
+  const uint32_t iter = (uint32_t)*s.iter;
+  float z = 0.0f;
+  if (lane < nb) {
+    Stream st(s.seed, SID_HMC_MOM, (uint64_t)s.hmc_D + (uint64_t)g * HMC_BLOCK_MAX + lane, iter);
+    z = normal(st);
+  }
+  const float* L = s.hmc_chol + g * HMC_TRI;
+  float p = 0.0f;
+  for (int q = 0; q < nb; ++q) {
+    const float zq = __shfl_sync(0xffffffffu, z, q);
+    if (lane < nb && q <= lane) p = fmaf(L[tri(lane, q)], zq, p);
+  }
+  if (lane < nb) {
+    const int64_t d = hmc_block_pos(s, lane, g);
     s.hmc_mom[d] = p;
     s.hmc_mom0[d] = p;
-    s.hmc_th0[d] = i == 0 ? s.alpha[g] : (i < s.K ? s.beta[(int64_t)i * s.Gp + g]
-                                                  : s.nu[(int64_t)(i - s.K + 1) * s.Gp + g]);
+    s.hmc_th0[d] = *hmc_block_ptr(s, lane, g);
   }
 }
 
 // Kick and drift of the gene blocks: p += c eps grad, u += eps M^{-1} p.
-__global__ void k_hmc_leap_blocks(DevState s, int first) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(128) k_hmc_leap_blocks(DevState s, int first) {
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (g >= s.G || s.hmc_nb == 0) return;
   const int nb = s.hmc_nb;
   const float eps = (float)s.hmc_sc[HS_EPS_USED];
-  const float c = first ? 0.5f : 1.0f;
-  float p[HMC_BLOCK_MAX], y[HMC_BLOCK_MAX], v[HMC_BLOCK_MAX];
-  for (int i = 0; i < nb; ++i) {
-    const int64_t d = hmc_block_pos(s, i, g);
-    p[i] = s.hmc_mom[d] + c * eps * s.hmc_grad[d];
-    s.hmc_mom[d] = p[i];
+  float p = 0.0f;
+  int64_t d = 0;
+  if (lane < nb) {
+    d = hmc_block_pos(s, lane, g);
+    p = s.hmc_mom[d] + (first ? 0.5f : 1.0f) * eps * s.hmc_grad[d];
+    s.hmc_mom[d] = p;
   }
-  hmc_lsolve(s, g, p, y);
-  hmc_ltsolve(s, g, y, v);
-  s.alpha[g] += eps * v[0];
-  for (int k = 1; k < s.K; ++k) s.beta[(int64_t)k * s.Gp + g] += eps * v[k];
-  for (int b = 1; b < s.B; ++b) s.nu[(int64_t)b * s.Gp + g] += eps * v[s.K - 1 + b];
+  const float v = hmc_row_dot(s.hmc_minv + g * HMC_SQ, nb, lane, p);
+  if (lane < nb) *hmc_block_ptr(s, lane, g) += eps * v;
 }
 
 // Closing half kick of the gene blocks, then their kinetic change
-// (|L^{-1} p|^2 - |L^{-1} p0|^2) / 2 minus the prior change, per CTA.
+// (p^T M^{-1} p - p0^T M^{-1} p0) / 2 minus the prior change, per CTA.
 __global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick) {
   __shared__ FF shf[8];
   __shared__ long long shn[8];
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   float e = 0.0f;
   if (g < s.G && s.hmc_nb > 0) {
     const int nb = s.hmc_nb, K = s.K;
     const float eps = (float)s.hmc_sc[HS_EPS_USED];
-    float p[HMC_BLOCK_MAX], p0[HMC_BLOCK_MAX], y[HMC_BLOCK_MAX], y0[HMC_BLOCK_MAX];
-    bool same = true;
-    for (int i = 0; i < nb; ++i) {
-      const int64_t d = hmc_block_pos(s, i, g);
-      p[i] = s.hmc_mom[d];
+    float p = 0.0f, p0 = 0.0f, dprior = 0.0f;
+    if (lane < nb) {
+      const int64_t d = hmc_block_pos(s, lane, g);
+      p = s.hmc_mom[d];
       if (kick) {
-        p[i] += 0.5f * eps * s.hmc_grad[d];
-        s.hmc_mom[d] = p[i];
+        p += 0.5f * eps * s.hmc_grad[d];
+        s.hmc_mom[d] = p;
       }
-      p0[i] = s.hmc_mom0[d];
-      same = same && p[i] == p0[i];
+      p0 = s.hmc_mom0[d];
+      // prior change of this coordinate (cancellation-free)
+      const float v1 = *hmc_block_ptr(s, lane, g), v0 = s.hmc_th0[d];
+      if (lane == 0) {
+        const float m = s.mu_alpha[g];
+        dprior = -(v1 - v0) * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_ALPHA);
+      } else if (lane < K) {
+        const double v = s.L[(int64_t)lane * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1];
+        dprior = (float)(-(double)(v1 - v0) * ((double)v1 + (double)v0) * 0.5 / v);
+      } else {
+        const float m = s.mu_nu[lane - K + 1];
+        dprior = -(v1 - v0) * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_NU);
+      }
     }
-    float dK = 0.0f;
+    const bool same = __all_sync(0xffffffffu, p == p0);
+    float dk = 0.0f;
     if (!same) {
-      hmc_lsolve(s, g, p, y);
-      hmc_lsolve(s, g, p0, y0);
-      for (int i = 0; i < nb; ++i) dK += (y[i] - y0[i]) * (y[i] + y0[i]);
-      dK *= 0.5f;
+      const float* a = s.hmc_minv + g * HMC_SQ;
+      const float v = hmc_row_dot(a, nb, lane, p);
+      const float v0 = hmc_row_dot(a, nb, lane, p0);
+      dk = 0.5f * (p * v - p0 * v0);
     }
-    // prior change of alpha, beta and nu (cancellation-free)
-    const float a1 = s.alpha[g], a0 = s.hmc_th0[g], ma = s.mu_alpha[g];
-    float dprior = -(a1 - a0) * ((a1 - ma) + (a0 - ma)) * (float)(0.5 / SIGMA2_ALPHA);
-    for (int k = 1; k < K; ++k) {
-      const int64_t d = hmc_block_pos(s, k, g);
-      const float v1 = s.beta[(int64_t)k * s.Gp + g], v0 = s.hmc_th0[d];
-      const double v = s.L[(int64_t)k * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1];
-      dprior += (float)(-(double)(v1 - v0) * ((double)v1 + (double)v0) * 0.5 / v);
-    }
-    for (int b = 1; b < s.B; ++b) {
-      const int64_t d = hmc_block_pos(s, K - 1 + b, g);
-      const float v1 = s.nu[(int64_t)b * s.Gp + g], v0 = s.hmc_th0[d], m = s.mu_nu[b];
-      dprior += -(v1 - v0) * ((v1 - m) + (v0 - m)) * (float)(0.5 / SIGMA2_NU);
-    }
-    e = dK - dprior;
+    e = dk - dprior;
   }
   FF f[1] = {FF{e, 0.0f}};
   long long n[1] = {0};
