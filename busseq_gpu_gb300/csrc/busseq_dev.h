@@ -161,6 +161,7 @@ struct DevState {
   float* hmc_grad;  // [D] gradient of the log posterior
   float* hmc_mass;  // [D] diagonal metric
   float* hmc_th0;   // [D] coordinates at the start of the transition
+  float* hmc_part;  // [cap_g][NSLOT][Gp] per-chunk gradient (and information) sums
   float* hmc_cpart; // [n_tiles][N] per-tile sums of d ll / d delta
   float* hmc_cpartw;// [n_tiles][N] per-tile Fisher information of delta
   FF* hmc_hpart;    // [n_tiles * cap_g] per-CTA log-likelihood change

@@ -191,7 +191,8 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
     }
     case KID_HMC_GRAD:
     case KID_HMC_GRAD_START:
-      k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s, which == KID_HMC_GRAD_START ? 1 : 0);
+      if (which == KID_HMC_GRAD_START) k_hmc_grad_metric<<<gene_grid, GENE_TILE, 0, st>>>(s, 1);
+      else k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_grad");
       break;
     case KID_HMC_ASSEMBLE:
@@ -479,6 +480,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_grad, s.hmc_D));
       TRY(h->alloc(&s.hmc_mass, s.hmc_D));
       TRY(h->alloc(&s.hmc_th0, s.hmc_D));
+      TRY(h->alloc(&s.hmc_part, (int64_t)s.cap_g * bq::NSLOT * Gp));
       TRY(h->alloc(&s.hmc_cpart, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_cpartw, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g));
@@ -1277,7 +1279,7 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   std::vector<float> mass_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
-  bq::k_hmc_grad<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
+  bq::k_hmc_grad_metric<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
   bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_assemble");

@@ -168,13 +168,26 @@ __device__ __forceinline__ int transpose_slot(int lane) {
 // eta) and 3 (observed information of psi); per-cell sums over the CTA's genes
 // go to hmc_cpart[tile][cell] (and hmc_cpartw for the Fisher information).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_mode) {
+// Sum of HMC partial slot `slot` of gene g over the chunks of segment (b, k),
+// in float (gradients need no more).
+__device__ __forceinline__ float hmc_seg_sum(const DevState& s, int b, int k, int slot, int64_t g) {
+  const int2 r = s.seg_chunk[b * s.K + k];
+  float acc = 0.0f;
+  for (int c = r.x; c < r.x + r.y; ++c) acc += __ldg(&s.hmc_part[((int64_t)c * NSLOT + slot) * s.Gp + g]);
+  return acc;
+}
+
+// METRIC: the variant run at the start of a transition, which (while the
+// metric adapts, or always for metric_mode 2) also sums the information terms;
+// the leapfrog passes run the lean variant (less shared memory, more CTAs).
+template <bool METRIC>
+__device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode) {
   __shared__ float tdg[HMC_TAB][GENE_TILE];
-  __shared__ float ttg[HMC_TAB][GENE_TILE];
+  __shared__ float ttg[METRIC ? HMC_TAB : 1][GENE_TILE];
   __shared__ __align__(16) int s_i[MAX_CG];
   __shared__ __align__(16) float s_D[MAX_CG];
   __shared__ float s_cell[GENE_TILE / 32][MAX_CG];
-  __shared__ float s_cellw[GENE_TILE / 32][MAX_CG];
+  __shared__ float s_cellw[METRIC ? GENE_TILE / 32 : 1][METRIC ? MAX_CG : 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tile = blockIdx.x, row = blockIdx.y;
   const int4 ch = s.gchunk[row];
@@ -182,7 +195,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   if (len == 0) return;
-  const bool adapt = hmc_metric_now(s, metric_mode);
+  const bool adapt = METRIC && hmc_metric_now(s, metric_mode);
   const int len8 = (len + 7) & ~7;
   for (int j = tid; j < len8; j += GENE_TILE) {
     const bool in = j < len;
@@ -194,12 +207,12 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
   const float ph = gv ? s.phi[(int64_t)b * Gp + g] : 1.0f;
   const float M = gv ? s.E[((int64_t)b * s.K + k) * Gp + g] : 0.0f;
   const float iph = fast_rcp(ph);
-  // sum_{j<x} 1/(ph + j) and 1/(ph + j)^2 for x < HMC_TAB
+  // sum_{j<x} 1/(ph + j) (and 1/(ph + j)^2) for x < HMC_TAB
   {
     float dg = 0.0f, tg = 0.0f;
     for (int x = 0; x < HMC_TAB; ++x) {
       tdg[x][tid] = dg;
-      ttg[x][tid] = tg;
+      if (METRIC) ttg[x][tid] = tg;
       const float r = fast_rcp(ph + (float)x);
       dg += r;
       tg = fmaf(r, r, tg);
@@ -208,8 +221,11 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
   const float z32 = ph + (float)HMC_TAB;
   const float dg32 = tdg[HMC_TAB - 1][tid] + fast_rcp(z32 - 1.0f);
   const float iz32h = fast_rcp(z32 - 0.5f);
-  const float tg32 = ttg[HMC_TAB - 1][tid] + fast_rcp((z32 - 1.0f) * (z32 - 1.0f));
-  const float tasym32 = trigamma_asym(z32);
+  float tg32 = 0.0f, tasym32 = 0.0f;
+  if (METRIC) {
+    tg32 = ttg[HMC_TAB - 1][tid] + fast_rcp((z32 - 1.0f) * (z32 - 1.0f));
+    tasym32 = trigamma_asym(z32);
+  }
   __syncthreads();
   const char* Xg = reinterpret_cast<const char*>(s.X + g);
   const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
@@ -239,7 +255,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
       fr += r;
       fp = fmaf(ph, d1, fp);
       rv[u] = gv ? r : 0.0f;
-      if (adapt) {
+      if (METRIC && adapt) {
         const float w = ph * mu * rc;
         const float tg = x < HMC_TAB ? ttg[x][tid] : tg32 + (tasym32 - trigamma_asym(ph + xf));
         const float d2 = -tg + iph - 2.0f * rc + (ph + xf) * rc * rc;  // d2 ll / d phi2
@@ -252,19 +268,19 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
     ap.add(fp);
     const float cs = transpose_sum8(rv, lane);
     if ((lane & 3) == 0) s_cell[warp][j0 + transpose_slot(lane)] = cs;
-    if (adapt) {
+    if (METRIC && adapt) {
       aw.add(fw);
       ai.add(fi);
       const float cw = transpose_sum8(wv, lane);
       if ((lane & 3) == 0) s_cellw[warp][j0 + transpose_slot(lane)] = cw;
     }
   }
-  double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
-  pr[0] = gv ? ar.value() : 0.0;
-  pr[Gp] = gv ? ap.value() : 0.0;
-  if (adapt) {
-    pr[2 * Gp] = gv ? aw.value() : 0.0;
-    pr[3 * Gp] = gv ? ai.value() : 0.0;
+  float* pr = s.hmc_part + (int64_t)row * NSLOT * Gp + g;
+  pr[0] = gv ? ar.s - ar.c : 0.0f;
+  pr[Gp] = gv ? ap.s - ap.c : 0.0f;
+  if (METRIC && adapt) {
+    pr[2 * Gp] = gv ? aw.s - aw.c : 0.0f;
+    pr[3 * Gp] = gv ? ai.s - ai.c : 0.0f;
   }
   __syncthreads();
   for (int j = tid; j < len; j += GENE_TILE) {
@@ -272,11 +288,16 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s, int metric_m
 #pragma unroll
     for (int w = 0; w < GENE_TILE / 32; ++w) {
       t += s_cell[w][j];
-      if (adapt) tw += s_cellw[w][j];
+      if (METRIC && adapt) tw += s_cellw[w][j];
     }
     s.hmc_cpart[(int64_t)tile * s.N + s_i[j]] = t;
-    if (adapt) s.hmc_cpartw[(int64_t)tile * s.N + s_i[j]] = tw;
+    if (METRIC && adapt) s.hmc_cpartw[(int64_t)tile * s.N + s_i[j]] = tw;
   }
+}
+
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad(DevState s) { hmc_grad_body<false>(s, 0); }
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_grad_metric(DevState s, int metric_mode) {
+  hmc_grad_body<true>(s, metric_mode);
 }
 
 // Precision of a free coordinate's prior; psi's (tau_phi phi) stays in the
@@ -306,21 +327,21 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode) {
     const int B = s.B, K = s.K;
     switch (c.kind) {
       case HK_ALPHA: {
-        double sr = 0.0, sw = 0.0;
+        float sr = 0.0f, sw = 0.0f;
         for (int b = 0; b < B; ++b)
           for (int k = 0; k < K; ++k) {
-            sr += seg_sum(s, b, k, 0, g);
-            if (adapt) sw += seg_sum(s, b, k, 2, g);
+            sr += hmc_seg_sum(s, b, k, 0, g);
+            if (adapt) sw += hmc_seg_sum(s, b, k, 2, g);
           }
         gr = sr - ((double)s.alpha[g] - (double)s.mu_alpha[g]) / SIGMA2_ALPHA;
         m = sw + 1.0 / SIGMA2_ALPHA;
         break;
       }
       case HK_BETA: {
-        double sr = 0.0, sw = 0.0;
+        float sr = 0.0f, sw = 0.0f;
         for (int b = 0; b < B; ++b) {
-          sr += seg_sum(s, b, c.seg, 0, g);
-          if (adapt) sw += seg_sum(s, b, c.seg, 2, g);
+          sr += hmc_seg_sum(s, b, c.seg, 0, g);
+          if (adapt) sw += hmc_seg_sum(s, b, c.seg, 2, g);
         }
         const double v = s.L[(int64_t)c.seg * s.Gp + g] == 1 ? TAU1 : (double)s.p_tau0[1];
         gr = sr - (double)*c.pos / v;
@@ -328,20 +349,20 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode) {
         break;
       }
       case HK_NU: {
-        double sr = 0.0, sw = 0.0;
+        float sr = 0.0f, sw = 0.0f;
         for (int k = 0; k < K; ++k) {
-          sr += seg_sum(s, c.seg, k, 0, g);
-          if (adapt) sw += seg_sum(s, c.seg, k, 2, g);
+          sr += hmc_seg_sum(s, c.seg, k, 0, g);
+          if (adapt) sw += hmc_seg_sum(s, c.seg, k, 2, g);
         }
         gr = sr - ((double)*c.pos - (double)s.mu_nu[c.seg]) / SIGMA2_NU;
         m = sw + 1.0 / SIGMA2_NU;
         break;
       }
       case HK_PSI: {
-        double sp = 0.0, si = 0.0;
+        float sp = 0.0f, si = 0.0f;
         for (int k = 0; k < K; ++k) {
-          sp += seg_sum(s, c.seg, k, 1, g);
-          if (adapt) si += seg_sum(s, c.seg, k, 3, g);
+          sp += hmc_seg_sum(s, c.seg, k, 1, g);
+          if (adapt) si += hmc_seg_sum(s, c.seg, k, 3, g);
         }
         const double ph = s.phi[(int64_t)c.seg * s.Gp + g];
         gr = sp + KAPPA_PHI - TAU_PHI * ph;
@@ -349,7 +370,7 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode) {
         break;
       }
       default: {  // delta
-        double sr = 0.0, sw = 0.0;
+        float sr = 0.0f, sw = 0.0f;
         for (int t = 0; t < s.n_tiles; ++t) {
           sr += s.hmc_cpart[(int64_t)t * s.N + c.idx];
           if (adapt) sw += s.hmc_cpartw[(int64_t)t * s.N + c.idx];
@@ -680,7 +701,7 @@ __global__ void k_hmc_metric_blocks(DevState s, int metric_mode) {
   for (int b = 0; b < B; ++b)
     for (int k = 0; k < K; ++k) {
       float* wp = s.hmc_wbk + ((int64_t)b * K + k) * s.G + g;
-      if (adapt) *wp = (float)seg_sum(s, b, k, 2, g);
+      if (adapt) *wp = hmc_seg_sum(s, b, k, 2, g);
       const float w = *wp;
       // a_bk has ones at 0, k (k >= 1) and K - 1 + b (b >= 1)
       int idx[3], n = 0;

@@ -27,7 +27,8 @@ __global__ void k_zlist_fill(DevState s, const int64_t* rowoff, int2* zij);
 __global__ void k_zval_from_mask(DevState s);
 __global__ void k_zmask_from_zval(DevState s);
 __global__ void k_zlist_gather_x(DevState s, int32_t* out);
-__global__ void k_hmc_grad(DevState s, int metric_mode);
+__global__ void k_hmc_grad(DevState s);
+__global__ void k_hmc_grad_metric(DevState s, int metric_mode);
 __global__ void k_hmc_assemble(DevState s, int metric_mode);
 __global__ void k_hmc_start(DevState s);
 __global__ void k_hmc_leap(DevState s, int first);
