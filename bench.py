@@ -177,7 +177,7 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (BUSseq generative model)",
-        "config": _config(args.workload, n_b),
+        "config": _config(args.workload, n_b, cfg),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference program has no CPU implementation of the sweep; this arm times the FP64 CPU "
@@ -187,8 +187,8 @@ def run_reference(args, rank):
     return 0
 
 
-def _config(name="config1", n_b=None):
-    cfg = WORKLOADS[name]
+def _config(name="config1", n_b=None, cfg=None):
+    cfg = cfg if cfg is not None else WORKLOADS[name]
     n_b = list(n_b if n_b is not None else cfg["n_b"])
     N, G, K = int(sum(n_b)), cfg["G"], cfg["K"]
     mb = N * G * 4 / 1e6
@@ -245,6 +245,8 @@ def main():
     ap.add_argument("--cells", type=int, default=0,
                     help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
+    ap.add_argument("--leapfrog", type=int, default=0,
+                    help="leapfrog steps of the HMC block update (overrides the workload's; 0 keeps it)")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
                     help="config1 (the headline, default), config2 (config-1 data, HMC block update with 10 "
                          "leapfrog steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
@@ -272,7 +274,9 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    cfg = WORKLOADS[args.workload]
+    cfg = dict(WORKLOADS[args.workload])
+    if args.leapfrog > 0:
+        cfg["hmc"] = args.leapfrog
     n_b, G, K = list(cfg["n_b"]), cfg["G"], cfg["K"]
     seed = cfg["seed"]
     if args.cells > 0:
@@ -315,7 +319,7 @@ def main():
     if args.only_value:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                              "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(args.workload, n_b),
+                              "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(args.workload, n_b, cfg),
                               "note": "device-resident sweep rate only (--only-value)"}))
         s.close()
         return 0
@@ -374,7 +378,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (BUSseq generative model, seed %d)" % seed,
-            "config": _config(args.workload, n_b),
+            "config": _config(args.workload, n_b, cfg),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "note": "one job per run: pinned-host upload, init, %d sweeps, posterior, all estimates to host"
