@@ -107,6 +107,7 @@ def lib():
         "busseq_get_estimates": ([H, C.POINTER(Estimates)], C.c_int),
         "busseq_get_preserved": ([H, C.POINTER(Preserved)], C.c_int),
         "busseq_bic": ([H, _PD], C.c_int),
+        "busseq_corrected_counts": ([H, C.c_void_p, C.c_int32], C.c_int),
         "busseq_get_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_set_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_run_stage": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
@@ -182,6 +183,7 @@ class Sampler:
                  keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+        self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
         self.B, self.K = len(self.n_b), int(K)
         self.N = int(self.n_b.sum())
         if isinstance(w_update, str):
@@ -297,6 +299,21 @@ class Sampler:
         v = C.c_double()
         _check(lib().busseq_bic(self._h, C.byref(v)))
         return v.value
+
+    def corrected_counts(self, out=None) -> np.ndarray:
+        """Batch-corrected counts [N, G] (int32): the last sweep's imputed counts
+        mapped by randomised quantile matching onto NB(exp(alpha + beta_w), phi_1),
+        with the posterior means and the posterior-mode types.  ``out`` may be
+        a CUDA tensor (int32, N x G, contiguous) to keep the result on the
+        device."""
+        if out is not None and hasattr(out, "data_ptr"):
+            if tuple(out.shape) != (self.N, self.G) or not out.is_contiguous() or out.element_size() != 4:
+                raise ValueError("out must be a contiguous int32 tensor of shape (N, G)")
+            _check(lib().busseq_corrected_counts(self._h, C.c_void_p(out.data_ptr()), 1))
+            return out
+        res = np.empty((self.N, self.G), np.int32)
+        _check(lib().busseq_corrected_counts(self._h, res.ctypes.data_as(C.c_void_p), 0))
+        return res
 
     def write_outputs(self, prefix: str, print_preserved: bool = False):
         _check(lib().busseq_write_outputs(self._h, prefix.encode(), int(print_preserved)))

@@ -813,6 +813,28 @@ int busseq_bic(busseq_handle* h, double* bic) {
   return BUSSEQ_OK;
 }
 
+int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_device) {
+  if (!h || !out) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  TRY(ensure_estimates(h));
+  const bq::DevState& s = h->s;
+  if (s.N == 0 || s.G == 0) return BUSSEQ_OK;
+  int32_t* dst = out;
+  if (!out_is_device) CUDA_TRY(cudaMallocAsync((void**)&dst, (size_t)s.N * s.G * 4, h->stream));
+  const dim3 grid((unsigned)((s.G + 255) / 256), (unsigned)std::min<int64_t>(s.N, 65535));
+  bq::k_correct<<<grid, 256, 0, h->stream>>>(s, h->est, dst, s.G);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !out_is_device)
+    e = cudaMemcpyAsync(out, dst, (size_t)s.N * s.G * 4, cudaMemcpyDeviceToHost, h->stream);
+  if (!out_is_device) {
+    const cudaError_t e2 = cudaFreeAsync(dst, h->stream);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "k_correct: %s", cudaGetErrorString(e));
+  return BUSSEQ_OK;
+}
+
 int busseq_get_state(busseq_handle* h, busseq_state* o) {
   if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
   CUDA_TRY(cudaSetDevice(h->device));

@@ -7,6 +7,8 @@
 //   --w-update=mh|gibbs   W move (default mh, the reference's)
 //   --device=D            CUDA device ordinal
 //   --stats               print per-phase wall times to stderr
+//   --corrected           also write <prefix>_corrected_X.txt, the batch-corrected
+//                         counts (randomised quantile matching of _post_X)
 #include "busseq_gb300.h"
 
 #include <getopt.h>
@@ -45,7 +47,7 @@ int main(int argc, char** argv) {
   char output_file[4096] = "demo_output";
   char n_file[4096] = "";
   int n_file_flag = 0, burnin_flag = 1, unchanged_flag = 1, seed_flag = 1;
-  int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0;
+  int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0, corrected = 0;
   std::string ck_path, resume_path;
 
   static struct option longopts[] = {{"w-update", required_argument, nullptr, 1000},
@@ -55,6 +57,7 @@ int main(int argc, char** argv) {
                                      {"checkpoint-every", required_argument, nullptr, 1004},
                                      {"resume", required_argument, nullptr, 1005},
                                      {"stop-after", required_argument, nullptr, 1006},
+                                     {"corrected", no_argument, nullptr, 1007},
                                      {nullptr, 0, nullptr, 0}};
   int opt;
   while ((opt = getopt_long(argc, argv, "B:N:G:K:s:c:i:b:u:po:", longopts, nullptr)) != -1) {
@@ -81,6 +84,7 @@ int main(int argc, char** argv) {
       case 1004: ck_every = atoi(optarg); break;
       case 1005: resume_path = optarg; break;
       case 1006: stop_after = atoi(optarg); break;
+      case 1007: corrected = 1; break;
       default:
         printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
                "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
@@ -206,6 +210,7 @@ int main(int argc, char** argv) {
   if (print_preserved) printf("Start writing preserved iterations.\n");
   fflush(stdout);
   if (busseq_write_outputs(h, output_file, print_preserved) != BUSSEQ_OK) die_lib("writing outputs");
+  if (corrected && busseq_write_corrected(h, output_file) != BUSSEQ_OK) die_lib("writing corrected counts");
   double t4 = now_s();
   if (stats) {
     fprintf(stderr,

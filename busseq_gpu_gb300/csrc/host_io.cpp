@@ -254,4 +254,19 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   return BUSSEQ_OK;
 }
 
+int busseq_write_corrected(busseq_handle* h, const char* prefix) {
+  if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
+  int32_t B, K, nk, kd;
+  int64_t G, N;
+  int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
+  if (r) return r;
+  std::vector<int32_t> C((size_t)N * G);
+  if ((r = busseq_corrected_counts(h, C.data(), 0))) return r;
+  Table t;
+  t.rows = N;
+  t.cols = G;
+  t.cell = [&C, G](int64_t i, int64_t g, char* b) { return fmt_int(C[i * G + g], b); };
+  return write_table(std::string(prefix) + "_corrected_X.txt", t);
+}
+
 }  // extern "C"

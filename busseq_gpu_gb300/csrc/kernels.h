@@ -51,6 +51,7 @@ __global__ void k_init_raw(DevState s);
 __global__ void k_init_finish(DevState s, int fresh);
 __global__ void k_finalize(DevState s, Estimates e, int n_kept);
 __global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik);
+__global__ void k_correct(DevState s, Estimates e, int32_t* out, int64_t ld);
 __global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double* out);
 
 }  // namespace bq

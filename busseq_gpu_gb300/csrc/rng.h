@@ -55,6 +55,7 @@ enum StreamId : uint32_t {
   SID_PI = 14,           // b*K+k       : Dirichlet component (Gamma draw)
   SID_HMC_MOM = 15,      // coordinate d: momentum of the HMC block update
   SID_HMC_ACC = 16,      // 0           : HMC accept (u0), step-size jitter (u1)
+  SID_CORRECT = 17,      // entry i*G+g : randomised PIT of the batch-corrected count (two words)
   SID_INIT_W = 20,       // cell i      : initial cell type
   SID_INIT_L = 21,       // k*G+g       : initial indicator L
   SID_SIM = 30           // synthetic-data generator (not used by the sampler)
@@ -102,6 +103,13 @@ BQ_HD U32x4 philox4x32_10(U32x4 c, uint32_t k0, uint32_t k1) {
 // restatement sees the very same numbers.
 BQ_HD float u32_to_unit(uint32_t r) {
   return ((float)(r >> 9) + 0.5f) * 1.1920928955078125e-07f;
+}
+
+// Uniform on (0,1) with 53-bit resolution: (2m+1) 2^-53, m = the top 52 bits
+// of the 64-bit word (w0, w1).  Exact in double, and so is 1 - v.
+BQ_HD double u64_to_unit_d(uint32_t w0, uint32_t w1) {
+  const uint64_t m = ((((uint64_t)w0) << 32) | (uint64_t)w1) >> 12;
+  return (double)(2 * m + 1) * 1.1102230246251565404236316680908203125e-16;
 }
 
 // Counter layout: x = entity bits 0..31, y = entity bits 32..47 | stream<<16,

@@ -194,6 +194,16 @@ int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev, const doub
 
 /* ---- state access, single stages, diagnostics ----------------------------- */
 
+/* Batch-corrected counts [N*G] (cells x genes, the layout of Y): each imputed
+ * count of the last sweep (_post_X) mapped by randomised quantile matching
+ * from NB(exp(alpha_g + beta_gw + nu_bg + delta_i), phi_bg) to the batch-free
+ * NB(exp(alpha_g + beta_gw), phi_1g), with the posterior means and the
+ * posterior-mode type w = W_i.  Not in BUSseq_gpu.cu: the BUSseq method's
+ * corrected read counts, computed from the outputs that BUSseq_gpu.cu writes
+ * (:1557-1813).  The uniforms are keyed by the handle's seed, so a call is
+ * reproducible.  out is a host buffer, or device memory when out_is_device. */
+int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_device);
+
 int busseq_get_state(busseq_handle* h, busseq_state* out);
 /* Replaces the whole state; derived data (exp(delta), exp(alpha+beta+nu), the
  * cell order) is recomputed on the device. */
@@ -262,6 +272,10 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out);
 /* Writes the _post_*, _BIC and (print_preserved) _preserved_* files with the
  * reference's names and formats (BUSseq_gpu.cu:1610-2018). */
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved);
+
+/* Writes <prefix>_corrected_X.txt: the batch-corrected counts of
+ * busseq_corrected_counts as an N x G table in the format of _post_X. */
+int busseq_write_corrected(busseq_handle* h, const char* prefix);
 
 /* ---- synthetic data (the BUSseq generative model) ------------------------- */
 

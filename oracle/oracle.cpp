@@ -1089,6 +1089,114 @@ int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Batch-corrected counts.  Not in the reference: the BUSseq method's corrected
+// read counts, computed from what the reference writes (_post_X, the
+// posterior means, the posterior-mode W; BUSseq_gpu.cu:1557-1813).  Each
+// imputed count x of cell i (batch b, type w) and gene g is mapped by
+// randomised quantile matching from NB(mu, phi_bg), mu = exp(alpha_g + beta_gw
+// + nu_bg + delta_i), to NB(mu*, phi_1g), mu* = exp(alpha_g + beta_gw):
+//   u  = F(x - 1) + v P(x),  v from stream 17 (entity i*G+g, sweep 0): the two
+//        words w0, w1 give v = (2m + 1) 2^-53, m = the top 52 bits of w0:w1;
+//   x* = min {k : F*(k) >= u}.
+// Restated by direct summation: every pmf term comes from its own logarithm,
+//   log P(k) = lgamma(k + phi) - lgamma(phi) - lgamma(k + 1) + phi log p + k log q,
+// p = phi / (phi + mu), q = mu / (phi + mu), and each tail is summed on the side
+// of the mode where it is small (lower tails from 0, upper tails outwards), so
+// both are accurate to a few ulps per term.  margin[e] is the relative distance
+// of the entry's position from the nearer of the two tail values bracketing x*,
+// negated where the position lies below 1e-300 and is floored there (as the
+// kernel does).
+// ---------------------------------------------------------------------------
+namespace {
+struct NbTerms {
+  double phi, lp, lq, lgphi, mode;
+  NbTerms(double mu, double ph)
+      : phi(ph), lp(-log1p(mu / ph)), lq(-log1p(ph / mu)), lgphi(lgamma(ph)),
+        mode(ph > 1.0 ? floor((ph - 1.0) * mu / ph) : 0.0) {}
+  double lpmf(double k) const { return lgamma(k + phi) - lgphi - lgamma(k + 1.0) + phi * lp + k * lq; }
+  double pmf(double k) const { return exp(lpmf(k)); }
+  double lower(int64_t k) const {  // F(k)
+    double s = 0.0;
+    for (int64_t j = 0; j <= k; ++j) s += pmf((double)j);
+    return s;
+  }
+  double upper(int64_t k) const {  // S(k)
+    double s = 0.0;
+    for (int64_t j = k + 1;; ++j) {
+      const double p = pmf((double)j);
+      s += p;
+      if ((double)j > mode && (p <= 1e-18 * s || p == 0.0)) break;
+    }
+    return s;
+  }
+};
+}  // namespace
+
+void orc_corrected_counts(const orc_state* st, int32_t* out, double* margin) {
+  const int64_t G = st->G, N = st->N;
+  auto off = batch_offsets(st);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < N; ++i) {
+    const int b = batch_of(off, i);
+    const int w = st->W[i];
+    for (int64_t g = 0; g < G; ++g) {
+      const int64_t e = i * G + g;
+      const int64_t x = st->X[e];
+      const double ab = st->alpha[g] + st->beta[(int64_t)w * G + g];
+      const double mu = exp((ab + st->nu[b * G + g]) + st->delta[i]);
+      Stream s(st->seed, 17u, (uint64_t)e, 0u);
+      const uint32_t w0 = s.u32(), w1 = s.u32();
+      const uint64_t m = ((((uint64_t)w0) << 32) | (uint64_t)w1) >> 12;
+      const double v = (double)(2 * m + 1) * 1.1102230246251565404236316680908203125e-16;
+      // position of u: the smaller of F(x-1) + v P(x) and S(x) + (1 - v) P(x)
+      const NbTerms src(mu, st->phi[b * G + g]);
+      const double px = src.pmf((double)x);
+      double Fm, Sx;
+      if ((double)x <= src.mode) {
+        Fm = x > 0 ? src.lower(x - 1) : 0.0;
+        Sx = 1.0 - Fm - px;
+      } else {
+        Sx = src.upper(x);
+        Fm = 1.0 - Sx - px;
+      }
+      const double ulo = Fm + v * px;
+      const bool up = ulo > 0.5;
+      const double t_raw = up ? Sx + (1.0 - v) * px : ulo;
+      const bool saturated = !(t_raw >= 1e-300);
+      const double t = saturated ? 1e-300 : t_raw;
+      // quantile under NB(exp(alpha + beta_w), phi_1g)
+      const NbTerms dst(exp(ab), st->phi[g]);
+      int64_t k;
+      double mg;
+      if (!up) {
+        double F = 0.0, p = 0.0;
+        for (k = 0;; ++k) {
+          p = dst.pmf((double)k);
+          F += p;
+          if (F >= t) break;
+        }
+        mg = std::min(t - (F - p), F - t) / t;
+      } else {
+        // a point beyond the answer: past the mode with P(k) below 1e-22 t
+        const double lthr = log(t) - 50.0;
+        int64_t hi = (int64_t)dst.mode + 1, step = 1;
+        while (dst.lpmf((double)hi) > lthr) { hi += step; step *= 2; }
+        double S = dst.upper(hi);
+        k = hi;
+        for (;;) {  // S(k - 1) = S(k) + P(k)
+          const double p = dst.pmf((double)k);
+          if (k == 0 || S + p > t) { mg = k == 0 ? 1.0 : std::min(t - S, S + p - t) / t; break; }
+          S += p;
+          --k;
+        }
+      }
+      out[e] = (int32_t)k;
+      if (margin) margin[e] = saturated ? -mg : mg;
+    }
+  }
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

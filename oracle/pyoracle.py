@@ -77,6 +77,7 @@ def lib():
         L.orc_hmc_logpost.argtypes = [C.POINTER(OrcState)]
         L.orc_hmc_logpost.restype = C.c_double
         L.orc_hmc_grad.argtypes = [C.POINTER(OrcState)] + [_PD] * 10
+        L.orc_corrected_counts.argtypes = [C.POINTER(OrcState), _PI32, _PD]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -186,6 +187,26 @@ class State:
         ll = np.zeros((self.K, self.N))
         v = lib().orc_bic(C.byref(self.c()), _ptr(ll, _PD))
         return v, ll
+
+
+def corrected_counts(X, n_b, seed, est):
+    """Oracle of the batch-corrected counts from the imputed counts X [N, G] and
+    the estimates (alpha [G], beta [K, G], nu [B, G], delta [N], phi [B, G],
+    W [N]).  Returns (counts [N, G] int32, margin [N, G]): margin is the
+    relative distance of each entry's probability position from the nearer
+    bracketing tail value of the corrected distribution, negative where the
+    position underflowed and was floored at 1e-300."""
+    X = np.ascontiguousarray(X, dtype=np.int32)
+    beta = np.ascontiguousarray(est["beta"], dtype=np.float64)
+    st = State(X, n_b, beta.shape[0], seed)
+    st.W = np.ascontiguousarray(est["W"], dtype=np.int32)
+    for f in ("alpha", "nu", "delta", "phi"):
+        setattr(st, f, np.ascontiguousarray(est[f], dtype=np.float64))
+    st.beta = beta
+    out = np.zeros(X.shape, np.int32)
+    mg = np.zeros(X.shape)
+    lib().orc_corrected_counts(C.byref(st.c()), _ptr(out, _PI32), _ptr(mg, _PD))
+    return out, mg
 
 
 class Debug:
