@@ -1105,7 +1105,7 @@ int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double
 // of the mode where it is small (lower tails from 0, upper tails outwards), so
 // both are accurate to a few ulps per term.  margin[e] is the relative distance
 // of the entry's position from the nearer of the two tail values bracketing x*,
-// negated where the position lies below 1e-300 and is floored there (as the
+// negated where the position lies below 1e-280 and is floored there (as the
 // kernel does).
 // ---------------------------------------------------------------------------
 namespace {
@@ -1163,8 +1163,8 @@ void orc_corrected_counts(const orc_state* st, int32_t* out, double* margin) {
       const double ulo = Fm + v * px;
       const bool up = ulo > 0.5;
       const double t_raw = up ? Sx + (1.0 - v) * px : ulo;
-      const bool saturated = !(t_raw >= 1e-300);
-      const double t = saturated ? 1e-300 : t_raw;
+      const bool saturated = !(t_raw >= 1e-280);
+      const double t = saturated ? 1e-280 : t_raw;
       // quantile under NB(exp(alpha + beta_w), phi_1g)
       const NbTerms dst(exp(ab), st->phi[g]);
       int64_t k;

@@ -195,7 +195,7 @@ def corrected_counts(X, n_b, seed, est):
     W [N]).  Returns (counts [N, G] int32, margin [N, G]): margin is the
     relative distance of each entry's probability position from the nearer
     bracketing tail value of the corrected distribution, negative where the
-    position underflowed and was floored at 1e-300."""
+    position underflowed and was floored at 1e-280."""
     X = np.ascontiguousarray(X, dtype=np.int32)
     beta = np.ascontiguousarray(est["beta"], dtype=np.float64)
     st = State(X, n_b, beta.shape[0], seed)

@@ -7,7 +7,7 @@ pmf recurrences on the device; term-by-term summation in the oracle), from
 the same estimates and the same 53-bit uniforms.  The counts must agree
 exactly, except at a certified near-tie: the two differ by one and the
 oracle's probability position lies within TIE of the tail value between
-them (relative).  Positions below 1e-300 are floored there on both sides.
+them (relative).  Positions below 1e-280 are floored there on both sides.
 """
 import numpy as np
 import pytest
@@ -82,7 +82,7 @@ def _crafted(rng, n_b, G, K, effects):
     for r in range(0, N, 7):
         X[r] = np.minimum(mu[r] + 12 * sd[r] + 3, 2e6).astype(np.int64)
     for r in range(3, N, 11):
-        X[r] = 0
+        X[r, ::2] = 0  # (every cell keeps some counts: empty cells are refused)
     X = np.minimum(X, 2_000_000).astype(np.int32)
     st = {"alpha": alpha, "beta": beta, "nu": nu, "delta": delta, "phi": phi, "W": W, "X": X}
     return st
@@ -110,8 +110,44 @@ def test_wide_range_matches_oracle(effects):
     assert np.array_equal(est["X"], st["X"])
     if not effects:
         # no batch or cell effect: the map is the identity, including the tails
-        # whose probability positions stay above 1e-300
+        # whose probability positions stay above 1e-280
         assert np.array_equal(want[mg > 0], st["X"][mg > 0])
+    _compare(got, want, mg)
+
+
+def _scattered(rng, n_b, G, K):
+    """Means from 1e-2 to 1e5 with strong batch and cell effects, dispersions
+    0.05 .. 1000 (at least mean / 1000), counts scattered over both tails
+    (including positions below the 1e-280 floor)."""
+    B, N = len(n_b), sum(n_b)
+    alpha = rng.uniform(-5, 9, G)
+    beta = np.zeros((K, G))
+    beta[1:] = rng.normal(0, 1, (K - 1, G))
+    nu = np.zeros((B, G))
+    nu[1:] = rng.normal(0, 1.5, (B - 1, G))
+    off = np.concatenate([[0], np.cumsum(n_b)])[:-1]
+    delta = rng.normal(0, 0.8, N)
+    delta[off] = 0
+    W = rng.integers(0, K, N).astype(np.int32)
+    b_of = np.repeat(np.arange(B), n_b)
+    mu = np.exp(alpha[None] + beta[W] + nu[b_of] + delta[:, None])
+    phi = np.maximum(np.exp(rng.uniform(np.log(0.05), np.log(1000), (B, G))), mu.max(axis=0)[None] / 1000 + 1e-9)
+    X = np.round(mu * np.exp(rng.normal(0, 1.5, (N, G)))).astype(np.int64)
+    X[rng.random((N, G)) < 0.2] = 0
+    X[:, 0] = np.maximum(X[:, 0], 1)  # every cell keeps some counts
+    X = np.minimum(X, 3_000_000).astype(np.int32)
+    return {"alpha": alpha, "beta": beta, "nu": nu, "delta": delta, "phi": phi, "W": W, "X": X}
+
+
+def test_scattered_counts_match_oracle():
+    rng = np.random.default_rng(101)
+    n_b, G, K = [70, 60], 80, 4
+    st = _scattered(rng, n_b, G, K)
+    h = _sampler_with(st, n_b, K)
+    got = h.corrected_counts()
+    _, want, mg = _oracle(h, n_b)
+    h.close()
+    assert (mg < 0).sum() > 0  # the floor is exercised
     _compare(got, want, mg)
 
 

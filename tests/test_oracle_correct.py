@@ -62,7 +62,7 @@ def test_identity_without_batch_effects():
     n_b, G, K = [40, 30, 30], 50, 3
     est = _est(n_b, G, K, rng, effects=False)
     X = _draw(n_b, est, rng)
-    X[0, :4] = [0, 1, 150, 300]  # far tails too (positions down to ~1e-170; below 1e-300 they saturate)
+    X[0, :4] = [0, 1, 150, 300]  # far tails too (positions down to ~1e-170; below 1e-280 they saturate)
     out, mg = po.corrected_counts(X, n_b, SEED, est)
     assert np.array_equal(out, X)
     assert np.all(mg > 0)
