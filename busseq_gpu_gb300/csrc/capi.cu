@@ -821,8 +821,8 @@ int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_devic
   if (s.N == 0 || s.G == 0) return BUSSEQ_OK;
   int32_t* dst = out;
   if (!out_is_device) CUDA_TRY(cudaMallocAsync((void**)&dst, (size_t)s.N * s.G * 4, h->stream));
-  const dim3 grid((unsigned)((s.G + 255) / 256), (unsigned)std::min<int64_t>(s.N, 65535));
-  bq::k_correct<<<grid, 256, 0, h->stream>>>(s, h->est, dst, s.G);
+  const dim3 grid((unsigned)((s.G + 1023) / 1024), (unsigned)std::min<int64_t>(s.N, 65535));
+  bq::k_correct<<<grid, 256, 0, h->stream>>>(s, h->est, dst, s.G);  // 1024 genes of a row per CTA
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !out_is_device)
     e = cudaMemcpyAsync(out, dst, (size_t)s.N * s.G * 4, cudaMemcpyDeviceToHost, h->stream);

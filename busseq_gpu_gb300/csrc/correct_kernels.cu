@@ -25,23 +25,64 @@
 
 namespace bq {
 
-// One thread per (cell, gene): blockIdx.x over gene tiles, cells strided over
-// blockIdx.y.  out has row stride ld.
-__global__ void __launch_bounds__(256) k_correct(DevState s, Estimates e, int32_t* out, int64_t ld) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= s.G) return;
-  const double alpha = e.alpha[g];
-  const double phi1 = e.phi[g];
+namespace {
+
+constexpr int CORR_THREADS = 256;
+constexpr int CORR_CHUNK = 1024;  // genes of one row per CTA pass (4 per thread)
+
+struct CorrEntry {
+  double mu, phi, mu_t, phi_t, v;
+  int x;
+};
+
+__device__ __forceinline__ CorrEntry corr_entry(const DevState& s, const Estimates& e, int64_t i, int64_t g, int b,
+                                                int w) {
+  CorrEntry c;
+  c.x = s.X[i * s.Gp + g];
+  const double ab = e.alpha[g] + e.beta[(int64_t)w * s.G + g];
+  c.mu = exp((ab + e.nu[(int64_t)b * s.G + g]) + e.delta[i]);
+  c.mu_t = exp(ab);
+  c.phi = e.phi[(int64_t)b * s.G + g];
+  c.phi_t = e.phi[g];
+  Stream st(s.seed, SID_CORRECT, (uint64_t)(i * s.G + g), 0u);
+  const uint32_t w0 = st.next_u32();
+  const uint32_t w1 = st.next_u32();
+  c.v = u64_to_unit_d(w0, w1);
+  return c;
+}
+
+}  // namespace
+
+// Each CTA takes CORR_CHUNK genes of one row at a time (rows strided over
+// blockIdx.y).  Pass 1 finishes every entry that the forward sums settle
+// (most of them) and queues the rest in shared memory; pass 2 hands the queue
+// to consecutive threads, so the continued-fraction work runs in full warps
+// instead of stalling the warps of the cheap entries.  out has row stride ld.
+__global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates e, int32_t* out, int64_t ld) {
+  __shared__ int queue[CORR_CHUNK];
+  __shared__ int n_queue;
+  const int64_t g0 = (int64_t)blockIdx.x * CORR_CHUNK;
+  const int n_g = (int)(s.G - g0 < CORR_CHUNK ? s.G - g0 : CORR_CHUNK);
   for (int64_t i = blockIdx.y; i < s.N; i += gridDim.y) {
+    if (threadIdx.x == 0) n_queue = 0;
+    __syncthreads();
     const int b = s.batch_of[i];
     const int w = e.W[i];
-    const int x = s.X[i * s.Gp + g];
-    const double ab = alpha + e.beta[(int64_t)w * s.G + g];
-    const double mu = exp((ab + e.nu[(int64_t)b * s.G + g]) + e.delta[i]);
-    Stream st(s.seed, SID_CORRECT, (uint64_t)(i * s.G + g), 0u);
-    const uint32_t w0 = st.next_u32();
-    const uint32_t w1 = st.next_u32();
-    out[i * ld + g] = corr::corrected_count(mu, e.phi[(int64_t)b * s.G + g], exp(ab), phi1, x, u64_to_unit_d(w0, w1));
+    for (int j = threadIdx.x; j < n_g; j += CORR_THREADS) {
+      const int64_t g = g0 + j;
+      const CorrEntry c = corr_entry(s, e, i, g, b, w);
+      const int r = corr::corrected_count_t<true>(c.mu, c.phi, c.mu_t, c.phi_t, c.x, c.v);
+      if (r >= 0) out[i * ld + g] = r;
+      else queue[atomicAdd(&n_queue, 1)] = j;
+    }
+    __syncthreads();
+    const int nq = n_queue;
+    for (int q = threadIdx.x; q < nq; q += CORR_THREADS) {
+      const int64_t g = g0 + queue[q];
+      const CorrEntry c = corr_entry(s, e, i, g, b, w);
+      out[i * ld + g] = corr::corrected_count(c.mu, c.phi, c.mu_t, c.phi_t, c.x, c.v);
+    }
+    __syncthreads();
   }
 }
 

@@ -17,10 +17,10 @@
 //    error ~1e-11 there);
 //  * otherwise the tail at a point comes from the continued fraction of the
 //    regularised incomplete beta function, F(k) = I_p(phi, k + 1),
-//    S(k) = I_q(k + 1, phi) (relative error ~1e-12), and the quantile is
-//    bracketed with it (exponential steps from a guess, then bisection) and
-//    finished by the pmf recurrence in the direction in which the kept tail
-//    grows (F upwards, S downwards), so that no step subtracts.
+//    S(k) = I_q(k + 1, phi) (relative error ~1e-12); the quantile search
+//    evaluates it once at a standardised-score guess and walks from there by
+//    the pmf recurrence (target_walk), with bracketing and bisection as the
+//    fallback for a guess that is far off (target_bracket).
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -44,6 +44,8 @@ constexpr int CORR_KMAX = 1 << 30;         // largest corrected count
 constexpr double CORR_LOG_TINY = -700.0;   // log P(0) above which the recurrence from 0 starts
 constexpr double CORR_T_MIN = 1e-280;      // floor of a tail probability (well inside the normal range)
 constexpr double CORR_UPPER_MIN = 1.0 / 1024.0;  // smallest upper tail taken from a forward sum
+constexpr int CORR_WALK_MAX = 64;          // pmf steps per walk from one continued fraction
+constexpr int CORR_ROUNDS = 8;             // walks before falling back to bracketing
 
 struct InvTab {
   double v[CORR_SMALL + 1];
@@ -100,31 +102,36 @@ struct Tail {
 //   I_x(a, b) = x^a (1 - x)^b / (a B(a, b)) / K,  K = 1 + d1 / (1 + d2 / (1 + ...)),
 //   d_{2m+1} = -(a + m)(a + b + m) x / ((a + 2m)(a + 2m + 1)),
 //   d_{2m}   = m (b - m) x / ((a + 2m - 1)(a + 2m)),
-// converging fast for x < (a + 1) / (a + b + 2).  K is evaluated forwards by
-// the modified Lentz method (Thompson and Barnett, J. Comput. Phys. 64, 1986).
+// converging fast for x < (a + 1) / (a + b + 2).  K is the limit of the
+// convergents A_j / B_j of the fundamental recurrences
+//   A_j = A_{j-1} + d_j A_{j-2},  B_j = B_{j-1} + d_j B_{j-2}
+//   (A_{-1} = 1, A_0 = 1, B_{-1} = 0, B_0 = 1),
+// carried scaled by the product of the denominators m_1 .. m_j of the
+// d_j = n_j / m_j, which turns each step into multiplications only:
+//   A'_j = m_j A'_{j-1} + n_j m_{j-1} A'_{j-2}  (likewise B').
+// After each pair of terms the four values are divided by B'_j (one division
+// per pair), which leaves B'_j = 1 and A'_j = the current convergent.
 CQ_HD double inc_beta_cf(double a, double b, double x) {
-  const double TINY = 1e-300, EPS = 1e-15;
-  double f = 1.0, C = 1.0, D = 0.0;
+  const double EPS = 1e-15;
+  double Am = 1.0, A = 1.0, Bm = 0.0, B = 1.0, mprev = 1.0, f = 1.0;
   for (int m = 0; m < CORR_CF_MAX; ++m) {
     const double a2m = a + 2.0 * m;
-    double d = -(a + m) * (a + b + m) * x / (a2m * (a2m + 1.0));
-    D = 1.0 + d * D;
-    if (fabs(D) < TINY) D = TINY;
-    C = 1.0 + d / C;
-    if (fabs(C) < TINY) C = TINY;
-    D = 1.0 / D;
-    const double del1 = C * D;
-    f *= del1;
-    const double m1 = m + 1.0;
-    d = m1 * (b - m1) * x / ((a2m + 1.0) * (a2m + 2.0));
-    D = 1.0 + d * D;
-    if (fabs(D) < TINY) D = TINY;
-    C = 1.0 + d / C;
-    if (fabs(C) < TINY) C = TINY;
-    D = 1.0 / D;
-    const double del2 = C * D;
-    f *= del2;
-    if (fabs(del1 - 1.0) < EPS && fabs(del2 - 1.0) < EPS) break;
+    const double n1 = -(a + m) * (a + b + m) * x, m1 = a2m * (a2m + 1.0);
+    double An = m1 * A + (n1 * mprev) * Am, Bn = m1 * B + (n1 * mprev) * Bm;
+    Am = A; A = An; Bm = B; B = Bn;
+    const double mm = m + 1.0;
+    const double n2 = mm * (b - mm) * x, m2 = (a2m + 1.0) * (a2m + 2.0);
+    An = m2 * A + (n2 * m1) * Am;
+    Bn = m2 * B + (n2 * m1) * Bm;
+    Am = A; A = An; Bm = B; B = Bn;
+    mprev = m2;
+    const double den = fabs(B) > 1e-250 ? B : (B < 0.0 ? -1e-250 : 1e-250);
+    const double r = 1.0 / den;
+    A *= r; Am *= r; Bm *= r; B *= r;
+    const double fn = A;
+    const bool done = fabs(fn - f) <= EPS * fabs(fn);
+    f = fn;
+    if (done) break;
   }
   return f;
 }
@@ -144,21 +151,24 @@ CQ_HD Tail nb_tail(NbDist& d, int k) {
   return r;
 }
 
-// Position of the randomised PIT of x under d.
-CQ_HD void source_position(NbDist& d, int x, double v, bool& upper, double& t) {
-  if (x <= CORR_SMALL && d.log_p0() > CORR_LOG_TINY) {
-    double pm = exp(d.log_p0()), F = 0.0;
-    for (int j = 0; j < x; ++j) {
-      F += pm;
-      pm *= (j + d.phi) * d.q * inv_int1(j);
-    }
-    const double u = F + v * pm;
-    if (u <= 1.0 - CORR_UPPER_MIN) {
-      upper = u > 0.5;
-      t = fmax(upper ? 1.0 - u : u, CORR_T_MIN);
-      return;
-    }
+// Position of the randomised PIT of x under d from the forward sum; false if
+// x is out of its range or the position lies in the far upper tail.
+CQ_HDI bool source_small(const NbDist& d, int x, double v, bool& upper, double& t) {
+  if (x > CORR_SMALL || !(d.log_p0() > CORR_LOG_TINY)) return false;
+  double pm = exp(d.log_p0()), F = 0.0;
+  for (int j = 0; j < x; ++j) {
+    F += pm;
+    pm *= (j + d.phi) * d.q * inv_int1(j);
   }
+  const double u = F + v * pm;
+  if (!(u <= 1.0 - CORR_UPPER_MIN)) return false;
+  upper = u > 0.5;
+  t = fmax(upper ? 1.0 - u : u, CORR_T_MIN);
+  return true;
+}
+
+// Position of the randomised PIT of x under d from the continued fraction at x.
+CQ_HD void source_cf(NbDist& d, int x, double v, bool& upper, double& t) {
   const Tail T = nb_tail(d, x);
   const double w = 1.0 - v;  // exact
   if (!T.upper) {
@@ -173,20 +183,26 @@ CQ_HD void source_position(NbDist& d, int x, double v, bool& upper, double& t) {
   t = fmax(t, CORR_T_MIN);
 }
 
-// min {k : F(k) >= u} for the position (upper, t) of u, starting from guess k0.
-CQ_HD int target_quantile(NbDist& d, bool upper, double t, int k0) {
-  if (k0 < CORR_GUESS_SMALL && d.log_p0() > CORR_LOG_TINY && (!upper || t >= CORR_UPPER_MIN)) {
-    const double u = upper ? 1.0 - t : t;
-    double pm = exp(d.log_p0()), F = pm;
-    int j = 0;
-    while (F < u && j < CORR_SMALL) {
-      pm *= (j + d.phi) * d.q * inv_int1(j);
-      ++j;
-      F += pm;
-    }
-    if (F >= u) return j;
-    k0 = CORR_SMALL;
+// min {k : F(k) >= u} by the forward sum from 0, for small guesses; false if
+// out of its range (the answer is then above CORR_SMALL or needs the tails).
+CQ_HDI bool target_small(const NbDist& d, bool upper, double t, int k0, int& out) {
+  if (k0 >= CORR_GUESS_SMALL || !(d.log_p0() > CORR_LOG_TINY) || (upper && t < CORR_UPPER_MIN)) return false;
+  const double u = upper ? 1.0 - t : t;
+  double pm = exp(d.log_p0()), F = pm;
+  int j = 0;
+  while (F < u && j < CORR_SMALL) {
+    pm *= (j + d.phi) * d.q * inv_int1(j);
+    ++j;
+    F += pm;
   }
+  out = j;
+  return F >= u;
+}
+
+// min {k : F(k) >= u} for the position (upper, t) of u: bracket from k0 by
+// exponential steps, bisect with the continued fraction, finish by the pmf
+// recurrence in the direction in which the kept tail grows.
+CQ_HD int target_bracket(NbDist& d, bool upper, double t, int k0) {
   // the answer is the least k with pred(k): F(k) >= t (lower) or S(k) <= t (upper)
   auto pred = [&](const Tail& T) { return upper ? T.S() <= t : T.F() >= t; };
   int lo, hi;  // pred(lo) false (lo = -1: F = 0), pred(hi) true
@@ -206,7 +222,7 @@ CQ_HD int target_quantile(NbDist& d, bool upper, double t, int k0) {
       if (!pred(Tlo)) break;
       hi = lo;
       Thi = Tlo;
-      step *= 2;
+      step = step < CORR_KMAX / 4 ? step * 2 : step;
     }
   } else {
     lo = k0;
@@ -261,20 +277,93 @@ CQ_HD int target_quantile(NbDist& d, bool upper, double t, int k0) {
   return lo + 1;
 }
 
-// The corrected count of x ~ NB(mu, phi) onto NB(mu_t, phi_t) for the uniform v.
-CQ_HD int corrected_count(double mu, double phi, double mu_t, double phi_t, int x, double v) {
+// min {k : F(k) >= u}: one continued fraction at the guess k0, then pmf walks
+// towards the answer.  A walk in which the kept tail shrinks (F downwards, S
+// upwards) subtracts, so it stops once that tail has fallen below 1/1024 of
+// the value it started from (relative error then below ~1e-12) and restarts
+// from a new continued fraction; a guess that is far off ends in bracketing.
+CQ_HD int target_walk(NbDist& d, bool upper, double t, int k0) {
+  int k = k0;
+  for (int round = 0; round < CORR_ROUNDS; ++round) {
+    const Tail T = nb_tail(d, k);
+    double pm = T.pmf;
+    if (!upper) {
+      double F = T.F();
+      if (F >= t) {
+        const double floor = F * (1.0 / 1024.0);
+        for (int n = 0; n < CORR_WALK_MAX; ++n) {  // F(k - 1) = F(k) - P(k)
+          if (k == 0) return 0;
+          const double Fm = F - pm;
+          if (Fm < t) return k;
+          pm *= (double)k / ((k - 1 + d.phi) * d.q);
+          F = Fm;
+          --k;
+          if (F < floor) break;
+        }
+      } else {
+        for (int n = 0; n < CORR_WALK_MAX; ++n) {  // F(k + 1) = F(k) + P(k + 1)
+          if (k >= CORR_KMAX) return CORR_KMAX;
+          pm *= (k + d.phi) * d.q / (double)(k + 1);
+          F += pm;
+          ++k;
+          if (F >= t) return k;
+        }
+      }
+    } else {
+      double S = T.S();
+      if (S <= t) {
+        for (int n = 0; n < CORR_WALK_MAX; ++n) {  // S(k - 1) = S(k) + P(k)
+          if (k == 0) return 0;
+          S += pm;
+          if (S > t) return k;
+          pm *= (double)k / ((k - 1 + d.phi) * d.q);
+          --k;
+        }
+      } else {
+        const double floor = S * (1.0 / 1024.0);
+        for (int n = 0; n < CORR_WALK_MAX; ++n) {  // S(k + 1) = S(k) - P(k + 1)
+          if (k >= CORR_KMAX) return CORR_KMAX;
+          pm *= (k + d.phi) * d.q / (double)(k + 1);
+          S -= pm;
+          ++k;
+          if (S <= t) return k;
+          if (S < floor) break;
+        }
+      }
+    }
+  }
+  return target_bracket(d, upper, t, k);
+}
+
+// The corrected count of x ~ NB(mu, phi) onto NB(mu_t, phi_t) for the uniform
+// v.  FAST_ONLY: return -1 instead of evaluating any continued fraction (the
+// caller then repeats the call with FAST_ONLY false); a result it does return
+// is the one the full call gives.
+template <bool FAST_ONLY>
+CQ_HD int corrected_count_t(double mu, double phi, double mu_t, double phi_t, int x, double v) {
   NbDist src;
   src.set(mu, phi);
   bool upper;
   double t;
-  source_position(src, x, v, upper, t);
+  if (!source_small(src, x, v, upper, t)) {
+    if (FAST_ONLY) return -1;
+    source_cf(src, x, v, upper, t);
+  }
   NbDist dst;
   dst.set(mu_t, phi_t);
   // standardised-score guess: mu_t + sd_t (x + 1/2 - mu) / sd
   const double sd = sqrt(mu + mu * mu / phi), sdt = sqrt(mu_t + mu_t * mu_t / phi_t);
   const double guess = mu_t + sdt * (((double)x + 0.5 - mu) / sd);
-  const int k0 = !(guess > 0.0) ? 0 : (guess >= (double)CORR_KMAX ? CORR_KMAX : (int)guess);
-  return target_quantile(dst, upper, t, k0);
+  int k0 = !(guess > 0.0) ? 0 : (guess >= (double)CORR_KMAX ? CORR_KMAX : (int)guess);
+  int r;
+  if (target_small(dst, upper, t, k0, r)) return r;
+  if (FAST_ONLY) return -1;
+  if (k0 < CORR_GUESS_SMALL && dst.log_p0() > CORR_LOG_TINY && (!upper || t >= CORR_UPPER_MIN)) k0 = CORR_SMALL;
+  return target_walk(dst, upper, t, k0);
+}
+
+CQ_HD int corrected_count(double mu, double phi, double mu_t, double phi_t, int x, double v) {
+  return corrected_count_t<false>(mu, phi, mu_t, phi_t, x, v);
 }
 
 }  // namespace corr
