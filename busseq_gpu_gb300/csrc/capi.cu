@@ -2,6 +2,7 @@
 // sweeps, stages, summaries.  See include/busseq_gb300.h for the contract.
 #include "busseq_gb300.h"
 #include "busseq_dev.h"
+#include "correct_math.h"
 #include "kernels.h"
 
 #include <cuda_runtime.h>
@@ -819,17 +820,26 @@ int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_devic
   TRY(ensure_estimates(h));
   const bq::DevState& s = h->s;
   if (s.N == 0 || s.G == 0) return BUSSEQ_OK;
-  int32_t* dst = out;
-  if (!out_is_device) CUDA_TRY(cudaMallocAsync((void**)&dst, (size_t)s.N * s.G * 4, h->stream));
-  const dim3 grid((unsigned)((s.G + 1023) / 1024), (unsigned)std::min<int64_t>(s.N, 65535));
-  bq::k_correct<<<grid, 256, 0, h->stream>>>(s, h->est, dst, s.G);  // 1024 genes of a row per CTA
+  const size_t n_tab = (size_t)s.K * s.G, out_bytes = out_is_device ? 0 : (size_t)s.N * s.G * 4;
+  const size_t off_sd = n_tab * sizeof(bq::corr::NbDist), off_nu = off_sd + n_tab * 8,
+               off_out = off_nu + (size_t)s.B * s.G * 8, bytes = off_out + out_bytes;
+  char* scratch = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&scratch, bytes, h->stream));
+  bq::CorrTables tb{reinterpret_cast<bq::corr::NbDist*>(scratch), reinterpret_cast<double*>(scratch + off_sd),
+                    reinterpret_cast<double*>(scratch + off_nu)};
+  int32_t* dst = out_is_device ? out : reinterpret_cast<int32_t*>(scratch + off_out);
+  bq::k_correct_prep<<<std::min<unsigned>(blocks_for((int64_t)n_tab, 256), 152 * 8), 256, 0, h->stream>>>(
+      s, h->est, tb);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && !out_is_device)
-    e = cudaMemcpyAsync(out, dst, (size_t)s.N * s.G * 4, cudaMemcpyDeviceToHost, h->stream);
-  if (!out_is_device) {
-    const cudaError_t e2 = cudaFreeAsync(dst, h->stream);
-    if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) {
+    const dim3 grid((unsigned)((s.G + 1023) / 1024), (unsigned)std::min<int64_t>(s.N, 65535));
+    bq::k_correct<<<grid, 256, 0, h->stream>>>(s, h->est, tb, dst, s.G);  // 1024 genes of a row per CTA
+    e = cudaGetLastError();
   }
+  if (e == cudaSuccess && !out_is_device)
+    e = cudaMemcpyAsync(out, dst, out_bytes, cudaMemcpyDeviceToHost, h->stream);
+  const cudaError_t e2 = cudaFreeAsync(scratch, h->stream);
+  if (e == cudaSuccess) e = e2;
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "k_correct: %s", cudaGetErrorString(e));
   return BUSSEQ_OK;

@@ -17,7 +17,9 @@
 // That removes the batch (nu_bg, phi_bg) and cell-size (delta_i) effects and
 // keeps the cell type's.
 //
-// The arithmetic (FP64, two regimes) is in correct_math.h.
+// The arithmetic (FP64, two regimes) is in correct_math.h.  The source mean is
+// formed as exp(alpha_g + beta_gw) exp(nu_bg) exp(delta_i) from per-call
+// tables (a few ulps from exp of the sum).
 #include "busseq_dev.h"
 #include "correct_math.h"
 #include "kernels.h"
@@ -30,35 +32,47 @@ namespace {
 constexpr int CORR_THREADS = 256;
 constexpr int CORR_CHUNK = 1024;  // genes of one row per CTA pass (4 per thread)
 
-struct CorrEntry {
-  double mu, phi, mu_t, phi_t, v;
-  int x;
-};
+// Source distribution of entry (i, g): mu = mu_t * exp(nu_bg) * exp(delta_i).
+__device__ __forceinline__ void corr_source(const CorrTables& tb, const Estimates& e, int64_t G, int64_t g, int b,
+                                            double mu_t, double dexp, corr::NbDist& src, double& sd) {
+  const double mu = mu_t * tb.nu_exp[(int64_t)b * G + g] * dexp;
+  const double ph = e.phi[(int64_t)b * G + g];
+  src.set(mu, ph);
+  sd = corr::nb_sd(mu, ph);
+}
 
-__device__ __forceinline__ CorrEntry corr_entry(const DevState& s, const Estimates& e, int64_t i, int64_t g, int b,
-                                                int w) {
-  CorrEntry c;
-  c.x = s.X[i * s.Gp + g];
-  const double ab = e.alpha[g] + e.beta[(int64_t)w * s.G + g];
-  c.mu = exp((ab + e.nu[(int64_t)b * s.G + g]) + e.delta[i]);
-  c.mu_t = exp(ab);
-  c.phi = e.phi[(int64_t)b * s.G + g];
-  c.phi_t = e.phi[g];
+__device__ __forceinline__ double corr_uniform(const DevState& s, int64_t i, int64_t g) {
   Stream st(s.seed, SID_CORRECT, (uint64_t)(i * s.G + g), 0u);
   const uint32_t w0 = st.next_u32();
   const uint32_t w1 = st.next_u32();
-  c.v = u64_to_unit_d(w0, w1);
-  return c;
+  return u64_to_unit_d(w0, w1);
 }
 
 }  // namespace
+
+// Per-call tables: the target distribution NB(exp(alpha_g + beta_gk), phi_1g)
+// of every (type, gene) with its standard deviation, and exp(nu_bg).
+__global__ void k_correct_prep(DevState s, Estimates e, CorrTables tb) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)s.K * s.G; t += stride) {
+    const int64_t g = t % s.G;
+    const double mu_t = exp(e.alpha[g] + e.beta[t]);
+    corr::NbDist d;
+    d.set(mu_t, e.phi[g]);
+    tb.target[t] = d;
+    tb.target_sd[t] = corr::nb_sd(mu_t, e.phi[g]);
+  }
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)s.B * s.G; t += stride)
+    tb.nu_exp[t] = exp(e.nu[t]);
+}
 
 // Each CTA takes CORR_CHUNK genes of one row at a time (rows strided over
 // blockIdx.y).  Pass 1 finishes every entry that the forward sums settle
 // (most of them) and queues the rest in shared memory; pass 2 hands the queue
 // to consecutive threads, so the continued-fraction work runs in full warps
 // instead of stalling the warps of the cheap entries.  out has row stride ld.
-__global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates e, int32_t* out, int64_t ld) {
+__global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates e, CorrTables tb, int32_t* out,
+                                                          int64_t ld) {
   __shared__ int queue[CORR_CHUNK];
   __shared__ int n_queue;
   const int64_t g0 = (int64_t)blockIdx.x * CORR_CHUNK;
@@ -67,11 +81,16 @@ __global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates 
     if (threadIdx.x == 0) n_queue = 0;
     __syncthreads();
     const int b = s.batch_of[i];
-    const int w = e.W[i];
+    const int64_t w = e.W[i];
+    const double dexp = exp(e.delta[i]);
     for (int j = threadIdx.x; j < n_g; j += CORR_THREADS) {
       const int64_t g = g0 + j;
-      const CorrEntry c = corr_entry(s, e, i, g, b, w);
-      const int r = corr::corrected_count_t<true>(c.mu, c.phi, c.mu_t, c.phi_t, c.x, c.v);
+      corr::NbDist dst = tb.target[w * s.G + g];
+      corr::NbDist src;
+      double sd;
+      corr_source(tb, e, s.G, g, b, dst.mu, dexp, src, sd);
+      const int r = corr::corrected_count_t<true>(src, dst, sd, tb.target_sd[w * s.G + g], s.X[i * s.Gp + g],
+                                                  corr_uniform(s, i, g));
       if (r >= 0) out[i * ld + g] = r;
       else queue[atomicAdd(&n_queue, 1)] = j;
     }
@@ -79,8 +98,12 @@ __global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates 
     const int nq = n_queue;
     for (int q = threadIdx.x; q < nq; q += CORR_THREADS) {
       const int64_t g = g0 + queue[q];
-      const CorrEntry c = corr_entry(s, e, i, g, b, w);
-      out[i * ld + g] = corr::corrected_count(c.mu, c.phi, c.mu_t, c.phi_t, c.x, c.v);
+      corr::NbDist dst = tb.target[w * s.G + g];
+      corr::NbDist src;
+      double sd;
+      corr_source(tb, e, s.G, g, b, dst.mu, dexp, src, sd);
+      out[i * ld + g] = corr::corrected_count_t<false>(src, dst, sd, tb.target_sd[w * s.G + g], s.X[i * s.Gp + g],
+                                                       corr_uniform(s, i, g));
     }
     __syncthreads();
   }

@@ -26,7 +26,7 @@
 #include <stdint.h>
 
 #if defined(__CUDACC__)
-#define CQ_HD __host__ __device__
+#define CQ_HD __host__ __device__ inline
 #define CQ_HDI __host__ __device__ __forceinline__
 #else
 #define CQ_HD inline
@@ -56,7 +56,7 @@ constexpr InvTab make_inv_tab() {
   return t;
 }
 #if defined(__CUDACC__)
-__constant__ InvTab c_inv_dev = make_inv_tab();  // 1 / (j + 1)
+static __constant__ InvTab c_inv_dev = make_inv_tab();  // 1 / (j + 1)
 #endif
 constexpr InvTab c_inv_host = make_inv_tab();
 
@@ -69,25 +69,30 @@ CQ_HDI double inv_int1(int j) {  // 1 / (j + 1), 0 <= j <= CORR_SMALL
 }
 
 struct NbDist {
-  double phi, p, q, lp, lq, lg_phi;
-  bool have_lg;
-  CQ_HDI void set(double mu, double ph) {
+  double mu, phi, q, lp, p0;  // p0 = P(0) = p^phi
+  double p, lq, lg_phi;       // continued-fraction regime only (cf_prepare)
+  bool cf_ready;
+  CQ_HDI void set(double m, double ph) {
+    mu = m;
     phi = ph;
-    p = ph / (ph + mu);
-    q = mu / (ph + mu);
-    lp = -log1p(mu / ph);
-    lq = -log1p(ph / mu);
-    have_lg = false;
+    q = m / (ph + m);
+    lp = -log1p(m / ph);
+    p0 = exp(ph * lp);
+    cf_ready = false;
   }
   CQ_HDI double log_p0() const { return phi * lp; }
-  CQ_HDI double lgamma_phi() {  // only the continued-fraction regime needs it
-    if (!have_lg) {
+  CQ_HDI void cf_prepare() {
+    if (!cf_ready) {
+      p = phi / (phi + mu);
+      lq = -log1p(phi / mu);
       lg_phi = lgamma(phi);
-      have_lg = true;
+      cf_ready = true;
     }
-    return lg_phi;
   }
 };
+
+// Standard deviation of NB(mu, phi): the scale of the quantile guess.
+CQ_HDI double nb_sd(double mu, double phi) { return sqrt(mu + mu * mu / phi); }
 
 struct Tail {
   double t;    // F(k) (upper false) or S(k) (upper true)
@@ -140,8 +145,9 @@ CQ_HD double inc_beta_cf(double a, double b, double x) {
 // c = p^phi q^(k+1) / B(phi, k + 1) is the common prefactor: F(k) = c / (phi K),
 // S(k) = c / ((k + 1) K'), and P(k) = c / (q (phi + k)).
 CQ_HD Tail nb_tail(NbDist& d, int k) {
+  d.cf_prepare();
   const double kk = (double)k;
-  const double lbeta = d.lgamma_phi() + lgamma(kk + 1.0) - lgamma(d.phi + kk + 1.0);
+  const double lbeta = d.lg_phi + lgamma(kk + 1.0) - lgamma(d.phi + kk + 1.0);
   const double c = exp(d.phi * d.lp + (kk + 1.0) * d.lq - lbeta);
   Tail r;
   r.pmf = c / (d.q * (d.phi + kk));
@@ -155,7 +161,7 @@ CQ_HD Tail nb_tail(NbDist& d, int k) {
 // x is out of its range or the position lies in the far upper tail.
 CQ_HDI bool source_small(const NbDist& d, int x, double v, bool& upper, double& t) {
   if (x > CORR_SMALL || !(d.log_p0() > CORR_LOG_TINY)) return false;
-  double pm = exp(d.log_p0()), F = 0.0;
+  double pm = d.p0, F = 0.0;
   for (int j = 0; j < x; ++j) {
     F += pm;
     pm *= (j + d.phi) * d.q * inv_int1(j);
@@ -188,7 +194,7 @@ CQ_HD void source_cf(NbDist& d, int x, double v, bool& upper, double& t) {
 CQ_HDI bool target_small(const NbDist& d, bool upper, double t, int k0, int& out) {
   if (k0 >= CORR_GUESS_SMALL || !(d.log_p0() > CORR_LOG_TINY) || (upper && t < CORR_UPPER_MIN)) return false;
   const double u = upper ? 1.0 - t : t;
-  double pm = exp(d.log_p0()), F = pm;
+  double pm = d.p0, F = pm;
   int j = 0;
   while (F < u && j < CORR_SMALL) {
     pm *= (j + d.phi) * d.q * inv_int1(j);
@@ -253,7 +259,7 @@ CQ_HD int target_bracket(NbDist& d, bool upper, double t, int k0) {
     int j;
     if (lo < 0) {
       j = 0;
-      pm = exp(d.log_p0());
+      pm = d.p0;
       F = pm;
     } else {
       j = lo + 1;
@@ -335,25 +341,20 @@ CQ_HD int target_walk(NbDist& d, bool upper, double t, int k0) {
   return target_bracket(d, upper, t, k);
 }
 
-// The corrected count of x ~ NB(mu, phi) onto NB(mu_t, phi_t) for the uniform
-// v.  FAST_ONLY: return -1 instead of evaluating any continued fraction (the
-// caller then repeats the call with FAST_ONLY false); a result it does return
-// is the one the full call gives.
+// The corrected count of x under src onto dst for the uniform v; sd and sd_t
+// are the two standard deviations.  FAST_ONLY: return -1 instead of
+// evaluating any continued fraction (the caller then repeats the call with
+// FAST_ONLY false); a result it does return is the one the full call gives.
 template <bool FAST_ONLY>
-CQ_HD int corrected_count_t(double mu, double phi, double mu_t, double phi_t, int x, double v) {
-  NbDist src;
-  src.set(mu, phi);
+CQ_HD int corrected_count_t(NbDist& src, NbDist& dst, double sd, double sd_t, int x, double v) {
   bool upper;
   double t;
   if (!source_small(src, x, v, upper, t)) {
     if (FAST_ONLY) return -1;
     source_cf(src, x, v, upper, t);
   }
-  NbDist dst;
-  dst.set(mu_t, phi_t);
   // standardised-score guess: mu_t + sd_t (x + 1/2 - mu) / sd
-  const double sd = sqrt(mu + mu * mu / phi), sdt = sqrt(mu_t + mu_t * mu_t / phi_t);
-  const double guess = mu_t + sdt * (((double)x + 0.5 - mu) / sd);
+  const double guess = dst.mu + sd_t * (((double)x + 0.5 - src.mu) / sd);
   int k0 = !(guess > 0.0) ? 0 : (guess >= (double)CORR_KMAX ? CORR_KMAX : (int)guess);
   int r;
   if (target_small(dst, upper, t, k0, r)) return r;
@@ -362,8 +363,12 @@ CQ_HD int corrected_count_t(double mu, double phi, double mu_t, double phi_t, in
   return target_walk(dst, upper, t, k0);
 }
 
+// The corrected count of x ~ NB(mu, phi) onto NB(mu_t, phi_t) for the uniform v.
 CQ_HD int corrected_count(double mu, double phi, double mu_t, double phi_t, int x, double v) {
-  return corrected_count_t<false>(mu, phi, mu_t, phi_t, x, v);
+  NbDist src, dst;
+  src.set(mu, phi);
+  dst.set(mu_t, phi_t);
+  return corrected_count_t<false>(src, dst, nb_sd(mu, phi), nb_sd(mu_t, phi_t), x, v);
 }
 
 }  // namespace corr

@@ -5,6 +5,18 @@
 
 namespace bq {
 
+namespace corr {
+struct NbDist;
+}
+
+// Per-call tables of the batch-corrected counts (k_correct_prep).
+struct CorrTables {
+  corr::NbDist* target;  // [K][G] NB(exp(alpha_g + beta_gk), phi_1g)
+  double* target_sd;     // [K][G]
+  double* nu_exp;        // [B][G] exp(nu_bg)
+};
+
+
 __global__ void k_propose(DevState s, int mask);
 __global__ void k_zx(DevState s);
 __global__ void k_alpha(DevState s);
@@ -51,7 +63,8 @@ __global__ void k_init_raw(DevState s);
 __global__ void k_init_finish(DevState s, int fresh);
 __global__ void k_finalize(DevState s, Estimates e, int n_kept);
 __global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik);
-__global__ void k_correct(DevState s, Estimates e, int32_t* out, int64_t ld);
+__global__ void k_correct_prep(DevState s, Estimates e, CorrTables tb);
+__global__ void k_correct(DevState s, Estimates e, CorrTables tb, int32_t* out, int64_t ld);
 __global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double* out);
 
 }  // namespace bq
