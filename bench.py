@@ -187,6 +187,25 @@ def run_reference(args, rank):
     return 0
 
 
+def corrected_cpu_rate(s, n_b, seed, cells_per_batch: int = 40):
+    """The FP64 oracle of the batch-corrected counts on the first cells of each
+    batch of a finished run: entries per second on the host cores."""
+    from oracle import pyoracle as po
+    est = s.estimates(with_XZ=True)
+    off = np.concatenate([[0], np.cumsum(n_b)])
+    rows = np.concatenate([np.arange(off[b], off[b] + min(cells_per_batch, n_b[b])) for b in range(len(n_b))])
+    sub = {k: est[k] for k in ("alpha", "beta", "nu", "phi")}
+    sub["delta"], sub["W"] = est["delta"][rows], est["W"][rows]
+    nb_s = [min(cells_per_batch, x) for x in n_b]
+    t0 = time.perf_counter()
+    po.corrected_counts(est["X"][rows], nb_s, seed, sub)
+    secs = time.perf_counter() - t0
+    n = rows.size * est["X"].shape[1]
+    return {"entries_per_s": n / secs, "cores": po.num_threads(), "kind": "port",
+            "sample": "FP64 oracle over the first %d cells of each batch (%d entries, %.1f s)"
+                      % (cells_per_batch, n, secs)}
+
+
 def _config(name="config1", n_b=None, cfg=None):
     cfg = cfg if cfg is not None else WORKLOADS[name]
     n_b = list(n_b if n_b is not None else cfg["n_b"])
@@ -336,6 +355,24 @@ def main():
     achieved = alg_bytes / (ms_launch / 1000.0) / 1e9
     peak, peak_kind = _peak_hbm()
     traffic = _traffic(dom, args.workload) if args.cells <= 0 else None
+
+    # ---- batch-corrected counts of the finished run (rank 0, device output) --
+    corrected = None
+    if rank == 0:
+        cc = torch.empty((N, G), dtype=torch.int32, device=f"cuda:{local}")
+        s.corrected_counts(out=cc)  # warm-up call
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        s.corrected_counts(out=cc)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        cms = c0.elapsed_time(c1)
+        corrected = {"ms": cms, "entries_per_s": N * G / (cms / 1000.0), "dtype": "f64",
+                     "note": "one call: tables, k_correct over N x G entries, device output"}
+        if world == 1 and not args.no_cpu_baseline:
+            corrected["cpu_baseline"] = corrected_cpu_rate(s, n_b, seed + 7919 * rank)
+        del cc
     s.close()
     del Yd
     torch.cuda.empty_cache()
@@ -392,6 +429,7 @@ def main():
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "quality": quality,
+            "corrected_counts": corrected,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -12,7 +12,8 @@
 // (upper = true, t = 1 - u).  Two regimes:
 //  * small counts (at most CORR_SMALL, p^phi representable, the position not
 //    in the far upper tail): F summed from k = 0 by the pmf recurrence
-//    P(k+1) = P(k) (k + phi) q / (k + 1), absolute error a few ulps per term,
+//    P(k+1) = P(k) (q + (phi - 1) q / (k + 1)) (one fused multiply-add with a
+//    table of 1 / (k + 1)), absolute error a few ulps per term,
 //    so positions in the upper tail are used only down to t = 2^-10 (relative
 //    error ~1e-11 there);
 //  * otherwise the tail at a point comes from the continued fraction of the
@@ -70,6 +71,7 @@ CQ_HDI double inv_int1(int j) {  // 1 / (j + 1), 0 <= j <= CORR_SMALL
 
 struct NbDist {
   double mu, phi, q, lp, p0;  // p0 = P(0) = p^phi
+  double cq;                  // (phi - 1) q: P(j+1) / P(j) = q + cq / (j + 1)
   double p, lq, lg_phi;       // continued-fraction regime only (cf_prepare)
   bool cf_ready;
   CQ_HDI void set(double m, double ph) {
@@ -78,6 +80,7 @@ struct NbDist {
     q = m / (ph + m);
     lp = -log1p(m / ph);
     p0 = exp(ph * lp);
+    cq = (ph - 1.0) * q;
     cf_ready = false;
   }
   CQ_HDI double log_p0() const { return phi * lp; }
@@ -164,7 +167,7 @@ CQ_HDI bool source_small(const NbDist& d, int x, double v, bool& upper, double& 
   double pm = d.p0, F = 0.0;
   for (int j = 0; j < x; ++j) {
     F += pm;
-    pm *= (j + d.phi) * d.q * inv_int1(j);
+    pm *= fma(d.cq, inv_int1(j), d.q);
   }
   const double u = F + v * pm;
   if (!(u <= 1.0 - CORR_UPPER_MIN)) return false;
@@ -197,7 +200,7 @@ CQ_HDI bool target_small(const NbDist& d, bool upper, double t, int k0, int& out
   double pm = d.p0, F = pm;
   int j = 0;
   while (F < u && j < CORR_SMALL) {
-    pm *= (j + d.phi) * d.q * inv_int1(j);
+    pm *= fma(d.cq, inv_int1(j), d.q);
     ++j;
     F += pm;
   }
