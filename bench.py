@@ -44,7 +44,8 @@ CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
 CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide")
 # config-1 data with the HMC block update (10 leapfrog steps) in place of the random-walk steps
 CFG2 = dict(CFG1, hmc=10)
-WORKLOADS = {"config1": CFG1, "config2": CFG2, "config4": CFG4}
+CFG3 = dict(CFG1, ks=list(range(3, 11)))  # config-1 data fitted by 8 chains, K = 3 .. 10
+WORKLOADS = {"config1": CFG1, "config2": CFG2, "config3": CFG3, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
 UNIT = "sweeps/s"
 
@@ -221,6 +222,133 @@ def _config(name="config1", n_b=None, cfg=None):
             "precision": "f32 likelihood terms, f64 acceptance sums"}
 
 
+def run_batch(args, cfg, rank, world, local):
+    """Config 3: the config-1 data fitted by one chain per K = 3 .. 10 (the BIC
+    sweep over K).  Each chain's gene-pass chunk length comes from the
+    autotuner.  The sequential arm times each chain alone; the batched arm
+    launches one sweep of all chains as one CUDA graph.  Both arms run the same
+    sweeps of the same chains; the metric is chain-sweeps per second."""
+    import torch
+    import busseq_gpu_gb300 as bq
+
+    dev = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    n_b, G, seed = list(cfg["n_b"]), cfg["G"], cfg["seed"]
+    if args.cells > 0:
+        n_b = [args.cells] * len(n_b)
+    Y, W_true, _ = make_data(seed, cfg, n_b)
+    N = int(sum(n_b))
+    ks = list(cfg["ks"])
+    Yd = torch.from_numpy(Y).to(dev)
+    t0 = time.perf_counter()
+    tuned = {K: bq.autotune_chunk(Yd, n_b, K, seed=seed, sweeps=6, device=local) for K in ks}
+    tune_s = time.perf_counter() - t0
+    total = args.warmup + args.steps
+    burn = args.warmup + args.steps // 2
+
+    def chains():
+        return [bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank + K, device=local, chunk_cells=tuned[K][0])
+                for K in ks]
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    # ---- sequential arm: every chain alone, on its own stream ----------------
+    seq_ms = {}
+    stream = torch.cuda.Stream(device=local)
+    for K, c in zip(ks, chains()):
+        c.set_stream(stream.cuda_stream)
+        c.begin(total, burn, args.warmup)
+        c.sweeps(args.warmup)
+        c.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        c.sweeps(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq_ms[K] = e0.elapsed_time(e1)
+        c.close()
+    seq_total = sum(seq_ms.values())
+
+    # ---- batched arm: one graph per sweep holding every chain ---------------
+    cs = chains()
+    for c in cs:
+        c.begin(total, burn, args.warmup)
+    b = bq.Batch(cs)
+    b.sweeps(args.warmup)
+    b.synchronize()
+    bstream = torch.cuda.ExternalStream(b.stream, device=dev)
+    e0, e1 = ev(), ev()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(bstream)
+        b.sweeps(args.steps)
+        e1.record(bstream)
+        torch.cuda.synchronize()
+    bat_ms = e0.elapsed_time(e1)
+    b.synchronize()
+    b.close()
+    bic, launches = {}, 0
+    for K, c in zip(ks, cs):
+        c.finish()
+        bic[K] = c.bic()
+        launches += (args.steps - max(0, burn - args.warmup)) * c.launches_per_sweep(True) + \
+            max(0, burn - args.warmup) * c.launches_per_sweep(False)
+        c.close()
+    value = len(ks) * args.steps / (bat_ms / 1000.0)
+    seq_value = len(ks) * args.steps / (seq_total / 1000.0)
+    del Yd
+    torch.cuda.empty_cache()
+
+    # ---- e2e: the whole BIC sweep from pinned host counts --------------------
+    Yp = torch.from_numpy(Y).pin_memory()
+    Yh = Yp.numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cs = [bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank + K, device=local, chunk_cells=tuned[K][0]) for K in ks]
+    for c in cs:
+        c.begin(args.steps, args.steps // 2, min(args.warmup, args.steps))
+    with bq.Batch(cs) as b2:
+        b2.sweeps(args.steps)
+        b2.synchronize()
+    bic_e2e = {}
+    d2h = 0
+    for K, c in zip(ks, cs):
+        c.finish()
+        bic_e2e[K] = c.bic()
+        d2h += sum(v.nbytes for v in c.estimates(with_XZ=False).values()) + 8
+        c.close()
+    e2e_s = time.perf_counter() - t0
+    if rank == 0:
+        k_best = min(bic, key=bic.get)
+        line = {
+            "metric": "chain_sweeps_per_s", "value": value, "unit": "chain-sweeps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": bat_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (BUSseq generative model, seed %d, K = 8)" % seed,
+            "config": {"workload": "config3: the config-1 data (B=4 x %d cells, G=%d) fitted by %d chains, K = %s, "
+                                   "batched: one CUDA graph per sweep of all chains" % (n_b[0], G, len(ks), ks),
+                       "N": N, "G": G, "Ks": ks, "chunk_cells": {str(K): tuned[K][0] for K in ks},
+                       "l2": "no flush: every chain's X and Y are %.0f MB" % (N * G * 4 / 1e6)},
+            "sequential": {"value": seq_value, "unit": "chain-sweeps/s", "ms": seq_total,
+                           "ms_per_chain": {str(K): v for K, v in seq_ms.items()},
+                           "note": "each chain alone for the same %d sweeps" % args.steps},
+            "batched_vs_sequential": value / seq_value,
+            "autotune": {"seconds": tune_s, "ms_per_sweep": {str(K): {str(c): m for c, m in tuned[K][1].items()}
+                                                             for K in ks}},
+            "bic": {str(K): v for K, v in bic.items()}, "k_min_bic": k_best,
+            "e2e": {"value": len(ks) * args.steps / e2e_s, "unit": "chain-sweeps/s",
+                    "h2d_bytes_per_step": len(ks) * Y.nbytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+                    "note": "pinned-host upload per chain, init, %d batched sweeps, posterior, estimates and BIC "
+                            "per K to the host; k_min_bic %d" % (args.steps, min(bic_e2e, key=bic_e2e.get))},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": None,
+        }
+        print(json.dumps(line))
+    return 0
+
+
 def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
     """One whole job with kept draws: ESS (Geyer, initial monotone sequence) of
     every beta (k >= 1) and nu (b >= 1) coordinate, ESS/s over the wall time of
@@ -257,7 +385,7 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=30)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -268,11 +396,15 @@ def main():
                     help="leapfrog steps of the HMC block update (overrides the workload's; 0 keeps it)")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
                     help="config1 (the headline, default), config2 (config-1 data, HMC block update with 10 "
-                         "leapfrog steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
+                         "leapfrog steps), config3 (config-1 data, 8 chains K=3..10 batched in one graph per "
+                         "sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.steps_given = args.steps
+    if args.steps is None:
+        args.steps = 3000
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -294,6 +426,10 @@ def main():
             dist.barrier()
 
     cfg = dict(WORKLOADS[args.workload])
+    if args.workload == "config3":
+        if args.steps_given is None:
+            args.steps = 1000
+        return run_batch(args, cfg, rank, world, local)
     if args.leapfrog > 0:
         cfg["hmc"] = args.leapfrog
     n_b, G, K = list(cfg["n_b"]), cfg["G"], cfg["K"]

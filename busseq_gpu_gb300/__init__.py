@@ -108,6 +108,13 @@ def lib():
         "busseq_get_preserved": ([H, C.POINTER(Preserved)], C.c_int),
         "busseq_bic": ([H, _PD], C.c_int),
         "busseq_corrected_counts": ([H, C.c_void_p, C.c_int32], C.c_int),
+        "busseq_batch_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(H)], C.c_int),
+        "busseq_batch_sweeps": ([H, C.c_int32], C.c_int),
+        "busseq_batch_synchronize": ([H], C.c_int),
+        "busseq_batch_stream": ([H], C.c_void_p),
+        "busseq_batch_destroy": ([H], None),
+        "busseq_autotune_chunk": ([C.POINTER(Dims), C.c_void_p, C.c_int32, C.POINTER(Options), _PI32, C.c_int32,
+                                   C.c_int32, _PI32, _PD], C.c_int),
         "busseq_get_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_set_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_run_stage": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
@@ -173,6 +180,70 @@ def read_counts(path: str, N: int, G: int) -> np.ndarray:
     out = np.zeros((N, G), np.int32)
     _check(lib().busseq_read_counts(path.encode(), N, G, _p(out, _PI32)))
     return out
+
+
+def autotune_chunk(Y, n_b, K: int, seed: int = 0, candidates=(64, 128, 192, 256), sweeps: int = 8,
+                   hmc_leapfrog: int = 0, device: int = 0):
+    """Gene-pass chunk length (cells per CTA of the gene passes) chosen by timing
+    ``sweeps`` burn-in sweeps of a scratch chain for every candidate.  Returns
+    (best, {candidate: ms per sweep})."""
+    n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+    on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
+    if on_dev:
+        yptr, G = C.c_void_p(Y.data_ptr()), int(Y.shape[1])
+    else:
+        Yh = np.ascontiguousarray(Y, dtype=np.int32)
+        yptr, G = Yh.ctypes.data_as(C.c_void_p), int(Yh.shape[1])
+    dims = Dims(len(n_b), int(K), G, _p(n_b, _PI32))
+    opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=0.25, w_update=W_MH, keep_draws=0, device=int(device),
+                  chunk_cells=0, hmc_leapfrog=int(hmc_leapfrog))
+    cand = np.ascontiguousarray(candidates, dtype=np.int32)
+    ms = np.zeros(cand.size)
+    best = C.c_int32()
+    _check(lib().busseq_autotune_chunk(C.byref(dims), yptr, int(on_dev), C.byref(opt), _p(cand, _PI32),
+                                       int(cand.size), int(sweeps), C.byref(best), _p(ms, _PD)))
+    return int(best.value), {int(c): float(m) for c, m in zip(cand, ms)}
+
+
+class Batch:
+    """Chains (Samplers on one GPU, begun with the same run length) whose sweeps
+    are launched together as one CUDA graph per sweep; each chain's draws are
+    those it makes alone."""
+
+    def __init__(self, samplers):
+        self.samplers = list(samplers)
+        arr = (C.c_void_p * len(self.samplers))(*[s._h.value if hasattr(s._h, "value") else s._h
+                                                  for s in self.samplers])
+        h = C.c_void_p()
+        _check(lib().busseq_batch_create(arr, len(self.samplers), C.byref(h)))
+        self._h = h
+
+    def sweeps(self, count: int):
+        _check(lib().busseq_batch_sweeps(self._h, int(count)))
+
+    def synchronize(self):
+        _check(lib().busseq_batch_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(lib().busseq_batch_stream(self._h) or 0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().busseq_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Sampler:

@@ -263,6 +263,30 @@ double busseq_kernel_bytes(busseq_handle* h, int32_t i);
 /* Number of kernel launches one sweep makes (burn-in and kept sweeps). */
 int busseq_launches_per_sweep(busseq_handle* h, int32_t kept);
 
+/* ---- batches of chains (not in the reference) ----------------------------- */
+
+/* A set of chains on one device -- for instance one per K of a BIC sweep --
+ * whose sweeps are launched together: one CUDA graph holds one sweep of every
+ * chain as independent branches, so a launch advances all of them and their
+ * kernels overlap.  Every handle must have begun a run with the same n_iter and
+ * n_burnin and have made the same number of sweeps; the draws of each chain
+ * are those it makes alone.  Restarting a chain (busseq_begin) invalidates the
+ * batch.  Handles stay owned by the caller. */
+typedef struct busseq_batch busseq_batch;
+int busseq_batch_create(busseq_handle* const* handles, int32_t n, busseq_batch** out);
+int busseq_batch_sweeps(busseq_batch* b, int32_t count);
+int busseq_batch_synchronize(busseq_batch* b);
+void* busseq_batch_stream(busseq_batch* b);  /* the cudaStream_t the batch launches on */
+void busseq_batch_destroy(busseq_batch* b);
+
+/* Autotuner of the gene-pass chunk length (cells of one (batch, type) segment
+ * per CTA): times `sweeps` burn-in sweeps of a scratch handle for each of the
+ * n_cand candidates (1..256) and returns the fastest in *best, with the
+ * per-sweep times in ms_per_sweep[n_cand] (may be NULL). */
+int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, const busseq_options* opt,
+                          const int32_t* candidates, int32_t n_cand, int32_t sweeps, int32_t* best,
+                          double* ms_per_sweep);
+
 /* ---- files (the reference's formats) -------------------------------------- */
 
 /* Parses a whitespace-separated N x G integer count file (BUSseq_gpu.cu:1143-1161)
