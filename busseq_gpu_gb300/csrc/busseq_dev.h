@@ -181,6 +181,13 @@ struct DevState {
   FF* hmc_epart_b;  // [ceil(G / 256)] per-CTA kinetic minus prior change of the gene blocks
   float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
+  // The lgamma part of the phi ratio depends on an entry only through x, and
+  // the entries with Y > 0 keep x = Y: their part comes from these static
+  // tables once per (batch, gene) instead of once per entry (k_phi_static).
+  int32_t* phi_cnt;      // [B][PHI_TAB][Gp] number of cells with Y = y, 0 < y < PHI_TAB
+  int64_t* phi_big_off;  // [B*G + 1] start of each (batch, gene) run in phi_big_y
+  int32_t* phi_big_y;    // the Y values >= PHI_TAB of each (batch, gene), in cell order
+  double* phi_static;    // [B][Gp] the static part of the current proposal's phi sum
   float* gamma_p;  // [2][B]
 
   // cell order and work lists

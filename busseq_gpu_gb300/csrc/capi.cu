@@ -168,6 +168,9 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_delta");
       break;
     case 8:
+      if (!s.phi_cnt) return fail(BUSSEQ_ERR_STATE, "the random-walk phi update is not set up on an HMC handle");
+      k_phi_static<<<blocks_for((int64_t)s.B * s.G * 32, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_phi_static");
       k_phi<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_phi");
       break;
@@ -434,8 +437,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.Y = Yd;
     // one extra all-zero row: the gene passes pad their cell chunks with it
     TRY(h->alloc(&s.X, (N + 1) * Gp));
-    uint32_t* y0m;
-    TRY(h->alloc(&y0m, N * s.Gw));
+    uint32_t* y0m;  // one extra all-zero row, read for the padding row of a chunk
+    TRY(h->alloc(&y0m, (N + 1) * s.Gw));
     s.y0m = y0m;
     TRY(h->alloc(&s.zm, N * s.Gw));
     int32_t *bo, *boff;
@@ -606,6 +609,27 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     bq::k_init_finish<<<blocks_for(nfin, 256), 256, 0, h->stream>>>(s, 1);
     LAUNCH_CHECK("k_init_finish");
     CUDA_TRY(cudaMemcpyAsync(s.X, s.Y, (size_t)N * Gp * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
+    if (s.hmc_L == 0) {
+      // static tables of the phi update: counts of small Y, the larger Y in cell order
+      const int64_t nbg = (int64_t)B * G;
+      TRY(h->alloc(&s.phi_cnt, (int64_t)B * bq::PHI_TAB * Gp));
+      TRY(h->alloc(&s.phi_static, B * Gp));
+      int64_t* nbig;
+      TRY(h->alloc(&nbig, nbg));
+      bq::k_phi_hist<<<blocks_for(nbg, 256), 256, 0, h->stream>>>(s, nbig, 0);
+      LAUNCH_CHECK("k_phi_hist");
+      std::vector<int64_t> off_h(nbg + 1, 0);
+      CUDA_TRY(cudaMemcpyAsync(off_h.data() + 1, nbig, nbg * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(cudaStreamSynchronize(h->stream));
+      for (int64_t t = 0; t < nbg; ++t) off_h[t + 1] += off_h[t];
+      TRY(h->alloc(&s.phi_big_off, nbg + 1));
+      TRY(h->alloc(&s.phi_big_y, std::max<int64_t>(1, off_h[nbg])));
+      CUDA_TRY(cudaMemcpyAsync(s.phi_big_off, off_h.data(), (nbg + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               h->stream));
+      bq::k_phi_hist<<<blocks_for(nbg, 256), 256, 0, h->stream>>>(s, nbig, 1);
+      LAUNCH_CHECK("k_phi_hist");
+      CUDA_TRY(cudaStreamSynchronize(h->stream));  // off_h leaves scope
+    }
     CUDA_TRY(cudaMemsetAsync(s.zm, 0, (size_t)N * s.Gw * sizeof(uint32_t), h->stream));
     CUDA_TRY(cudaMemsetAsync(s.zval, 0, (size_t)std::max<int64_t>(1, s.nz0), h->stream));
     CUDA_TRY(cudaMemsetAsync(s.iter, 0, sizeof(int), h->stream));

@@ -15,7 +15,8 @@
 //                   outcomes of the beta of the cell's type
 //   k_decide_beta   beta decisions (:696-707)
 //   k_decide_nu_E   nu decisions (:730-737) and the table E = exp(alpha+beta+nu)
-//   k_phi           phi sums (:789-804)
+//   k_phi_static    phi sums, the lgamma part of the entries with Y > 0
+//   k_phi           phi sums (:789-804), the rest
 //   k_decide_phi    phi decisions (:806-818)
 //
 // Gene passes: a CTA owns GENE_TILE consecutive genes (one per thread) and one
@@ -570,24 +571,65 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   const float c1 = pp * log_ratio(pp, ph, dl);
   const char* Xg = reinterpret_cast<const char*>(s.X + g);
   const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
+  // Y == 0 bit of the entry (row N, the padding row, is all zero); the lgamma
+  // part of the entries with Y > 0 is k_phi_static's
+  const uint32_t* ym = s.y0m + (g >> 5);
+  const int64_t Gw = s.Gw;
+  const int bit = (int)(g & 31);
   KahanF acc;
   for (int j0 = 0; j0 < len8; j0 += 8) {
     int xr[8];
     float dv[8];
     load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    uint32_t zw[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
     float f = 0.0f;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int x = xr[u];
       const float mu = M * dv[u];
       const float xf = (float)x;
-      // x >= PHI_TAB >= 8: both arguments are past the shift range
-      const float hx = (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
+      const bool y0 = (zw[u] >> bit) & 1u;
+      float hx = y0 && (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : 0.0f;
+      // an imputed count past the table (rare): both arguments are past the shift range
+      if (y0 && x >= PHI_TAB) hx = lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
       f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
     }
     acc.add(f);
   }
   s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
+}
+
+// The lgamma part of the phi sums of the entries with Y > 0, one warp per
+// (batch, gene): sum over y < PHI_TAB of count(y) * table(y), plus the Stirling
+// difference of every larger Y of the (batch, gene), lanes taking the values
+// in turn.  Fixed-order float-float sums, so the result is reproducible.
+__global__ void __launch_bounds__(256) k_phi_static(DevState s) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (int64_t)s.B * s.G) return;  // uniform per warp
+  const int b = (int)(w / s.G);
+  const int64_t g = w % s.G, Gp = s.Gp;
+  const int64_t pos = (int64_t)b * Gp + g;
+  const float* tab = s.phi_tab + (int64_t)b * PHI_TAB * Gp + g;
+  const int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
+  KahanF acc;
+  for (int y = 1 + lane; y < PHI_TAB; y += 32) {
+    const int c = cnt[(int64_t)y * Gp];
+    if (c) acc.add((float)c * tab[(int64_t)y * Gp]);
+  }
+  const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
+  if (o1 > o0) {
+    const float ph = s.phi[pos], pp = s.phi_p[pos];
+    const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
+    for (int64_t q = o0 + lane; q < o1; q += 32) {
+      const float y = (float)s.phi_big_y[q];
+      acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
+    }
+  }
+  const FF tot = ff_warp_sum(acc.ff());
+  if (lane == 0) s.phi_static[pos] = ff_value(tot);
 }
 
 // ---------------------------------------------------------------------------
@@ -775,6 +817,7 @@ __global__ void k_decide_phi(DevState s) {
   double S = 0.0;
   for (int k = 0; k < s.K; ++k) S += seg_sum(s, b, k, 0, g);
   const int64_t pos = (int64_t)b * Gp + g;
+  S += s.phi_static[pos];
   const float ph = s.phi[pos], pp = s.phi_p[pos];
   const float dl = pp - ph;
   const double lgd0 = (double)lgamma_diff(ph, pp, dl);  // lgamma(pp) - lgamma(ph)

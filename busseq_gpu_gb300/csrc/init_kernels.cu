@@ -300,6 +300,33 @@ __global__ void k_init_finish(DevState s, int fresh) {
 // Posterior summaries: means over kept sweeps, P(L = 1), W mode.
 // est layout: gamma[2B] alpha[G] L[(K-1)G] beta[K G] ptau[2] nu[B G] delta[N] phi[B G] pi[B K]
 // ---------------------------------------------------------------------------
+// Static tables of the phi update: one thread per (batch, gene) walks the
+// batch's cells in order.  fill = 0: counts of Y = 1 .. PHI_TAB-1 into phi_cnt
+// and the number of larger values into n_big; fill = 1: the larger values
+// into phi_big_y from phi_big_off, in cell order (so every sum over them has a
+// fixed order).
+__global__ void k_phi_hist(DevState s, int64_t* n_big, int fill) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)s.B * s.G) return;
+  const int b = (int)(t / s.G);
+  const int64_t g = t % s.G, Gp = s.Gp;
+  int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
+  int64_t pos = fill ? s.phi_big_off[t] : 0;
+  int64_t nb = 0;
+  const int i1 = s.batch_off[b + 1];
+#pragma unroll 4
+  for (int i = s.batch_off[b]; i < i1; ++i) {
+    const int y = s.Y[(int64_t)i * Gp + g];
+    if (y >= PHI_TAB) {
+      if (fill) s.phi_big_y[pos++] = y;
+      ++nb;
+    } else if (y > 0 && !fill) {
+      ++cnt[(int64_t)y * Gp];
+    }
+  }
+  if (!fill) n_big[t] = nb;
+}
+
 __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
