@@ -400,6 +400,8 @@ def main():
                          "sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
+    ap.add_argument("--corrected-counts", action="store_true",
+                    help="with --only-value: also run one batch-corrected-count pass after the sweeps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.steps_given = args.steps
@@ -472,6 +474,11 @@ def main():
     launches = (args.steps // 2) * s.launches_per_sweep(False) + (args.steps - args.steps // 2) * s.launches_per_sweep(True)
 
     if args.only_value:
+        if args.corrected_counts:  # one corrected-count pass of the finished run (for profiler captures)
+            cc = torch.empty((N, G), dtype=torch.int32, device=f"cuda:{local}")
+            s.corrected_counts(out=cc)
+            torch.cuda.synchronize()
+            del cc
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "config": _config(args.workload, n_b, cfg),
