@@ -183,7 +183,8 @@ struct DevState {
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   // The lgamma part of the phi ratio depends on an entry only through x, and
   // the entries with Y > 0 keep x = Y: their part comes from these static
-  // tables once per (batch, gene) instead of once per entry (k_phi_static).
+  // tables once per (batch, gene) instead of once per entry (k_propose for
+  // Y < PHI_TAB, k_phi_static for the rest).
   int32_t* phi_cnt;      // [B][PHI_TAB][Gp] number of cells with Y = y, 0 < y < PHI_TAB
   int64_t* phi_big_off;  // [B*G + 1] start of each (batch, gene) run in phi_big_y
   int32_t* phi_big_y;    // the Y values >= PHI_TAB of each (batch, gene), in cell order

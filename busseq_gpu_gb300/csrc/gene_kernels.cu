@@ -15,7 +15,8 @@
 //                   outcomes of the beta of the cell's type
 //   k_decide_beta   beta decisions (:696-707)
 //   k_decide_nu_E   nu decisions (:730-737) and the table E = exp(alpha+beta+nu)
-//   k_phi_static    phi sums, the lgamma part of the entries with Y > 0
+//   k_phi_static    phi sums, the lgamma part of the entries with Y >= 64 (k_propose
+//                   sums that of the smaller Y > 0 with the lgamma table)
 //   k_phi           phi sums (:789-804), the rest
 //   k_decide_phi    phi decisions (:806-818)
 //
@@ -107,13 +108,27 @@ __global__ void k_propose(DevState s, int mask) {
       // for x < PHI_TAB, and lgamma(pn) - lgamma(ph)
       const float dl = pn - ph;
       float* tab = s.phi_tab + (int64_t)b * PHI_TAB * Gp + g;
+      // with the static counts of Y = x (entries with Y > 0), their share of the
+      // phi sum below the table's end; k_phi_static adds the larger Y
+      const int32_t* cnt = s.phi_cnt ? s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g : nullptr;
+      KahanF stat;
       float h = 0.0f;
       tab[0] = 0.0f;
-      for (int x = 1; x < PHI_TAB; ++x) {
-        const float j = (float)(x - 1);
-        h += log_ratio(pn + j, ph + j, dl);
-        tab[(int64_t)x * Gp] = h;
+      for (int x0 = 0; x0 < PHI_TAB; x0 += 16) {
+        int c[16];  // the block's counts, loaded ahead of the serial sum
+#pragma unroll
+        for (int u = 0; u < 16; ++u) c[u] = (cnt && x0 + u > 0) ? __ldg(cnt + (int64_t)(x0 + u) * Gp) : 0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int x = x0 + u;
+          if (x == 0) continue;
+          const float j = (float)(x - 1);
+          h += log_ratio(pn + j, ph + j, dl);
+          tab[(int64_t)x * Gp] = h;
+          if (c[u]) stat.add((float)c[u] * h);
+        }
       }
+      if (cnt) s.phi_static[b * Gp + g] = stat.value();
       s.phi_lgd0[b * Gp + g] = lgamma_diff(ph, pn, dl);
     }
   }
@@ -601,35 +616,28 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
 }
 
-// The lgamma part of the phi sums of the entries with Y > 0, one warp per
-// (batch, gene): sum over y < PHI_TAB of count(y) * table(y), plus the Stirling
-// difference of every larger Y of the (batch, gene), lanes taking the values
-// in turn.  Fixed-order float-float sums, so the result is reproducible.
+// The lgamma part of the phi sums of the entries with Y >= PHI_TAB, one warp
+// per (batch, gene), lanes taking the gene's values in turn, added to the part
+// below the table that k_propose left in phi_static.  Fixed-order float-float
+// sums, so the result is reproducible.
 __global__ void __launch_bounds__(256) k_phi_static(DevState s) {
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= (int64_t)s.B * s.G) return;  // uniform per warp
-  const int b = (int)(w / s.G);
-  const int64_t g = w % s.G, Gp = s.Gp;
-  const int64_t pos = (int64_t)b * Gp + g;
-  const float* tab = s.phi_tab + (int64_t)b * PHI_TAB * Gp + g;
-  const int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
-  KahanF acc;
-  for (int y = 1 + lane; y < PHI_TAB; y += 32) {
-    const int c = cnt[(int64_t)y * Gp];
-    if (c) acc.add((float)c * tab[(int64_t)y * Gp]);
-  }
   const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
-  if (o1 > o0) {
-    const float ph = s.phi[pos], pp = s.phi_p[pos];
-    const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
-    for (int64_t q = o0 + lane; q < o1; q += 32) {
-      const float y = (float)s.phi_big_y[q];
-      acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
-    }
+  if (o1 == o0) return;
+  const int b = (int)(w / s.G);
+  const int64_t g = w % s.G;
+  const int64_t pos = (int64_t)b * s.Gp + g;
+  const float ph = s.phi[pos], pp = s.phi_p[pos];
+  const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
+  KahanF acc;
+  for (int64_t q = o0 + lane; q < o1; q += 32) {
+    const float y = (float)s.phi_big_y[q];
+    acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
   }
   const FF tot = ff_warp_sum(acc.ff());
-  if (lane == 0) s.phi_static[pos] = ff_value(tot);
+  if (lane == 0) s.phi_static[pos] += ff_value(tot);
 }
 
 // ---------------------------------------------------------------------------
