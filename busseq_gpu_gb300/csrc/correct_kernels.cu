@@ -67,23 +67,63 @@ __global__ void k_correct_prep(DevState s, Estimates e, CorrTables tb) {
 }
 
 // Each CTA takes CORR_CHUNK genes of one row at a time (rows strided over
-// blockIdx.y).  Pass 1 finishes every entry that the forward sums settle
-// (most of them) and queues the rest in shared memory; pass 2 hands the queue
-// to consecutive threads, so the continued-fraction work runs in full warps
-// instead of stalling the warps of the cheap entries.  out has row stride ld.
+// blockIdx.y).  The entries are first ordered by count with a counting sort in
+// shared memory, so that the lanes of a warp run forward sums of about the
+// same length (the source sum runs to x, the target's to about x again).
+// Pass 1 finishes every entry that the forward sums settle (most of them) and
+// queues the rest; pass 2 hands the queue to consecutive threads, so the
+// continued-fraction work runs in full warps instead of stalling the warps of
+// the cheap entries.  Each entry's result depends only on the entry, so the
+// order of work does not change the output.  out has row stride ld.
+constexpr int CORR_BINS = corr::CORR_SMALL + 2;  // counts 0 .. CORR_SMALL, and larger
+
 __global__ void __launch_bounds__(CORR_THREADS) k_correct(DevState s, Estimates e, CorrTables tb, int32_t* out,
                                                           int64_t ld) {
   __shared__ int queue[CORR_CHUNK];
+  __shared__ uint16_t order[CORR_CHUNK];
+  __shared__ int bin_base[CORR_BINS];
   __shared__ int n_queue;
   const int64_t g0 = (int64_t)blockIdx.x * CORR_CHUNK;
   const int n_g = (int)(s.G - g0 < CORR_CHUNK ? s.G - g0 : CORR_CHUNK);
+  constexpr int PER = CORR_CHUNK / CORR_THREADS;
   for (int64_t i = blockIdx.y; i < s.N; i += gridDim.y) {
     if (threadIdx.x == 0) n_queue = 0;
+    for (int q = threadIdx.x; q < CORR_BINS; q += CORR_THREADS) bin_base[q] = 0;
     __syncthreads();
     const int b = s.batch_of[i];
     const int64_t w = e.W[i];
     const double dexp = exp(e.delta[i]);
-    for (int j = threadIdx.x; j < n_g; j += CORR_THREADS) {
+    int key[PER];
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+      const int j = threadIdx.x + r * CORR_THREADS;
+      const int x = j < n_g ? s.X[i * s.Gp + g0 + j] : 0;
+      key[r] = j < n_g ? (x > corr::CORR_SMALL ? CORR_BINS - 1 : x) : -1;
+      if (key[r] >= 0) atomicAdd(&bin_base[key[r]], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the bin counts, then each bin's cursor
+      int carry = 0;
+      for (int q0 = 0; q0 < CORR_BINS; q0 += 32) {
+        const int q = q0 + (int)threadIdx.x;
+        const int v = q < CORR_BINS ? bin_base[q] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if ((int)threadIdx.x >= o) incl += t;
+        }
+        if (q < CORR_BINS) bin_base[q] = carry + incl - v;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < PER; ++r)
+      if (key[r] >= 0) order[atomicAdd(&bin_base[key[r]], 1)] = (uint16_t)(threadIdx.x + r * CORR_THREADS);
+    __syncthreads();
+    for (int q = threadIdx.x; q < n_g; q += CORR_THREADS) {
+      const int j = order[q];
       const int64_t g = g0 + j;
       corr::NbDist dst = tb.target[w * s.G + g];
       corr::NbDist src;
