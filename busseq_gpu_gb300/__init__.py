@@ -45,7 +45,7 @@ class Dims(C.Structure):
 class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
                 ("device", C.c_int32), ("chunk_cells", C.c_int32), ("hmc_leapfrog", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("zx_summaries", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class Estimates(C.Structure):
@@ -108,6 +108,8 @@ def lib():
         "busseq_get_preserved": ([H, C.POINTER(Preserved)], C.c_int),
         "busseq_bic": ([H, _PD], C.c_int),
         "busseq_corrected_counts": ([H, C.c_void_p, C.c_int32], C.c_int),
+        "busseq_get_zx_summaries": ([H, C.c_void_p, C.c_void_p], C.c_int),
+        "busseq_write_zx_summaries": ([H, C.c_char_p], C.c_int),
         "busseq_batch_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(H)], C.c_int),
         "busseq_batch_sweeps": ([H, C.c_int32], C.c_int),
         "busseq_batch_synchronize": ([H], C.c_int),
@@ -251,7 +253,8 @@ class Sampler:
     read counts -> initialise -> sweeps -> posterior -> files)."""
 
     def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
-                 keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0):
+                 keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0,
+                 zx_summaries: bool = False):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -261,7 +264,7 @@ class Sampler:
             w_update = {"mh": W_MH, "gibbs": W_GIBBS}[w_update]
         opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
                       keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells),
-                      hmc_leapfrog=int(hmc_leapfrog))
+                      hmc_leapfrog=int(hmc_leapfrog), zx_summaries=int(bool(zx_summaries)))
         on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
         if on_dev:
             assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2
@@ -370,6 +373,14 @@ class Sampler:
         v = C.c_double()
         _check(lib().busseq_bic(self._h, C.byref(v)))
         return v.value
+
+    def zx_summaries(self) -> dict:
+        """Posterior mean of X and P(Z = 1) per entry over the kept sweeps (needs
+        zx_summaries=True and a finished run)."""
+        xm = np.zeros((self.N, self.G), np.float32)
+        zp = np.zeros((self.N, self.G), np.float32)
+        _check(lib().busseq_get_zx_summaries(self._h, xm.ctypes.data_as(C.c_void_p), zp.ctypes.data_as(C.c_void_p)))
+        return {"x_mean": xm, "z_prob": zp}
 
     def corrected_counts(self, out=None) -> np.ndarray:
         """Batch-corrected counts [N, G] (int32): the last sweep's imputed counts

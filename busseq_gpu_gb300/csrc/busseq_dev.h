@@ -239,6 +239,8 @@ struct DevState {
   double* acc_pi;     // [B*K]
   double* acc_ptau;   // [2]
   int32_t* acc_wcnt;  // [N][K]
+  int32_t* acc_zn;    // [nz0] kept sweeps with Z = 1 at each Y == 0 entry (zx_summaries, else null)
+  int64_t* acc_xs;    // [nz0] sum of X there over the kept sweeps
 
   // preserved draws, [kept sweep][scalar] (only when keep_draws)
   float* keep_gamma;

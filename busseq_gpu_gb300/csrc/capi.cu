@@ -140,7 +140,8 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_propose");
       break;
     case 1:
-      k_zx<<<(unsigned)(s.n_zcta + s.n_static) > 0 ? (unsigned)(s.n_zcta + s.n_static) : 1u, ZX_THREADS, 0, st>>>(s);
+      k_zx<<<(unsigned)(s.n_zcta + s.n_static) > 0 ? (unsigned)(s.n_zcta + s.n_static) : 1u, ZX_THREADS, 0, st>>>(
+          s, kept);
       LAUNCH_CHECK("k_zx");
       break;
     case 2:
@@ -684,6 +685,12 @@ int busseq_begin(busseq_handle* h, int32_t n_iter, int32_t n_burnin, int32_t n_u
   TRY(h->alloc(&s.acc_pi, B * K, true));
   TRY(h->alloc(&s.acc_ptau, 2, true));
   TRY(h->alloc(&s.acc_wcnt, N * K, true));
+  s.acc_zn = nullptr;
+  s.acc_xs = nullptr;
+  if (h->opt.zx_summaries && h->n_kept > 0) {
+    TRY(h->alloc(&s.acc_zn, std::max<int64_t>(1, s.nz0), true));
+    TRY(h->alloc(&s.acc_xs, std::max<int64_t>(1, s.nz0), true));
+  }
   s.keep_gamma = s.keep_alpha = s.keep_beta = s.keep_ptau = s.keep_nu = s.keep_delta = s.keep_phi = s.keep_pi =
       nullptr;
   s.keep_L = nullptr;
@@ -869,6 +876,35 @@ int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_devic
   return BUSSEQ_OK;
 }
 
+int busseq_get_zx_summaries(busseq_handle* h, float* x_mean, float* z_prob) {
+  if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");
+  if (!h->opt.zx_summaries) return fail(BUSSEQ_ERR_STATE, "the chain was created without zx_summaries");
+  if (!h->finished || h->n_kept <= 0 || !h->s.acc_zn)
+    return fail(BUSSEQ_ERR_STATE, "no finished run with kept sweeps");
+  if (!x_mean && !z_prob) return BUSSEQ_OK;
+  CUDA_TRY(cudaSetDevice(h->device));
+  const bq::DevState& s = h->s;
+  const size_t bytes = (size_t)s.N * s.G * sizeof(float);
+  float* d = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&d, 2 * bytes, h->stream));
+  float* dx = x_mean ? d : nullptr;
+  float* dz = z_prob ? d + (size_t)s.N * s.G : nullptr;
+  const unsigned grid = 152 * 8;
+  bq::k_zx_summary<<<grid, 256, 0, h->stream>>>(s, h->n_kept, dx, dz);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && s.nz0 > 0) {
+    bq::k_zx_summary_zeros<<<grid, 256, 0, h->stream>>>(s, h->n_kept, dx, dz);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && x_mean) e = cudaMemcpyAsync(x_mean, dx, bytes, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && z_prob) e = cudaMemcpyAsync(z_prob, dz, bytes, cudaMemcpyDeviceToHost, h->stream);
+  const cudaError_t e2 = cudaFreeAsync(d, h->stream);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "zx summaries: %s", cudaGetErrorString(e));
+  return BUSSEQ_OK;
+}
+
 int busseq_get_state(busseq_handle* h, busseq_state* o) {
   if (!h || !o) return fail(BUSSEQ_ERR_ARG, "NULL argument");
   CUDA_TRY(cudaSetDevice(h->device));
@@ -1026,9 +1062,10 @@ struct CkHeader {
   int32_t begun, finished, n_iter, n_burnin, n_unchanged, iter_host, iter_dev;
   int64_t G, N, nz0;
   uint64_t seed, y_fingerprint;
+  int32_t hmc_leapfrog, zx_summaries;
 };
 constexpr char kCkMagic[8] = {'B', 'U', 'S', 'S', 'E', 'Q', 'C', 'K'};
-constexpr uint32_t kCkVersion = 1;
+constexpr uint32_t kCkVersion = 2;
 
 struct DevBlock {
   void* p;
@@ -1053,6 +1090,10 @@ std::vector<DevBlock> run_blocks(const busseq_handle* h) {
         {s.keep_delta, nk * N * 4},     {s.keep_phi, nk * B * G * 4},    {s.keep_W, nk * N * 2},
         {s.keep_pi, nk * B * K * 4}};
     v.insert(v.end(), k.begin(), k.end());
+  }
+  if (s.acc_zn) {
+    v.push_back({s.acc_zn, (size_t)std::max<int64_t>(1, s.nz0) * 4});
+    v.push_back({s.acc_xs, (size_t)std::max<int64_t>(1, s.nz0) * 8});
   }
   if (s.hmc_L > 0) {  // log phi as the chain holds it, the adapted metric and the step size
     v.push_back({s.psi, (size_t)s.B * s.Gp * 4});
@@ -1125,6 +1166,8 @@ int busseq_checkpoint_save(busseq_handle* h, const char* path) {
   hd.seed = h->opt.seed;
   hd.w_update = h->opt.w_update;
   hd.keep_draws = h->opt.keep_draws;
+  hd.hmc_leapfrog = h->s.hmc_L;
+  hd.zx_summaries = h->opt.zx_summaries ? 1 : 0;
   hd.begun = h->begun ? 1 : 0;
   hd.finished = h->finished ? 1 : 0;
   hd.n_iter = h->n_iter;
@@ -1213,8 +1256,10 @@ int busseq_checkpoint_load(busseq_handle* h, const char* path) {
   if (hd.B != B || hd.K != K || hd.G != G || hd.N != N || hd.nz0 != s.nz0)
     return fail(BUSSEQ_ERR_ARG, "%s was written for B=%d K=%d G=%lld N=%lld, this chain has B=%d K=%d G=%lld N=%lld",
                 path, hd.B, hd.K, (long long)hd.G, (long long)hd.N, B, K, (long long)G, (long long)N);
-  if (hd.seed != h->opt.seed || hd.w_update != h->opt.w_update || hd.keep_draws != h->opt.keep_draws)
-    return fail(BUSSEQ_ERR_ARG, "%s was written with another seed, W move or keep_draws setting", path);
+  if (hd.seed != h->opt.seed || hd.w_update != h->opt.w_update || hd.keep_draws != h->opt.keep_draws ||
+      hd.hmc_leapfrog != h->s.hmc_L || hd.zx_summaries != (h->opt.zx_summaries ? 1 : 0))
+    return fail(BUSSEQ_ERR_ARG, "%s was written with another seed, W move, keep_draws, HMC or zx_summaries setting",
+                path);
   uint64_t fp = 0;
   TRY(y_fingerprint(h, &fp));
   if (fp != hd.y_fingerprint) return fail(BUSSEQ_ERR_ARG, "%s was written for different counts", path);

@@ -9,6 +9,8 @@
 //   --stats               print per-phase wall times to stderr
 //   --corrected           also write <prefix>_corrected_X.txt, the batch-corrected
 //                         counts (randomised quantile matching of _post_X)
+//   --posterior-zx        also write <prefix>_post_X_mean.txt and _post_Z_prob.txt,
+//                         E[X] and P(Z = 1) over the kept sweeps
 #include "busseq_gb300.h"
 
 #include <getopt.h>
@@ -47,7 +49,7 @@ int main(int argc, char** argv) {
   char output_file[4096] = "demo_output";
   char n_file[4096] = "";
   int n_file_flag = 0, burnin_flag = 1, unchanged_flag = 1, seed_flag = 1;
-  int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0, corrected = 0;
+  int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0, corrected = 0, posterior_zx = 0;
   std::string ck_path, resume_path;
 
   static struct option longopts[] = {{"w-update", required_argument, nullptr, 1000},
@@ -58,6 +60,7 @@ int main(int argc, char** argv) {
                                      {"resume", required_argument, nullptr, 1005},
                                      {"stop-after", required_argument, nullptr, 1006},
                                      {"corrected", no_argument, nullptr, 1007},
+                                     {"posterior-zx", no_argument, nullptr, 1008},
                                      {nullptr, 0, nullptr, 0}};
   int opt;
   while ((opt = getopt_long(argc, argv, "B:N:G:K:s:c:i:b:u:po:", longopts, nullptr)) != -1) {
@@ -85,6 +88,7 @@ int main(int argc, char** argv) {
       case 1005: resume_path = optarg; break;
       case 1006: stop_after = atoi(optarg); break;
       case 1007: corrected = 1; break;
+      case 1008: posterior_zx = 1; break;
       default:
         printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
                "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
@@ -148,6 +152,7 @@ int main(int argc, char** argv) {
   o.p0 = p0 > 0.0 ? p0 : 1e-9;
   o.w_update = w_update;
   o.keep_draws = print_preserved;
+  o.zx_summaries = posterior_zx;
   o.device = device;
   busseq_handle* h = nullptr;
   if (busseq_create(&dims, Y.data(), 0, &o, &h) != BUSSEQ_OK) die_lib("initialisation");
@@ -211,6 +216,7 @@ int main(int argc, char** argv) {
   fflush(stdout);
   if (busseq_write_outputs(h, output_file, print_preserved) != BUSSEQ_OK) die_lib("writing outputs");
   if (corrected && busseq_write_corrected(h, output_file) != BUSSEQ_OK) die_lib("writing corrected counts");
+  if (posterior_zx && busseq_write_zx_summaries(h, output_file) != BUSSEQ_OK) die_lib("writing Z/X summaries");
   double t4 = now_s();
   if (stats) {
     fprintf(stderr,

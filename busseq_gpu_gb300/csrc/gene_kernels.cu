@@ -224,7 +224,7 @@ __device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
   return 16 - bin;
 }
 
-__global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
+__global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
   __shared__ double sh[(ZX_THREADS / 32) * 6];
   __shared__ FF shf[ZX_WARPS * 3];
   __shared__ long long shn[ZX_WARPS * 3];
@@ -400,6 +400,10 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s) {
     if (err) atomicOr(s.err, err);
     if (x != xo) s.X[(int64_t)ig.x * Gp + ig.y] = x;
     s.zval[j] = 1;
+    if (kept && s.acc_zn) {  // posterior summaries (entries with Z = 0 keep X = 0 and add nothing)
+      s.acc_zn[j] += 1;
+      s.acc_xs[j] += x;
+    }
     ++nz;
     xz += x;
     if (x == 0) {
@@ -697,7 +701,8 @@ __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
   double lv[2] = {0.0, 0.0};
   if (g < s.G && s.hmc_L == 0) {  // alpha: random-walk MH (the HMC block updates it otherwise)
     double Sx = 0.0, La = 0.0;
-    for (int c = 0; c < s.cap_g; ++c) {
+#pragma unroll 8
+    for (int c = 0; c < s.cap_g; ++c) {  // unrolled: eight chunks' loads in flight
       const bool used = s.gchunk[c].w > 0;
       const double a0 = __ldg(&s.part[((int64_t)c * NSLOT + 0) * Gp + g]);
       const double a1 = __ldg(&s.part[((int64_t)c * NSLOT + 1) * Gp + g]);

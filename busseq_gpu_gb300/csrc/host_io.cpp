@@ -254,6 +254,26 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   return BUSSEQ_OK;
 }
 
+int busseq_write_zx_summaries(busseq_handle* h, const char* prefix) {
+  if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
+  int32_t B, K, nk, kd;
+  int64_t G, N;
+  int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
+  if (r) return r;
+  std::vector<float> xm((size_t)N * G), zp((size_t)N * G);
+  if ((r = busseq_get_zx_summaries(h, xm.data(), zp.data()))) return r;
+  auto table = [N, G](const std::vector<float>& v) {
+    Table t;
+    t.rows = N;
+    t.cols = G;
+    t.cell = [&v, G](int64_t i, int64_t g, char* b) { return fmt_lf((double)v[i * G + g], b); };
+    return t;
+  };
+  const std::string pre(prefix);
+  if ((r = write_table(pre + "_post_X_mean.txt", table(xm)))) return r;
+  return write_table(pre + "_post_Z_prob.txt", table(zp));
+}
+
 int busseq_write_corrected(busseq_handle* h, const char* prefix) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
   int32_t B, K, nk, kd;

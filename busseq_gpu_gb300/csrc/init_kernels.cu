@@ -327,6 +327,31 @@ __global__ void k_phi_hist(DevState s, int64_t* n_big, int fill) {
   if (!fill) n_big[t] = nb;
 }
 
+// Posterior summaries of the imputation as dense [N][G] tables: E[X] and
+// P(Z = 1), from Y where Y > 0 and from the kept-sweep sums at the Y == 0
+// entries (one thread per entry of the dense table, then of the zero list).
+__global__ void k_zx_summary(DevState s, int n_kept, float* x_mean, float* z_prob) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t NG = s.N * s.G;
+  for (int64_t t = t0; t < NG; t += stride) {
+    const int64_t i = t / s.G, g = t - i * s.G;
+    if (x_mean) x_mean[t] = (float)s.Y[i * s.Gp + g];
+    if (z_prob) z_prob[t] = 0.0f;
+  }
+}
+
+__global__ void k_zx_summary_zeros(DevState s, int n_kept, float* x_mean, float* z_prob) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const double inv = 1.0 / (double)n_kept;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < s.nz0; e += stride) {
+    const int2 ig = s.zij[e];
+    const int64_t t = (int64_t)ig.x * s.G + ig.y;
+    if (x_mean) x_mean[t] = (float)((double)s.acc_xs[e] * inv);
+    if (z_prob) z_prob[t] = (float)((double)s.acc_zn[e] * inv);
+  }
+}
+
 __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

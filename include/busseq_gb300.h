@@ -70,7 +70,10 @@ typedef struct busseq_options {
                            reference's sampler); L > 0: one Hamiltonian Monte Carlo
                            transition of that block per sweep with L leapfrog
                            steps (not in the reference)                         */
-  int32_t reserved[7];
+  int32_t zx_summaries; /* 1: over the kept sweeps, count Z = 1 and sum X at every
+                           Y == 0 entry (busseq_get_zx_summaries; not in the
+                           reference, which writes the last sweep's Z and X)    */
+  int32_t reserved[6];
 } busseq_options;
 
 /* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
@@ -204,6 +207,12 @@ int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev, const doub
  * reproducible.  out is a host buffer, or device memory when out_is_device. */
 int busseq_corrected_counts(busseq_handle* h, int32_t* out, int32_t out_is_device);
 
+/* Posterior summaries of the imputation [N*G] (cells x genes), over the kept
+ * sweeps of a finished run made with opt.zx_summaries: x_mean = E[X] (= Y
+ * where Y > 0) and z_prob = P(Z = 1) (0 where Y > 0).  NULL pointers are
+ * skipped. */
+int busseq_get_zx_summaries(busseq_handle* h, float* x_mean, float* z_prob);
+
 int busseq_get_state(busseq_handle* h, busseq_state* out);
 /* Replaces the whole state; derived data (exp(delta), exp(alpha+beta+nu), the
  * cell order) is recomputed on the device. */
@@ -296,6 +305,10 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out);
 /* Writes the _post_*, _BIC and (print_preserved) _preserved_* files with the
  * reference's names and formats (BUSseq_gpu.cu:1610-2018). */
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved);
+
+/* Writes <prefix>_post_X_mean.txt and <prefix>_post_Z_prob.txt, the tables of
+ * busseq_get_zx_summaries in the format of _post_X (%lf values). */
+int busseq_write_zx_summaries(busseq_handle* h, const char* prefix);
 
 /* Writes <prefix>_corrected_X.txt: the batch-corrected counts of
  * busseq_corrected_counts as an N x G table in the format of _post_X. */
