@@ -133,6 +133,7 @@ def lib():
         "busseq_kernel_bytes": ([H, C.c_int32], C.c_double),
         "busseq_launches_per_sweep": ([H, C.c_int32], C.c_int),
         "busseq_read_counts": ([C.c_char_p, C.c_int64, C.c_int64, _PI32], C.c_int),
+        "busseq_write_counts_binary": ([C.c_char_p, C.c_int64, C.c_int64, _PI32], C.c_int),
         "busseq_write_outputs": ([H, C.c_char_p, C.c_int32], C.c_int),
         "busseq_simulate": ([C.POINTER(Dims), C.POINTER(SimParams), C.c_uint64, _PI32, _PI32, _PI32], C.c_int),
         "busseq_last_error": ([], C.c_char_p),
@@ -179,9 +180,18 @@ def simulate(n_b, G: int, K: int, seed: int, **params):
 
 
 def read_counts(path: str, N: int, G: int) -> np.ndarray:
+    """An N x G count file: the reference's text format, or binary counts
+    (recognised by their magic)."""
     out = np.zeros((N, G), np.int32)
     _check(lib().busseq_read_counts(path.encode(), N, G, _p(out, _PI32)))
     return out
+
+
+def write_counts_binary(path: str, Y) -> None:
+    """Y (N x G) as a binary count file that read_counts and the command line load
+    without parsing."""
+    Yc = np.ascontiguousarray(Y, dtype=np.int32)
+    _check(lib().busseq_write_counts_binary(path.encode(), Yc.shape[0], Yc.shape[1], _p(Yc, _PI32)))
 
 
 def autotune_chunk(Y, n_b, K: int, seed: int = 0, candidates=(64, 128, 192, 256), sweeps: int = 8,

@@ -5,11 +5,19 @@
 // count the tokens of each slice, then parse each slice into its place).
 // Writing: BUSseq_gpu.cu:1610-2018 -- tab-separated rows, "%lf" for floating
 // point, "%d" for integers; rows are formatted in parallel and written in order.
+//
+// Binary counts (not in the reference): a file that starts with the 8 bytes
+// "BUSSEQY1" holds int64 N, int64 G and then N*G int32 counts, row-major,
+// little-endian.  busseq_read_counts recognises it by that magic and reads it
+// with one pread per host thread; busseq_write_counts_binary writes it (a text
+// count file converted once loads without parsing afterwards).
 #include "busseq_gb300.h"
 
+#include <fcntl.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <functional>
@@ -118,8 +126,100 @@ int write_table(const std::string& path, const Table& t) {
 
 extern "C" {
 
+}  // extern "C"
+
+namespace {
+
+constexpr char kBinMagic[8] = {'B', 'U', 'S', 'S', 'E', 'Q', 'Y', '1'};
+constexpr int64_t kBinHeader = 24;
+
+bool host_little_endian() {
+  const uint32_t one = 1;
+  unsigned char c;
+  memcpy(&c, &one, 1);
+  return c == 1;
+}
+
+// Reads the N*G int32 payload of a binary count file, one pread per thread.
+int read_counts_binary(int fd, const char* path, int64_t N, int64_t G, int64_t file_size, int32_t* out) {
+  int64_t hdr[2];
+  if (pread(fd, hdr, sizeof hdr, 8) != (ssize_t)sizeof hdr)
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("short header in ") + path).c_str());
+  if (hdr[0] != N || hdr[1] != G) {
+    char msg[240];
+    snprintf(msg, sizeof(msg), "binary count file %s holds N=%lld G=%lld, expected N=%lld G=%lld", path,
+             (long long)hdr[0], (long long)hdr[1], (long long)N, (long long)G);
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, msg);
+  }
+  const int64_t bytes = N * G * 4;
+  if (file_size != kBinHeader + bytes)
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("binary count file of the wrong size: ") + path).c_str());
+  const int nt = std::max(1, std::min(nthreads(), (int)(bytes >> 24) + 1));
+  std::vector<int> ok(nt, 1);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t) {
+    th.emplace_back([&, t]() {
+      int64_t a = (bytes / nt) * t, b = t + 1 == nt ? bytes : (bytes / nt) * (t + 1);
+      a &= ~int64_t(3);
+      if (t + 1 != nt) b &= ~int64_t(3);
+      char* dst = reinterpret_cast<char*>(out);
+      while (a < b) {
+        const ssize_t r = pread(fd, dst + a, (size_t)std::min<int64_t>(b - a, 1 << 30), kBinHeader + a);
+        if (r <= 0) { ok[t] = 0; return; }
+        a += r;
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  for (int t = 0; t < nt; ++t)
+    if (!ok[t]) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("short read of ") + path).c_str());
+  return BUSSEQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int busseq_write_counts_binary(const char* path, int64_t N, int64_t G, const int32_t* Y) {
+  if (!path || !Y || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
+  if (!host_little_endian()) return busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
+  FILE* f = fopen(path, "wb");
+  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open ") + path + " for writing").c_str());
+  const int64_t hdr[2] = {N, G};
+  bool ok = fwrite(kBinMagic, 1, 8, f) == 8 && fwrite(hdr, 8, 2, f) == 2;
+  const size_t n = (size_t)(N * G);
+  for (size_t o = 0; ok && o < n;) {
+    const size_t c = std::min<size_t>(n - o, (size_t)1 << 26);
+    ok = fwrite(Y + o, 4, c, f) == c;
+    o += c;
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("write failed: ") + path).c_str());
+  return BUSSEQ_OK;
+}
+
 int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
   if (!path || !out || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
+  {
+    const int fd = open(path, O_RDONLY);
+    if (fd >= 0) {
+      char magic[8];
+      const off_t size = lseek(fd, 0, SEEK_END);
+      const bool bin = size >= kBinHeader && pread(fd, magic, 8, 0) == 8 && memcmp(magic, kBinMagic, 8) == 0;
+      int r = BUSSEQ_OK;
+      if (bin) {
+        r = host_little_endian() ? read_counts_binary(fd, path, N, G, (int64_t)size, out)
+                                 : busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
+      }
+      close(fd);
+      if (bin) {
+        if (r != BUSSEQ_OK) return r;
+        for (int64_t i = 0; i < N * G; ++i)
+          if (out[i] < 0) return busseq_internal_set_error(BUSSEQ_ERR_IO, "negative count in the count file");
+        return BUSSEQ_OK;
+      }
+    }
+  }
   FILE* f = fopen(path, "rb");
   if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open count file ") + path).c_str());
   fseek(f, 0, SEEK_END);

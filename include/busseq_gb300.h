@@ -299,8 +299,14 @@ int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_i
 /* ---- files (the reference's formats) -------------------------------------- */
 
 /* Parses a whitespace-separated N x G integer count file (BUSseq_gpu.cu:1143-1161)
- * with all host threads. */
+ * with all host threads.  A file that starts with "BUSSEQY1" is read as binary
+ * counts instead (see busseq_write_counts_binary). */
 int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out);
+
+/* Writes Y [N*G] as a binary count file: the 8 bytes "BUSSEQY1", int64 N,
+ * int64 G, then the N*G int32 counts row-major, little-endian (not in the
+ * reference; a text count file converted once loads without parsing). */
+int busseq_write_counts_binary(const char* path, int64_t N, int64_t G, const int32_t* Y);
 
 /* Writes the _post_*, _BIC and (print_preserved) _preserved_* files with the
  * reference's names and formats (BUSseq_gpu.cu:1610-2018). */

@@ -64,6 +64,30 @@ def test_read_counts_large_parallel(tmp_path):
     np.testing.assert_array_equal(bq.read_counts(str(p), 1200, 900), Y)
 
 
+def test_binary_counts_roundtrip_and_errors(tmp_path):
+    Y, _, _ = bq.simulate([400, 300], 700, 3, 9)
+    p = str(tmp_path / "y.bin")
+    bq.write_counts_binary(p, Y)
+    np.testing.assert_array_equal(bq.read_counts(p, 700, 700), Y)
+    with open(p, "rb") as f:
+        head = f.read(24)
+    assert head[:8] == b"BUSSEQY1"
+    assert np.frombuffer(head[8:], "<i8").tolist() == [700, 700]
+    with pytest.raises(bq.BusseqError):
+        bq.read_counts(p, 700, 699)              # other dimensions
+    trunc = str(tmp_path / "t.bin")
+    with open(p, "rb") as f, open(trunc, "wb") as g:
+        g.write(f.read(24 + 4 * 1000))
+    with pytest.raises(bq.BusseqError):
+        bq.read_counts(trunc, 700, 700)          # truncated payload
+    neg = np.array(Y)
+    neg[3, 5] = -1
+    pn = str(tmp_path / "n.bin")
+    bq.write_counts_binary(pn, neg)
+    with pytest.raises(bq.BusseqError):
+        bq.read_counts(pn, 700, 700)             # negative count
+
+
 def test_simulate_deterministic_and_model_shaped():
     a = bq.simulate([50, 40, 30], 400, 4, 123)
     b = bq.simulate([50, 40, 30], 400, 4, 123)

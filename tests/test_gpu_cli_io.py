@@ -1,0 +1,30 @@
+"""The command line with binary count input: a run from the binary file writes
+the same output files as the run from the reference's text format."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import busseq_gpu_gb300 as bq
+
+pytestmark = pytest.mark.gpu
+
+
+def test_binary_and_text_counts_give_identical_outputs(tmp_path):
+    n_b, G, K = [30, 25, 20], 90, 3
+    Y, _, _ = bq.simulate(n_b, G, K, 4)
+    txt, binf, dim = tmp_path / "c.txt", str(tmp_path / "c.bin"), tmp_path / "dim.txt"
+    np.savetxt(txt, Y, fmt="%d", delimiter=" ")
+    bq.write_counts_binary(binf, Y)
+    dim.write_text("\n".join(str(x) for x in n_b))
+    for src, tag in ((str(txt), "t"), (binf, "b")):
+        r = subprocess.run([bq.CLI_PATH, "-B", "3", "-N", str(dim), "-G", str(G), "-K", str(K), "-s", "3", "-c", src,
+                            "-i", "20", "-b", "10", "-u", "5", "-p", "-o", str(tmp_path / tag)],
+                           stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+    names = sorted(f[1:] for f in os.listdir(tmp_path) if f.startswith("t_"))
+    assert len(names) == 23
+    for suffix in names:
+        with open(str(tmp_path / "t") + suffix) as a, open(str(tmp_path / "b") + suffix) as b:
+            assert a.read() == b.read(), suffix
