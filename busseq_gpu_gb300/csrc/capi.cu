@@ -129,6 +129,9 @@ int check_device_error(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
+// CTAs of the per-(batch, gene) static kernels of the HMC pass (one warp each).
+unsigned hmc_static_blocks(const bq::DevState& s) { return blocks_for((int64_t)s.B * s.G * 32, 256); }
+
 // Enqueue kernel `which` of a sweep on `st` (used for graph capture, for
 // profiling and for single stages).
 int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const bq::DevState& s) {
@@ -196,6 +199,8 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
     }
     case KID_HMC_GRAD:
     case KID_HMC_GRAD_START:
+      k_hmc_grad_static<<<hmc_static_blocks(s), 256, 0, st>>>(s, which == KID_HMC_GRAD_START ? 1 : 0);
+      LAUNCH_CHECK("k_hmc_grad_static");
       if (which == KID_HMC_GRAD_START) k_hmc_grad_metric<<<gene_grid, GENE_TILE, 0, st>>>(s, 1);
       else k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_grad");
@@ -219,6 +224,10 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_refresh_E");
       break;
     case KID_HMC_DLL:
+      k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_dll_prep");
+      k_hmc_dll_static<<<hmc_static_blocks(s), 256, 0, st>>>(s, s.n_tiles * s.cap_g);
+      LAUNCH_CHECK("k_hmc_dll_static");
       k_hmc_dll<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_dll");
       break;
@@ -227,7 +236,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_energy");
       break;
     case KID_HMC_ACCEPT:
-      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
+      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g + hmc_static_blocks(s), (int)blocks_for(s.hmc_D, 256),
                                       (int)blocks_for(s.G * 32, 256), 0);
       LAUNCH_CHECK("k_hmc_accept");
       break;
@@ -488,7 +497,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_part, (int64_t)s.cap_g * bq::NSLOT * Gp));
       TRY(h->alloc(&s.hmc_cpart, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_cpartw, (int64_t)s.n_tiles * N));
-      TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g));
+      TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g + hmc_static_blocks(s)));
+      TRY(h->alloc(&s.hmc_sbig, 2 * (int64_t)B * Gp));
       TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
       TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
       TRY(h->alloc(&s.hmc_fis, s.hmc_D));
@@ -610,8 +620,9 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     bq::k_init_finish<<<blocks_for(nfin, 256), 256, 0, h->stream>>>(s, 1);
     LAUNCH_CHECK("k_init_finish");
     CUDA_TRY(cudaMemcpyAsync(s.X, s.Y, (size_t)N * Gp * sizeof(int32_t), cudaMemcpyDeviceToDevice, h->stream));
-    if (s.hmc_L == 0) {
-      // static tables of the phi update: counts of small Y, the larger Y in cell order
+    {
+      // static tables of the phi update and of the HMC log-likelihood change:
+      // counts of small Y, the larger Y in cell order
       const int64_t nbg = (int64_t)B * G;
       TRY(h->alloc(&s.phi_cnt, (int64_t)B * bq::PHI_TAB * Gp));
       TRY(h->alloc(&s.phi_static, B * Gp));
@@ -1380,6 +1391,7 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   std::vector<float> mass_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
+  bq::k_hmc_grad_static<<<hmc_static_blocks(s), 256, 0, h->stream>>>(s, 2);
   bq::k_hmc_grad_metric<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
   bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);
@@ -1418,10 +1430,13 @@ int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* 
   if (e == cudaSuccess) {
     const dim3 gene_grid(s.n_tiles, s.cap_g);
     bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
+    bq::k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, h->stream>>>(s);
+    bq::k_hmc_dll_static<<<hmc_static_blocks(s), 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g);
     bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
     bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
     if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0);
-    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, (int)blocks_for(s.hmc_D, 256),
+    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g + hmc_static_blocks(s),
+                                               (int)blocks_for(s.hmc_D, 256),
                                                (int)blocks_for(s.G * 32, 256), 1);
     e = cudaGetLastError();
   }

@@ -46,10 +46,13 @@ __global__ void k_zlist_gather_x(DevState s, int32_t* out);
 __global__ void k_hmc_grad(DevState s);
 __global__ void k_hmc_grad_metric(DevState s, int metric_mode);
 __global__ void k_hmc_assemble(DevState s, int metric_mode);
+__global__ void k_hmc_grad_static(DevState s, int metric_mode);
 __global__ void k_hmc_start(DevState s);
 __global__ void k_hmc_leap(DevState s, int first);
 __global__ void k_hmc_refresh_E(DevState s);
 __global__ void k_hmc_dll(DevState s);
+__global__ void k_hmc_dll_prep(DevState s);
+__global__ void k_hmc_dll_static(DevState s, int base);
 __global__ void k_hmc_energy(DevState s, int kick);
 __global__ void k_hmc_accept(DevState s, int n_hpart, int n_epart, int n_epart_b, int mode);
 __global__ void k_hmc_metric_blocks(DevState s, int metric_mode);
