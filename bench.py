@@ -491,7 +491,7 @@ def main():
     big = {k: v for k, v in prof.items() if k in ("k_zx", "k_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w",
                                                   "k_hmc_grad", "k_hmc_dll")}
     dom = max(big, key=big.get)
-    kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(16)].index(dom)
+    kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(64)].index(dom)
     alg_bytes = s.kernel_bytes(kid)
     n_launch = hmc if dom == "k_hmc_grad" else 1  # launches of the kernel per sweep (one per leapfrog step)
     ms_launch = prof[dom] / n_launch

@@ -53,8 +53,9 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish", "k_hmc_metric_blocks",
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
-                                    "k_hmc_assemble_start"};
-constexpr int kNumKernels = 31;
+                                    "k_hmc_assemble_start", "k_phi_static", "k_hmc_grad_static",
+                                    "k_hmc_dll_static", "k_hmc_grad_static_start"};
+constexpr int kNumKernels = 35;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -62,7 +63,8 @@ enum : int {
   KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
-  KID_HMC_ASSEMBLE_START = 30
+  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_GRAD_STATIC = 32, KID_HMC_DLL_STATIC = 33,
+  KID_HMC_GRAD_STATIC_START = 34
 };
 
 }  // namespace
@@ -129,8 +131,10 @@ int check_device_error(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
-// CTAs of the per-(batch, gene) static kernels of the HMC pass (one warp each).
-unsigned hmc_static_blocks(const bq::DevState& s) { return blocks_for((int64_t)s.B * s.G * 32, 256); }
+// CTAs of the per-(batch, gene) static kernels: one wave, warps striding over
+// the (batch, gene) pairs.
+constexpr unsigned STATIC_CTAS = 152 * 8;
+unsigned hmc_static_blocks(const bq::DevState&) { return STATIC_CTAS; }
 
 // Enqueue kernel `which` of a sweep on `st` (used for graph capture, for
 // profiling and for single stages).
@@ -172,11 +176,23 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_delta");
       break;
     case 8:
-      if (!s.phi_cnt) return fail(BUSSEQ_ERR_STATE, "the random-walk phi update is not set up on an HMC handle");
-      k_phi_static<<<blocks_for((int64_t)s.B * s.G * 32, 256), 256, 0, st>>>(s);
-      LAUNCH_CHECK("k_phi_static");
       k_phi<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_phi");
+      break;
+    case KID_PHI_STATIC:
+      k_phi_static<<<STATIC_CTAS, 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_phi_static");
+      break;
+    case KID_HMC_GRAD_STATIC:
+    case KID_HMC_GRAD_STATIC_START:
+      k_hmc_grad_static<<<STATIC_CTAS, 256, 0, st>>>(s, which == KID_HMC_GRAD_STATIC_START ? 1 : 0);
+      LAUNCH_CHECK("k_hmc_grad_static");
+      break;
+    case KID_HMC_DLL_STATIC:
+      k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      LAUNCH_CHECK("k_hmc_dll_prep");
+      k_hmc_dll_static<<<STATIC_CTAS, 256, 0, st>>>(s, s.n_tiles * s.cap_g);
+      LAUNCH_CHECK("k_hmc_dll_static");
       break;
     case 9:
       k_decide_phi<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
@@ -199,8 +215,6 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
     }
     case KID_HMC_GRAD:
     case KID_HMC_GRAD_START:
-      k_hmc_grad_static<<<hmc_static_blocks(s), 256, 0, st>>>(s, which == KID_HMC_GRAD_START ? 1 : 0);
-      LAUNCH_CHECK("k_hmc_grad_static");
       if (which == KID_HMC_GRAD_START) k_hmc_grad_metric<<<gene_grid, GENE_TILE, 0, st>>>(s, 1);
       else k_hmc_grad<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_grad");
@@ -224,10 +238,6 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_refresh_E");
       break;
     case KID_HMC_DLL:
-      k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
-      LAUNCH_CHECK("k_hmc_dll_prep");
-      k_hmc_dll_static<<<hmc_static_blocks(s), 256, 0, st>>>(s, s.n_tiles * s.cap_g);
-      LAUNCH_CHECK("k_hmc_dll_static");
       k_hmc_dll<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_dll");
       break;
@@ -279,7 +289,8 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
     const bool blocks = h->s.hmc_nb > 0;
-    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START, KID_HMC_MASS};
+    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_STATIC_START, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START,
+         KID_HMC_MASS};
     if (blocks) q.push_back(KID_HMC_METRIC_BLOCKS);
     q.push_back(KID_HMC_START);
     if (blocks) q.push_back(KID_HMC_START_BLOCKS);
@@ -287,16 +298,21 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
       q.push_back(l == 0 ? KID_HMC_LEAP0 : KID_HMC_LEAP);
       if (blocks) q.push_back(l == 0 ? KID_HMC_LEAP_BLOCKS0 : KID_HMC_LEAP_BLOCKS);
       q.push_back(KID_HMC_E);
+      q.push_back(KID_HMC_GRAD_STATIC);
       q.push_back(KID_HMC_GRAD);
       q.push_back(KID_HMC_ASSEMBLE);
     }
+    q.push_back(KID_HMC_DLL_STATIC);
     q.push_back(KID_HMC_DLL);
     q.push_back(KID_HMC_ENERGY);
     if (blocks) q.push_back(KID_HMC_ENERGY_BLOCKS);
     const int tail[] = {KID_HMC_ACCEPT, KID_HMC_FINISH, KID_HMC_E, KID_W, KID_SORT_PI};
     q.insert(q.end(), tail, tail + 5);
   } else {
-    for (int k = 0; k <= KID_SORT_PI; ++k) q.push_back(k);
+    for (int k = 0; k <= KID_SORT_PI; ++k) {
+      if (k == KID_PHI) q.push_back(KID_PHI_STATIC);
+      q.push_back(k);
+    }
   }
   if (kept) q.push_back(KID_POSTERIOR);
   return q;
@@ -1041,7 +1057,7 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
     case BUSSEQ_STAGE_PHI:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_PHI);
       LAUNCH_CHECK("k_propose");
-      TRY(run({8, 9}));
+      TRY(run({KID_PHI_STATIC, 8, 9}));
       break;
     case BUSSEQ_STAGE_W:
       TRY(run({10}));
@@ -1391,7 +1407,7 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   std::vector<float> mass_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
-  bq::k_hmc_grad_static<<<hmc_static_blocks(s), 256, 0, h->stream>>>(s, 2);
+  bq::k_hmc_grad_static<<<STATIC_CTAS, 256, 0, h->stream>>>(s, 2);
   bq::k_hmc_grad_metric<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
   bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);
@@ -1431,7 +1447,7 @@ int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* 
     const dim3 gene_grid(s.n_tiles, s.cap_g);
     bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
     bq::k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, h->stream>>>(s);
-    bq::k_hmc_dll_static<<<hmc_static_blocks(s), 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g);
+    bq::k_hmc_dll_static<<<STATIC_CTAS, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g);
     bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
     bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
     if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0);

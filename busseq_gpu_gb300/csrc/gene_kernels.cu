@@ -621,27 +621,29 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
 }
 
 // The lgamma part of the phi sums of the entries with Y >= PHI_TAB, one warp
-// per (batch, gene), lanes taking the gene's values in turn, added to the part
+// per (batch, gene) (warps striding over the pairs), lanes taking the gene's
+// values in turn, added to the part
 // below the table that k_propose left in phi_static.  Fixed-order float-float
 // sums, so the result is reproducible.
 __global__ void __launch_bounds__(256) k_phi_static(DevState s) {
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (w >= (int64_t)s.B * s.G) return;  // uniform per warp
-  const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
-  if (o1 == o0) return;
-  const int b = (int)(w / s.G);
-  const int64_t g = w % s.G;
-  const int64_t pos = (int64_t)b * s.Gp + g;
-  const float ph = s.phi[pos], pp = s.phi_p[pos];
-  const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
-  KahanF acc;
-  for (int64_t q = o0 + lane; q < o1; q += 32) {
-    const float y = (float)s.phi_big_y[q];
-    acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
+  const int64_t nbg = (int64_t)s.B * s.G, nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nbg; w += nw) {  // uniform per warp
+    const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
+    if (o1 == o0) continue;
+    const int b = (int)(w / s.G);
+    const int64_t g = w % s.G;
+    const int64_t pos = (int64_t)b * s.Gp + g;
+    const float ph = s.phi[pos], pp = s.phi_p[pos];
+    const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
+    KahanF acc;
+    for (int64_t q = o0 + lane; q < o1; q += 32) {
+      const float y = (float)s.phi_big_y[q];
+      acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
+    }
+    const FF tot = ff_warp_sum(acc.ff());
+    if (lane == 0) s.phi_static[pos] += ff_value(tot);
   }
-  const FF tot = ff_warp_sum(acc.ff());
-  if (lane == 0) s.phi_static[pos] += ff_value(tot);
 }
 
 // ---------------------------------------------------------------------------

@@ -369,47 +369,48 @@ __device__ void hmc_static_dense(const DevState& s, int b, int64_t g, float ph, 
 }
 
 __global__ void __launch_bounds__(256) k_hmc_grad_static(DevState s, int metric_mode) {
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (w >= (int64_t)s.B * s.G) return;  // uniform per warp
-  const int b = (int)(w / s.G);
-  const int64_t g = w % s.G, pos = (int64_t)b * s.Gp + g;
-  const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
   const bool tri = hmc_metric_now(s, metric_mode);
-  float* out_dg = s.hmc_sbig + pos;
-  float* out_tg = s.hmc_sbig + (int64_t)s.B * s.Gp + pos;
-  if (o1 == o0) {
-    if (lane == 0) {
-      *out_dg = 0.0f;
-      if (tri) *out_tg = 0.0f;
+  const int64_t nbg = (int64_t)s.B * s.G, nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nbg; w += nw) {  // uniform per warp
+    const int b = (int)(w / s.G);
+    const int64_t g = w % s.G, pos = (int64_t)b * s.Gp + g;
+    const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
+    float* out_dg = s.hmc_sbig + pos;
+    float* out_tg = s.hmc_sbig + (int64_t)s.B * s.Gp + pos;
+    if (o1 == o0) {
+      if (lane == 0) {
+        *out_dg = 0.0f;
+        if (tri) *out_tg = 0.0f;
+      }
+      continue;
     }
-    return;
-  }
-  const float ph = s.phi[pos];
-  // sums to 32 of 1/(ph + j) and 1/(ph + j)^2, lane j taking term j
-  const float r = fast_rcp(ph + (float)lane);
-  float dg32 = r, tg32 = r * r;
+    const float ph = s.phi[pos];
+    // sums to 32 of 1/(ph + j) and 1/(ph + j)^2, lane j taking term j
+    const float r = fast_rcp(ph + (float)lane);
+    float dg32 = r, tg32 = r * r;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    dg32 += __shfl_xor_sync(0xffffffffu, dg32, o);
-    tg32 += __shfl_xor_sync(0xffffffffu, tg32, o);
-  }
-  const float z32 = ph + (float)HMC_TAB;
-  const float iz32h = fast_rcp(z32 - 0.5f);
-  const float tasym32 = trigamma_asym(z32);
-  KahanF adg, atg;
-  for (int64_t q = o0 + lane; q < o1; q += 32) {
-    const float y = (float)s.phi_big_y[q];
-    const float iz = fast_rcp(ph + y - 0.5f);
-    adg.add(dg32 + log_hw((ph + y - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f));
-    if (tri) atg.add(tg32 + (tasym32 - trigamma_asym(ph + y)));
-  }
-  const FF td = ff_warp_sum(adg.ff());
-  FF tt{0.0f, 0.0f};
-  if (tri) tt = ff_warp_sum(atg.ff());
-  if (lane == 0) {
-    *out_dg = (float)ff_value(td);
-    if (tri) *out_tg = (float)ff_value(tt);
+    for (int o = 16; o > 0; o >>= 1) {
+      dg32 += __shfl_xor_sync(0xffffffffu, dg32, o);
+      tg32 += __shfl_xor_sync(0xffffffffu, tg32, o);
+    }
+    const float z32 = ph + (float)HMC_TAB;
+    const float iz32h = fast_rcp(z32 - 0.5f);
+    const float tasym32 = trigamma_asym(z32);
+    KahanF adg, atg;
+    for (int64_t q = o0 + lane; q < o1; q += 32) {
+      const float y = (float)s.phi_big_y[q];
+      const float iz = fast_rcp(ph + y - 0.5f);
+      adg.add(dg32 + log_hw((ph + y - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f));
+      if (tri) atg.add(tg32 + (tasym32 - trigamma_asym(ph + y)));
+    }
+    const FF td = ff_warp_sum(adg.ff());
+    FF tt{0.0f, 0.0f};
+    if (tri) tt = ff_warp_sum(atg.ff());
+    if (lane == 0) {
+      *out_dg = (float)ff_value(td);
+      if (tri) *out_tg = (float)ff_value(tt);
+    }
   }
 }
 
@@ -605,15 +606,16 @@ __global__ void k_hmc_dll_prep(DevState s) {
   s.phi_static[(int64_t)b * Gp + g] = stat.value();
 }
 
-// One warp per (batch, gene): the Stirling differences of its Y >= PHI_TAB
-// values plus the part k_hmc_dll_prep left, summed per CTA (fixed order) into
-// hmc_hpart[base + blockIdx.x], next to k_hmc_dll's per-CTA partials.
+// One warp per (batch, gene) (warps striding over the pairs): the Stirling
+// differences of its Y >= PHI_TAB values plus the part k_hmc_dll_prep left,
+// summed per CTA (fixed order) into hmc_hpart[base + blockIdx.x], next to
+// k_hmc_dll's per-CTA partials.
 __global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
   __shared__ FF sw[8];
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  FF v{0.0f, 0.0f};
-  if (w < (int64_t)s.B * s.G) {  // uniform per warp
+  const int64_t nbg = (int64_t)s.B * s.G, nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  FF v{0.0f, 0.0f};  // this warp's (batch, gene) pairs, in order
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nbg; w += nw) {  // uniform per warp
     const int b = (int)(w / s.G);
     const int64_t g = w % s.G, pos = (int64_t)b * s.Gp + g;
     KahanF acc;
@@ -627,14 +629,15 @@ __global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
         acc.add(lgamma_diff_large(ph0 + y, ph1 + y, dph) - lgd0);
       }
     }
-    v = acc.ff();
+    FF f = acc.ff();
     if (lane == 0) {
       const double d = s.phi_static[pos];
       const float hi = (float)d;
-      v = ff_add(v, FF{hi, (float)(d - (double)hi)});
+      f = ff_add(f, FF{hi, (float)(d - (double)hi)});
     }
-    v = ff_warp_sum(v);
+    v = ff_add(v, f);
   }
+  v = ff_warp_sum(v);
   if (lane == 0) sw[warp] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
