@@ -179,7 +179,6 @@ struct DevState {
   float* hmc_fis;
   float* hmc_wbk;
   FF* hmc_epart_b;  // [ceil(G / 256)] per-CTA kinetic minus prior change of the gene blocks
-  float* hmc_sbig;  // [2][B][Gp] digamma / trigamma differences summed over the Y >= PHI_TAB entries
   float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   // The lgamma part of the phi ratio depends on an entry only through x, and

@@ -53,9 +53,8 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish", "k_hmc_metric_blocks",
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
-                                    "k_hmc_assemble_start", "k_phi_static", "k_hmc_grad_static",
-                                    "k_hmc_dll_static", "k_hmc_grad_static_start"};
-constexpr int kNumKernels = 35;
+                                    "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static"};
+constexpr int kNumKernels = 33;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -63,8 +62,7 @@ enum : int {
   KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
-  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_GRAD_STATIC = 32, KID_HMC_DLL_STATIC = 33,
-  KID_HMC_GRAD_STATIC_START = 34
+  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32
 };
 
 }  // namespace
@@ -183,11 +181,6 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       k_phi_static<<<STATIC_CTAS, 256, 0, st>>>(s);
       LAUNCH_CHECK("k_phi_static");
       break;
-    case KID_HMC_GRAD_STATIC:
-    case KID_HMC_GRAD_STATIC_START:
-      k_hmc_grad_static<<<STATIC_CTAS, 256, 0, st>>>(s, which == KID_HMC_GRAD_STATIC_START ? 1 : 0);
-      LAUNCH_CHECK("k_hmc_grad_static");
-      break;
     case KID_HMC_DLL_STATIC:
       k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_dll_prep");
@@ -289,8 +282,7 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
     const bool blocks = h->s.hmc_nb > 0;
-    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_STATIC_START, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START,
-         KID_HMC_MASS};
+    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START, KID_HMC_MASS};
     if (blocks) q.push_back(KID_HMC_METRIC_BLOCKS);
     q.push_back(KID_HMC_START);
     if (blocks) q.push_back(KID_HMC_START_BLOCKS);
@@ -298,7 +290,6 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
       q.push_back(l == 0 ? KID_HMC_LEAP0 : KID_HMC_LEAP);
       if (blocks) q.push_back(l == 0 ? KID_HMC_LEAP_BLOCKS0 : KID_HMC_LEAP_BLOCKS);
       q.push_back(KID_HMC_E);
-      q.push_back(KID_HMC_GRAD_STATIC);
       q.push_back(KID_HMC_GRAD);
       q.push_back(KID_HMC_ASSEMBLE);
     }
@@ -514,7 +505,6 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_cpart, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_cpartw, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g + hmc_static_blocks(s)));
-      TRY(h->alloc(&s.hmc_sbig, 2 * (int64_t)B * Gp));
       TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
       TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
       TRY(h->alloc(&s.hmc_fis, s.hmc_D));
@@ -1407,7 +1397,6 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   std::vector<float> mass_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
-  bq::k_hmc_grad_static<<<STATIC_CTAS, 256, 0, h->stream>>>(s, 2);
   bq::k_hmc_grad_metric<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
   bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);

@@ -637,9 +637,19 @@ __global__ void __launch_bounds__(256) k_phi_static(DevState s) {
     const float ph = s.phi[pos], pp = s.phi_p[pos];
     const float dl = pp - ph, lgd0 = s.phi_lgd0[pos];
     KahanF acc;
-    for (int64_t q = o0 + lane; q < o1; q += 32) {
-      const float y = (float)s.phi_big_y[q];
-      acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
+    for (int64_t q0 = o0; q0 < o1; q0 += 32 * 8) {  // eight values per lane in flight
+      int yv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t q = q0 + u * 32 + lane;
+        yv[u] = q < o1 ? __ldg(s.phi_big_y + q) : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (yv[u] >= 0) {
+          const float y = (float)yv[u];
+          acc.add(lgamma_diff_large(ph + y, pp + y, dl) - lgd0);
+        }
     }
     const FF tot = ff_warp_sum(acc.ff());
     if (lane == 0) s.phi_static[pos] += ff_value(tot);

@@ -229,20 +229,11 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
   __syncthreads();
   const char* Xg = reinterpret_cast<const char*>(s.X + g);
   const uint32_t row_bytes = (uint32_t)(Gp * sizeof(int));
-  // Y == 0 bit of the entry (row N, the padding row, is all zero): the digamma
-  // and trigamma differences of the entries with Y > 0 depend on x = Y alone
-  // and are added per (batch, gene) by k_hmc_assemble
-  const uint32_t* ym = s.y0m + (g >> 5);
-  const int64_t Gw = s.Gw;
-  const int bit = (int)(g & 31);
   KahanF ar, ap, aw, ai;
   for (int j0 = 0; j0 < len8; j0 += 8) {
     int xr[8];
     float dv[8], rv[8], wv[8];
     load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
-    uint32_t zw[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
     float fr = 0.0f, fp = 0.0f, fw = 0.0f, fi = 0.0f;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -251,11 +242,12 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
       const float mu = M * dv[u];
       const float rc = fast_rcp(ph + mu);
       const float r = ph * (xf - mu) * rc;
-      const bool y0 = (zw[u] >> bit) & 1u;
-      // psi(ph + x) - psi(ph): table, or for x >= 32 (rare among the Y == 0
-      // entries) the asymptotic series psi(z) = log(z - 1/2) + 1/(24 (z - 1/2)^2) + ...
-      float dg = y0 && x < HMC_TAB ? tdg[x][tid] : 0.0f;
-      if (y0 && x >= HMC_TAB) {
+      // psi(ph + x) - psi(ph): table, or for x >= 32 the asymptotic series
+      // psi(z) = log(z - 1/2) + 1/(24 (z - 1/2)^2) + O((z - 1/2)^-4)
+      float dg;
+      if (x < HMC_TAB) {
+        dg = tdg[x][tid];
+      } else {
         const float iz = fast_rcp(ph + xf - 0.5f);
         dg = dg32 + log_hw((ph + xf - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f);
       }
@@ -265,8 +257,7 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
       rv[u] = gv ? r : 0.0f;
       if (METRIC && adapt) {
         const float w = ph * mu * rc;
-        float tg = y0 && x < HMC_TAB ? ttg[x][tid] : 0.0f;
-        if (y0 && x >= HMC_TAB) tg = tg32 + (tasym32 - trigamma_asym(ph + xf));
+        const float tg = x < HMC_TAB ? ttg[x][tid] : tg32 + (tasym32 - trigamma_asym(ph + xf));
         const float d2 = -tg + iph - 2.0f * rc + (ph + xf) * rc * rc;  // d2 ll / d phi2
         fw += w;
         fi -= ph * (d1 + ph * d2);
@@ -325,95 +316,6 @@ __device__ __forceinline__ double hmc_prior_precision(const DevState& s, const H
 // priors (thread per coordinate).
 constexpr float HMC_MASS_FLOOR = 1e-2f;
 
-// Per (batch, gene), over the entries with Y > 0 (x = Y): the digamma
-// differences psi(phi + y) - psi(phi) and trigamma differences
-// psi'(phi) - psi'(phi + y), with the gradient pass's formulas (exact sums below
-// HMC_TAB, its asymptotic series above).  hmc_static_dense takes the counts of
-// y = 1 .. PHI_TAB-1 (one thread, counts loaded ahead of the serial sums);
-// k_hmc_grad_static the lists of larger Y (one warp each) into hmc_sbig.
-__device__ void hmc_static_dense(const DevState& s, int b, int64_t g, float ph, bool tri, float& sdg, float& stg) {
-  const int64_t Gp = s.Gp;
-  const int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
-  const float z32 = ph + (float)HMC_TAB;
-  const float iz32h = fast_rcp(z32 - 0.5f);
-  const float tasym32 = trigamma_asym(z32);
-  KahanF adg, atg;
-  float dg = 0.0f, tg = 0.0f;  // sums over j < y of 1/(ph + j) and 1/(ph + j)^2
-  for (int x0 = 0; x0 < PHI_TAB; x0 += 16) {
-    int c[16];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) c[u] = __ldg(cnt + (int64_t)(x0 + u) * Gp);
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int y = x0 + u;
-      float dgy = dg, tgy = tg;
-      if (y >= HMC_TAB) {
-        const float yf = (float)y;
-        const float iz = fast_rcp(ph + yf - 0.5f);
-        dgy = dg + log_hw((ph + yf - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f);
-        if (tri) tgy = tg + (tasym32 - trigamma_asym(ph + yf));
-      }
-      if (c[u]) {
-        adg.add((float)c[u] * dgy);
-        if (tri) atg.add((float)c[u] * tgy);
-      }
-      if (y < HMC_TAB) {  // after y = HMC_TAB - 1 these hold the sums to 32
-        const float r = fast_rcp(ph + (float)y);
-        dg += r;
-        tg = fmaf(r, r, tg);
-      }
-    }
-  }
-  sdg = (float)adg.value();
-  stg = tri ? (float)atg.value() : 0.0f;
-}
-
-__global__ void __launch_bounds__(256) k_hmc_grad_static(DevState s, int metric_mode) {
-  const int lane = threadIdx.x & 31;
-  const bool tri = hmc_metric_now(s, metric_mode);
-  const int64_t nbg = (int64_t)s.B * s.G, nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nbg; w += nw) {  // uniform per warp
-    const int b = (int)(w / s.G);
-    const int64_t g = w % s.G, pos = (int64_t)b * s.Gp + g;
-    const int64_t o0 = s.phi_big_off[w], o1 = s.phi_big_off[w + 1];
-    float* out_dg = s.hmc_sbig + pos;
-    float* out_tg = s.hmc_sbig + (int64_t)s.B * s.Gp + pos;
-    if (o1 == o0) {
-      if (lane == 0) {
-        *out_dg = 0.0f;
-        if (tri) *out_tg = 0.0f;
-      }
-      continue;
-    }
-    const float ph = s.phi[pos];
-    // sums to 32 of 1/(ph + j) and 1/(ph + j)^2, lane j taking term j
-    const float r = fast_rcp(ph + (float)lane);
-    float dg32 = r, tg32 = r * r;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      dg32 += __shfl_xor_sync(0xffffffffu, dg32, o);
-      tg32 += __shfl_xor_sync(0xffffffffu, tg32, o);
-    }
-    const float z32 = ph + (float)HMC_TAB;
-    const float iz32h = fast_rcp(z32 - 0.5f);
-    const float tasym32 = trigamma_asym(z32);
-    KahanF adg, atg;
-    for (int64_t q = o0 + lane; q < o1; q += 32) {
-      const float y = (float)s.phi_big_y[q];
-      const float iz = fast_rcp(ph + y - 0.5f);
-      adg.add(dg32 + log_hw((ph + y - 0.5f) * iz32h) + (iz * iz - iz32h * iz32h) * (1.0f / 24.0f));
-      if (tri) atg.add(tg32 + (tasym32 - trigamma_asym(ph + y)));
-    }
-    const FF td = ff_warp_sum(adg.ff());
-    FF tt{0.0f, 0.0f};
-    if (tri) tt = ff_warp_sum(atg.ff());
-    if (lane == 0) {
-      *out_dg = (float)ff_value(td);
-      if (tri) *out_tg = (float)ff_value(tt);
-    }
-  }
-}
-
 __global__ void k_hmc_assemble(DevState s, int metric_mode) {
   const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= s.hmc_D) return;
@@ -462,20 +364,9 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode) {
           sp += hmc_seg_sum(s, c.seg, k, 1, g);
           if (adapt) si += hmc_seg_sum(s, c.seg, k, 3, g);
         }
-        const float phf = s.phi[(int64_t)c.seg * s.Gp + g];
-        const double ph = phf;
-        // the entries with Y > 0: sum_y count(y) psi-differences (and psi'-differences)
-        float sdg, stg;
-        hmc_static_dense(s, c.seg, g, phf, adapt, sdg, stg);
-        const int64_t pos = (int64_t)c.seg * s.Gp + g;
-        sdg += s.hmc_sbig[pos];
-        gr = (double)sp + ph * (double)sdg + KAPPA_PHI - TAU_PHI * ph;
-        if (adapt) {
-          stg += s.hmc_sbig[(int64_t)s.B * s.Gp + pos];
-          m = (double)si - ph * (double)sdg + ph * ph * (double)stg + TAU_PHI * ph;
-        } else {
-          m = si + TAU_PHI * ph;
-        }
+        const double ph = s.phi[(int64_t)c.seg * s.Gp + g];
+        gr = sp + KAPPA_PHI - TAU_PHI * ph;
+        m = si + TAU_PHI * ph;
         break;
       }
       default: {  // delta
@@ -624,9 +515,19 @@ __global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
       float ph0, ph1, dph;
       hmc_phi_pair(s, b, g, ph0, ph1, dph);
       const float lgd0 = s.phi_lgd0[pos];
-      for (int64_t q = o0 + lane; q < o1; q += 32) {
-        const float y = (float)s.phi_big_y[q];
-        acc.add(lgamma_diff_large(ph0 + y, ph1 + y, dph) - lgd0);
+      for (int64_t q0 = o0; q0 < o1; q0 += 32 * 8) {  // eight values per lane in flight
+        int yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int64_t q = q0 + u * 32 + lane;
+          yv[u] = q < o1 ? __ldg(s.phi_big_y + q) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (yv[u] >= 0) {
+            const float y = (float)yv[u];
+            acc.add(lgamma_diff_large(ph0 + y, ph1 + y, dph) - lgd0);
+          }
       }
     }
     FF f = acc.ff();

@@ -46,7 +46,6 @@ __global__ void k_zlist_gather_x(DevState s, int32_t* out);
 __global__ void k_hmc_grad(DevState s);
 __global__ void k_hmc_grad_metric(DevState s, int metric_mode);
 __global__ void k_hmc_assemble(DevState s, int metric_mode);
-__global__ void k_hmc_grad_static(DevState s, int metric_mode);
 __global__ void k_hmc_start(DevState s);
 __global__ void k_hmc_leap(DevState s, int first);
 __global__ void k_hmc_refresh_E(DevState s);
