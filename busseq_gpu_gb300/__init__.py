@@ -217,6 +217,20 @@ def autotune_chunk(Y, n_b, K: int, seed: int = 0, candidates=(64, 128, 192, 256)
     return int(best.value), {int(c): float(m) for c, m in zip(cand, ms)}
 
 
+def estimate_buffers(B: int, K: int, G: int, N: int, with_XZ: bool = True, alloc=np.zeros) -> dict:
+    """Arrays of the shapes and types Sampler.estimates() fills; ``alloc(shape,
+    dtype)`` may return pinned host memory (for instance through torch) to speed
+    up the copies of X and Z."""
+    o = {"gamma": alloc((2, B), np.float64), "alpha": alloc((G,), np.float64),
+         "L": alloc((max(K - 1, 1), G), np.float64), "beta": alloc((K, G), np.float64),
+         "p_tau0": alloc((2,), np.float64), "nu": alloc((B, G), np.float64), "delta": alloc((N,), np.float64),
+         "phi": alloc((B, G), np.float64), "W": alloc((N,), np.int32), "pi": alloc((B, K), np.float64)}
+    if with_XZ:
+        o["X"] = alloc((N, G), np.int32)
+        o["Z"] = alloc((N, G), np.int32)
+    return o
+
+
 class Batch:
     """Chains (Samplers on one GPU, begun with the same run length) whose sweeps
     are launched together as one CUDA graph per sweep; each chain's draws are
@@ -330,17 +344,21 @@ class Sampler:
         _check(lib().busseq_finish(self._h))
 
     # -- results ---------------------------------------------------------------
-    def estimates(self, with_XZ: bool = True) -> dict:
-        B, K, G, N = self.B, self.K, self.G, self.N
-        o = {"gamma": np.zeros((2, B)), "alpha": np.zeros(G), "L": np.zeros((max(K - 1, 1), G)),
-             "beta": np.zeros((K, G)), "p_tau0": np.zeros(2), "nu": np.zeros((B, G)), "delta": np.zeros(N),
-             "phi": np.zeros((B, G)), "W": np.zeros(N, np.int32), "pi": np.zeros((B, K))}
+    def estimate_buffers(self, with_XZ: bool = True, alloc=np.zeros) -> dict:
+        return estimate_buffers(self.B, self.K, self.G, self.N, with_XZ, alloc)
+
+    def estimates(self, with_XZ: bool = True, out: dict | None = None) -> dict:
+        """Posterior estimates (and the last sweep's X and Z), into ``out`` when
+        given (arrays from estimate_buffers)."""
+        o = out if out is not None else self.estimate_buffers(with_XZ)
         e = Estimates()
         for k, v in o.items():
+            if k in ("X", "Z"):
+                continue
+            assert v.flags.c_contiguous
             setattr(e, k, _p(v, _PI32 if v.dtype == np.int32 else _PD))
-        if with_XZ:
-            o["X"] = np.zeros((N, G), np.int32)
-            o["Z"] = np.zeros((N, G), np.int32)
+        if "X" in o:
+            assert o["X"].flags.c_contiguous and o["Z"].flags.c_contiguous
             e.X, e.Z = _p(o["X"], _PI32), _p(o["Z"], _PI32)
         _check(lib().busseq_get_estimates(self._h, C.byref(e)))
         return o

@@ -326,6 +326,26 @@ int zmask_from_zval(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
+// Z as a dense host table [N][G] of int32 (esize 4) or uint8 (esize 1),
+// unpacked from the bit mask on the device.
+int z_to_host(busseq_handle* h, void* dst, int esize) {
+  const bq::DevState& s = h->s;
+  TRY(zmask_from_zval(h));
+  const size_t bytes = (size_t)s.N * s.G * esize;
+  void* d = nullptr;
+  CUDA_TRY(cudaMallocAsync(&d, bytes, h->stream));
+  const unsigned grid = std::min<unsigned>(blocks_for(s.N * s.Gw, 256), 152 * 16);
+  if (esize == 4) bq::k_z_dense_i32<<<grid, 256, 0, h->stream>>>(s, static_cast<int32_t*>(d), s.G);
+  else bq::k_z_dense_u8<<<grid, 256, 0, h->stream>>>(s, static_cast<uint8_t*>(d), s.G);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, h->stream);
+  const cudaError_t e2 = cudaFreeAsync(d, h->stream);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "Z table: %s", cudaGetErrorString(e));
+  return BUSSEQ_OK;
+}
+
 int capture(busseq_handle* h, int kept, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   CUDA_TRY(cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal));
@@ -797,13 +817,7 @@ int busseq_get_estimates(busseq_handle* h, busseq_estimates* o) {
   TRY(cp(o->W, e.W, N * sizeof(int32_t)));
   TRY(cp(o->pi, e.pi, B * K * sizeof(double)));
   if (o->X) CUDA_TRY(cudaMemcpy2D(o->X, G * 4, s.X, s.Gp * 4, G * 4, N, cudaMemcpyDeviceToHost));
-  if (o->Z) {
-    TRY(zmask_from_zval(h));
-    std::vector<uint32_t> zm((size_t)N * s.Gw);
-    CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < N; ++i)
-      for (int64_t g = 0; g < G; ++g) o->Z[i * G + g] = (zm[i * s.Gw + (g >> 5)] >> (g & 31)) & 1u;
-  }
+  if (o->Z) TRY(z_to_host(h, o->Z, 4));
   return BUSSEQ_OK;
 }
 
@@ -938,13 +952,7 @@ int busseq_get_state(busseq_handle* h, busseq_state* o) {
     return BUSSEQ_OK;
   };
   TRY(rows(o->X, s.X, 4, N));
-  if (o->Z) {
-    TRY(zmask_from_zval(h));
-    std::vector<uint32_t> zm((size_t)N * s.Gw);
-    CUDA_TRY(cudaMemcpy(zm.data(), s.zm, zm.size() * 4, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < N; ++i)
-      for (int64_t g = 0; g < G; ++g) o->Z[i * G + g] = (uint8_t)((zm[i * s.Gw + (g >> 5)] >> (g & 31)) & 1u);
-  }
+  if (o->Z) TRY(z_to_host(h, o->Z, 1));
   TRY(flat(o->W, s.W, N * 4));
   TRY(rows(o->L, s.L, 1, K));
   TRY(flat(o->alpha, s.alpha, G * 4));

@@ -352,6 +352,30 @@ __global__ void k_zx_summary_zeros(DevState s, int n_kept, float* x_mean, float*
   }
 }
 
+// Z as a dense [N][ld] table from the bit mask [N][Gw]: one thread per mask
+// word, 32 outputs each (int32 for the estimates, uint8 for the state).
+__global__ void k_z_dense_i32(DevState s, int32_t* out, int64_t ld) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < s.N * s.Gw; t += stride) {
+    const int64_t i = t / s.Gw, w = t - i * s.Gw;
+    const uint32_t m = s.zm[t];
+    const int64_t g0 = w * 32;
+    const int n = (int)(s.G - g0 < 32 ? s.G - g0 : 32);
+    for (int j = 0; j < n; ++j) out[i * ld + g0 + j] = (int32_t)((m >> j) & 1u);
+  }
+}
+
+__global__ void k_z_dense_u8(DevState s, uint8_t* out, int64_t ld) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < s.N * s.Gw; t += stride) {
+    const int64_t i = t / s.Gw, w = t - i * s.Gw;
+    const uint32_t m = s.zm[t];
+    const int64_t g0 = w * 32;
+    const int n = (int)(s.G - g0 < 32 ? s.G - g0 : 32);
+    for (int j = 0; j < n; ++j) out[i * ld + g0 + j] = (uint8_t)((m >> j) & 1u);
+  }
+}
+
 __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
