@@ -132,7 +132,6 @@ int check_device_error(busseq_handle* h) {
 // CTAs of the per-(batch, gene) static kernels: one wave, warps striding over
 // the (batch, gene) pairs.
 constexpr unsigned STATIC_CTAS = 152 * 8;
-unsigned hmc_static_blocks(const bq::DevState&) { return STATIC_CTAS; }
 
 // Enqueue kernel `which` of a sweep on `st` (used for graph capture, for
 // profiling and for single stages).
@@ -239,7 +238,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_energy");
       break;
     case KID_HMC_ACCEPT:
-      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g + hmc_static_blocks(s), (int)blocks_for(s.hmc_D, 256),
+      k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g + STATIC_CTAS, (int)blocks_for(s.hmc_D, 256),
                                       (int)blocks_for(s.G * 32, 256), 0);
       LAUNCH_CHECK("k_hmc_accept");
       break;
@@ -524,7 +523,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_part, (int64_t)s.cap_g * bq::NSLOT * Gp));
       TRY(h->alloc(&s.hmc_cpart, (int64_t)s.n_tiles * N));
       TRY(h->alloc(&s.hmc_cpartw, (int64_t)s.n_tiles * N));
-      TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g + hmc_static_blocks(s)));
+      TRY(h->alloc(&s.hmc_hpart, (int64_t)s.n_tiles * s.cap_g + STATIC_CTAS));
       TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
       TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
       TRY(h->alloc(&s.hmc_fis, s.hmc_D));
@@ -1448,7 +1447,7 @@ int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* 
     bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
     bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
     if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0);
-    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g + hmc_static_blocks(s),
+    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g + STATIC_CTAS,
                                                (int)blocks_for(s.hmc_D, 256),
                                                (int)blocks_for(s.G * 32, 256), 1);
     e = cudaGetLastError();
