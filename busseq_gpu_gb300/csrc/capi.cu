@@ -1,7 +1,6 @@
 // C ABI of the GB300 BUSseq sampler: memory, initialisation, CUDA-graph
 // sweeps, stages, summaries.  See include/busseq_gb300.h for the contract.
-#include "busseq_gb300.h"
-#include "busseq_dev.h"
+#include "capi_internal.h"
 #include "correct_math.h"
 #include "kernels.h"
 
@@ -16,7 +15,7 @@
 #include <string>
 #include <vector>
 
-namespace {
+namespace bqc {
 
 thread_local std::string g_err;
 
@@ -30,20 +29,11 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
-#define CUDA_TRY(x)                                                                                   \
-  do {                                                                                                \
-    cudaError_t e_ = (x);                                                                             \
-    if (e_ != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_));        \
-  } while (0)
+}  // namespace bqc
 
-#define LAUNCH_CHECK(name)                                                                            \
-  do {                                                                                                \
-    cudaError_t e_ = cudaGetLastError();                                                              \
-    if (e_ != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "launch of %s: %s", name, cudaGetErrorString(e_)); \
-  } while (0)
+using namespace bqc;
 
-int64_t round_up(int64_t a, int64_t m) { return (a + m - 1) / m * m; }
-unsigned blocks_for(int64_t n, int t) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+namespace {
 
 const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha",      "k_decide_alpha",
                                     "k_beta_nu",      "k_decide_beta",  "k_decide_nu_E", "k_delta",
@@ -67,54 +57,7 @@ enum : int {
 
 }  // namespace
 
-struct busseq_handle {
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  bq::DevState s{};
-  busseq_options opt{};
-  std::vector<int32_t> n_b, off;
-  std::vector<void*> allocs;
-  // run
-  bool begun = false, finished = false;
-  int n_iter = 0, n_burnin = 0, n_unchanged = 0, iter_host = 0, n_kept = 0;
-  cudaGraphExec_t g_burn = nullptr, g_keep = nullptr;
-  std::vector<void*> run_allocs;  // accumulators and kept draws of the current run
-  // summaries
-  bq::Estimates est{};
-  double* ll_ik = nullptr;
-  double* bic_out = nullptr;
-  bool est_valid = false;
-
-  ~busseq_handle() {
-    if (g_burn) cudaGraphExecDestroy(g_burn);
-    if (g_keep) cudaGraphExecDestroy(g_keep);
-    for (void* p : run_allocs) cudaFree(p);
-    for (void* p : allocs) cudaFree(p);
-    if (own_stream) cudaStreamDestroy(own_stream);
-  }
-
-  template <class T>
-  int alloc(T** p, size_t count, bool run_scoped = false) {
-    void* q = nullptr;
-    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
-    cudaError_t e = cudaMalloc(&q, bytes);
-    if (e != cudaSuccess) return fail(BUSSEQ_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
-    e = cudaMemsetAsync(q, 0, bytes, stream);
-    if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
-    (run_scoped ? run_allocs : allocs).push_back(q);
-    *p = static_cast<T*>(q);
-    return BUSSEQ_OK;
-  }
-};
-
-#define TRY(x)                   \
-  do {                           \
-    int r_ = (x);                \
-    if (r_ != BUSSEQ_OK) return r_; \
-  } while (0)
-
-namespace {
+namespace bqc {
 
 int check_device_error(busseq_handle* h) {
   CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -387,7 +330,7 @@ int ensure_estimates(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
-}  // namespace
+}  // namespace bqc
 
 extern "C" {
 
@@ -1076,284 +1019,6 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
 // so the chain state, the run's accumulators and the sweep counters are all a
 // run needs to continue exactly where it stopped.
 // ---------------------------------------------------------------------------
-namespace {
-
-struct CkHeader {
-  char magic[8];
-  uint32_t version;
-  int32_t B, K;
-  int32_t w_update, keep_draws;
-  int32_t begun, finished, n_iter, n_burnin, n_unchanged, iter_host, iter_dev;
-  int64_t G, N, nz0;
-  uint64_t seed, y_fingerprint;
-  int32_t hmc_leapfrog, zx_summaries;
-};
-constexpr char kCkMagic[8] = {'B', 'U', 'S', 'S', 'E', 'Q', 'C', 'K'};
-constexpr uint32_t kCkVersion = 2;
-
-struct DevBlock {
-  void* p;
-  size_t bytes;
-};
-
-// The run's accumulators and kept draws, in file order (sizes as allocated by
-// busseq_begin).
-std::vector<DevBlock> run_blocks(const busseq_handle* h) {
-  const bq::DevState& s = h->s;
-  const int64_t G = s.G, N = s.N, nk = h->n_kept;
-  const int B = s.B, K = s.K;
-  std::vector<DevBlock> v = {
-      {s.acc_alpha, G * 8},     {s.acc_beta, K * G * 8},  {s.acc_L, K * G * 8},   {s.acc_nu, B * G * 8},
-      {s.acc_delta, N * 8},     {s.acc_phi, B * G * 8},   {s.acc_gamma, 2 * B * 8}, {s.acc_pi, B * K * 8},
-      {s.acc_ptau, 2 * 8},      {s.acc_wcnt, N * K * 4}};
-  if (s.keep_draws) {
-    const int64_t km = std::max(1, K - 1);
-    const std::vector<DevBlock> k = {
-        {s.keep_gamma, nk * 2 * B * 4}, {s.keep_alpha, nk * G * 4},      {s.keep_beta, nk * km * G * 4},
-        {s.keep_L, nk * km * G},        {s.keep_ptau, nk * 2 * 4},       {s.keep_nu, nk * (B - 1) * G * 4},
-        {s.keep_delta, nk * N * 4},     {s.keep_phi, nk * B * G * 4},    {s.keep_W, nk * N * 2},
-        {s.keep_pi, nk * B * K * 4}};
-    v.insert(v.end(), k.begin(), k.end());
-  }
-  if (s.acc_zn) {
-    v.push_back({s.acc_zn, (size_t)std::max<int64_t>(1, s.nz0) * 4});
-    v.push_back({s.acc_xs, (size_t)std::max<int64_t>(1, s.nz0) * 8});
-  }
-  if (s.hmc_L > 0) {  // log phi as the chain holds it, the adapted metric and the step size
-    v.push_back({s.psi, (size_t)s.B * s.Gp * 4});
-    v.push_back({s.hmc_mass, (size_t)s.hmc_D * 4});
-    v.push_back({s.hmc_sc, (size_t)bq::HS_COUNT * 8});
-    v.push_back({s.hmc_fis, (size_t)s.hmc_D * 4});
-    if (s.hmc_nb > 0) {
-      v.push_back({s.hmc_chol, (size_t)bq::HMC_BLOCK_MAX * (bq::HMC_BLOCK_MAX + 1) / 2 * s.G * 4});
-      v.push_back({s.hmc_wbk, (size_t)s.B * s.K * s.G * 4});
-      v.push_back({s.hmc_minv, (size_t)bq::HMC_BLOCK_MAX * bq::HMC_BLOCK_MAX * s.G * 4});
-    }
-  }
-  return v;
-}
-
-int y_fingerprint(busseq_handle* h, uint64_t* out) {
-  unsigned long long* d = nullptr;
-  CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), h->stream);
-  if (e == cudaSuccess) {
-    bq::k_y_fingerprint<<<152 * 8, 256, 0, h->stream>>>(h->s, d);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  cudaFree(d);
-  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "Y fingerprint: %s", cudaGetErrorString(e));
-  return BUSSEQ_OK;
-}
-
-struct File {
-  FILE* f = nullptr;
-  ~File() {
-    if (f) fclose(f);
-  }
-};
-
-int write_block(FILE* f, const void* host, uint64_t bytes, const char* path) {
-  if (fwrite(&bytes, 8, 1, f) != 1 || (bytes && fwrite(host, 1, bytes, f) != bytes))
-    return fail(BUSSEQ_ERR_IO, "cannot write %s", path);
-  return BUSSEQ_OK;
-}
-
-int read_block(FILE* f, void* host, uint64_t bytes, const char* path, const char* what) {
-  uint64_t n = 0;
-  if (fread(&n, 8, 1, f) != 1) return fail(BUSSEQ_ERR_IO, "%s: truncated before %s", path, what);
-  if (n != bytes) return fail(BUSSEQ_ERR_IO, "%s: %s holds %llu bytes, expected %llu", path, what,
-                              (unsigned long long)n, (unsigned long long)bytes);
-  if (bytes && fread(host, 1, bytes, f) != bytes) return fail(BUSSEQ_ERR_IO, "%s: truncated in %s", path, what);
-  return BUSSEQ_OK;
-}
-
-}  // namespace
-
-int busseq_checkpoint_save(busseq_handle* h, const char* path) {
-  if (!h || !path) return fail(BUSSEQ_ERR_ARG, "NULL argument");
-  CUDA_TRY(cudaSetDevice(h->device));
-  TRY(check_device_error(h));
-  const bq::DevState& s = h->s;
-  const int64_t G = s.G, N = s.N;
-  const int B = s.B, K = s.K;
-  CkHeader hd{};
-  memcpy(hd.magic, kCkMagic, 8);
-  hd.version = kCkVersion;
-  hd.B = B;
-  hd.K = K;
-  hd.G = G;
-  hd.N = N;
-  hd.nz0 = s.nz0;
-  hd.seed = h->opt.seed;
-  hd.w_update = h->opt.w_update;
-  hd.keep_draws = h->opt.keep_draws;
-  hd.hmc_leapfrog = h->s.hmc_L;
-  hd.zx_summaries = h->opt.zx_summaries ? 1 : 0;
-  hd.begun = h->begun ? 1 : 0;
-  hd.finished = h->finished ? 1 : 0;
-  hd.n_iter = h->n_iter;
-  hd.n_burnin = h->n_burnin;
-  hd.n_unchanged = h->n_unchanged;
-  hd.iter_host = h->iter_host;
-  CUDA_TRY(cudaMemcpy(&hd.iter_dev, s.iter, sizeof(int), cudaMemcpyDeviceToHost));
-  TRY(y_fingerprint(h, &hd.y_fingerprint));
-
-  // chain state: parameters through busseq_get_state, X and Z at the Y == 0 entries
-  std::vector<int32_t> W(N), zx(std::max<int64_t>(s.nz0, 1));
-  std::vector<int8_t> L((size_t)K * G);
-  std::vector<float> alpha(G), mu_alpha(G), beta((size_t)K * G), nu((size_t)B * G), mu_nu(B), delta(N),
-      mu_delta(N), phi((size_t)B * G), gamma(2 * B), pi((size_t)B * K), ptau(2);
-  std::vector<uint8_t> zval(std::max<int64_t>(s.nz0, 1));
-  busseq_state st{};
-  st.W = W.data();
-  st.L = L.data();
-  st.alpha = alpha.data();
-  st.mu_alpha = mu_alpha.data();
-  st.beta = beta.data();
-  st.nu = nu.data();
-  st.mu_nu = mu_nu.data();
-  st.delta = delta.data();
-  st.mu_delta = mu_delta.data();
-  st.phi = phi.data();
-  st.gamma = gamma.data();
-  st.pi = pi.data();
-  st.p_tau0 = ptau.data();
-  TRY(busseq_get_state(h, &st));
-  if (s.nz0 > 0) {
-    int32_t* d = nullptr;
-    CUDA_TRY(cudaMalloc(&d, s.nz0 * 4));
-    bq::k_zlist_gather_x<<<blocks_for(s.nz0, 256), 256, 0, h->stream>>>(s, d);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(zx.data(), d, s.nz0 * 4, cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(zval.data(), s.zval, s.nz0, cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(d);
-    if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "checkpoint gather: %s", cudaGetErrorString(e));
-  }
-
-  File out;
-  const std::string tmp = std::string(path) + ".tmp";
-  out.f = fopen(tmp.c_str(), "wb");
-  if (!out.f) return fail(BUSSEQ_ERR_IO, "cannot open %s for writing", tmp.c_str());
-  if (fwrite(&hd, sizeof hd, 1, out.f) != 1) return fail(BUSSEQ_ERR_IO, "cannot write %s", tmp.c_str());
-  TRY(write_block(out.f, h->n_b.data(), 4ull * B, path));
-  TRY(write_block(out.f, zx.data(), 4ull * s.nz0, path));
-  TRY(write_block(out.f, zval.data(), (uint64_t)s.nz0, path));
-  TRY(write_block(out.f, W.data(), 4ull * N, path));
-  TRY(write_block(out.f, L.data(), (uint64_t)K * G, path));
-  for (const std::vector<float>* v : {&alpha, &mu_alpha, &beta, &nu, &mu_nu, &delta, &mu_delta, &phi, &gamma, &pi,
-                                      &ptau})
-    TRY(write_block(out.f, v->data(), 4ull * v->size(), path));
-  if (h->begun) {
-    for (const DevBlock& blk : run_blocks(h)) {
-      std::vector<uint8_t> buf(blk.bytes);
-      CUDA_TRY(cudaMemcpy(buf.data(), blk.p, blk.bytes, cudaMemcpyDeviceToHost));
-      TRY(write_block(out.f, buf.data(), blk.bytes, path));
-    }
-  }
-  if (fclose(out.f) != 0) {
-    out.f = nullptr;
-    return fail(BUSSEQ_ERR_IO, "cannot write %s", tmp.c_str());
-  }
-  out.f = nullptr;
-  if (rename(tmp.c_str(), path) != 0) return fail(BUSSEQ_ERR_IO, "cannot rename %s to %s", tmp.c_str(), path);
-  return BUSSEQ_OK;
-}
-
-int busseq_checkpoint_load(busseq_handle* h, const char* path) {
-  if (!h || !path) return fail(BUSSEQ_ERR_ARG, "NULL argument");
-  CUDA_TRY(cudaSetDevice(h->device));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  bq::DevState& s = h->s;
-  const int64_t G = s.G, N = s.N;
-  const int B = s.B, K = s.K;
-  File in;
-  in.f = fopen(path, "rb");
-  if (!in.f) return fail(BUSSEQ_ERR_IO, "cannot open %s", path);
-  CkHeader hd{};
-  if (fread(&hd, sizeof hd, 1, in.f) != 1) return fail(BUSSEQ_ERR_IO, "%s: truncated header", path);
-  if (memcmp(hd.magic, kCkMagic, 8) != 0 || hd.version != kCkVersion)
-    return fail(BUSSEQ_ERR_IO, "%s is not a busseq checkpoint (version %u)", path, kCkVersion);
-  if (hd.B != B || hd.K != K || hd.G != G || hd.N != N || hd.nz0 != s.nz0)
-    return fail(BUSSEQ_ERR_ARG, "%s was written for B=%d K=%d G=%lld N=%lld, this chain has B=%d K=%d G=%lld N=%lld",
-                path, hd.B, hd.K, (long long)hd.G, (long long)hd.N, B, K, (long long)G, (long long)N);
-  if (hd.seed != h->opt.seed || hd.w_update != h->opt.w_update || hd.keep_draws != h->opt.keep_draws ||
-      hd.hmc_leapfrog != h->s.hmc_L || hd.zx_summaries != (h->opt.zx_summaries ? 1 : 0))
-    return fail(BUSSEQ_ERR_ARG, "%s was written with another seed, W move, keep_draws, HMC or zx_summaries setting",
-                path);
-  uint64_t fp = 0;
-  TRY(y_fingerprint(h, &fp));
-  if (fp != hd.y_fingerprint) return fail(BUSSEQ_ERR_ARG, "%s was written for different counts", path);
-  std::vector<int32_t> nb(B), W(N), zx(std::max<int64_t>(s.nz0, 1));
-  TRY(read_block(in.f, nb.data(), 4ull * B, path, "n_b"));
-  if (nb != h->n_b) return fail(BUSSEQ_ERR_ARG, "%s was written for other batch sizes", path);
-  std::vector<uint8_t> zval(std::max<int64_t>(s.nz0, 1));
-  std::vector<int8_t> L((size_t)K * G);
-  std::vector<float> alpha(G), mu_alpha(G), beta((size_t)K * G), nu((size_t)B * G), mu_nu(B), delta(N),
-      mu_delta(N), phi((size_t)B * G), gamma(2 * B), pi((size_t)B * K), ptau(2);
-  TRY(read_block(in.f, zx.data(), 4ull * s.nz0, path, "X"));
-  TRY(read_block(in.f, zval.data(), (uint64_t)s.nz0, path, "Z"));
-  TRY(read_block(in.f, W.data(), 4ull * N, path, "W"));
-  TRY(read_block(in.f, L.data(), (uint64_t)K * G, path, "L"));
-  const char* names[] = {"alpha", "mu_alpha", "beta", "nu", "mu_nu", "delta", "mu_delta", "phi", "gamma", "pi",
-                         "p_tau0"};
-  int ni = 0;
-  for (std::vector<float>* v : {&alpha, &mu_alpha, &beta, &nu, &mu_nu, &delta, &mu_delta, &phi, &gamma, &pi, &ptau})
-    TRY(read_block(in.f, v->data(), 4ull * v->size(), path, names[ni++]));
-  for (int64_t j = 0; j < s.nz0; ++j)
-    if (zx[j] < 0 || zval[j] > 1) return fail(BUSSEQ_ERR_IO, "%s: invalid X or Z value at entry %lld", path, (long long)j);
-
-  // the state first (busseq_set_state recomputes the derived arrays), then
-  // the run (busseq_begin resets its counters; the saved ones replace them)
-  busseq_state st{};
-  st.W = W.data();
-  st.L = L.data();
-  st.alpha = alpha.data();
-  st.mu_alpha = mu_alpha.data();
-  st.beta = beta.data();
-  st.nu = nu.data();
-  st.mu_nu = mu_nu.data();
-  st.delta = delta.data();
-  st.mu_delta = mu_delta.data();
-  st.phi = phi.data();
-  st.gamma = gamma.data();
-  st.pi = pi.data();
-  st.p_tau0 = ptau.data();
-  TRY(busseq_set_state(h, &st));
-  if (s.nz0 > 0) {
-    int32_t* d = nullptr;
-    CUDA_TRY(cudaMalloc(&d, s.nz0 * 4));
-    cudaError_t e = cudaMemcpyAsync(d, zx.data(), s.nz0 * 4, cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess) {
-      bq::k_zlist_scatter_x<<<blocks_for(s.nz0, 256), 256, 0, h->stream>>>(s, d);
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s.zval, zval.data(), s.nz0, cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(d);
-    if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "checkpoint scatter: %s", cudaGetErrorString(e));
-  }
-  if (hd.begun) {
-    if (hd.iter_host < 0 || hd.iter_host > hd.n_iter || hd.iter_dev != hd.iter_host)
-      return fail(BUSSEQ_ERR_IO, "%s: inconsistent sweep counters", path);
-    TRY(busseq_begin(h, hd.n_iter, hd.n_burnin, hd.n_unchanged));
-    for (const DevBlock& blk : run_blocks(h)) {
-      std::vector<uint8_t> buf(blk.bytes);
-      TRY(read_block(in.f, buf.data(), blk.bytes, path, "run accumulators"));
-      CUDA_TRY(cudaMemcpy(blk.p, buf.data(), blk.bytes, cudaMemcpyHostToDevice));
-    }
-    CUDA_TRY(cudaMemcpy(s.iter, &hd.iter_dev, sizeof(int), cudaMemcpyHostToDevice));
-    h->iter_host = hd.iter_host;
-  }
-  h->est_valid = false;
-  if (hd.begun && hd.finished) TRY(busseq_finish(h));
-  return check_device_error(h);
-}
-
-// ---- gradient-based block update: statistics and test entry points --------
 }  // extern "C"
 
 namespace {
@@ -1564,185 +1229,3 @@ int busseq_launches_per_sweep(busseq_handle* h, int32_t kept) {
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------
-// Batches of chains: one CUDA graph holds one sweep of every chain as
-// independent branches (forked from and joined to the batch's stream), so a
-// single launch advances all chains and the kernels of different chains run
-// concurrently, filling the SMs that one chain's small or tail-heavy kernels
-// leave idle.  Each chain keeps its own state, streams of random numbers and
-// device sweep counter, so its draws are those of the chain run alone.
-// ---------------------------------------------------------------------------
-struct busseq_batch {
-  int device = 0;
-  std::vector<busseq_handle*> hs;
-  cudaStream_t root = nullptr;
-  cudaEvent_t fork = nullptr, done = nullptr;
-  std::vector<cudaEvent_t> join;
-  cudaGraphExec_t g_burn = nullptr, g_keep = nullptr;
-  ~busseq_batch() {
-    if (g_burn) cudaGraphExecDestroy(g_burn);
-    if (g_keep) cudaGraphExecDestroy(g_keep);
-    for (cudaEvent_t e : join) cudaEventDestroy(e);
-    if (fork) cudaEventDestroy(fork);
-    if (done) cudaEventDestroy(done);
-    if (root) cudaStreamDestroy(root);
-  }
-};
-
-namespace {
-
-int capture_batch(busseq_batch* b, int kept, cudaGraphExec_t* out) {
-  cudaGraph_t g = nullptr;
-  CUDA_TRY(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
-  int r = BUSSEQ_OK;
-  cudaError_t e = cudaEventRecord(b->fork, b->root);
-  for (size_t c = 0; c < b->hs.size() && r == BUSSEQ_OK && e == cudaSuccess; ++c) {
-    busseq_handle* h = b->hs[c];
-    e = cudaStreamWaitEvent(h->own_stream, b->fork, 0);
-    if (e == cudaSuccess) r = launch_sweep(h, h->own_stream, kept);
-    if (r == BUSSEQ_OK && e == cudaSuccess) e = cudaEventRecord(b->join[c], h->own_stream);
-    if (r == BUSSEQ_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->root, b->join[c], 0);
-  }
-  const cudaError_t e_end = cudaStreamEndCapture(b->root, &g);
-  if (r != BUSSEQ_OK) {
-    if (g) cudaGraphDestroy(g);
-    return r;
-  }
-  if (e == cudaSuccess) e = e_end;
-  if (e != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
-    return fail(BUSSEQ_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
-  }
-  e = cudaGraphInstantiate(out, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
-  return BUSSEQ_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int busseq_batch_create(busseq_handle* const* hs, int32_t n, busseq_batch** out) {
-  if (!hs || !out || n <= 0) return fail(BUSSEQ_ERR_ARG, "a batch needs at least one handle");
-  *out = nullptr;
-  for (int c = 0; c < n; ++c) {
-    busseq_handle* h = hs[c];
-    if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle %d", c);
-    if (!h->begun) return fail(BUSSEQ_ERR_STATE, "handle %d: busseq_begin has not been called", c);
-    if (h->device != hs[0]->device) return fail(BUSSEQ_ERR_ARG, "handle %d is on another device", c);
-    if (h->n_iter != hs[0]->n_iter || h->n_burnin != hs[0]->n_burnin || h->iter_host != hs[0]->iter_host)
-      return fail(BUSSEQ_ERR_ARG, "handle %d: the chains of a batch need the same run length, burn-in and "
-                  "progress", c);
-    for (int d = 0; d < c; ++d)
-      if (hs[d] == h) return fail(BUSSEQ_ERR_ARG, "handle %d appears twice", c);
-  }
-  CUDA_TRY(cudaSetDevice(hs[0]->device));
-  for (int c = 0; c < n; ++c) CUDA_TRY(cudaStreamSynchronize(hs[c]->stream));
-  auto* b = new busseq_batch();
-  b->device = hs[0]->device;
-  b->hs.assign(hs, hs + n);
-  int r = BUSSEQ_OK;
-  cudaError_t e = cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
-  b->join.assign(n, nullptr);
-  for (int c = 0; c < n && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming);
-  if (e != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "batch streams: %s", cudaGetErrorString(e));
-  if (r == BUSSEQ_OK) r = capture_batch(b, 0, &b->g_burn);
-  if (r == BUSSEQ_OK) r = capture_batch(b, 1, &b->g_keep);
-  if (r != BUSSEQ_OK) {
-    delete b;
-    return r;
-  }
-  *out = b;
-  return BUSSEQ_OK;
-}
-
-int busseq_batch_sweeps(busseq_batch* b, int32_t count) {
-  if (!b) return fail(BUSSEQ_ERR_ARG, "NULL batch");
-  busseq_handle* h0 = b->hs[0];
-  for (busseq_handle* h : b->hs)
-    if (!h->begun || h->iter_host != h0->iter_host || h->n_iter != h0->n_iter || h->n_burnin != h0->n_burnin)
-      return fail(BUSSEQ_ERR_STATE, "a chain of the batch was restarted or advanced on its own");
-  if (count < 0 || h0->iter_host + count > h0->n_iter)
-    return fail(BUSSEQ_ERR_ARG, "requested sweeps exceed the run length (%d of %d done)", h0->iter_host, h0->n_iter);
-  CUDA_TRY(cudaSetDevice(b->device));
-  // order the batch after whatever the chains' own streams hold
-  for (busseq_handle* h : b->hs) {
-    CUDA_TRY(cudaEventRecord(b->done, h->stream));
-    CUDA_TRY(cudaStreamWaitEvent(b->root, b->done, 0));
-  }
-  for (int c = 0; c < count; ++c) {
-    CUDA_TRY(cudaGraphLaunch(h0->iter_host < h0->n_burnin ? b->g_burn : b->g_keep, b->root));
-    for (busseq_handle* h : b->hs) ++h->iter_host;
-  }
-  // and the chains' later work after the batch
-  CUDA_TRY(cudaEventRecord(b->done, b->root));
-  for (busseq_handle* h : b->hs) CUDA_TRY(cudaStreamWaitEvent(h->stream, b->done, 0));
-  return BUSSEQ_OK;
-}
-
-int busseq_batch_synchronize(busseq_batch* b) {
-  if (!b) return fail(BUSSEQ_ERR_ARG, "NULL batch");
-  CUDA_TRY(cudaSetDevice(b->device));
-  CUDA_TRY(cudaStreamSynchronize(b->root));
-  for (busseq_handle* h : b->hs) TRY(check_device_error(h));
-  return BUSSEQ_OK;
-}
-
-void* busseq_batch_stream(busseq_batch* b) { return b ? (void*)b->root : nullptr; }
-
-void busseq_batch_destroy(busseq_batch* b) {
-  if (!b) return;
-  cudaSetDevice(b->device);
-  if (b->root) cudaStreamSynchronize(b->root);
-  delete b;
-}
-
-// Gene-pass chunk length by measurement: for every candidate, a scratch
-// handle on the same counts (a device copy when Y is on the host) runs `warm`
-// untimed and `sweeps` timed burn-in sweeps; the fastest candidate wins.  The
-// scratch handles use the options' seed, so the caller's chains are untouched.
-int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, const busseq_options* opt,
-                          const int32_t* candidates, int32_t n_cand, int32_t sweeps, int32_t* best,
-                          double* ms_per_sweep) {
-  if (!dims || !Y || !opt || !candidates || n_cand <= 0 || sweeps <= 0 || !best)
-    return fail(BUSSEQ_ERR_ARG, "bad autotune arguments");
-  const int warm = 3;
-  double best_ms = 0.0;
-  *best = 0;
-  for (int c = 0; c < n_cand; ++c) {
-    if (candidates[c] <= 0 || candidates[c] > bq::MAX_CG)
-      return fail(BUSSEQ_ERR_ARG, "chunk candidate %d outside 1..%d", candidates[c], bq::MAX_CG);
-    busseq_options o = *opt;
-    o.chunk_cells = candidates[c];
-    o.keep_draws = 0;
-    busseq_handle* h = nullptr;
-    TRY(busseq_create(dims, Y, Y_is_device, &o, &h));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int r = busseq_begin(h, warm + sweeps, warm + sweeps, 0);
-    if (r == BUSSEQ_OK) r = busseq_sweeps(h, warm);
-    if (r == BUSSEQ_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
-      r = fail(BUSSEQ_ERR_CUDA, "cudaEventCreate failed");
-    float ms = 0.0f;
-    if (r == BUSSEQ_OK && cudaEventRecord(e0, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
-    if (r == BUSSEQ_OK) r = busseq_sweeps(h, sweeps);
-    if (r == BUSSEQ_OK && cudaEventRecord(e1, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
-    if (r == BUSSEQ_OK) r = check_device_error(h);
-    if (r == BUSSEQ_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event time");
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    busseq_destroy(h);
-    if (r != BUSSEQ_OK) return r;
-    const double per = (double)ms / sweeps;
-    if (ms_per_sweep) ms_per_sweep[c] = per;
-    if (*best == 0 || per < best_ms) {
-      best_ms = per;
-      *best = candidates[c];
-    }
-  }
-  return BUSSEQ_OK;
-}
-
-}  // extern "C"
