@@ -21,6 +21,8 @@ CASES = {
     "small_warm": ([40, 30, 30], 256, 4, 12, 25),
     "demo_warm": ([300, 300, 200, 200], 3000, 5, 13579, 30),
     "ragged_warm": ([9, 61, 17, 33, 5], 333, 5, 7, 15),
+    "minimal_warm": ([12, 9], 97, 2, 3, 10),                      # B = 2, K = 2
+    "many_types_warm": ([20, 35, 50, 25, 40, 30], 150, 12, 9, 10),  # B = 6, K = 12
 }
 
 
