@@ -231,7 +231,6 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
     for (int l = 0; l < h->s.hmc_L; ++l) {
       q.push_back(l == 0 ? KID_HMC_LEAP0 : KID_HMC_LEAP);
       if (blocks) q.push_back(l == 0 ? KID_HMC_LEAP_BLOCKS0 : KID_HMC_LEAP_BLOCKS);
-      q.push_back(KID_HMC_E);
       q.push_back(KID_HMC_GRAD);
       q.push_back(KID_HMC_ASSEMBLE);
     }

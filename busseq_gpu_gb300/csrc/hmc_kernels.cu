@@ -205,7 +205,8 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
   }
   const bool gv = g < s.G;
   const float ph = gv ? s.phi[(int64_t)b * Gp + g] : 1.0f;
-  const float M = gv ? s.E[((int64_t)b * s.K + k) * Gp + g] : 0.0f;
+  // exp(alpha + beta + nu) at the current position, as k_hmc_refresh_E forms it
+  const float M = gv ? exp_sum3(s.alpha[g], s.beta[(int64_t)k * Gp + g], s.nu[(int64_t)b * Gp + g]) : 0.0f;
   const float iph = fast_rcp(ph);
   // sum_{j<x} 1/(ph + j) (and 1/(ph + j)^2) for x < HMC_TAB
   {
