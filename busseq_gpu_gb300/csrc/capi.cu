@@ -337,6 +337,18 @@ const char* busseq_last_error(void) { return g_err.c_str(); }
 
 int busseq_internal_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// Z of the last sweep as its bit mask [N][Gw] (bit g & 31 of word g >> 5, Gw
+// words per row, padded), for the file writer.  out == NULL: only *Gw.
+int busseq_internal_zmask(busseq_handle* h, uint32_t* out, int64_t* Gw) {
+  if (!h || !Gw) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  *Gw = h->s.Gw;
+  if (!out) return BUSSEQ_OK;
+  CUDA_TRY(cudaSetDevice(h->device));
+  TRY(zmask_from_zval(h));
+  CUDA_TRY(cudaMemcpy(out, h->s.zm, (size_t)h->s.N * h->s.Gw * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  return BUSSEQ_OK;
+}
+
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
                          int32_t* kept_draws) {
   if (!h) return fail(BUSSEQ_ERR_ARG, "NULL handle");

@@ -279,6 +279,7 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
 
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
                          int32_t* kept_draws);
+int busseq_internal_zmask(busseq_handle* h, uint32_t* out, int64_t* Gw);
 
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
@@ -286,11 +287,16 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   int64_t G, N;
   int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
   if (r) return r;
-  std::vector<int32_t> Z((size_t)N * G), X((size_t)N * G), W(N);
+  std::vector<int32_t> X((size_t)N * G), W(N);
   std::vector<double> gamma(2 * B), alpha(G), L((size_t)std::max(1, K - 1) * G), beta((size_t)K * G), ptau(2),
       nu((size_t)B * G), delta(N), phi((size_t)B * G), pi((size_t)B * K);
+  // Z is formatted from its bit mask (N*G/8 bytes instead of an int table)
+  int64_t Gw = 0;
+  if ((r = busseq_internal_zmask(h, nullptr, &Gw))) return r;
+  std::vector<uint32_t> zm((size_t)N * Gw);
+  if ((r = busseq_internal_zmask(h, zm.data(), &Gw))) return r;
   busseq_estimates e{};
-  e.Z = Z.data(); e.X = X.data(); e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
+  e.X = X.data(); e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
   e.beta = beta.data(); e.p_tau0 = ptau.data(); e.nu = nu.data(); e.delta = delta.data();
   e.phi = phi.data(); e.W = W.data(); e.pi = pi.data();
   if ((r = busseq_get_estimates(h, &e))) return r;
@@ -310,7 +316,16 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
     return t;
   };
   // _post_Z, _post_X: last sweep's state (BUSseq_gpu.cu:1613-1645)
-  if ((r = write_table(pre + "_post_Z.txt", ints(Z, G)))) return r;
+  {
+    Table t;
+    t.rows = N;
+    t.cols = G;
+    t.cell = [&zm, Gw](int64_t i, int64_t g, char* b) {
+      b[0] = (char)('0' + ((zm[(size_t)(i * Gw + (g >> 5))] >> (g & 31)) & 1u));
+      return 1;
+    };
+    if ((r = write_table(pre + "_post_Z.txt", t))) return r;
+  }
   if ((r = write_table(pre + "_post_X.txt", ints(X, G)))) return r;
   if ((r = write_table(pre + "_post_gamma.txt", dbls(gamma.data(), 2, B)))) return r;
   if ((r = write_table(pre + "_post_alpha.txt", dbls(alpha.data(), G, 1)))) return r;
