@@ -17,14 +17,16 @@
 // (padding genes, beta_0, nu_0 and the first cell of each batch are fixed).
 //
 // One transition: gradient at theta0 (with the metric during its adaptation),
-// momentum p ~ N(0, M), L leapfrog steps (kick, drift, refresh of exp(.)
-// tables, gradient), a final half kick, the change of the Hamiltonian
-// (likelihood part from a cancellation-free per-entry pass, prior and kinetic
-// parts per coordinate), the Metropolis decision and, if rejected, a restore.
+// momentum p ~ N(0, M), L leapfrog steps (kick, drift, gradient; the gradient
+// pass forms exp(alpha + beta + nu) itself), a final half kick, the change of
+// the Hamiltonian (likelihood part from a cancellation-free per-entry pass,
+// prior and kinetic parts per coordinate), the Metropolis decision and, if
+// rejected, a restore; the E table is refreshed once, after the transition.
 // Step size: dual averaging (Hoffman and Gelman, JMLR 15, 2014, algorithm 5)
-// during burn-in with a random jitter of +-10 %; metric: the diagonal Fisher
-// information of the eta-coordinates and the observed information of psi,
-// recomputed at every transition of the first half of burn-in, then frozen.
+// during burn-in with a random jitter of +-10 %; metric: a block per gene over
+// (alpha, beta, nu) from the Fisher sums, the diagonal Fisher information of
+// delta and the observed information of psi, adapted at the transition starts
+// of the first half of burn-in, then frozen.
 #include "kernels_common.cuh"
 
 namespace bq {
@@ -442,7 +444,7 @@ __global__ void k_hmc_leap(DevState s, int first) {
   hmc_derived(s, c, v);
 }
 
-// E = exp(alpha + beta + nu) after the coordinates moved.
+// E = exp(alpha + beta + nu) after the transition (for the W move).
 __global__ void k_hmc_refresh_E(DevState s) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t Gp = s.Gp;
