@@ -1234,7 +1234,9 @@ double busseq_kernel_bytes(busseq_handle* h, int32_t i) {
 
 int busseq_launches_per_sweep(busseq_handle* h, int32_t kept) {
   if (!h) return 0;
-  return (int)sweep_sequence(h, kept).size();
+  int n = 0;
+  for (int k : sweep_sequence(h, kept)) n += k == KID_HMC_DLL_STATIC ? 2 : 1;  // prep + static
+  return n;
 }
 
 
