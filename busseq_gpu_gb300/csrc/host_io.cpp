@@ -280,6 +280,7 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
                          int32_t* kept_draws);
 int busseq_internal_zmask(busseq_handle* h, uint32_t* out, int64_t* Gw);
+int busseq_internal_format_x(busseq_handle* h, char** buf, int64_t* len);
 
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
@@ -287,7 +288,7 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   int64_t G, N;
   int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
   if (r) return r;
-  std::vector<int32_t> X((size_t)N * G), W(N);
+  std::vector<int32_t> W(N);
   std::vector<double> gamma(2 * B), alpha(G), L((size_t)std::max(1, K - 1) * G), beta((size_t)K * G), ptau(2),
       nu((size_t)B * G), delta(N), phi((size_t)B * G), pi((size_t)B * K);
   // Z is formatted from its bit mask (N*G/8 bytes instead of an int table)
@@ -296,7 +297,7 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   std::vector<uint32_t> zm((size_t)N * Gw);
   if ((r = busseq_internal_zmask(h, zm.data(), &Gw))) return r;
   busseq_estimates e{};
-  e.X = X.data(); e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
+  e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
   e.beta = beta.data(); e.p_tau0 = ptau.data(); e.nu = nu.data(); e.delta = delta.data();
   e.phi = phi.data(); e.W = W.data(); e.pi = pi.data();
   if ((r = busseq_get_estimates(h, &e))) return r;
@@ -326,7 +327,17 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
     };
     if ((r = write_table(pre + "_post_Z.txt", t))) return r;
   }
-  if ((r = write_table(pre + "_post_X.txt", ints(X, G)))) return r;
+  {  // the N x G table of X is formatted on the device
+    char* txt = nullptr;
+    int64_t len = 0;
+    if ((r = busseq_internal_format_x(h, &txt, &len))) return r;
+    FILE* f = fopen((pre + "_post_X.txt").c_str(), "wb");
+    const bool ok = f && (len == 0 || fwrite(txt, 1, (size_t)len, f) == (size_t)len);
+    const bool closed = f && fclose(f) == 0;
+    free(txt);
+    if (!ok || !closed)
+      return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + pre + "_post_X.txt").c_str());
+  }
   if ((r = write_table(pre + "_post_gamma.txt", dbls(gamma.data(), 2, B)))) return r;
   if ((r = write_table(pre + "_post_alpha.txt", dbls(alpha.data(), G, 1)))) return r;
   if ((r = write_table(pre + "_post_L.txt", dbls(L.data(), K - 1, G)))) return r;
