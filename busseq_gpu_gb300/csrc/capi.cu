@@ -338,9 +338,10 @@ const char* busseq_last_error(void) { return g_err.c_str(); }
 
 int busseq_internal_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
-// X of the last sweep as the text of _post_X.txt (the host writer's layout),
-// formatted on the device; *buf is malloc'ed, the caller frees it.
-int busseq_internal_format_x(busseq_handle* h, char** buf, int64_t* len) {
+// X (which = 0) or Z (which = 1) of the last sweep as the text of _post_X.txt
+// / _post_Z.txt (the host writer's layout), formatted on the device; *buf is
+// malloc'ed, the caller frees it.
+int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len) {
   if (!h || !buf || !len) return fail(BUSSEQ_ERR_ARG, "NULL argument");
   *buf = nullptr;
   *len = 0;
@@ -348,54 +349,55 @@ int busseq_internal_format_x(busseq_handle* h, char** buf, int64_t* len) {
   const bq::DevState& s = h->s;
   const int64_t N = s.N;
   if (N == 0 || s.G == 0) return BUSSEQ_OK;
+  const int32_t* M = s.X;
+  int64_t ld = s.Gp;
+  int32_t* d_z = nullptr;
+  if (which == 1) {  // Z unpacked from its bit mask into a temporary int table
+    TRY(zmask_from_zval(h));
+    CUDA_TRY(cudaMallocAsync((void**)&d_z, (size_t)N * s.G * sizeof(int32_t), h->stream));
+    bq::k_z_dense_i32<<<std::min<unsigned>(blocks_for(N * s.Gw, 256), 152 * 16), 256, 0, h->stream>>>(s, d_z, s.G);
+    M = d_z;
+    ld = s.G;
+  }
   int64_t* d_len = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&d_len, (size_t)(N + 1) * sizeof(int64_t), h->stream));
-  bq::k_fmt_row_len<<<(unsigned)N, 256, 0, h->stream>>>(s.X, s.Gp, s.G, d_len);
+  char* d_txt = nullptr;
+  char* host = nullptr;
   std::vector<int64_t> off((size_t)N + 1, 0);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(off.data() + 1, d_len, (size_t)N * sizeof(int64_t),
-                                            cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_len, (size_t)(N + 1) * sizeof(int64_t), h->stream);
+  if (e == cudaSuccess) {
+    bq::k_fmt_row_len<<<(unsigned)N, 256, 0, h->stream>>>(M, ld, s.G, d_len);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(off.data() + 1, d_len, (size_t)N * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  if (e != cudaSuccess) {
-    cudaFreeAsync(d_len, h->stream);
-    return fail(BUSSEQ_ERR_CUDA, "formatting X: %s", cudaGetErrorString(e));
+  int64_t total = 0;
+  if (e == cudaSuccess) {
+    for (int64_t i = 0; i < N; ++i) off[i + 1] += off[i];
+    total = off[N];
+    host = static_cast<char*>(malloc((size_t)total));
+    if (!host) e = cudaErrorMemoryAllocation;
   }
-  for (int64_t i = 0; i < N; ++i) off[i + 1] += off[i];
-  const int64_t total = off[N];
-  char* d_txt = nullptr;
-  char* host = static_cast<char*>(malloc((size_t)total));
-  if (!host) {
-    cudaFreeAsync(d_len, h->stream);
-    return fail(BUSSEQ_ERR_NOMEM, "cannot allocate %lld bytes for _post_X", (long long)total);
-  }
-  e = cudaMemcpyAsync(d_len, off.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_len, off.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_txt, (size_t)total, h->stream);
   if (e == cudaSuccess) {
-    bq::k_fmt_rows<<<(unsigned)N, 256, 0, h->stream>>>(s.X, s.Gp, s.G, d_len, d_txt);
+    bq::k_fmt_rows<<<(unsigned)N, 256, 0, h->stream>>>(M, ld, s.G, d_len, d_txt);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(host, d_txt, (size_t)total, cudaMemcpyDeviceToHost, h->stream);
   if (d_txt) cudaFreeAsync(d_txt, h->stream);
-  cudaFreeAsync(d_len, h->stream);
+  if (d_len) cudaFreeAsync(d_len, h->stream);
+  if (d_z) cudaFreeAsync(d_z, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     free(host);
-    return fail(BUSSEQ_ERR_CUDA, "formatting X: %s", cudaGetErrorString(e));
+    return fail(e == cudaErrorMemoryAllocation ? BUSSEQ_ERR_NOMEM : BUSSEQ_ERR_CUDA, "formatting %s: %s",
+                which ? "Z" : "X", cudaGetErrorString(e));
   }
   *buf = host;
   *len = total;
-  return BUSSEQ_OK;
-}
-
-// Z of the last sweep as its bit mask [N][Gw] (bit g & 31 of word g >> 5, Gw
-// words per row, padded), for the file writer.  out == NULL: only *Gw.
-int busseq_internal_zmask(busseq_handle* h, uint32_t* out, int64_t* Gw) {
-  if (!h || !Gw) return fail(BUSSEQ_ERR_ARG, "NULL argument");
-  *Gw = h->s.Gw;
-  if (!out) return BUSSEQ_OK;
-  CUDA_TRY(cudaSetDevice(h->device));
-  TRY(zmask_from_zval(h));
-  CUDA_TRY(cudaMemcpy(out, h->s.zm, (size_t)h->s.N * h->s.Gw * sizeof(uint32_t), cudaMemcpyDeviceToHost));
   return BUSSEQ_OK;
 }
 

@@ -279,8 +279,7 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
 
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
                          int32_t* kept_draws);
-int busseq_internal_zmask(busseq_handle* h, uint32_t* out, int64_t* Gw);
-int busseq_internal_format_x(busseq_handle* h, char** buf, int64_t* len);
+int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len);
 
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
@@ -291,11 +290,6 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   std::vector<int32_t> W(N);
   std::vector<double> gamma(2 * B), alpha(G), L((size_t)std::max(1, K - 1) * G), beta((size_t)K * G), ptau(2),
       nu((size_t)B * G), delta(N), phi((size_t)B * G), pi((size_t)B * K);
-  // Z is formatted from its bit mask (N*G/8 bytes instead of an int table)
-  int64_t Gw = 0;
-  if ((r = busseq_internal_zmask(h, nullptr, &Gw))) return r;
-  std::vector<uint32_t> zm((size_t)N * Gw);
-  if ((r = busseq_internal_zmask(h, zm.data(), &Gw))) return r;
   busseq_estimates e{};
   e.gamma = gamma.data(); e.alpha = alpha.data(); e.L = L.data();
   e.beta = beta.data(); e.p_tau0 = ptau.data(); e.nu = nu.data(); e.delta = delta.data();
@@ -317,26 +311,17 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
     return t;
   };
   // _post_Z, _post_X: last sweep's state (BUSseq_gpu.cu:1613-1645)
-  {
-    Table t;
-    t.rows = N;
-    t.cols = G;
-    t.cell = [&zm, Gw](int64_t i, int64_t g, char* b) {
-      b[0] = (char)('0' + ((zm[(size_t)(i * Gw + (g >> 5))] >> (g & 31)) & 1u));
-      return 1;
-    };
-    if ((r = write_table(pre + "_post_Z.txt", t))) return r;
-  }
-  {  // the N x G table of X is formatted on the device
+  // the N x G tables of Z and X are formatted on the device
+  for (int which = 1; which >= 0; --which) {
+    const std::string path = pre + (which ? "_post_Z.txt" : "_post_X.txt");
     char* txt = nullptr;
     int64_t len = 0;
-    if ((r = busseq_internal_format_x(h, &txt, &len))) return r;
-    FILE* f = fopen((pre + "_post_X.txt").c_str(), "wb");
+    if ((r = busseq_internal_format_xz(h, which, &txt, &len))) return r;
+    FILE* f = fopen(path.c_str(), "wb");
     const bool ok = f && (len == 0 || fwrite(txt, 1, (size_t)len, f) == (size_t)len);
     const bool closed = f && fclose(f) == 0;
     free(txt);
-    if (!ok || !closed)
-      return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + pre + "_post_X.txt").c_str());
+    if (!ok || !closed) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + path).c_str());
   }
   if ((r = write_table(pre + "_post_gamma.txt", dbls(gamma.data(), 2, B)))) return r;
   if ((r = write_table(pre + "_post_alpha.txt", dbls(alpha.data(), G, 1)))) return r;

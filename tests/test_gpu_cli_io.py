@@ -30,18 +30,19 @@ def test_binary_and_text_counts_give_identical_outputs(tmp_path):
             assert a.read() == b.read(), suffix
 
 
-def test_post_x_text_is_byte_exact(tmp_path):
-    """_post_X.txt is formatted on the device; its bytes equal the host layout
-    (tab-separated decimal integers, one row per cell)."""
+def test_post_x_z_text_is_byte_exact(tmp_path):
+    """_post_X.txt and _post_Z.txt are formatted on the device; their bytes equal
+    the host layout (tab-separated decimal integers, one row per cell)."""
     n_b, G, K = [40, 35, 30], 333, 3
     Y, _, _ = bq.simulate(n_b, G, K, 12)
     s = bq.Sampler(Y, n_b, K, seed=12)
     s.run(12, 6, 3)
-    X = s.get_state()["X"]
+    st = s.get_state()
     prefix = str(tmp_path / "o")
     s.write_outputs(prefix)
     s.close()
-    with open(prefix + "_post_X.txt", "rb") as f:
-        got = f.read()
-    want = "".join("\t".join(str(int(v)) for v in row) + "\n" for row in X).encode()
-    assert got == want
+    for name, M in (("_post_X.txt", st["X"]), ("_post_Z.txt", st["Z"])):
+        with open(prefix + name, "rb") as f:
+            got = f.read()
+        want = "".join("\t".join(str(int(v)) for v in row) + "\n" for row in M).encode()
+        assert got == want, name
