@@ -338,9 +338,10 @@ const char* busseq_last_error(void) { return g_err.c_str(); }
 
 int busseq_internal_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
-// X (which = 0) or Z (which = 1) of the last sweep as the text of _post_X.txt
-// / _post_Z.txt (the host writer's layout), formatted on the device; *buf is
-// malloc'ed, the caller frees it.
+// X (which = 0) or Z (which = 1) of the last sweep, or the batch-corrected
+// counts (which = 2), as the text of _post_X.txt / _post_Z.txt /
+// _corrected_X.txt (the host writer's layout), formatted on the device; *buf
+// is malloc'ed, the caller frees it.
 int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len) {
   if (!h || !buf || !len) return fail(BUSSEQ_ERR_ARG, "NULL argument");
   *buf = nullptr;
@@ -356,6 +357,15 @@ int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* 
     TRY(zmask_from_zval(h));
     CUDA_TRY(cudaMallocAsync((void**)&d_z, (size_t)N * s.G * sizeof(int32_t), h->stream));
     bq::k_z_dense_i32<<<std::min<unsigned>(blocks_for(N * s.Gw, 256), 152 * 16), 256, 0, h->stream>>>(s, d_z, s.G);
+    M = d_z;
+    ld = s.G;
+  } else if (which == 2) {  // the corrected counts into a temporary int table
+    CUDA_TRY(cudaMalloc((void**)&d_z, (size_t)N * s.G * sizeof(int32_t)));
+    const int r = busseq_corrected_counts(h, d_z, 1);
+    if (r != BUSSEQ_OK) {
+      cudaFree(d_z);
+      return r;
+    }
     M = d_z;
     ld = s.G;
   }
@@ -389,12 +399,20 @@ int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* 
   if (e == cudaSuccess) e = cudaMemcpyAsync(host, d_txt, (size_t)total, cudaMemcpyDeviceToHost, h->stream);
   if (d_txt) cudaFreeAsync(d_txt, h->stream);
   if (d_len) cudaFreeAsync(d_len, h->stream);
-  if (d_z) cudaFreeAsync(d_z, h->stream);
+  if (d_z) {
+    if (which == 2) {
+      const cudaError_t e3 = cudaStreamSynchronize(h->stream);
+      if (e == cudaSuccess) e = e3;
+      cudaFree(d_z);
+    } else {
+      cudaFreeAsync(d_z, h->stream);
+    }
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     free(host);
     return fail(e == cudaErrorMemoryAllocation ? BUSSEQ_ERR_NOMEM : BUSSEQ_ERR_CUDA, "formatting %s: %s",
-                which ? "Z" : "X", cudaGetErrorString(e));
+                which == 0 ? "X" : (which == 1 ? "Z" : "corrected counts"), cudaGetErrorString(e));
   }
   *buf = host;
   *len = total;

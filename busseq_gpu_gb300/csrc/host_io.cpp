@@ -387,17 +387,17 @@ int busseq_write_zx_summaries(busseq_handle* h, const char* prefix) {
 
 int busseq_write_corrected(busseq_handle* h, const char* prefix) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
-  int32_t B, K, nk, kd;
-  int64_t G, N;
-  int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
+  const std::string path = std::string(prefix) + "_corrected_X.txt";
+  char* txt = nullptr;
+  int64_t len = 0;
+  int r = busseq_internal_format_xz(h, 2, &txt, &len);  // counts and text on the device
   if (r) return r;
-  std::vector<int32_t> C((size_t)N * G);
-  if ((r = busseq_corrected_counts(h, C.data(), 0))) return r;
-  Table t;
-  t.rows = N;
-  t.cols = G;
-  t.cell = [&C, G](int64_t i, int64_t g, char* b) { return fmt_int(C[i * G + g], b); };
-  return write_table(std::string(prefix) + "_corrected_X.txt", t);
+  FILE* f = fopen(path.c_str(), "wb");
+  const bool ok = f && (len == 0 || fwrite(txt, 1, (size_t)len, f) == (size_t)len);
+  const bool closed = f && fclose(f) == 0;
+  free(txt);
+  if (!ok || !closed) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + path).c_str());
+  return BUSSEQ_OK;
 }
 
 }  // extern "C"
