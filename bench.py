@@ -127,6 +127,23 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist=None, device="cpu") -> float:
+    """The largest of one timing over all ranks (every rank gets it); the
+    timing of a multi-GPU run is its slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(steps_per_rank: int, world: int, seconds: float) -> float:
+    """Sweeps per second of the whole job: every rank runs its own chain (replicas,
+    weak scaling), so the units are steps x ranks over the slowest rank's time."""
+    return steps_per_rank * world / seconds
+
+
 def make_data(seed, cfg=CFG1, n_b=None):
     import busseq_gpu_gb300 as bq
     prm = bq.CONFIG_SIM[cfg.get("sim", "default")]
@@ -466,11 +483,8 @@ def main():
     barrier()
     ms = ev0.elapsed_time(ev1)
     s.finish()
-    ms_t = torch.tensor([ms], device=f"cuda:{local}")
-    if dist is not None:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = args.steps * world / (ms_max / 1000.0)
+    ms_max = max_over_ranks(ms, dist, f"cuda:{local}")
+    value = whole_job_rate(args.steps, world, ms_max / 1000.0)
     launches = (args.steps // 2) * s.launches_per_sweep(False) + (args.steps - args.steps // 2) * s.launches_per_sweep(True)
 
     if args.only_value:
@@ -542,10 +556,7 @@ def main():
     t1 = time.perf_counter()
     s2.close()
     e2e_s = t1 - t0
-    e2e_t = torch.tensor([e2e_s], device=f"cuda:{local}")
-    if dist is not None:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = args.steps * world / float(e2e_t.item())
+    e2e_value = whole_job_rate(args.steps, world, max_over_ranks(e2e_s, dist, f"cuda:{local}"))
     h2d = Y.nbytes
     d2h = sum(v.nbytes for v in est.values())
 
