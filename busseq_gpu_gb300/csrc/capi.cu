@@ -338,85 +338,130 @@ const char* busseq_last_error(void) { return g_err.c_str(); }
 
 int busseq_internal_set_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+}  // extern "C"
+
+namespace {
+
+// Formats the device table `src` (rows x cols) as text on the device into a
+// malloc'ed host buffer.  Returns 1 (nothing allocated) when an entry lies
+// outside what the device formatter covers.
+int format_table(busseq_handle* h, const bq::FmtSrc& src, int64_t rows, int64_t cols, char** buf, int64_t* len) {
+  *buf = nullptr;
+  *len = 0;
+  if (rows == 0 || cols == 0) return BUSSEQ_OK;
+  if (rows > INT_MAX) return fail(BUSSEQ_ERR_ARG, "table of %lld rows", (long long)rows);
+  int64_t* d_len = nullptr;
+  int* d_bad = nullptr;
+  char* d_txt = nullptr;
+  char* host = nullptr;
+  int bad = 0;
+  std::vector<int64_t> off((size_t)rows + 1, 0);
+  cudaError_t e = cudaMallocAsync((void**)&d_len, (size_t)(rows + 1) * sizeof(int64_t), h->stream);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_bad, sizeof(int), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream);
+  if (e == cudaSuccess) {
+    bq::k_fmt_row_len<<<(unsigned)rows, 256, 0, h->stream>>>(src, cols, d_len, d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(off.data() + 1, d_len, (size_t)rows * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  int64_t total = 0;
+  if (e == cudaSuccess && !bad) {
+    for (int64_t i = 0; i < rows; ++i) off[i + 1] += off[i];
+    total = off[rows];
+    host = static_cast<char*>(malloc((size_t)std::max<int64_t>(total, 1)));
+    if (!host) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_len, off.data(), (size_t)rows * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_txt, (size_t)std::max<int64_t>(total, 1), h->stream);
+    if (e == cudaSuccess) {
+      bq::k_fmt_rows<<<(unsigned)rows, 256, 0, h->stream>>>(src, cols, d_len, d_txt);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, d_txt, (size_t)total, cudaMemcpyDeviceToHost, h->stream);
+  }
+  if (d_txt) cudaFreeAsync(d_txt, h->stream);
+  if (d_bad) cudaFreeAsync(d_bad, h->stream);
+  if (d_len) cudaFreeAsync(d_len, h->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) {
+    free(host);
+    return fail(e == cudaErrorMemoryAllocation ? BUSSEQ_ERR_NOMEM : BUSSEQ_ERR_CUDA, "formatting a table: %s",
+                cudaGetErrorString(e));
+  }
+  if (bad) return 1;
+  *buf = host;
+  *len = total;
+  return BUSSEQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 // X (which = 0) or Z (which = 1) of the last sweep, or the batch-corrected
 // counts (which = 2), as the text of _post_X.txt / _post_Z.txt /
 // _corrected_X.txt (the host writer's layout), formatted on the device; *buf
 // is malloc'ed, the caller frees it.
 int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len) {
   if (!h || !buf || !len) return fail(BUSSEQ_ERR_ARG, "NULL argument");
-  *buf = nullptr;
-  *len = 0;
   CUDA_TRY(cudaSetDevice(h->device));
   const bq::DevState& s = h->s;
   const int64_t N = s.N;
-  if (N == 0 || s.G == 0) return BUSSEQ_OK;
-  const int32_t* M = s.X;
-  int64_t ld = s.Gp;
-  int32_t* d_z = nullptr;
+  bq::FmtSrc src{s.X, bq::FMT_I32, s.Gp, 1};
+  int32_t* d_tab = nullptr;
   if (which == 1) {  // Z unpacked from its bit mask into a temporary int table
     TRY(zmask_from_zval(h));
-    CUDA_TRY(cudaMallocAsync((void**)&d_z, (size_t)N * s.G * sizeof(int32_t), h->stream));
-    bq::k_z_dense_i32<<<std::min<unsigned>(blocks_for(N * s.Gw, 256), 152 * 16), 256, 0, h->stream>>>(s, d_z, s.G);
-    M = d_z;
-    ld = s.G;
+    CUDA_TRY(cudaMalloc((void**)&d_tab, std::max<size_t>((size_t)N * s.G * sizeof(int32_t), 4)));
+    bq::k_z_dense_i32<<<std::min<unsigned>(blocks_for(N * s.Gw, 256), 152 * 16), 256, 0, h->stream>>>(s, d_tab, s.G);
+    src = bq::FmtSrc{d_tab, bq::FMT_I32, s.G, 1};
   } else if (which == 2) {  // the corrected counts into a temporary int table
-    CUDA_TRY(cudaMalloc((void**)&d_z, (size_t)N * s.G * sizeof(int32_t)));
-    const int r = busseq_corrected_counts(h, d_z, 1);
+    CUDA_TRY(cudaMalloc((void**)&d_tab, std::max<size_t>((size_t)N * s.G * sizeof(int32_t), 4)));
+    const int r = busseq_corrected_counts(h, d_tab, 1);
     if (r != BUSSEQ_OK) {
-      cudaFree(d_z);
+      cudaFree(d_tab);
       return r;
     }
-    M = d_z;
-    ld = s.G;
+    src = bq::FmtSrc{d_tab, bq::FMT_I32, s.G, 1};
   }
-  int64_t* d_len = nullptr;
-  char* d_txt = nullptr;
-  char* host = nullptr;
-  std::vector<int64_t> off((size_t)N + 1, 0);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_len, (size_t)(N + 1) * sizeof(int64_t), h->stream);
-  if (e == cudaSuccess) {
-    bq::k_fmt_row_len<<<(unsigned)N, 256, 0, h->stream>>>(M, ld, s.G, d_len);
-    e = cudaGetLastError();
+  const int r = format_table(h, src, N, s.G, buf, len);
+  if (d_tab) cudaFree(d_tab);
+  if (r == 1) return fail(BUSSEQ_ERR_STATE, "table outside the device formatter");  // integers never are
+  return r;
+}
+
+// One _preserved_*.txt table (which: 0 gamma, 1 alpha, 2 L, 3 beta, 4 p, 5 nu,
+// 6 delta, 7 phi, 8 W, 9 pi; rows = scalars, columns = kept sweeps, as
+// busseq_get_preserved lays them out), formatted on the device.  Returns 1 when
+// a value lies outside the device formatter (the caller then formats on the
+// host).
+int busseq_internal_format_preserved(busseq_handle* h, int which, char** buf, int64_t* len) {
+  if (!h || !buf || !len) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  const bq::DevState& s = h->s;
+  if (!h->finished || !s.keep_draws) return fail(BUSSEQ_ERR_STATE, "no finished run with kept draws");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const int64_t nk = h->n_kept, G = s.G, N = s.N;
+  const int B = s.B, K = s.K;
+  const void* p = nullptr;
+  int kind = bq::FMT_F32;
+  int64_t nscal = 0;
+  switch (which) {
+    case 0: p = s.keep_gamma; nscal = 2 * B; break;
+    case 1: p = s.keep_alpha; nscal = G; break;
+    case 2: p = s.keep_L; nscal = (K - 1) * G; kind = bq::FMT_I8; break;
+    case 3: p = s.keep_beta; nscal = (K - 1) * G; break;
+    case 4: p = s.keep_ptau; nscal = 2; break;
+    case 5: p = s.keep_nu; nscal = (B - 1) * G; break;
+    case 6: p = s.keep_delta; nscal = N; break;
+    case 7: p = s.keep_phi; nscal = (int64_t)B * G; break;
+    case 8: p = s.keep_W; nscal = N; kind = bq::FMT_I16; break;
+    case 9: p = s.keep_pi; nscal = (int64_t)B * K; break;
+    default: return fail(BUSSEQ_ERR_ARG, "no preserved table %d", which);
   }
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(off.data() + 1, d_len, (size_t)N * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  int64_t total = 0;
-  if (e == cudaSuccess) {
-    for (int64_t i = 0; i < N; ++i) off[i + 1] += off[i];
-    total = off[N];
-    host = static_cast<char*>(malloc((size_t)total));
-    if (!host) e = cudaErrorMemoryAllocation;
-  }
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_len, off.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_txt, (size_t)total, h->stream);
-  if (e == cudaSuccess) {
-    bq::k_fmt_rows<<<(unsigned)N, 256, 0, h->stream>>>(M, ld, s.G, d_len, d_txt);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host, d_txt, (size_t)total, cudaMemcpyDeviceToHost, h->stream);
-  if (d_txt) cudaFreeAsync(d_txt, h->stream);
-  if (d_len) cudaFreeAsync(d_len, h->stream);
-  if (d_z) {
-    if (which == 2) {
-      const cudaError_t e3 = cudaStreamSynchronize(h->stream);
-      if (e == cudaSuccess) e = e3;
-      cudaFree(d_z);
-    } else {
-      cudaFreeAsync(d_z, h->stream);
-    }
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  if (e != cudaSuccess) {
-    free(host);
-    return fail(e == cudaErrorMemoryAllocation ? BUSSEQ_ERR_NOMEM : BUSSEQ_ERR_CUDA, "formatting %s: %s",
-                which == 0 ? "X" : (which == 1 ? "Z" : "corrected counts"), cudaGetErrorString(e));
-  }
-  *buf = host;
-  *len = total;
-  return BUSSEQ_OK;
+  return format_table(h, bq::FmtSrc{p, kind, 1, nscal}, nscal, nk, buf, len);
 }
 
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,

@@ -280,6 +280,7 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,
                          int32_t* kept_draws);
 int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len);
+int busseq_internal_format_preserved(busseq_handle* h, int which, char** buf, int64_t* len);
 
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
@@ -344,6 +345,33 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
   if ((r = write_table(pre + "_BIC.txt", dbls(&bic, 1, 1)))) return r;
   if (!print_preserved) return BUSSEQ_OK;
   if (!kd || nk <= 0) return busseq_internal_set_error(BUSSEQ_ERR_STATE, "no kept draws to print (keep_draws off)");
+  // the kept-draw tables are formatted on the device ("%f" exactly for the float
+  // draws); a table holding a value outside the device formatter (|v| >= 2^43,
+  // never expected) sends all of them to the host writer below
+  {
+    static const char* const names[10] = {"_preserved_gamma.txt", "_preserved_alpha.txt", "_preserved_L.txt",
+                                          "_preserved_beta.txt",  "_preserved_p.txt",     "_preserved_nu.txt",
+                                          "_preserved_delta.txt", "_preserved_phi.txt",   "_preserved_W.txt",
+                                          "_preserved_pi.txt"};
+    bool device_ok = true;
+    for (int which = 0; which < 10 && device_ok; ++which) {
+      char* txt = nullptr;
+      int64_t len = 0;
+      r = busseq_internal_format_preserved(h, which, &txt, &len);
+      if (r == 1) {
+        device_ok = false;
+        break;
+      }
+      if (r) return r;
+      const std::string path = pre + names[which];
+      FILE* f = fopen(path.c_str(), "wb");
+      const bool ok = f && (len == 0 || fwrite(txt, 1, (size_t)len, f) == (size_t)len);
+      const bool closed = f && fclose(f) == 0;
+      free(txt);
+      if (!ok || !closed) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + path).c_str());
+    }
+    if (device_ok) return BUSSEQ_OK;
+  }
   const int64_t n = nk;
   std::vector<double> pg((size_t)2 * B * n), pa((size_t)G * n), pb((size_t)(K - 1) * G * n), pp((size_t)2 * n),
       pn((size_t)(B - 1) * G * n), pd((size_t)N * n), pf((size_t)B * G * n), ppi((size_t)B * K * n);

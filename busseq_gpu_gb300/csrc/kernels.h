@@ -68,8 +68,15 @@ __global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell
 __global__ void k_init_raw(DevState s);
 __global__ void k_init_finish(DevState s, int fresh);
 __global__ void k_finalize(DevState s, Estimates e, int n_kept);
-__global__ void k_fmt_row_len(const int32_t* M, int64_t ld, int64_t cols, int64_t* row_len);
-__global__ void k_fmt_rows(const int32_t* M, int64_t ld, int64_t cols, const int64_t* row_off, char* out);
+// A table to format as text (format_kernels.cu): entry (r, c) at p[r sr + c sc].
+enum FmtKind : int { FMT_I32 = 0, FMT_F32 = 1, FMT_I8 = 2, FMT_I16 = 3 };
+struct FmtSrc {
+  const void* p;
+  int kind;  // FmtKind
+  int64_t sr, sc;
+};
+__global__ void k_fmt_row_len(FmtSrc src, int64_t cols, int64_t* row_len, int* bad);
+__global__ void k_fmt_rows(FmtSrc src, int64_t cols, const int64_t* row_off, char* out);
 __global__ void k_z_dense_i32(DevState s, int32_t* out, int64_t ld);
 __global__ void k_z_dense_u8(DevState s, uint8_t* out, int64_t ld);
 __global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik);

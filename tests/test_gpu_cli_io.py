@@ -46,3 +46,26 @@ def test_post_x_z_text_is_byte_exact(tmp_path):
             got = f.read()
         want = "".join("\t".join(str(int(v)) for v in row) + "\n" for row in M).encode()
         assert got == want, name
+
+
+def test_preserved_files_are_byte_exact(tmp_path):
+    """The -p tables are formatted on the device ("%f" of the float draws, ints
+    for L and W); their bytes equal printf's layout of the kept draws."""
+    n_b, G, K = [30, 25, 20], 90, 3
+    Y, _, _ = bq.simulate(n_b, G, K, 5)
+    s = bq.Sampler(Y, n_b, K, seed=5, keep_draws=True)
+    s.run(16, 8, 4)
+    pres = s.preserved()
+    prefix = str(tmp_path / "o")
+    s.write_outputs(prefix, True)
+    s.close()
+    files = {"gamma": "_preserved_gamma.txt", "alpha": "_preserved_alpha.txt", "L": "_preserved_L.txt",
+             "beta": "_preserved_beta.txt", "p_tau0": "_preserved_p.txt", "nu": "_preserved_nu.txt",
+             "delta": "_preserved_delta.txt", "phi": "_preserved_phi.txt", "W": "_preserved_W.txt",
+             "pi": "_preserved_pi.txt"}
+    for key, name in files.items():
+        M = pres[key]
+        fmt = (lambda v: "%d" % v) if M.dtype.kind == "i" else (lambda v: "%f" % v)
+        want = "".join("\t".join(fmt(v) for v in row) + "\n" for row in M).encode()
+        with open(prefix + name, "rb") as f:
+            assert f.read() == want, name
