@@ -433,6 +433,35 @@ int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* 
   return r;
 }
 
+// The posterior summaries of the imputation as text (which: 0 E[X] for
+// _post_X_mean.txt, 1 P(Z = 1) for _post_Z_prob.txt), formatted on the device.
+// Returns 1 when a value lies outside the device formatter.
+int busseq_internal_format_zx_summary(busseq_handle* h, int which, char** buf, int64_t* len) {
+  if (!h || !buf || !len) return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  if (!h->opt.zx_summaries) return fail(BUSSEQ_ERR_STATE, "the chain was created without zx_summaries");
+  if (!h->finished || h->n_kept <= 0 || !h->s.acc_zn)
+    return fail(BUSSEQ_ERR_STATE, "no finished run with kept sweeps");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const bq::DevState& s = h->s;
+  float* d = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&d, std::max<size_t>((size_t)s.N * s.G * sizeof(float), 4), h->stream));
+  float* xm = which == 0 ? d : nullptr;
+  float* zp = which == 0 ? nullptr : d;
+  bq::k_zx_summary<<<152 * 8, 256, 0, h->stream>>>(s, h->n_kept, xm, zp);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && s.nz0 > 0) {
+    bq::k_zx_summary_zeros<<<152 * 8, 256, 0, h->stream>>>(s, h->n_kept, xm, zp);
+    e = cudaGetLastError();
+  }
+  int r = BUSSEQ_OK;
+  if (e == cudaSuccess) r = format_table(h, bq::FmtSrc{d, bq::FMT_F32, s.G, 1}, s.N, s.G, buf, len);
+  cudaFreeAsync(d, h->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess && r == BUSSEQ_OK) e = e2;
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "zx summaries: %s", cudaGetErrorString(e));
+  return r;
+}
+
 // One _preserved_*.txt table (which: 0 gamma, 1 alpha, 2 L, 3 beta, 4 p, 5 nu,
 // 6 delta, 7 phi, 8 W, 9 pi; rows = scalars, columns = kept sweeps, as
 // busseq_get_preserved lays them out), formatted on the device.  Returns 1 when

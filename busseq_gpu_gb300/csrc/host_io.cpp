@@ -281,6 +281,7 @@ int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, i
                          int32_t* kept_draws);
 int busseq_internal_format_xz(busseq_handle* h, int which, char** buf, int64_t* len);
 int busseq_internal_format_preserved(busseq_handle* h, int which, char** buf, int64_t* len);
+int busseq_internal_format_zx_summary(busseq_handle* h, int which, char** buf, int64_t* len);
 
 int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_preserved) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
@@ -395,22 +396,34 @@ int busseq_write_outputs(busseq_handle* h, const char* prefix, int32_t print_pre
 
 int busseq_write_zx_summaries(busseq_handle* h, const char* prefix) {
   if (!h || !prefix) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "NULL argument");
-  int32_t B, K, nk, kd;
-  int64_t G, N;
-  int r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd);
-  if (r) return r;
-  std::vector<float> xm((size_t)N * G), zp((size_t)N * G);
-  if ((r = busseq_get_zx_summaries(h, xm.data(), zp.data()))) return r;
-  auto table = [N, G](const std::vector<float>& v) {
-    Table t;
-    t.rows = N;
-    t.cols = G;
-    t.cell = [&v, G](int64_t i, int64_t g, char* b) { return fmt_lf((double)v[i * G + g], b); };
-    return t;
-  };
   const std::string pre(prefix);
-  if ((r = write_table(pre + "_post_X_mean.txt", table(xm)))) return r;
-  return write_table(pre + "_post_Z_prob.txt", table(zp));
+  for (int which = 0; which < 2; ++which) {
+    const std::string path = pre + (which ? "_post_Z_prob.txt" : "_post_X_mean.txt");
+    char* txt = nullptr;
+    int64_t len = 0;
+    int r = busseq_internal_format_zx_summary(h, which, &txt, &len);  // tables and text on the device
+    if (r == 1) {  // a value outside the device formatter: format on the host
+      int32_t B, K, nk, kd;
+      int64_t G, N;
+      if ((r = busseq_internal_dims(h, &B, &K, &G, &N, &nk, &kd))) return r;
+      std::vector<float> xm((size_t)N * G), zp((size_t)N * G);
+      if ((r = busseq_get_zx_summaries(h, xm.data(), zp.data()))) return r;
+      const std::vector<float>& v = which ? zp : xm;
+      Table t;
+      t.rows = N;
+      t.cols = G;
+      t.cell = [&v, G](int64_t i, int64_t g, char* b) { return fmt_lf((double)v[i * G + g], b); };
+      if ((r = write_table(path, t))) return r;
+      continue;
+    }
+    if (r) return r;
+    FILE* f = fopen(path.c_str(), "wb");
+    const bool ok = f && (len == 0 || fwrite(txt, 1, (size_t)len, f) == (size_t)len);
+    const bool closed = f && fclose(f) == 0;
+    free(txt);
+    if (!ok || !closed) return busseq_internal_set_error(BUSSEQ_ERR_IO, ("write failed: " + path).c_str());
+  }
+  return BUSSEQ_OK;
 }
 
 int busseq_write_corrected(busseq_handle* h, const char* prefix) {

@@ -93,6 +93,10 @@ def test_cli_writes_summary_tables(data, tmp_path):
     assert r.returncode == 0, r.stderr
     xm = np.loadtxt(str(tmp_path / "out") + "_post_X_mean.txt").reshape(Y.shape)
     zp = np.loadtxt(str(tmp_path / "out") + "_post_Z_prob.txt").reshape(Y.shape)
+    # the device formatter prints each value as printf("%f") of the float
+    with open(str(tmp_path / "out") + "_post_Z_prob.txt") as f:
+        first = f.readline().rstrip("\n").split("\t")
+    assert first == ["%f" % float(np.float32(v)) for v in zp[0]]
     assert np.all(xm[Y > 0] == Y[Y > 0]) and np.all(zp[Y > 0] == 0)
     assert np.all((zp >= 0) & (zp <= 1)) and zp.max() > 0
     assert os.path.exists(str(tmp_path / "out") + "_post_X.txt")
