@@ -196,15 +196,18 @@ struct GammaTerms {
 // of its Philox stream (an entry with X = 0 reads its Z uniform there, and
 // every NB proposal starts there) and the Z draw.  Entries that need an NB
 // proposal are staged in shared memory with their block 0 and a cost class:
-// class 0 for Gamma-Poisson draws, classes 1..16 for CDF inversions ordered
+// class 0 for Gamma-Poisson draws, classes 1..31 for CDF inversions ordered
 // by the expected length of the search, mu (-log(1 - u)) with u the uniform
 // the inversion will use, longest first.
 // Phase 2: a counting sort over (class, warp, rank) - all counts come from
 // ballots and match masks, so the order is deterministic - lays the staged
-// entries out as one CTA-wide queue, and thread t takes queue positions
-// t, t + 256, ...  The rare, expensive Gamma-Poisson draws thus share a few
-// warps instead of idling most lanes of every warp, and lanes of one warp run
-// inversion searches of similar length.
+// entries out as one CTA-wide queue.
+// Phase 3: warps claim 32 consecutive queue positions at a time from a shared
+// counter.  The rare, expensive Gamma-Poisson draws thus share a few warps
+// instead of idling most lanes of every warp, the warps that drew them take
+// fewer of the inversions, and lanes of one warp run inversion searches of
+// similar length.
+// Phase 4: the gamma statistics of the drawn values, in a fixed order.
 //
 // The gamma terms depend on the entry only through x, so values below ZX_HIST
 // are counted in a shared histogram and each bin's terms are evaluated once;
@@ -213,15 +216,15 @@ constexpr int ZX_WARPS = ZX_THREADS / 32;
 constexpr int ZX_PER_WARP = ZX_PER_CTA / ZX_WARPS;
 constexpr int ZX_PER_LANE = ZX_PER_WARP / 32;
 constexpr int ZX_HIST = 128;
-constexpr int ZX_NCLS = 17;
+constexpr int ZX_NCLS = 32;
 static_assert(ZX_HIST <= ZX_THREADS, "one thread per histogram bin");
 static_assert(ZX_NCLS <= 32 && ZX_PER_WARP <= 128 && ZX_WARPS <= 8, "queue index packing");
 
 __device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
   if (!inv) return 0;
   const float key = mu * -log_fast(1.0f - u_nb);  // 1 - u is exact for u = (2m+1) 2^-24
-  const int bin = key < 30.0f ? (int)(key * 0.5f) : 15;
-  return 16 - bin;
+  const int bin = key < 60.0f ? (int)(key * 0.5f) : 30;
+  return 31 - bin;
 }
 
 __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
   __shared__ uint32_t q_w[4][ZX_WARPS][ZX_PER_WARP];
   __shared__ uint16_t perm[ZX_PER_CTA];
   __shared__ int cnt_w[ZX_WARPS][ZX_NCLS], off[ZX_NCLS][ZX_WARPS], n_need_w[ZX_WARPS];
-  __shared__ int n_queue;
+  __shared__ int n_queue, q_next;
   __shared__ float sp_tab[ZX_HIST];
   __shared__ int xhist[ZX_HIST];
   const int c = blockIdx.x;
@@ -365,6 +368,7 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
       }
     }
     if (lane == ZX_NCLS - 1) n_queue = incl;
+    if (lane == 0) q_next = 0;
   }
   __syncthreads();
   for (int q = lane; q < n_need_w[warp]; q += 32) {
@@ -374,11 +378,19 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
   __syncthreads();
 
   // ---- phase 3: the queued imputations, X ~ NB independence MH
-  //      (BUSseq_gpu.cu:497-506)
+  //      (BUSseq_gpu.cu:497-506).  Warps claim 32 consecutive queue positions
+  //      at a time, so the warp that drew the Gamma-Poisson entries at the head
+  //      of the queue takes fewer of the rest.  Each entry's draws come from
+  //      its own stream, so the result does not depend on which warp takes
+  //      it; the drawn x goes back into q_xo for phase 4.
   const int nq = n_queue;
-  long long nz = 0, xz = 0;
-  float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-  for (int q = tid; q < nq; q += ZX_THREADS) {
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&q_next, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);  // warp-uniform: the whole warp leaves together
+    if (base >= nq) break;
+    const int q = base + lane;
+    if (q >= nq) continue;
     const int ws = perm[q];
     const int qw = ws >> 7, slot = ws & 127;
     const bool is_inv = (q_kr[qw][slot] >> 16) != 0;
@@ -404,6 +416,18 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
       s.acc_zn[j] += 1;
       s.acc_xs[j] += x;
     }
+    q_xo[qw][slot] = x;
+  }
+  __syncthreads();
+
+  // ---- phase 4: gamma statistics of the imputed entries, thread t taking
+  //      queue positions t, t + 256, ... (a fixed order: the float sums are
+  //      bit-reproducible)
+  long long nz = 0, xz = 0;
+  float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
+  for (int q = tid; q < nq; q += ZX_THREADS) {
+    const int ws = perm[q];
+    const int x = q_xo[ws >> 7][ws & 127];
     ++nz;
     xz += x;
     if (x == 0) {

@@ -388,7 +388,7 @@ BQ_HD int poisson(Stream& s, float lam, int* err) {
 //    (BUSseq_gpu.cu:199-210).
 // Both draw exactly from NB(mu, phi); the switch keeps the common small-mean
 // draws to one uniform and a short loop.
-constexpr float NB_INV_MU = 16.0f;
+constexpr float NB_INV_MU = 32.0f;
 constexpr int NB_INV_MAX_K = 1024;
 enum : int { ERR_NB_INV_CAP = 4 };
 

@@ -206,13 +206,13 @@ static int poisson(Stream& s, double lam, double* mg) {
   return (int)lam;
 }
 
-// NB(mu, phi): inversion of the distribution function when mu < 16 and
+// NB(mu, phi): inversion of the distribution function when mu < 32 and
 // phi >= 1 (one uniform), Gamma-Poisson otherwise; the same method switch as
 // the kernels, so both consume the same uniforms.
 static int negbin(Stream& s, double mu, double phi, double* mg) {
-  mark(mg, mu - 16.0, 16.0);
+  mark(mg, mu - 32.0, 32.0);
   mark(mg, phi - 1.0, 1.0);
-  if (mu < 16.0 && phi >= 1.0) {
+  if (mu < 32.0 && phi >= 1.0) {
     const double q = mu / (phi + mu);
     double p = exp(phi * log1p(-q));
     double F = p;

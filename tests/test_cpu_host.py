@@ -141,8 +141,10 @@ def test_oracle_sampler_moments():
     assert abs(p.mean() - 3.3) < 0.03 and abs(p.var() - 3.3) < 0.08
     p = po.sample_poisson(10, 250.0, 100000)
     assert abs(p.mean() - 250) < 0.3 and abs(p.var() / 250 - 1) < 0.03
-    nb = po.sample_negbin(11, 40.0, 4.0, 100000)
+    nb = po.sample_negbin(11, 40.0, 4.0, 100000)  # Gamma-Poisson
     assert abs(nb.mean() - 40) < 0.5 and abs(nb.var() / (40 + 1600 / 4) - 1) < 0.05
+    nb = po.sample_negbin(12, 24.0, 3.0, 100000)  # distribution-function inversion (mu < 32, phi >= 1)
+    assert abs(nb.mean() - 24) < 0.25 and abs(nb.var() / (24 + 576 / 3) - 1) < 0.05
 
 
 def test_philox_known_answers():
