@@ -1220,10 +1220,12 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   CUDA_TRY(cudaSetDevice(h->device));
   const bq::DevState& s = h->s;
   const dim3 gene_grid(s.n_tiles, s.cap_g);
-  // the adapted metric of the chain is kept: the call works on a copy
-  std::vector<float> mass_keep(s.hmc_D);
+  // the adapted metric of the chain (the mass and its frozen information
+  // part) is kept: the call works on copies
+  std::vector<float> mass_keep(s.hmc_D), fis_keep(s.hmc_D);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(cudaMemcpy(mass_keep.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(fis_keep.data(), s.hmc_fis, s.hmc_D * 4, cudaMemcpyDeviceToHost));
   bq::k_hmc_grad_metric<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, 2);
   LAUNCH_CHECK("k_hmc_grad");
   bq::k_hmc_assemble<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 2);
@@ -1233,6 +1235,7 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
   CUDA_TRY(cudaMemcpy(gf.data(), s.hmc_grad, s.hmc_D * 4, cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemcpy(mf.data(), s.hmc_mass, s.hmc_D * 4, cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemcpy(s.hmc_mass, mass_keep.data(), s.hmc_D * 4, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(s.hmc_fis, fis_keep.data(), s.hmc_D * 4, cudaMemcpyHostToDevice));
   hmc_unpad(s, gf.data(), grad);
   if (metric) hmc_unpad(s, mf.data(), metric);
   return BUSSEQ_OK;

@@ -24,9 +24,14 @@
 // rejected, a restore; the E table is refreshed once, after the transition.
 // Step size: dual averaging (Hoffman and Gelman, JMLR 15, 2014, algorithm 5)
 // during burn-in with a random jitter of +-10 %; metric: a block per gene over
-// (alpha, beta, nu) from the Fisher sums, the diagonal Fisher information of
-// delta and the observed information of psi, adapted at the transition starts
-// of the first half of burn-in, then frozen.
+// (alpha, beta, nu) from the sums of the observed information, the diagonal
+// observed information of delta and of psi, adapted at the transition starts
+// of the first half of burn-in, then frozen.  The observed information
+// phi mu (phi + x) / (phi + mu)^2 of an entry's eta is positive and is the
+// actual curvature where the chain is; the expected (Fisher) information
+// phi mu / (phi + mu) equals it only on average over x ~ NB(mu, phi) and
+// understates it wherever the counts run above the current means (a chain
+// still far from equilibrium), which shrinks the adapted step size.
 #include "kernels_common.cuh"
 
 namespace bq {
@@ -166,9 +171,9 @@ __device__ __forceinline__ int transpose_slot(int lane) {
 // ---------------------------------------------------------------------------
 // Gradient pass (gene-pass layout: CTA = 128 genes x one chunk of cells of one
 // (batch, type)).  Per-gene partial sums go to part slots 0 (sum d ll / d eta),
-// 1 (sum d ll / d psi), and, while the metric adapts, 2 (Fisher information of
-// eta) and 3 (observed information of psi); per-cell sums over the CTA's genes
-// go to hmc_cpart[tile][cell] (and hmc_cpartw for the Fisher information).
+// 1 (sum d ll / d psi), and, while the metric adapts, 2 (observed information
+// of eta) and 3 (observed information of psi); per-cell sums over the CTA's
+// genes go to hmc_cpart[tile][cell] (and hmc_cpartw for the information).
 // ---------------------------------------------------------------------------
 // Sum of HMC partial slot `slot` of gene g over the chunks of segment (b, k),
 // in float (gradients need no more).
@@ -259,7 +264,7 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
       fp = fmaf(ph, d1, fp);
       rv[u] = gv ? r : 0.0f;
       if (METRIC && adapt) {
-        const float w = ph * mu * rc;
+        const float w = ph * mu * (ph + xf) * (rc * rc);  // -d2 ll / d eta2
         const float tg = x < HMC_TAB ? ttg[x][tid] : tg32 + (tasym32 - trigamma_asym(ph + xf));
         const float d2 = -tg + iph - 2.0f * rc + (ph + xf) * rc * rc;  // d2 ll / d phi2
         fw += w;
@@ -778,9 +783,9 @@ __global__ void k_hmc_finish(DevState s) {
 // Per-gene block metric.  Within gene g the coordinates
 //   u = (alpha_g, beta_g1 .. beta_g(K-1), nu_g1 .. nu_g(B-1))
 // enter every entry's eta through a_bk . u (a_bk: 1 for alpha, 1 for beta_k if
-// k >= 1, 1 for nu_b if b >= 1), so the Fisher information of u is
+// k >= 1, 1 for nu_b if b >= 1), so the observed information of u is
 //   F_g = sum_{b,k} W_bkg a_bk a_bk^T,   W_bkg = sum over the cells of (b, k) of
-//   phi mu / (phi + mu)  (part slot 2, per segment),
+//   phi mu (phi + x) / (phi + mu)^2  (part slot 2, per segment),
 // plus the priors' precisions on the diagonal.  Its Cholesky factor turns the
 // strong alpha-beta and alpha-nu correlations (alpha is informed only by
 // type-0 cells once the betas are free) into unit scale.

@@ -1004,9 +1004,9 @@ double orc_hmc_logpost(const orc_state* st) {
 }
 
 // Gradient of orc_hmc_logpost with respect to theta (psi = log phi), and the
-// diagonal metric used by the kernels: the Fisher information of the
-// eta-coordinates, sum phi mu / (phi + mu) over the coordinate's entries, and
-// the observed information of psi, each plus the prior's curvature.  Fixed
+// diagonal metric used by the kernels: the observed information of the
+// eta-coordinates, sum phi mu (phi + x) / (phi + mu)^2 over the coordinate's
+// entries, and of psi, each plus the prior's curvature.  Fixed
 // coordinates (beta_0, nu_0, the first cell of each batch) get gradient 0 and
 // metric 1.  Any output pointer may be NULL.
 int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double* gd, double* gp, double* ma,
@@ -1027,7 +1027,7 @@ int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double
         const double x = st->X[i * G + g];
         const double mu = exp(st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g] + st->delta[i]);
         const double r = ph * (x - mu) / (ph + mu);
-        const double w = ph * mu / (ph + mu);
+        const double w = ph * mu * (ph + x) / ((ph + mu) * (ph + mu));
         sa[g] += r;
         wa[g] += w;
         sb[(size_t)k * G + g] += r;
@@ -1056,7 +1056,7 @@ int orc_hmc_grad(const orc_state* st, double* ga, double* gb, double* gn, double
       const double x = st->X[i * G + g];
       const double mu = exp(st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g] + st->delta[i]);
       s += ph * (x - mu) / (ph + mu);
-      w += ph * mu / (ph + mu);
+      w += ph * mu * (ph + x) / ((ph + mu) * (ph + mu));
     }
     sd[i] = s;
     wd[i] = w;

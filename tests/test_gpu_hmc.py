@@ -146,3 +146,23 @@ def test_hmc_checkpoint_resume_is_exact(warm, tmp_path):
     b.close()
     for k in st_ref:
         assert np.array_equal(st_ref[k], st[k]), k
+
+
+def test_gradient_accessor_leaves_the_chain_unchanged(warm):
+    """Reading the gradient and metric mid-run (after the metric froze) must not
+    change the chain: the adapted mass and its information part are kept."""
+    Y, _, _ = warm
+    ref = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4)
+    ref.run(30, 16, 8)
+    st_ref = ref.get_state()
+    ref.close()
+    a = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4)
+    a.begin(30, 16, 8)
+    a.sweeps(20)
+    a.hmc_gradient(with_metric=True)
+    a.sweeps(10)
+    a.finish()
+    st = a.get_state()
+    a.close()
+    for k in st_ref:
+        assert np.array_equal(st_ref[k], st[k]), k

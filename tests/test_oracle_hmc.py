@@ -70,3 +70,27 @@ def test_fixed_coordinates_and_metric(warm):
         assert np.all(np.isfinite(m)), k
     for k in ("alpha", "beta", "nu", "delta"):
         assert np.all(gm["metric"][k] > 0), k
+
+
+def test_metric_is_the_negative_hessian_diagonal(warm):
+    """The eta-coordinates' metric is the observed information: minus the
+    diagonal of the log posterior's Hessian, checked by central differences of
+    the oracle's own gradient (alpha_g, beta_gk, nu_bg and delta_i each enter
+    their own entries only, so a one-coordinate difference is the diagonal)."""
+    o = warm
+    gm = o.hmc_grad()
+    rng = np.random.default_rng(3)
+    h = 1e-4
+    for name, j in _coords(o, rng, 5):
+        if name == "psi":
+            continue
+        arr = getattr(o, name).reshape(-1)
+        base = arr[j]
+        arr[j] = base + h
+        gp = o.hmc_grad()["grad"][name].reshape(-1)[j]
+        arr[j] = base - h
+        gmn = o.hmc_grad()["grad"][name].reshape(-1)[j]
+        arr[j] = base
+        hess = -(gp - gmn) / (2 * h)
+        m = gm["metric"][name].reshape(-1)[j]
+        assert abs(hess - m) <= 1e-4 * abs(m) + 1e-6, (name, j, hess, m)
