@@ -40,8 +40,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
-# the large uneven workload: 6 batches, 15 % differential genes, phi ~ U(2, 30)
-CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide")
+# the large uneven workload: 6 batches, 15 % differential genes, phi ~ U(2, 30), HMC block
+# update (10 leapfrog steps; --mh runs the plain sampler on it)
+CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide", hmc=10)
 # config-1 data with the HMC block update (10 leapfrog steps) in place of the random-walk steps
 CFG2 = dict(CFG1, hmc=10)
 CFG3 = dict(CFG1, ks=list(range(3, 11)))  # config-1 data fitted by 8 chains, K = 3 .. 10
@@ -195,7 +196,8 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (BUSseq generative model)",
-        "config": _config(args.workload, n_b, cfg),
+        # the reference has only the random-walk sampler: its arm runs that on every workload
+        "config": _config(args.workload, n_b, dict(cfg, hmc=0)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference program has no CPU implementation of the sweep; this arm times the FP64 CPU "
@@ -411,10 +413,13 @@ def main():
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
     ap.add_argument("--leapfrog", type=int, default=0,
                     help="leapfrog steps of the HMC block update (overrides the workload's; 0 keeps it)")
+    ap.add_argument("--mh", action="store_true",
+                    help="run the plain random-walk sampler even where the workload uses the HMC update")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
                     help="config1 (the headline, default), config2 (config-1 data, HMC block update with 10 "
                          "leapfrog steps), config3 (config-1 data, 8 chains K=3..10 batched in one graph per "
-                         "sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, uneven batches)")
+                         "sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, uneven batches, "
+                         "HMC block update with 10 leapfrog steps)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     ap.add_argument("--corrected-counts", action="store_true",
@@ -451,6 +456,8 @@ def main():
         return run_batch(args, cfg, rank, world, local)
     if args.leapfrog > 0:
         cfg["hmc"] = args.leapfrog
+    if args.mh:
+        cfg["hmc"] = 0
     n_b, G, K = list(cfg["n_b"]), cfg["G"], cfg["K"]
     seed = cfg["seed"]
     if args.cells > 0:
@@ -564,6 +571,16 @@ def main():
     quality = None
     if rank == 0 and not args.no_ess:
         quality = ess_run(Y, W_true, n_b, K, seed, hmc=hmc)
+        if hmc:
+            # the same whole job with the plain random-walk sampler, for the ESS/s ratios
+            mh = ess_run(Y, W_true, n_b, K, seed, hmc=0)
+
+            def ratio(name):
+                a, r = quality[name]["ess_per_s_median"], mh[name]["ess_per_s_median"]
+                return a / r if a and r else None
+
+            quality["vs_mh"] = {"beta_ess_per_s_median_ratio": ratio("beta"),
+                                "nu_ess_per_s_median_ratio": ratio("nu"), "ari_W_mh": mh["ari_W"], "mh": mh}
 
     # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
     cpu = None
