@@ -231,11 +231,13 @@ def _config(name="config1", n_b=None, cfg=None):
     n_b = list(n_b if n_b is not None else cfg["n_b"])
     N, G, K = int(sum(n_b)), cfg["G"], cfg["K"]
     mb = N * G * 4 / 1e6
-    sampler = ("HMC block update, %d leapfrog steps" % cfg["hmc"]) if cfg.get("hmc") else "plain MH sampler"
+    gene = bool(cfg.get("gene")) and bool(cfg.get("hmc"))
+    sampler = ("HMC block update, %d leapfrog steps%s" % (cfg["hmc"], ", per-gene decisions" if gene else "")
+               if cfg.get("hmc") else "plain MH sampler")
     desc = "%s: B=%d batches of %s cells (N=%d), G=%d, K=%d, %s" % (
         name, len(n_b), "/".join(str(n) for n in n_b), N, G, K, sampler)
     return {"workload": desc, "B": len(n_b), "N": N, "G": G, "K": K, "w_update": "mh",
-            "sampler": "hmc" if cfg.get("hmc") else "mh", "hmc_leapfrog": cfg.get("hmc", 0),
+            "sampler": "hmc" if cfg.get("hmc") else "mh", "hmc_leapfrog": cfg.get("hmc", 0), "hmc_gene_accept": gene,
             "parallelism": "replicas (one chain per GPU)",
             "l2": "no flush: X and Y are %.0f MB each, larger than L2" % mb,
             "precision": "f32 likelihood terms, f64 acceptance sums"}
@@ -368,7 +370,7 @@ def run_batch(args, cfg, rank, world, local):
     return 0
 
 
-def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
+def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=False):
     """One whole job with kept draws: ESS (Geyer, initial monotone sequence) of
     every beta (k >= 1) and nu (b >= 1) coordinate, ESS/s over the wall time of
     the whole job (upload, init, burn-in, kept sweeps, estimates), and the ARI
@@ -377,7 +379,7 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
     from busseq_gpu_gb300.diagnostics import adjusted_rand_index, ess_geyer
 
     t0 = time.perf_counter()
-    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True, hmc_leapfrog=hmc)
+    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True, hmc_leapfrog=hmc, hmc_gene_accept=gene and hmc > 0)
     s.run(n_iter, n_burnin, min(500, n_burnin))
     est = s.estimates(with_XZ=False)
     wall = time.perf_counter() - t0
@@ -386,7 +388,8 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0):
     s.close()
     out = {"sweeps": n_iter, "burnin": n_burnin, "kept": n_iter - n_burnin, "wall_s": wall,
            "ari_W": adjusted_rand_index(est["W"], W_true), "estimator": "Geyer initial monotone sequence",
-           "sampler": ("HMC, %d leapfrog steps" % hmc) if hmc else "random-walk MH (the reference's)"}
+           "sampler": ("HMC, %d leapfrog steps%s" % (hmc, ", per-gene decisions" if gene else "")) if hmc
+           else "random-walk MH (the reference's)"}
     if hstats:
         out["hmc"] = {k: float(v) for k, v in hstats.items()}
     for name in ("beta", "nu"):
@@ -413,6 +416,9 @@ def main():
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
     ap.add_argument("--leapfrog", type=int, default=0,
                     help="leapfrog steps of the HMC block update (overrides the workload's; 0 keeps it)")
+    ap.add_argument("--gene-accept", type=int, default=None, choices=[0, 1],
+                    help="HMC workloads: 1 accepts or rejects each gene's block on its own (delta by the "
+                         "random-walk step), 0 one decision for the whole block (default: the workload's)")
     ap.add_argument("--mh", action="store_true",
                     help="run the plain random-walk sampler even where the workload uses the HMC update")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
@@ -458,6 +464,8 @@ def main():
         cfg["hmc"] = args.leapfrog
     if args.mh:
         cfg["hmc"] = 0
+    if args.gene_accept is not None:
+        cfg["gene"] = bool(args.gene_accept)
     n_b, G, K = list(cfg["n_b"]), cfg["G"], cfg["K"]
     seed = cfg["seed"]
     if args.cells > 0:
@@ -471,7 +479,8 @@ def main():
     stream = torch.cuda.Stream(device=local)
     torch.cuda.set_stream(stream)
     hmc = cfg.get("hmc", 0)
-    s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc)
+    gene = bool(cfg.get("gene")) and hmc > 0
+    s = bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc, hmc_gene_accept=gene)
     assert stream.cuda_stream != 0
     s.set_stream(stream.cuda_stream)
     total = args.warmup + args.steps
@@ -557,7 +566,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    s2 = bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc)
+    s2 = bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank, device=local, hmc_leapfrog=hmc, hmc_gene_accept=gene)
     s2.run(args.steps, args.steps // 2, min(args.warmup, args.steps))
     est = s2.estimates(with_XZ=True, out=est_out)
     t1 = time.perf_counter()
@@ -570,7 +579,7 @@ def main():
     # ---- mixing and recovery: ESS of beta and nu, ARI of W (rank 0) -------
     quality = None
     if rank == 0 and not args.no_ess:
-        quality = ess_run(Y, W_true, n_b, K, seed, hmc=hmc)
+        quality = ess_run(Y, W_true, n_b, K, seed, hmc=hmc, gene=gene)
         if hmc:
             # the same whole job with the plain random-walk sampler, for the ESS/s ratios
             mh = ess_run(Y, W_true, n_b, K, seed, hmc=0)

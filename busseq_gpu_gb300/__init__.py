@@ -45,7 +45,7 @@ class Dims(C.Structure):
 class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
                 ("device", C.c_int32), ("chunk_cells", C.c_int32), ("hmc_leapfrog", C.c_int32),
-                ("zx_summaries", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("zx_summaries", C.c_int32), ("hmc_gene_accept", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Estimates(C.Structure):
@@ -128,6 +128,7 @@ def lib():
         "busseq_hmc_stats": ([H, _PD], C.c_int),
         "busseq_hmc_gradient": ([H, _PD, _PD], C.c_int),
         "busseq_hmc_logpost_diff": ([H, C.POINTER(State), _PD], C.c_int),
+        "busseq_hmc_gene_logpost_diff": ([H, C.POINTER(State), _PD], C.c_int),
         "busseq_profile": ([H, C.c_int32, _PD, C.c_int32, _PI32], C.c_int),
         "busseq_kernel_name": ([C.c_int32], C.c_char_p),
         "busseq_kernel_bytes": ([H, C.c_int32], C.c_double),
@@ -278,7 +279,7 @@ class Sampler:
 
     def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
                  keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0,
-                 zx_summaries: bool = False):
+                 zx_summaries: bool = False, hmc_gene_accept: bool = False):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -288,7 +289,8 @@ class Sampler:
             w_update = {"mh": W_MH, "gibbs": W_GIBBS}[w_update]
         opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
                       keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells),
-                      hmc_leapfrog=int(hmc_leapfrog), zx_summaries=int(bool(zx_summaries)))
+                      hmc_leapfrog=int(hmc_leapfrog), zx_summaries=int(bool(zx_summaries)),
+                      hmc_gene_accept=int(bool(hmc_gene_accept)))
         on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
         if on_dev:
             assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2
@@ -530,6 +532,15 @@ class Sampler:
         _check(lib().busseq_hmc_logpost_diff(self._h, C.byref(st), C.byref(out)))
         del keep
         return float(out.value)
+
+    def hmc_gene_logpost_diff(self, from_state: dict) -> np.ndarray:
+        """Per gene (hmc_gene_accept chains): the change of gene g's block log
+        posterior from `from_state` (which must carry the current delta)."""
+        st, keep = self._state_struct(from_state)
+        out = np.zeros(self.G)
+        _check(lib().busseq_hmc_gene_logpost_diff(self._h, C.byref(st), _p(out, _PD)))
+        del keep
+        return out
 
     def kernel_bytes(self, i: int) -> float:
         return float(lib().busseq_kernel_bytes(self._h, i))

@@ -154,6 +154,7 @@ struct DevState {
   // gradient-based block update (hmc_L > 0 selects it); flat layout
   // alpha [Gp] | beta [K][Gp] | nu [B][Gp] | psi [B][Gp] | delta [N]
   int hmc_L;
+  int hmc_gene;     // 1: per-gene decisions, delta fixed in the transition
   int64_t hmc_D;
   float* psi;       // [B][Gp] log phi: the position of the phi block
   float* hmc_mom;   // [D] momentum
@@ -179,6 +180,11 @@ struct DevState {
   float* hmc_fis;
   float* hmc_wbk;
   FF* hmc_epart_b;  // [ceil(G / 256)] per-CTA kinetic minus prior change of the gene blocks
+  // per-gene decisions (hmc_gene): kinetic minus prior change per diagonal
+  // coordinate [D] and per gene block [Gp], and each gene's outcome [Gp]
+  float* hmc_e;
+  float* hmc_eb;
+  uint8_t* hmc_gacc;
   float* phi_tab;  // [B][PHI_TAB][Gp]: sum_{j<x} log((phi_p + j) / (phi + j)) for the current proposal
   float* phi_lgd0; // [B][Gp]: lgamma(phi_p) - lgamma(phi)
   // The lgamma part of the phi ratio depends on an entry only through x, and

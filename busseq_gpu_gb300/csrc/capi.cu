@@ -44,8 +44,9 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_energy",   "k_hmc_accept",   "k_hmc_finish", "k_hmc_metric_blocks",
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
-                                    "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static"};
-constexpr int kNumKernels = 33;
+                                    "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static",
+                                    "k_hmc_accept_genes"};
+constexpr int kNumKernels = 34;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -53,7 +54,7 @@ enum : int {
   KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
-  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32
+  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32, KID_HMC_ACCEPT_GENES = 33
 };
 
 }  // namespace
@@ -84,7 +85,8 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
   const dim3 gene_grid(s.n_tiles, s.cap_g);
   switch (which) {
     case 0:
-      k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(s, s.hmc_L > 0 ? (int)PROP_GAMMA : (int)PROP_ALL);
+      k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(
+          s, s.hmc_L > 0 ? (int)(s.hmc_gene ? PROP_GAMMA | PROP_DELTA : PROP_GAMMA) : (int)PROP_ALL);
       LAUNCH_CHECK("k_propose");
       break;
     case 1:
@@ -127,7 +129,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
     case KID_HMC_DLL_STATIC:
       k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
       LAUNCH_CHECK("k_hmc_dll_prep");
-      k_hmc_dll_static<<<STATIC_CTAS, 256, 0, st>>>(s, s.n_tiles * s.cap_g);
+      k_hmc_dll_static<<<STATIC_CTAS, 256, 0, st>>>(s, s.n_tiles * s.cap_g, s.hmc_gene);
       LAUNCH_CHECK("k_hmc_dll_static");
       break;
     case 9:
@@ -174,14 +176,24 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_refresh_E");
       break;
     case KID_HMC_DLL:
-      k_hmc_dll<<<gene_grid, GENE_TILE, 0, st>>>(s);
+      k_hmc_dll<<<gene_grid, GENE_TILE, 0, st>>>(s, s.hmc_gene);
       LAUNCH_CHECK("k_hmc_dll");
       break;
     case KID_HMC_ENERGY:
-      k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, 1);
+      k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, st>>>(s, 1, s.hmc_gene);
       LAUNCH_CHECK("k_hmc_energy");
       break;
+    case KID_HMC_ACCEPT_GENES:
+      k_hmc_accept_genes<<<blocks_for(s.G, 256), 256, 0, st>>>(s, nullptr);
+      LAUNCH_CHECK("k_hmc_accept_genes");
+      break;
     case KID_HMC_ACCEPT:
+      if (s.hmc_gene) {
+        const int ng = (int)blocks_for(s.G, 256);
+        k_hmc_accept<<<1, 256, 0, st>>>(s, ng, ng, 0, 2);
+        LAUNCH_CHECK("k_hmc_accept");
+        break;
+      }
       k_hmc_accept<<<1, 256, 0, st>>>(s, s.n_tiles * s.cap_g + STATIC_CTAS, (int)blocks_for(s.hmc_D, 256),
                                       (int)blocks_for(s.G * 32, 256), 0);
       LAUNCH_CHECK("k_hmc_accept");
@@ -204,7 +216,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_mass");
       break;
     case KID_HMC_ENERGY_BLOCKS:
-      k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, st>>>(s, 1);
+      k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, st>>>(s, 1, s.hmc_gene);
       LAUNCH_CHECK("k_hmc_energy_blocks");
       break;
     case KID_HMC_FINISH:
@@ -220,7 +232,9 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
 // The kernels of one sweep, in order.  Random-walk MH (the reference's sweep):
 // proposals, Z/X, alpha, L, p/tau0, gamma, beta, nu, delta, phi, W, pi.  HMC:
 // proposals of gamma, Z/X, L, p/tau0, gamma, one HMC transition of
-// (alpha, beta, nu, delta, log phi), W, pi.
+// (alpha, beta, nu, delta, log phi), W, pi; with per-gene decisions the
+// transition moves (alpha, beta, nu, log phi) gene by gene and delta follows by
+// the random-walk step.
 std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
@@ -239,8 +253,13 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
     q.push_back(KID_HMC_DLL);
     q.push_back(KID_HMC_ENERGY);
     if (blocks) q.push_back(KID_HMC_ENERGY_BLOCKS);
-    const int tail[] = {KID_HMC_ACCEPT, KID_HMC_FINISH, KID_HMC_E, KID_W, KID_SORT_PI};
-    q.insert(q.end(), tail, tail + 5);
+    if (h->s.hmc_gene) q.push_back(KID_HMC_ACCEPT_GENES);
+    q.push_back(KID_HMC_ACCEPT);
+    q.push_back(KID_HMC_FINISH);
+    q.push_back(KID_HMC_E);
+    if (h->s.hmc_gene) q.push_back(KID_DELTA);  // delta by the random-walk step, given the new genes
+    q.push_back(KID_W);
+    q.push_back(KID_SORT_PI);
   } else {
     for (int k = 0; k <= KID_SORT_PI; ++k) {
       if (k == KID_PHI) q.push_back(KID_PHI_STATIC);
@@ -610,6 +629,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&s.part, (int64_t)s.cap_g * bq::NSLOT * Gp));
     // the gradient-based block update
     s.hmc_L = std::max(0, opt.hmc_leapfrog);
+    s.hmc_gene = s.hmc_L > 0 && opt.hmc_gene_accept ? 1 : 0;
     s.hmc_D = Gp * (1 + K + 2 * B) + N;
     if (s.hmc_L > 0) {
       TRY(h->alloc(&s.psi, B * Gp));
@@ -625,6 +645,12 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.hmc_epart, (int64_t)blocks_for(s.hmc_D, 256)));
       TRY(h->alloc(&s.hmc_sc, (int64_t)bq::HS_COUNT));
       TRY(h->alloc(&s.hmc_fis, s.hmc_D));
+      CUDA_TRY(cudaMemsetAsync(s.hmc_fis, 0, (size_t)s.hmc_D * sizeof(float), h->stream));
+      if (s.hmc_gene) {
+        TRY(h->alloc(&s.hmc_e, s.hmc_D));
+        TRY(h->alloc(&s.hmc_eb, Gp));
+        TRY(h->alloc(&s.hmc_gacc, Gp));
+      }
       s.hmc_nb = (K + B - 1 <= bq::HMC_BLOCK_MAX) ? K + B - 1 : 0;
       if (s.hmc_nb > 0) {
         TRY(h->alloc(&s.hmc_chol, (int64_t)bq::HMC_BLOCK_MAX * (bq::HMC_BLOCK_MAX + 1) / 2 * G));
@@ -1196,6 +1222,63 @@ int need_hmc(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
+// The change of the block's log posterior from `from` to the current state:
+// in total (per_gene 0, out[0]) or per gene (per_gene 1, out[G]; delta is
+// held, so the two states must share it).
+int logpost_diff(busseq_handle* h, const busseq_state* from, int per_gene, double* out) {
+  TRY(need_hmc(h));
+  if (!from || !out || !from->alpha || !from->beta || !from->nu || !from->phi || !from->delta)
+    return fail(BUSSEQ_ERR_ARG, "NULL argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const bq::DevState& s = h->s;
+  const int64_t G = s.G, Gp = s.Gp, N = s.N;
+  const int B = s.B, K = s.K;
+  std::vector<float> th((size_t)s.hmc_D, 0.0f);
+  for (int64_t g = 0; g < G; ++g) {
+    th[g] = from->alpha[g];
+    for (int k = 0; k < K; ++k) th[Gp + k * Gp + g] = from->beta[k * G + g];
+    for (int b = 0; b < B; ++b) {
+      th[Gp * (1 + K) + b * Gp + g] = from->nu[b * G + g];
+      th[Gp * (1 + K + B) + b * Gp + g] = logf(from->phi[b * G + g]);
+    }
+  }
+  for (int64_t i = 0; i < N; ++i) th[Gp * (1 + K + 2 * B) + i] = from->delta[i];
+  float* d = nullptr;
+  double* dg = nullptr;
+  CUDA_TRY(cudaMalloc(&d, s.hmc_D * 4));
+  if (per_gene && cudaMalloc(&dg, std::max<int64_t>(G, 1) * sizeof(double)) != cudaSuccess) {
+    cudaFree(d);
+    return fail(BUSSEQ_ERR_NOMEM, "log posterior difference: no device memory");
+  }
+  cudaError_t e = cudaMemcpyAsync(d, th.data(), s.hmc_D * 4, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) {
+    const dim3 gene_grid(s.n_tiles, s.cap_g);
+    bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
+    bq::k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, h->stream>>>(s);
+    bq::k_hmc_dll_static<<<STATIC_CTAS, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g, per_gene);
+    bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s, per_gene);
+    bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0, per_gene);
+    if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0, per_gene);
+    if (per_gene) {
+      bq::k_hmc_accept_genes<<<blocks_for(s.G, 256), 256, 0, h->stream>>>(s, dg);
+    } else {
+      bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g + STATIC_CTAS,
+                                                 (int)blocks_for(s.hmc_D, 256),
+                                                 (int)blocks_for(s.G * 32, 256), 1);
+    }
+    e = cudaGetLastError();
+  }
+  double sc[bq::HS_COUNT];
+  if (e == cudaSuccess && !per_gene) e = cudaMemcpyAsync(sc, s.hmc_sc, sizeof sc, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess && per_gene) e = cudaMemcpyAsync(out, dg, G * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  cudaFree(dg);
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "log posterior difference: %s", cudaGetErrorString(e));
+  if (!per_gene) *out = sc[bq::HS_LAST_DH];
+  return check_device_error(h);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1242,46 +1325,13 @@ int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric) {
 }
 
 int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* out) {
+  return logpost_diff(h, from, 0, out);
+}
+
+int busseq_hmc_gene_logpost_diff(busseq_handle* h, const busseq_state* from, double* out) {
   TRY(need_hmc(h));
-  if (!from || !out || !from->alpha || !from->beta || !from->nu || !from->phi || !from->delta)
-    return fail(BUSSEQ_ERR_ARG, "NULL argument");
-  CUDA_TRY(cudaSetDevice(h->device));
-  const bq::DevState& s = h->s;
-  const int64_t G = s.G, Gp = s.Gp, N = s.N;
-  const int B = s.B, K = s.K;
-  std::vector<float> th((size_t)s.hmc_D, 0.0f);
-  for (int64_t g = 0; g < G; ++g) {
-    th[g] = from->alpha[g];
-    for (int k = 0; k < K; ++k) th[Gp + k * Gp + g] = from->beta[k * G + g];
-    for (int b = 0; b < B; ++b) {
-      th[Gp * (1 + K) + b * Gp + g] = from->nu[b * G + g];
-      th[Gp * (1 + K + B) + b * Gp + g] = logf(from->phi[b * G + g]);
-    }
-  }
-  for (int64_t i = 0; i < N; ++i) th[Gp * (1 + K + 2 * B) + i] = from->delta[i];
-  float* d = nullptr;
-  CUDA_TRY(cudaMalloc(&d, s.hmc_D * 4));
-  cudaError_t e = cudaMemcpyAsync(d, th.data(), s.hmc_D * 4, cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess) {
-    const dim3 gene_grid(s.n_tiles, s.cap_g);
-    bq::k_hmc_set_th0<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, d);
-    bq::k_hmc_dll_prep<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, h->stream>>>(s);
-    bq::k_hmc_dll_static<<<STATIC_CTAS, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g);
-    bq::k_hmc_dll<<<gene_grid, bq::GENE_TILE, 0, h->stream>>>(s);
-    bq::k_hmc_energy<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s, 0);
-    if (s.hmc_nb > 0) bq::k_hmc_energy_blocks<<<blocks_for(s.G * 32, 256), 256, 0, h->stream>>>(s, 0);
-    bq::k_hmc_accept<<<1, 256, 0, h->stream>>>(s, s.n_tiles * s.cap_g + STATIC_CTAS,
-                                               (int)blocks_for(s.hmc_D, 256),
-                                               (int)blocks_for(s.G * 32, 256), 1);
-    e = cudaGetLastError();
-  }
-  double sc[bq::HS_COUNT];
-  if (e == cudaSuccess) e = cudaMemcpyAsync(sc, s.hmc_sc, sizeof sc, cudaMemcpyDeviceToHost, h->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-  cudaFree(d);
-  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "log posterior difference: %s", cudaGetErrorString(e));
-  *out = sc[bq::HS_LAST_DH];
-  return check_device_error(h);
+  if (!h->s.hmc_gene) return fail(BUSSEQ_ERR_STATE, "the chain was created without hmc_gene_accept");
+  return logpost_diff(h, from, 1, out);
 }
 
 int busseq_get_progress(busseq_handle* h, int32_t* n_done, int32_t* n_iter, int32_t* n_burnin) {

@@ -22,10 +22,10 @@ struct CkHeader {
   int32_t begun, finished, n_iter, n_burnin, n_unchanged, iter_host, iter_dev;
   int64_t G, N, nz0;
   uint64_t seed, y_fingerprint;
-  int32_t hmc_leapfrog, zx_summaries;
+  int32_t hmc_leapfrog, zx_summaries, hmc_gene_accept, pad;
 };
 constexpr char kCkMagic[8] = {'B', 'U', 'S', 'S', 'E', 'Q', 'C', 'K'};
-constexpr uint32_t kCkVersion = 2;
+constexpr uint32_t kCkVersion = 3;
 
 struct DevBlock {
   void* p;
@@ -130,6 +130,7 @@ int busseq_checkpoint_save(busseq_handle* h, const char* path) {
   hd.keep_draws = h->opt.keep_draws;
   hd.hmc_leapfrog = h->s.hmc_L;
   hd.zx_summaries = h->opt.zx_summaries ? 1 : 0;
+  hd.hmc_gene_accept = h->s.hmc_gene;
   hd.begun = h->begun ? 1 : 0;
   hd.finished = h->finished ? 1 : 0;
   hd.n_iter = h->n_iter;
@@ -219,7 +220,8 @@ int busseq_checkpoint_load(busseq_handle* h, const char* path) {
     return fail(BUSSEQ_ERR_ARG, "%s was written for B=%d K=%d G=%lld N=%lld, this chain has B=%d K=%d G=%lld N=%lld",
                 path, hd.B, hd.K, (long long)hd.G, (long long)hd.N, B, K, (long long)G, (long long)N);
   if (hd.seed != h->opt.seed || hd.w_update != h->opt.w_update || hd.keep_draws != h->opt.keep_draws ||
-      hd.hmc_leapfrog != h->s.hmc_L || hd.zx_summaries != (h->opt.zx_summaries ? 1 : 0))
+      hd.hmc_leapfrog != h->s.hmc_L || hd.zx_summaries != (h->opt.zx_summaries ? 1 : 0) ||
+      hd.hmc_gene_accept != h->s.hmc_gene)
     return fail(BUSSEQ_ERR_ARG, "%s was written with another seed, W move, keep_draws, HMC or zx_summaries setting",
                 path);
   uint64_t fp = 0;

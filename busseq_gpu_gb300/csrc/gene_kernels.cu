@@ -88,7 +88,12 @@ __global__ void k_propose(DevState s, int mask) {
   if (t < s.N) {
     if (mask & PROP_DELTA) {
       Stream st(s.seed, SID_DELTA, (uint64_t)t, iter);
-      s.delta_p[t] = __fmaf_rn(RW_STEP, normal(st), s.delta[t]);
+      // the reference's step; with the per-gene HMC decisions, 2.4 conditional
+      // standard deviations from the cell's adapted observed information (the
+      // optimal scale of a one-dimensional random walk)
+      const float step = s.hmc_gene ? 2.4f / sqrtf(s.hmc_fis[s.hmc_D - s.N + t] + (float)(1.0 / SIGMA2_DELTA))
+                                    : RW_STEP;
+      s.delta_p[t] = __fmaf_rn(step, normal(st), s.delta[t]);
     }
     return;
   }

@@ -91,7 +91,7 @@ __device__ __forceinline__ HmcCoord hmc_coord(const DevState& s, int64_t d) {
   c.kind = HK_DELTA;
   c.idx = d;
   c.seg = s.batch_of[d];
-  c.free = d != s.batch_off[c.seg];
+  c.free = d != s.batch_off[c.seg] && !s.hmc_gene;  // per-gene decisions: delta is held
   c.pos = s.delta + d;
   return c;
 }
@@ -100,6 +100,18 @@ __device__ __forceinline__ HmcCoord hmc_coord(const DevState& s, int64_t d) {
 // kernels when the block metric is on.
 __device__ __forceinline__ bool hmc_in_block(const DevState& s, const HmcCoord& c) {
   return s.hmc_nb > 0 && c.kind <= HK_NU;
+}
+
+// Leapfrog step of gene g's coordinates.  With per-gene decisions every gene
+// scales the transition's step by its own factor in [0.5, 1.5), drawn per
+// transition: the genes' trajectories then differ in length, and none stays at
+// a period of its (nearly Gaussian) conditional, where a fixed length would
+// return it to its start or reflect it (the factor does not depend on the
+// state, so each gene's transition stays reversible).
+__device__ __forceinline__ float hmc_eps_gene(const DevState& s, int64_t g) {
+  const float eps = (float)s.hmc_sc[HS_EPS_USED];
+  if (!s.hmc_gene) return eps;
+  return eps * (0.5f + uniform_at(s.seed, SID_HMC_ACC, 1 + (uint64_t)g, (uint32_t)*s.iter, 1));
 }
 
 __device__ __forceinline__ bool hmc_adapt_metric(const DevState& s, int iter) {
@@ -203,6 +215,11 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   if (len == 0) return;
   const bool adapt = METRIC && hmc_metric_now(s, metric_mode);
+  // per-cell (delta) sums of the gradient: not with per-gene decisions (delta is
+  // held); of the information: while the metric adapts (with per-gene
+  // decisions it scales delta's random-walk step)
+  const bool cells = !s.hmc_gene;
+  const bool cellw = METRIC && adapt;
   const int len8 = (len + 7) & ~7;
   for (int j = tid; j < len8; j += GENE_TILE) {
     const bool in = j < len;
@@ -274,8 +291,10 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
     }
     ar.add(fr);
     ap.add(fp);
-    const float cs = transpose_sum8(rv, lane);
-    if ((lane & 3) == 0) s_cell[warp][j0 + transpose_slot(lane)] = cs;
+    if (cells) {
+      const float cs = transpose_sum8(rv, lane);
+      if ((lane & 3) == 0) s_cell[warp][j0 + transpose_slot(lane)] = cs;
+    }
     if (METRIC && adapt) {
       aw.add(fw);
       ai.add(fi);
@@ -290,16 +309,17 @@ __device__ __forceinline__ void hmc_grad_body(const DevState& s, int metric_mode
     pr[2 * Gp] = gv ? aw.s - aw.c : 0.0f;
     pr[3 * Gp] = gv ? ai.s - ai.c : 0.0f;
   }
+  if (!cells && !cellw) return;  // uniform over the grid
   __syncthreads();
   for (int j = tid; j < len; j += GENE_TILE) {
     float t = 0.0f, tw = 0.0f;
 #pragma unroll
     for (int w = 0; w < GENE_TILE / 32; ++w) {
-      t += s_cell[w][j];
-      if (METRIC && adapt) tw += s_cellw[w][j];
+      if (cells) t += s_cell[w][j];
+      if (cellw) tw += s_cellw[w][j];
     }
-    s.hmc_cpart[(int64_t)tile * s.N + s_i[j]] = t;
-    if (METRIC && adapt) s.hmc_cpartw[(int64_t)tile * s.N + s_i[j]] = tw;
+    if (cells) s.hmc_cpart[(int64_t)tile * s.N + s_i[j]] = t;
+    if (cellw) s.hmc_cpartw[(int64_t)tile * s.N + s_i[j]] = tw;
   }
 }
 
@@ -393,6 +413,12 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode) {
   if (adapt) {
     s.hmc_mass[d] = c.free ? fmaxf((float)m, HMC_MASS_FLOOR) : 1.0f;
     s.hmc_fis[d] = c.free ? (float)(m - hmc_prior_precision(s, c)) : 0.0f;
+    if (s.hmc_gene && c.kind == HK_DELTA && c.idx != s.batch_off[c.seg]) {
+      // held in the transition; its information scales its random-walk step
+      float sw = 0.0f;
+      for (int t = 0; t < s.n_tiles; ++t) sw += s.hmc_cpartw[(int64_t)t * s.N + c.idx];
+      s.hmc_fis[d] = sw;
+    }
   }
 }
 
@@ -441,7 +467,7 @@ __global__ void k_hmc_leap(DevState s, int first) {
   if (d >= s.hmc_D) return;
   const HmcCoord c = hmc_coord(s, d);
   if (!c.free || hmc_in_block(s, c)) return;
-  const float eps = (float)s.hmc_sc[HS_EPS_USED];
+  const float eps = c.kind == HK_DELTA ? (float)s.hmc_sc[HS_EPS_USED] : hmc_eps_gene(s, c.idx);
   const float p = s.hmc_mom[d] + (first ? 0.5f : 1.0f) * eps * s.hmc_grad[d];
   s.hmc_mom[d] = p;
   const float v = *c.pos + eps * p / s.hmc_mass[d];
@@ -508,8 +534,9 @@ __global__ void k_hmc_dll_prep(DevState s) {
 // One warp per (batch, gene) (warps striding over the pairs): the Stirling
 // differences of its Y >= PHI_TAB values plus the part k_hmc_dll_prep left,
 // summed per CTA (fixed order) into hmc_hpart[base + blockIdx.x], next to
-// k_hmc_dll's per-CTA partials.
-__global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
+// k_hmc_dll's per-CTA partials; with per_gene, each pair's total goes to
+// phi_static[b][g] instead.
+__global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base, int per_gene) {
   __shared__ FF sw[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t nbg = (int64_t)s.B * s.G, nw = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -539,6 +566,11 @@ __global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
       }
     }
     FF f = acc.ff();
+    if (per_gene) {  // uniform over the grid
+      f = ff_warp_sum(f);
+      if (lane == 0) s.phi_static[pos] += ff_value(f);
+      continue;
+    }
     if (lane == 0) {
       const double d = s.phi_static[pos];
       const float hi = (float)d;
@@ -563,9 +595,10 @@ __global__ void __launch_bounds__(256) k_hmc_dll_static(DevState s, int base) {
 //        - dphi log1p(mu0 / phi0) + x deta,
 //   H(x) = [lgamma(phi1 + x) - lgamma(phi1)] - [lgamma(phi0 + x) - lgamma(phi0)],
 //   mu1 - mu0 = mu0 expm1(deta), phi1 - phi0 = phi0 expm1(psi1 - psi0).
-// One float-float partial per CTA in hmc_hpart.
+// One float-float partial per CTA in hmc_hpart; with per_gene, each gene's
+// chunk sum in part slot 0 instead (the decisions sum them per gene).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(GENE_TILE) k_hmc_dll(DevState s) {
+__global__ void __launch_bounds__(GENE_TILE) k_hmc_dll(DevState s, int per_gene) {
   __shared__ float tab[PHI_TAB][GENE_TILE];
   __shared__ __align__(16) int s_i[MAX_CG];
   __shared__ __align__(16) float s_D[MAX_CG];
@@ -653,6 +686,10 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_dll(DevState s) {
     }
     acc.add(f);
   }
+  if (per_gene) {  // uniform over the grid
+    if (gv) s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
+    return;
+  }
   FF fsum[1] = {gv ? acc.ff() : FF{0.0f, 0.0f}};
   long long nn[1] = {0};
   block_sum_ff<1, 1>(fsum, nn, shf, shn);
@@ -661,7 +698,7 @@ __global__ void __launch_bounds__(GENE_TILE) k_hmc_dll(DevState s) {
 
 // Closing half kick, then per coordinate the kinetic change minus the prior
 // change (cancellation-free), summed per CTA into hmc_epart.
-__global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
+__global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick, int per_gene) {
   __shared__ FF shf[8];
   __shared__ long long shn[8];
   const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -671,7 +708,8 @@ __global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
     if (c.free && !hmc_in_block(s, c)) {
       float p = s.hmc_mom[d];
       if (kick) {
-        p += 0.5f * (float)s.hmc_sc[HS_EPS_USED] * s.hmc_grad[d];
+        const float eps = c.kind == HK_DELTA ? (float)s.hmc_sc[HS_EPS_USED] : hmc_eps_gene(s, c.idx);
+        p += 0.5f * eps * s.hmc_grad[d];
         s.hmc_mom[d] = p;
       }
       const float p0 = s.hmc_mom0[d];
@@ -706,45 +744,108 @@ __global__ void __launch_bounds__(256) k_hmc_energy(DevState s, int kick) {
       }
       e = dK - dprior;
     }
+    if (per_gene) s.hmc_e[d] = e;
   }
+  if (per_gene) return;  // uniform over the grid
   FF f[1] = {FF{e, 0.0f}};
   long long n[1] = {0};
   block_sum_ff<1, 1>(f, n, shf, shn);
   if (threadIdx.x == 0) s.hmc_epart[blockIdx.x] = f[0];
 }
 
+// Per-gene decisions (hmc_gene): gene g's change of H = -log p + K is
+//   dH_g = -(its log-likelihood change: the chunk sums in part slot 0 over its
+//           (batch, type) segments, plus phi_static[b][g] over the batches)
+//          + (kinetic minus prior change of its coordinates: hmc_e over
+//             alpha_g, beta_gk, nu_bg, psi_bg, and hmc_eb[g] for its block),
+// decided on its own uniform (stream SID_HMC_ACC, entity 1 + g).  Per CTA: the
+// sum of the acceptance probabilities into hmc_hpart and the number accepted
+// into hmc_epart, for k_hmc_accept (mode 2).  With dlp, only the change of
+// each gene's log posterior (-dH_g, zero momenta) is written there.
+__global__ void __launch_bounds__(256) k_hmc_accept_genes(DevState s, double* dlp) {
+  __shared__ FF shf[8 * 2];
+  __shared__ long long shn[8];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t Gp = s.Gp;
+  const int B = s.B, K = s.K;
+  const uint32_t iter = (uint32_t)*s.iter;
+  double a = 0.0;
+  long long nacc = 0;
+  if (g < s.G) {
+    double dll = 0.0, e = 0.0;
+    for (int b = 0; b < B; ++b) {
+      for (int k = 0; k < K; ++k) dll += seg_sum(s, b, k, 0, g);
+      dll += s.phi_static[(int64_t)b * Gp + g];
+    }
+    e += s.hmc_e[g];
+    for (int k = 1; k < K; ++k) e += s.hmc_e[Gp + (int64_t)k * Gp + g];
+    for (int b = 1; b < B; ++b) e += s.hmc_e[Gp * (1 + K) + (int64_t)b * Gp + g];
+    for (int b = 0; b < B; ++b) e += s.hmc_e[Gp * (1 + K + B) + (int64_t)b * Gp + g];
+    if (s.hmc_nb > 0) e += s.hmc_eb[g];
+    const double dH = -dll + e;
+    if (dlp) {
+      dlp[g] = -dH;
+    } else {
+      a = dH == dH ? fmin(1.0, exp(-dH)) : 0.0;
+      const float u = uniform_at(s.seed, SID_HMC_ACC, 1 + (uint64_t)g, iter, 0);
+      const bool accept = dH == dH && (double)logf(u) < -dH;
+      s.hmc_gacc[g] = accept ? 1 : 0;
+      nacc = accept ? 1 : 0;
+    }
+  }
+  if (dlp) return;  // uniform over the grid
+  const float ah = (float)a;
+  FF f[1] = {FF{ah, (float)(a - (double)ah)}};
+  long long n[1] = {nacc};
+  block_sum_ff<1, 1>(f, n, shf, shn);
+  if (threadIdx.x == 0) {
+    s.hmc_hpart[blockIdx.x] = f[0];
+    s.hmc_epart[blockIdx.x] = FF{(float)n[0], 0.0f};
+  }
+}
+
 // The Metropolis decision on H = -log p + K (one CTA), and the step-size
 // adaptation.  mode 1 only reports the change of the log posterior
-// (-(H1 - H0) with zero momenta) in HS_LAST_DH.
+// (-(H1 - H0) with zero momenta) in HS_LAST_DH; mode 2 takes the per-gene
+// decisions of k_hmc_accept_genes (n_hpart = n_epart = its CTAs) and adapts the
+// step size to their mean acceptance probability.
 __global__ void __launch_bounds__(256) k_hmc_accept(DevState s, int n_hpart, int n_epart, int n_epart_b, int mode) {
   __shared__ FF shf[8 * 2];
   __shared__ long long shn[8];
   FF acc{0.0f, 0.0f}, ace{0.0f, 0.0f};
   for (int t = threadIdx.x; t < n_hpart; t += blockDim.x) acc = ff_add(acc, s.hmc_hpart[t]);
   for (int t = threadIdx.x; t < n_epart; t += blockDim.x) ace = ff_add(ace, s.hmc_epart[t]);
-  if (s.hmc_nb > 0)
+  if (s.hmc_nb > 0 && mode != 2)
     for (int t = threadIdx.x; t < n_epart_b; t += blockDim.x) ace = ff_add(ace, s.hmc_epart_b[t]);
   FF f[2] = {acc, ace};
   long long n[1] = {0};
   block_sum_ff<2, 1>(f, n, shf, shn);
   if (threadIdx.x != 0) return;
-  const double dll = ff_value(f[0]);
-  const double dH = -dll + ff_value(f[1]);
   double* sc = s.hmc_sc;
-  sc[HS_LAST_DH] = dH;
-  if (mode == 1) {
-    sc[HS_LAST_DH] = -dH;
-    return;
-  }
   const int iter = *s.iter;
-  const double a = dH == dH ? fmin(1.0, exp(-dH)) : 0.0;
-  const float u = uniform_at(s.seed, SID_HMC_ACC, 0, (uint32_t)iter, 0);
-  const bool accept = dH == dH && (double)logf(u) < -dH;
-  sc[HS_ACCEPTED] = accept ? 1.0 : 0.0;
+  double a, acc_frac;
+  if (mode == 2) {
+    a = ff_value(f[0]) / (double)s.G;         // mean acceptance probability over the genes
+    acc_frac = ff_value(f[1]) / (double)s.G;  // fraction of genes accepted
+    sc[HS_LAST_DH] = 0.0;
+  } else {
+    const double dll = ff_value(f[0]);
+    const double dH = -dll + ff_value(f[1]);
+    sc[HS_LAST_DH] = dH;
+    if (mode == 1) {
+      sc[HS_LAST_DH] = -dH;
+      return;
+    }
+    a = dH == dH ? fmin(1.0, exp(-dH)) : 0.0;
+    const float u = uniform_at(s.seed, SID_HMC_ACC, 0, (uint32_t)iter, 0);
+    const bool accept = dH == dH && (double)logf(u) < -dH;
+    sc[HS_ACCEPTED] = accept ? 1.0 : 0.0;
+    acc_frac = accept ? 1.0 : 0.0;
+  }
   sc[HS_LAST_ACC] = a;
   if (iter >= s.n_burnin) {
     sc[HS_N_KEPT] += 1.0;
-    sc[HS_ACC_KEPT] += accept ? 1.0 : 0.0;
+    sc[HS_ACC_KEPT] += acc_frac;
   }
   // dual averaging during burn-in, restarted when the metric freezes
   if (iter < s.n_burnin) {
@@ -767,13 +868,15 @@ __global__ void __launch_bounds__(256) k_hmc_accept(DevState s, int n_hpart, int
   }
 }
 
-// Restores the start of the trajectory when the transition was rejected.
+// Restores the start of the trajectory when the transition was rejected (with
+// per-gene decisions: the coordinates of each rejected gene).
 __global__ void k_hmc_finish(DevState s) {
   const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= s.hmc_D) return;
-  if (s.hmc_sc[HS_ACCEPTED] != 0.0) return;
+  if (!s.hmc_gene && s.hmc_sc[HS_ACCEPTED] != 0.0) return;
   const HmcCoord c = hmc_coord(s, d);
   if (!c.free) return;
+  if (s.hmc_gene && s.hmc_gacc[c.idx]) return;  // c.idx is the gene of every free coordinate there
   const float v = s.hmc_th0[d];
   *c.pos = v;
   hmc_derived(s, c, v);
@@ -924,7 +1027,7 @@ __global__ void __launch_bounds__(128) k_hmc_leap_blocks(DevState s, int first) 
   const int lane = threadIdx.x & 31;
   if (g >= s.G || s.hmc_nb == 0) return;
   const int nb = s.hmc_nb;
-  const float eps = (float)s.hmc_sc[HS_EPS_USED];
+  const float eps = hmc_eps_gene(s, g);
   float p = 0.0f;
   int64_t d = 0;
   if (lane < nb) {
@@ -938,7 +1041,7 @@ __global__ void __launch_bounds__(128) k_hmc_leap_blocks(DevState s, int first) 
 
 // Closing half kick of the gene blocks, then their kinetic change
 // (p^T M^{-1} p - p0^T M^{-1} p0) / 2 minus the prior change, per CTA.
-__global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick) {
+__global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick, int per_gene) {
   __shared__ FF shf[8];
   __shared__ long long shn[8];
   const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -946,7 +1049,7 @@ __global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick)
   float e = 0.0f;
   if (g < s.G && s.hmc_nb > 0) {
     const int nb = s.hmc_nb, K = s.K;
-    const float eps = (float)s.hmc_sc[HS_EPS_USED];
+    const float eps = hmc_eps_gene(s, g);
     float p = 0.0f, p0 = 0.0f, dprior = 0.0f;
     if (lane < nb) {
       const int64_t d = hmc_block_pos(s, lane, g);
@@ -978,6 +1081,11 @@ __global__ void __launch_bounds__(256) k_hmc_energy_blocks(DevState s, int kick)
       dk = 0.5f * (p * v - p0 * v0);
     }
     e = dk - dprior;
+  }
+  if (per_gene) {  // uniform over the grid; warps are whole genes
+    const double eg = warp_sum((double)e);
+    if (g < s.G && s.hmc_nb > 0 && lane == 0) s.hmc_eb[g] = (float)eg;
+    return;
   }
   FF f[1] = {FF{e, 0.0f}};
   long long n[1] = {0};

@@ -49,16 +49,17 @@ __global__ void k_hmc_assemble(DevState s, int metric_mode);
 __global__ void k_hmc_start(DevState s);
 __global__ void k_hmc_leap(DevState s, int first);
 __global__ void k_hmc_refresh_E(DevState s);
-__global__ void k_hmc_dll(DevState s);
+__global__ void k_hmc_dll(DevState s, int per_gene);
 __global__ void k_hmc_dll_prep(DevState s);
-__global__ void k_hmc_dll_static(DevState s, int base);
-__global__ void k_hmc_energy(DevState s, int kick);
+__global__ void k_hmc_dll_static(DevState s, int base, int per_gene);
+__global__ void k_hmc_energy(DevState s, int kick, int per_gene);
 __global__ void k_hmc_accept(DevState s, int n_hpart, int n_epart, int n_epart_b, int mode);
+__global__ void k_hmc_accept_genes(DevState s, double* dlp);
 __global__ void k_hmc_metric_blocks(DevState s, int metric_mode);
 __global__ void k_hmc_mass(DevState s);
 __global__ void k_hmc_start_blocks(DevState s);
 __global__ void k_hmc_leap_blocks(DevState s, int first);
-__global__ void k_hmc_energy_blocks(DevState s, int kick);
+__global__ void k_hmc_energy_blocks(DevState s, int kick, int per_gene);
 __global__ void k_hmc_finish(DevState s);
 __global__ void k_hmc_set_th0(DevState s, const float* src);
 __global__ void k_hmc_unit_mass(DevState s);

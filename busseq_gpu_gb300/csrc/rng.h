@@ -54,7 +54,8 @@ enum StreamId : uint32_t {
   SID_W = 13,            // cell i      : proposal / categorical (u0), accept (u1)
   SID_PI = 14,           // b*K+k       : Dirichlet component (Gamma draw)
   SID_HMC_MOM = 15,      // coordinate d: momentum of the HMC block update
-  SID_HMC_ACC = 16,      // 0           : HMC accept (u0), step-size jitter (u1)
+  SID_HMC_ACC = 16,      // 0           : HMC accept (u0), step-size jitter (u1);
+                         // 1 + gene g  : per-gene accept (u0), the gene's step factor (u1)
   SID_CORRECT = 17,      // entry i*G+g : randomised PIT of the batch-corrected count (two words)
   SID_INIT_W = 20,       // cell i      : initial cell type
   SID_INIT_L = 21,       // k*G+g       : initial indicator L

@@ -73,7 +73,13 @@ typedef struct busseq_options {
   int32_t zx_summaries; /* 1: over the kept sweeps, count Z = 1 and sum X at every
                            Y == 0 entry (busseq_get_zx_summaries; not in the
                            reference, which writes the last sweep's Z and X)    */
-  int32_t reserved[6];
+  int32_t hmc_gene_accept; /* with hmc_leapfrog > 0: 1 moves every gene's block
+                           (alpha, beta, nu, log phi) along one shared trajectory
+                           and accepts or rejects each gene on its own energy
+                           change (the block posterior factorises over genes
+                           given delta); delta then takes the random-walk step.
+                           0: one decision for the whole block, delta included */
+  int32_t reserved[5];
 } busseq_options;
 
 /* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
@@ -238,12 +244,19 @@ int busseq_checkpoint_load(busseq_handle* h, const char* path);
  * current state, and (when `metric` is not NULL) the diagonal metric the
  * transitions would adapt to there, in the flat layout
  *   alpha [G] | beta [K*G] | nu [B*G] | log phi [B*G] | delta [N]
- * (fixed coordinates: gradient 0, metric 1).
+ * (fixed coordinates: gradient 0, metric 1; with hmc_gene_accept delta is
+ * fixed).
  * busseq_hmc_logpost_diff: log posterior of the current state minus that of
- * `from` (same conditioning: X, W, L, p, tau0 of the current state).  */
+ * `from` (same conditioning: X, W, L, p, tau0 of the current state).
+ * busseq_hmc_gene_logpost_diff (hmc_gene_accept chains): the same change per
+ * gene, out[G]: gene g's block (alpha_g, beta_g., nu_g., phi_.g) with delta
+ * held at the current state's (`from` must carry the same delta).
+ * With hmc_gene_accept, out[1] of busseq_hmc_stats is the mean fraction of
+ * genes accepted and out[2] their mean acceptance probability.  */
 int busseq_hmc_stats(busseq_handle* h, double out[4]);
 int busseq_hmc_gradient(busseq_handle* h, double* grad, double* metric);
 int busseq_hmc_logpost_diff(busseq_handle* h, const busseq_state* from, double* out);
+int busseq_hmc_gene_logpost_diff(busseq_handle* h, const busseq_state* from, double* out);
 
 /* Position of the current run: sweeps launched so far, run length and burn-in
  * length (all 0 before busseq_begin).  NULL pointers are skipped. */

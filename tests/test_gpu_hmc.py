@@ -166,3 +166,92 @@ def test_gradient_accessor_leaves_the_chain_unchanged(warm):
     a.close()
     for k in st_ref:
         assert np.array_equal(st_ref[k], st[k]), k
+
+
+def _perturbed_genes(st, rng):
+    """st with alpha, beta, nu and phi moved (delta kept: the per-gene blocks)."""
+    masks = _free_masks()
+    B = len(N_B)
+    st_b = {k: np.array(v, copy=True) for k, v in st.items()}
+    st_b["alpha"] = st["alpha"] + rng.normal(0, 0.01, G).astype(np.float32)
+    st_b["beta"] = st["beta"] + (rng.normal(0, 0.01, (K, G)) * masks["beta"]).astype(np.float32)
+    st_b["nu"] = st["nu"] + (rng.normal(0, 0.01, (B, G)) * masks["nu"]).astype(np.float32)
+    st_b["phi"] = (st["phi"] * np.exp(rng.normal(0, 0.05, (B, G)))).astype(np.float32)
+    return st_b
+
+
+def test_gene_logpost_differences_match_oracle(warm):
+    """Per-gene decisions: each gene's change of its block log posterior (delta
+    held) against the oracle's log posterior of the state that differs in that
+    gene only, and their sum against the whole change."""
+    Y, _, st = warm
+    rng = np.random.default_rng(4)
+    st_b = _perturbed_genes(st, rng)
+    h = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=5, hmc_gene_accept=True)
+    h.set_state(st_b)
+    got = h.hmc_gene_logpost_diff(st)
+    h.close()
+    oa = oracle_state(Y, np.array(N_B), K, SEED, st)
+    base = oa.hmc_logpost()
+    total = oracle_state(Y, np.array(N_B), K, SEED, st_b).hmc_logpost() - base
+    assert abs(got.sum() - total) <= 5e-3 + 1e-5 * abs(total), (got.sum(), total)
+    for g in rng.choice(G, 5, replace=False):
+        st_g = {k: np.array(v, copy=True) for k, v in st.items()}
+        st_g["alpha"][g] = st_b["alpha"][g]
+        for f in ("beta", "nu", "phi"):
+            st_g[f][:, g] = st_b[f][:, g]
+        want = oracle_state(Y, np.array(N_B), K, SEED, st_g).hmc_logpost() - base
+        assert abs(got[g] - want) <= 2e-3 + 1e-5 * abs(want), (g, got[g], want)
+
+
+def test_gene_decision_chain(warm, tmp_path):
+    """Per-gene decisions: adaptation, acceptance, recovery of the types, the
+    invariants, bit-identical reruns and exact checkpoint / resume."""
+    Y, W_true, _ = warm
+    mh = bq.Sampler(Y, N_B, K, seed=SEED)
+    mh.run(160, 80, 40)
+    ari_mh = _ari(mh.estimates()["W"], W_true)
+    mh.close()
+    runs = []
+    for _ in range(2):
+        h = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=10, hmc_gene_accept=True, keep_draws=True)
+        h.run(160, 80, 40)
+        runs.append((h.hmc_stats(), h.estimates(), h.get_state(), h.preserved()))
+        h.close()
+    stats, est, st, pres = runs[0]
+    ari = _ari(est["W"], W_true)
+    print("per-gene HMC", stats, "ARI", ari, "MH ARI", ari_mh)
+    assert np.isfinite(stats["step_size"]) and stats["step_size"] > 0
+    assert 0.4 <= stats["accept_rate_kept"] <= 0.99, stats
+    assert ari > min(0.7, ari_mh - 0.05)
+    assert np.array_equal(st["X"][Y > 0], Y[Y > 0]) and not st["Z"][Y > 0].any()
+    assert np.all(st["beta"][0] == 0) and np.all(st["nu"][0] == 0)
+    off = np.concatenate([[0], np.cumsum(N_B)])[:-1]
+    assert np.all(st["delta"][off] == 0)
+    moved = np.mean(np.abs(np.diff(pres["beta"], axis=1)) > 0, axis=1)
+    assert np.median(moved) > 0.3
+    for k in st:
+        assert np.array_equal(st[k], runs[1][2][k]), k
+    # checkpoint / resume, and a chain with one decision for the whole block refuses it
+    ref = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4, hmc_gene_accept=True)
+    ref.run(30, 16, 8)
+    st_ref = ref.get_state()
+    ref.close()
+    a = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4, hmc_gene_accept=True)
+    a.begin(30, 16, 8)
+    a.sweeps(11)
+    path = str(tmp_path / "gene.ck")
+    a.checkpoint_save(path)
+    a.close()
+    c = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4)
+    with pytest.raises(bq.BusseqError):
+        c.checkpoint_load(path)
+    c.close()
+    b = bq.Sampler(Y, N_B, K, seed=SEED, hmc_leapfrog=4, hmc_gene_accept=True)
+    b.checkpoint_load(path)
+    b.sweeps(19)
+    b.finish()
+    st2 = b.get_state()
+    b.close()
+    for k in st_ref:
+        assert np.array_equal(st_ref[k], st2[k]), k
