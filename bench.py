@@ -41,11 +41,12 @@ sys.path.insert(0, ROOT)
 
 CFG1 = dict(n_b=[2500, 2500, 2500, 2500], G=10000, K=8, seed=13580)
 # the large uneven workload: 6 batches, 15 % differential genes, phi ~ U(2, 30), HMC block
-# update (10 leapfrog steps, per-gene decisions; --mh runs the plain sampler on it)
-CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide", hmc=10, gene=True)
-# config-1 data with the HMC block update (10 leapfrog steps, per-gene decisions) in place of
-# the random-walk steps (--gene-accept 0: one decision for the whole block)
-CFG2 = dict(CFG1, hmc=10, gene=True)
+# update (10 leapfrog steps; --mh runs the plain sampler on it, --gene-accept 1 the per-gene
+# decisions)
+CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=13583, sim="wide", hmc=10)
+# config-1 data with the HMC block update (10 leapfrog steps) in place of the random-walk
+# steps (--gene-accept 1: per-gene decisions)
+CFG2 = dict(CFG1, hmc=10)
 CFG3 = dict(CFG1, ks=list(range(3, 11)))  # config-1 data fitted by 8 chains, K = 3 .. 10
 WORKLOADS = {"config1": CFG1, "config2": CFG2, "config3": CFG3, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
@@ -424,9 +425,9 @@ def main():
                     help="run the plain random-walk sampler even where the workload uses the HMC update")
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS),
                     help="config1 (the headline, default), config2 (config-1 data, HMC block update with 10 "
-                         "leapfrog steps and per-gene decisions), config3 (config-1 data, 8 chains K=3..10 batched "
-                         "in one graph per sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, "
-                         "uneven batches, the same HMC update)")
+                         "leapfrog steps), config3 (config-1 data, 8 chains K=3..10 batched in one graph per "
+                         "sweep; 1000 steps unless --steps) or config4 (N=50000, G=20000, K=12, uneven batches, "
+                         "the same HMC update)")
     ap.add_argument("--only-value", action="store_true",
                     help="measure only the device-resident sweep rate (the short run used under ncu)")
     ap.add_argument("--corrected-counts", action="store_true",
