@@ -1,0 +1,48 @@
+"""Host logic of bench.py's CPU baselines (no GPU): the batch-corrected-count
+baseline keeps its oracle sample to genes whose tail sums stay short."""
+import numpy as np
+
+import bench
+
+
+class _FakeRun:
+    """Stands in for a finished sampler: estimates() of a small state."""
+
+    def __init__(self, est):
+        self._est = est
+
+    def estimates(self, with_XZ=True):
+        return self._est
+
+
+def _est(rng, n_b, G, K, tiny_phi_genes=()):
+    B, N = len(n_b), sum(n_b)
+    alpha = rng.uniform(0.5, 2.5, G)
+    beta = np.zeros((K, G))
+    beta[1:] = rng.normal(0, 0.5, (K - 1, G))
+    nu = np.zeros((B, G))
+    nu[1:] = rng.normal(0.3, 0.2, (B - 1, G))
+    phi = rng.uniform(5, 20, (B, G))
+    for g in tiny_phi_genes:
+        phi[1, g] = 1e-6  # a gene whose posterior dispersion collapsed in one batch
+    delta = rng.normal(0, 0.1, N)
+    W = rng.integers(0, K, N).astype(np.int32)
+    X = rng.poisson(5.0, (N, G)).astype(np.int32)
+    return {"alpha": alpha, "beta": beta, "nu": nu, "phi": phi, "delta": delta, "W": W, "X": X}
+
+
+def test_corrected_baseline_skips_genes_with_collapsed_dispersion():
+    rng = np.random.default_rng(0)
+    n_b, G, K = [12, 10], 30, 3
+    est = _est(rng, n_b, G, K, tiny_phi_genes=(3, 17))
+    out = bench.corrected_cpu_rate(_FakeRun(est), n_b, 7, cells_per_batch=5)
+    assert out is not None and out["entries_per_s"] > 0
+    assert "28 of 30 genes" in out["sample"], out["sample"]
+    assert "%d entries" % (10 * 28) in out["sample"]
+
+
+def test_corrected_baseline_keeps_every_gene_of_a_moderate_run():
+    rng = np.random.default_rng(1)
+    n_b, G, K = [8, 8, 6], 20, 2
+    out = bench.corrected_cpu_rate(_FakeRun(_est(rng, n_b, G, K)), n_b, 3, cells_per_batch=4)
+    assert "20 of 20 genes" in out["sample"], out["sample"]
