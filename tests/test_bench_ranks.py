@@ -34,7 +34,7 @@ def test_two_gloo_ranks_agree_on_the_slowest_time():
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
     world, port = 2, _free_port()
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:  # no fork of a process that may hold OpenMP threads
         out = man.dict()
         mp.start_processes(_rank, args=(world, port, out), nprocs=world, join=True, start_method="spawn")
         res = dict(out)
