@@ -164,7 +164,7 @@ struct DevState {
   float* hmc_th0;   // [D] coordinates at the start of the transition
   float* hmc_part;  // [cap_g][NSLOT][Gp] per-chunk gradient (and information) sums
   float* hmc_cpart; // [n_tiles][N] per-tile sums of d ll / d delta
-  float* hmc_cpartw;// [n_tiles][N] per-tile Fisher information of delta
+  float* hmc_cpartw;// [n_tiles][N] per-tile observed information of delta
   FF* hmc_hpart;    // [n_tiles * cap_g] per-CTA log-likelihood change
   FF* hmc_epart;    // [ceil(D / 256)] per-CTA kinetic minus prior change
   double* hmc_sc;   // [HS_COUNT]
@@ -176,7 +176,7 @@ struct DevState {
   float* hmc_minv;  // [nb * nb][G] inverse of each gene's block metric (velocity and kinetic energy)
   // frozen data of the metric: the information part of every diagonal mass
   // (without the priors, which follow the current L and tau0) and the
-  // per-segment Fisher sums W_bkg of the blocks [B*K][G]
+  // per-segment information sums W_bkg of the blocks [B*K][G]
   float* hmc_fis;
   float* hmc_wbk;
   FF* hmc_epart_b;  // [ceil(G / 256)] per-CTA kinetic minus prior change of the gene blocks

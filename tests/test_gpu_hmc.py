@@ -4,7 +4,7 @@ chains (adaptation, acceptance, recovery of the cell types, reproducibility,
 checkpoint / resume).
 
 Tolerances: the gradient within 2e-3 posterior standard deviations (scale
-sqrt(metric)) plus 1e-4 relative; the Fisher metric of the eta-coordinates
+sqrt(metric)) plus 1e-4 relative; the metric (observed information) of the eta-coordinates
 within 1e-3 relative; the observed information of log phi within 1e-2 relative
 + 0.5 (it sums terms of both signs); log-posterior differences within
 5e-3 + 1e-5 |diff| (per-entry float terms of a few units over ~10^5 entries).
