@@ -11,6 +11,11 @@
 //                         counts (randomised quantile matching of _post_X)
 //   --posterior-zx        also write <prefix>_post_X_mean.txt and _post_Z_prob.txt,
 //                         E[X] and P(Z = 1) over the kept sweeps
+//   --hmc=L               replace the random-walk steps of alpha, beta, nu, delta and
+//                         phi by one Hamiltonian Monte Carlo transition with L
+//                         leapfrog steps per sweep
+//   --hmc-gene            with --hmc: accept or reject each gene's block on its own
+//                         (delta by an adapted random-walk step)
 #include "busseq_gb300.h"
 
 #include <getopt.h>
@@ -50,6 +55,7 @@ int main(int argc, char** argv) {
   char n_file[4096] = "";
   int n_file_flag = 0, burnin_flag = 1, unchanged_flag = 1, seed_flag = 1;
   int w_update = BUSSEQ_W_MH, device = 0, stats = 0, ck_every = 0, stop_after = 0, corrected = 0, posterior_zx = 0;
+  int hmc_leapfrog = 0, hmc_gene = 0;
   std::string ck_path, resume_path;
 
   static struct option longopts[] = {{"w-update", required_argument, nullptr, 1000},
@@ -61,6 +67,8 @@ int main(int argc, char** argv) {
                                      {"stop-after", required_argument, nullptr, 1006},
                                      {"corrected", no_argument, nullptr, 1007},
                                      {"posterior-zx", no_argument, nullptr, 1008},
+                                     {"hmc", required_argument, nullptr, 1009},
+                                     {"hmc-gene", no_argument, nullptr, 1010},
                                      {nullptr, 0, nullptr, 0}};
   int opt;
   while ((opt = getopt_long(argc, argv, "B:N:G:K:s:c:i:b:u:po:", longopts, nullptr)) != -1) {
@@ -89,6 +97,17 @@ int main(int argc, char** argv) {
       case 1006: stop_after = atoi(optarg); break;
       case 1007: corrected = 1; break;
       case 1008: posterior_zx = 1; break;
+      case 1009: {
+        char* end = nullptr;
+        const long L = strtol(optarg, &end, 10);
+        if (!end || *end || L < 1 || L > 1000) {
+          fprintf(stderr, "--hmc takes a number of leapfrog steps from 1 to 1000\n");
+          return 1;
+        }
+        hmc_leapfrog = (int)L;
+        break;
+      }
+      case 1010: hmc_gene = 1; break;
       default:
         printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
                "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
@@ -96,6 +115,10 @@ int main(int argc, char** argv) {
                argv[0]);
         exit(1);
     }
+  }
+  if (hmc_gene && !hmc_leapfrog) {
+    fprintf(stderr, "--hmc-gene needs --hmc=L\n");
+    return 1;
   }
   if (B > BUSSEQ_MAX_BATCHES || B > (int)n_b.size()) {
     printf("At most %d batches are supported.\n", BUSSEQ_MAX_BATCHES);
@@ -153,6 +176,8 @@ int main(int argc, char** argv) {
   o.w_update = w_update;
   o.keep_draws = print_preserved;
   o.zx_summaries = posterior_zx;
+  o.hmc_leapfrog = hmc_leapfrog;
+  o.hmc_gene_accept = hmc_gene;
   o.device = device;
   busseq_handle* h = nullptr;
   if (busseq_create(&dims, Y.data(), 0, &o, &h) != BUSSEQ_OK) die_lib("initialisation");

@@ -124,6 +124,14 @@ def test_cli_argument_checks_match_reference(tmp_path):
     assert r.returncode == 1 and r.stdout.startswith("Error Usage:")
 
 
+def test_cli_hmc_flags_are_checked():
+    for bad in ("--hmc=0", "--hmc=abc", "--hmc=2000"):
+        r = _cli(bad, "-s", "1")
+        assert r.returncode == 1 and "--hmc takes a number of leapfrog steps" in r.stderr, bad
+    r = _cli("--hmc-gene", "-s", "1")
+    assert r.returncode == 1 and "--hmc-gene needs --hmc=L" in r.stderr
+
+
 def test_cli_missing_count_file_fails_cleanly(tmp_path):
     dim = tmp_path / "dim.txt"
     dim.write_text("10 10")

@@ -69,3 +69,31 @@ def test_preserved_files_are_byte_exact(tmp_path):
         want = "".join("\t".join(fmt(v) for v in row) + "\n" for row in M).encode()
         with open(prefix + name, "rb") as f:
             assert f.read() == want, name
+
+
+@pytest.mark.parametrize("gene", [False, True])
+def test_cli_hmc_matches_the_library_chain(tmp_path, gene):
+    """--hmc=L (and --hmc-gene) run the gradient-based update: the posterior
+    means the command line writes are those of the same chain run through the
+    library (same seed and initial p)."""
+    import ctypes
+    n_b, G, K = [30, 25, 20], 90, 3
+    Y, _, _ = bq.simulate(n_b, G, K, 5)
+    txt, dim = tmp_path / "c.txt", tmp_path / "dim.txt"
+    np.savetxt(txt, Y, fmt="%d", delimiter=" ")
+    dim.write_text("\n".join(str(x) for x in n_b))
+    args = [bq.CLI_PATH, "-B", "3", "-N", str(dim), "-G", str(G), "-K", str(K), "-s", "5", "-c", str(txt),
+            "-i", "20", "-b", "10", "-u", "5", "-o", str(tmp_path / "h"), "--hmc=4"] + (["--hmc-gene"] if gene else [])
+    r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    alpha = np.loadtxt(str(tmp_path / "h") + "_post_alpha.txt")
+    phi = np.loadtxt(str(tmp_path / "h") + "_post_phi.txt")
+    libc = ctypes.CDLL(None)
+    libc.srand(5)
+    p0 = libc.rand() * 0.5 / 2147483647.0  # the command line's initial p (glibc rand)
+    s = bq.Sampler(Y, n_b, K, seed=5, p0=p0, hmc_leapfrog=4, hmc_gene_accept=gene)
+    s.run(20, 10, 5)
+    est = s.estimates()
+    s.close()
+    np.testing.assert_allclose(alpha, est["alpha"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(phi, est["phi"], rtol=0, atol=1e-6)
