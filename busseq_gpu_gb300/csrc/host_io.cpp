@@ -11,8 +11,13 @@
 // little-endian.  busseq_read_counts recognises it by that magic and reads it
 // with one pread per host thread; busseq_write_counts_binary writes it (a text
 // count file converted once loads without parsing afterwards).
+//
+// Compressed counts (not in the reference): a gzip file (magic 1f 8b) of either
+// format is inflated into memory and then parsed as above.  zlib is loaded at
+// run time (libz.so.1), so the build does not depend on its headers.
 #include "busseq_gb300.h"
 
+#include <dlfcn.h>
 #include <fcntl.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -176,62 +181,27 @@ int read_counts_binary(int fd, const char* path, int64_t N, int64_t G, int64_t f
   return BUSSEQ_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int busseq_write_counts_binary(const char* path, int64_t N, int64_t G, const int32_t* Y) {
-  if (!path || !Y || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
-  if (!host_little_endian()) return busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
-  FILE* f = fopen(path, "wb");
-  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open ") + path + " for writing").c_str());
-  const int64_t hdr[2] = {N, G};
-  bool ok = fwrite(kBinMagic, 1, 8, f) == 8 && fwrite(hdr, 8, 2, f) == 2;
-  const size_t n = (size_t)(N * G);
-  for (size_t o = 0; ok && o < n;) {
-    const size_t c = std::min<size_t>(n - o, (size_t)1 << 26);
-    ok = fwrite(Y + o, 4, c, f) == c;
-    o += c;
+// The same payload from a buffer holding the whole (inflated) file.
+int binary_from_buffer(const char* buf, int64_t size, const char* path, int64_t N, int64_t G, int32_t* out) {
+  int64_t hdr[2];
+  memcpy(hdr, buf + 8, sizeof hdr);
+  if (hdr[0] != N || hdr[1] != G) {
+    char msg[240];
+    snprintf(msg, sizeof(msg), "binary count file %s holds N=%lld G=%lld, expected N=%lld G=%lld", path,
+             (long long)hdr[0], (long long)hdr[1], (long long)N, (long long)G);
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, msg);
   }
-  if (fclose(f) != 0) ok = false;
-  if (!ok) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("write failed: ") + path).c_str());
+  if (size != kBinHeader + N * G * 4)
+    return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("binary count file of the wrong size: ") + path).c_str());
+  memcpy(out, buf + kBinHeader, (size_t)(N * G * 4));
   return BUSSEQ_OK;
 }
 
-int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
-  if (!path || !out || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
-  {
-    const int fd = open(path, O_RDONLY);
-    if (fd >= 0) {
-      char magic[8];
-      const off_t size = lseek(fd, 0, SEEK_END);
-      const bool bin = size >= kBinHeader && pread(fd, magic, 8, 0) == 8 && memcmp(magic, kBinMagic, 8) == 0;
-      int r = BUSSEQ_OK;
-      if (bin) {
-        r = host_little_endian() ? read_counts_binary(fd, path, N, G, (int64_t)size, out)
-                                 : busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
-      }
-      close(fd);
-      if (bin) {
-        if (r != BUSSEQ_OK) return r;
-        for (int64_t i = 0; i < N * G; ++i)
-          if (out[i] < 0) return busseq_internal_set_error(BUSSEQ_ERR_IO, "negative count in the count file");
-        return BUSSEQ_OK;
-      }
-    }
-  }
-  FILE* f = fopen(path, "rb");
-  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open count file ") + path).c_str());
-  fseek(f, 0, SEEK_END);
-  const long sz = ftell(f);
-  fseek(f, 0, SEEK_SET);
-  std::vector<char> buf((size_t)std::max(0L, sz));
-  const size_t got = sz > 0 ? fread(buf.data(), 1, (size_t)sz, f) : 0;
-  fclose(f);
-  if ((long)got != sz) return busseq_internal_set_error(BUSSEQ_ERR_IO, "short read of the count file");
+// N*G whitespace-separated integers from a buffer, parsed by every host thread
+// (two passes: count the tokens of each slice, then parse each into place).
+int text_from_buffer(const char* base, int64_t sz, const char* path, int64_t N, int64_t G, int32_t* out) {
   const int nt = std::max(1, std::min(nthreads(), (int)(sz / (1 << 16)) + 1));
   std::vector<const char*> starts(nt + 1);
-  const char* base = buf.data();
   const char* end = base + sz;
   starts[0] = base;
   starts[nt] = end;
@@ -272,9 +242,119 @@ int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
       th.emplace_back([&, t]() { parse_slice(starts[t], starts[t + 1], out + pre[t], cnt[t], &bad[t]); });
     for (auto& x : th) x.join();
   }
-  for (int64_t i = 0; i < N * G; ++i)
-    if (out[i] < 0) return busseq_internal_set_error(BUSSEQ_ERR_IO, "negative count in the count file");
   return BUSSEQ_OK;
+}
+
+// A whole gzip file inflated into `buf` through zlib's gz interface, loaded
+// from libz.so.1 at run time.
+int inflate_gzip(const char* path, std::vector<char>& buf) {
+  using gz_open_t = void* (*)(const char*, const char*);
+  using gz_buffer_t = int (*)(void*, unsigned);
+  using gz_read_t = int (*)(void*, void*, unsigned);
+  using gz_close_t = int (*)(void*);
+  void* lib = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+  if (!lib) return busseq_internal_set_error(BUSSEQ_ERR_IO, "compressed count files need zlib (libz.so.1)");
+  const auto gz_open = reinterpret_cast<gz_open_t>(dlsym(lib, "gzopen"));
+  const auto gz_buffer = reinterpret_cast<gz_buffer_t>(dlsym(lib, "gzbuffer"));
+  const auto gz_read = reinterpret_cast<gz_read_t>(dlsym(lib, "gzread"));
+  const auto gz_close = reinterpret_cast<gz_close_t>(dlsym(lib, "gzclose"));
+  int r = BUSSEQ_OK;
+  if (!gz_open || !gz_read || !gz_close) {
+    r = busseq_internal_set_error(BUSSEQ_ERR_IO, "libz.so.1 lacks the gz interface");
+  } else if (void* gz = gz_open(path, "rb")) {
+    if (gz_buffer) gz_buffer(gz, 1u << 20);
+    constexpr size_t kChunk = size_t(1) << 26;
+    size_t have = 0;
+    for (;;) {
+      buf.resize(have + kChunk);
+      const int got = gz_read(gz, buf.data() + have, (unsigned)kChunk);
+      if (got < 0) {
+        r = busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("corrupt compressed count file ") + path).c_str());
+        break;
+      }
+      have += (size_t)got;
+      if (got == 0) break;
+    }
+    buf.resize(r == BUSSEQ_OK ? have : 0);
+    gz_close(gz);
+  } else {
+    r = busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open count file ") + path).c_str());
+  }
+  dlclose(lib);
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int busseq_write_counts_binary(const char* path, int64_t N, int64_t G, const int32_t* Y) {
+  if (!path || !Y || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
+  if (!host_little_endian()) return busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
+  FILE* f = fopen(path, "wb");
+  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open ") + path + " for writing").c_str());
+  const int64_t hdr[2] = {N, G};
+  bool ok = fwrite(kBinMagic, 1, 8, f) == 8 && fwrite(hdr, 8, 2, f) == 2;
+  const size_t n = (size_t)(N * G);
+  for (size_t o = 0; ok && o < n;) {
+    const size_t c = std::min<size_t>(n - o, (size_t)1 << 26);
+    ok = fwrite(Y + o, 4, c, f) == c;
+    o += c;
+  }
+  if (fclose(f) != 0) ok = false;
+  if (!ok) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("write failed: ") + path).c_str());
+  return BUSSEQ_OK;
+}
+
+int busseq_read_counts(const char* path, int64_t N, int64_t G, int32_t* out) {
+  if (!path || !out || N <= 0 || G <= 0) return busseq_internal_set_error(BUSSEQ_ERR_ARG, "bad arguments");
+  auto no_negative = [&]() {
+    for (int64_t i = 0; i < N * G; ++i)
+      if (out[i] < 0) return busseq_internal_set_error(BUSSEQ_ERR_IO, "negative count in the count file");
+    return (int)BUSSEQ_OK;
+  };
+  {
+    const int fd = open(path, O_RDONLY);
+    if (fd >= 0) {
+      char magic[8];
+      const off_t size = lseek(fd, 0, SEEK_END);
+      const bool head = size >= 2 && pread(fd, magic, 8, 0) >= 2;
+      const bool gz = head && (unsigned char)magic[0] == 0x1f && (unsigned char)magic[1] == 0x8b;
+      if (gz) {
+        close(fd);
+        std::vector<char> buf;
+        int r = inflate_gzip(path, buf);
+        if (r != BUSSEQ_OK) return r;
+        const int64_t n = (int64_t)buf.size();
+        if (n >= kBinHeader && memcmp(buf.data(), kBinMagic, 8) == 0) {
+          r = host_little_endian() ? binary_from_buffer(buf.data(), n, path, N, G, out)
+                                   : busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
+        } else {
+          r = text_from_buffer(buf.data(), n, path, N, G, out);
+        }
+        return r != BUSSEQ_OK ? r : no_negative();
+      }
+      const bool bin = size >= kBinHeader && head && memcmp(magic, kBinMagic, 8) == 0;
+      int r = BUSSEQ_OK;
+      if (bin) {
+        r = host_little_endian() ? read_counts_binary(fd, path, N, G, (int64_t)size, out)
+                                 : busseq_internal_set_error(BUSSEQ_ERR_IO, "binary counts need a little-endian host");
+      }
+      close(fd);
+      if (bin) return r != BUSSEQ_OK ? r : no_negative();
+    }
+  }
+  FILE* f = fopen(path, "rb");
+  if (!f) return busseq_internal_set_error(BUSSEQ_ERR_IO, (std::string("cannot open count file ") + path).c_str());
+  fseek(f, 0, SEEK_END);
+  const long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  std::vector<char> buf((size_t)std::max(0L, sz));
+  const size_t got = sz > 0 ? fread(buf.data(), 1, (size_t)sz, f) : 0;
+  fclose(f);
+  if ((long)got != sz) return busseq_internal_set_error(BUSSEQ_ERR_IO, "short read of the count file");
+  const int r = text_from_buffer(buf.data(), (int64_t)sz, path, N, G, out);
+  return r != BUSSEQ_OK ? r : no_negative();
 }
 
 int busseq_internal_dims(busseq_handle* h, int32_t* B, int32_t* K, int64_t* G, int64_t* N, int32_t* n_kept,

@@ -88,6 +88,27 @@ def test_binary_counts_roundtrip_and_errors(tmp_path):
         bq.read_counts(pn, 700, 700)             # negative count
 
 
+def test_gzip_counts_text_and_binary(tmp_path):
+    import gzip
+    Y, _, _ = bq.simulate([60, 50], 90, 3, 21)
+    txt, binf = str(tmp_path / "y.txt"), str(tmp_path / "y.bin")
+    np.savetxt(txt, Y, fmt="%d", delimiter=" ")
+    bq.write_counts_binary(binf, Y)
+    for src in (txt, binf):
+        with open(src, "rb") as f, gzip.open(src + ".gz", "wb") as g:
+            g.write(f.read())
+        np.testing.assert_array_equal(bq.read_counts(src + ".gz", 110, 90), Y)
+        with pytest.raises(bq.BusseqError):
+            bq.read_counts(src + ".gz", 110, 91)     # other dimensions
+    with open(txt + ".gz", "rb") as f:
+        data = f.read()
+    bad = str(tmp_path / "bad.gz")
+    with open(bad, "wb") as f:
+        f.write(data[: len(data) // 2])              # a truncated stream
+    with pytest.raises(bq.BusseqError):
+        bq.read_counts(bad, 110, 90)
+
+
 def test_simulate_deterministic_and_model_shaped():
     a = bq.simulate([50, 40, 30], 400, 4, 123)
     b = bq.simulate([50, 40, 30], 400, 4, 123)
