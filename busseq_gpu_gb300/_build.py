@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(lambda s: _compile(s, force), srcs))
     if force or _newer(LIB, objs):
-        _run([NVCC, "-shared", *ARCH, "-o", LIB, *objs, "-lpthread", "-ldl"])
+        _run([NVCC, "-shared", *ARCH, "-o", LIB, *objs, "-lpthread"])  # dlopen: in libc (glibc >= 2.34)
     cli_src = os.path.join(CSRC, "cli_main.cpp")
     if force or _newer(CLI, [cli_src, LIB, os.path.join(INCLUDE, "busseq_gb300.h")]):
         _run(["g++", "-std=c++17", "-O2", "-I", INCLUDE, "-o", CLI, cli_src, "-L", os.path.dirname(LIB),
