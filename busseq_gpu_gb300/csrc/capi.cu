@@ -585,16 +585,16 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.n_burnin = 0;
     s.n_unchanged = INT_MAX;
     const int64_t Gp = s.Gp;
-    int32_t* Yd;
+    int32_t* Yd = nullptr;
     TRY(h->alloc(&Yd, N * Gp));
     s.Y = Yd;
     // one extra all-zero row: the gene passes pad their cell chunks with it
     TRY(h->alloc(&s.X, (N + 1) * Gp));
-    uint32_t* y0m;  // one extra all-zero row, read for the padding row of a chunk
+    uint32_t* y0m = nullptr;  // one extra all-zero row, read for the padding row of a chunk
     TRY(h->alloc(&y0m, (N + 1) * s.Gw));
     s.y0m = y0m;
     TRY(h->alloc(&s.zm, N * s.Gw));
-    int32_t *bo, *boff;
+    int32_t *bo = nullptr, *boff = nullptr;
     TRY(h->alloc(&bo, N));
     TRY(h->alloc(&boff, B + 1));
     s.batch_of = bo;

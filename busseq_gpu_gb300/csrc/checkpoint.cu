@@ -36,14 +36,14 @@ struct DevBlock {
 // busseq_begin).
 std::vector<DevBlock> run_blocks(const busseq_handle* h) {
   const bq::DevState& s = h->s;
-  const int64_t G = s.G, N = s.N, nk = h->n_kept;
-  const int B = s.B, K = s.K;
+  const size_t G = (size_t)s.G, N = (size_t)s.N, nk = (size_t)h->n_kept;
+  const size_t B = (size_t)s.B, K = (size_t)s.K;  // B >= 2, K >= 1
   std::vector<DevBlock> v = {
       {s.acc_alpha, G * 8},     {s.acc_beta, K * G * 8},  {s.acc_L, K * G * 8},   {s.acc_nu, B * G * 8},
       {s.acc_delta, N * 8},     {s.acc_phi, B * G * 8},   {s.acc_gamma, 2 * B * 8}, {s.acc_pi, B * K * 8},
       {s.acc_ptau, 2 * 8},      {s.acc_wcnt, N * K * 4}};
   if (s.keep_draws) {
-    const int64_t km = std::max(1, K - 1);
+    const size_t km = K > 1 ? K - 1 : 1;
     const std::vector<DevBlock> k = {
         {s.keep_gamma, nk * 2 * B * 4}, {s.keep_alpha, nk * G * 4},      {s.keep_beta, nk * km * G * 4},
         {s.keep_L, nk * km * G},        {s.keep_ptau, nk * 2 * 4},       {s.keep_nu, nk * (B - 1) * G * 4},
