@@ -174,6 +174,9 @@ def test_oracle_sampler_moments():
     assert abs(nb.mean() - 40) < 0.5 and abs(nb.var() / (40 + 1600 / 4) - 1) < 0.05
     nb = po.sample_negbin(12, 24.0, 3.0, 100000)  # distribution-function inversion (mu < 32, phi >= 1)
     assert abs(nb.mean() - 24) < 0.25 and abs(nb.var() / (24 + 576 / 3) - 1) < 0.05
+    for seed, mu in ((13, 31.5), (14, 32.5)):  # either side of the switch, phi = 1 (a long tail)
+        nb = po.sample_negbin(seed, mu, 1.0, 200000)
+        assert abs(nb.mean() - mu) < 0.5 and abs(nb.var() / (mu + mu * mu) - 1) < 0.05, (mu, nb.mean(), nb.var())
 
 
 def test_philox_known_answers():
