@@ -62,6 +62,22 @@ def _peak_hbm():
         return 6800.0, "fallback"
 
 
+def sweep_roofline(N: int, G: int, hmc: int, sweeps_per_s: float, peak_gbs: float) -> dict:
+    """The whole sweep against HBM bandwidth, with the bytes of the reference's
+    pass structure (one pass over the N x G tensor per conditional that the
+    dependency order forces): per entry 12.125 B for Z/X (read Y and X, write X
+    and a 1-bit Z), 4.125 B for gamma (X and Z), and 4 B for each of alpha, beta,
+    nu, delta, phi and W -- 40.25 B in all; with the HMC update, Z/X, gamma, L + 1
+    gradient passes and W: 12.125 + 4.125 + 4 (L + 1) + 4 B."""
+    per_entry = 40.25 if hmc <= 0 else 12.125 + 4.125 + 4.0 * (hmc + 1) + 4.0
+    bytes_per_sweep = per_entry * float(N) * float(G)
+    achieved = bytes_per_sweep * sweeps_per_s / 1e9
+    return {"bound": "hbm", "bytes_per_entry": per_entry, "bytes_per_sweep": bytes_per_sweep,
+            "achieved": achieved, "peak": peak_gbs, "unit": "GB/s", "frac": achieved / peak_gbs,
+            "note": "bytes of the reference's passes over the count tensor x sweeps/s (this build reads "
+                    "fewer: the per-kernel figures are in roofline and kernels_ms)"}
+
+
 def _traffic(kernel: str, workload: str = "config1"):
     """DRAM bytes per launch of `kernel` from the committed ncu summary of this
     workload, or None."""
@@ -623,6 +639,7 @@ def main():
                     "d2h_bytes_per_step": d2h / args.steps,
                     "note": "one job per run: pinned-host upload, init, %d sweeps, posterior, all estimates "
                             "(and the last sweep's X and Z) to pinned host buffers" % args.steps},
+            "sweep_roofline": sweep_roofline(N, G, hmc, value / world, peak),  # per GPU: replicas
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "ms_per_launch": ms_launch,

@@ -1,5 +1,6 @@
-"""Host logic of bench.py's CPU baselines (no GPU): the batch-corrected-count
-baseline keeps its oracle sample to genes whose tail sums stay short."""
+"""Host logic of bench.py (no GPU): the batch-corrected-count CPU baseline
+keeps its oracle sample to genes whose tail sums stay short, and the sweep-level
+roofline counts the reference's passes."""
 import numpy as np
 
 import bench
@@ -46,3 +47,10 @@ def test_corrected_baseline_keeps_every_gene_of_a_moderate_run():
     n_b, G, K = [8, 8, 6], 20, 2
     out = bench.corrected_cpu_rate(_FakeRun(_est(rng, n_b, G, K)), n_b, 3, cells_per_batch=4)
     assert "20 of 20 genes" in out["sample"], out["sample"]
+
+
+def test_sweep_roofline_counts_the_reference_passes():
+    r = bench.sweep_roofline(10000, 10000, 0, 594.0, 6786.2)
+    assert r["bytes_per_entry"] == 40.25 and r["bytes_per_sweep"] == 40.25e8
+    assert abs(r["achieved"] - 40.25e8 * 594.0 / 1e9) < 1e-6 and abs(r["frac"] - r["achieved"] / 6786.2) < 1e-12
+    assert bench.sweep_roofline(10000, 10000, 10, 1.0, 1.0)["bytes_per_entry"] == 64.25  # HMC, L = 10
