@@ -384,6 +384,8 @@ def run_batch(args, cfg, rank, world, local):
                            "ms_per_chain": {str(K): v for K, v in seq_ms.items()},
                            "note": "each chain alone for the same %d sweeps" % args.steps},
             "batched_vs_sequential": value / seq_value,
+            # per chain-sweep, every chain passes over its own copy of the tensor
+            "sweep_roofline": sweep_roofline(N, G, 0, value / world, _peak_hbm()[0]),
             "autotune": {"seconds": tune_s, "ms_per_sweep": {str(K): {str(c): m for c, m in tuned[K][1].items()}
                                                              for K in ks}},
             "bic": {str(K): v for K, v in bic.items()}, "k_min_bic": k_best,
