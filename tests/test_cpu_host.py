@@ -109,6 +109,17 @@ def test_gzip_counts_text_and_binary(tmp_path):
         bq.read_counts(bad, 110, 90)
 
 
+def test_documented_python_api_exists():
+    """The names the integration notes and the README call exist on the package."""
+    for name in ("run", "begin", "sweeps", "finish", "estimates", "bic", "write_outputs", "corrected_counts",
+                 "checkpoint_save", "checkpoint_load", "zx_summaries", "hmc_stats", "hmc_gradient",
+                 "hmc_logpost_diff", "hmc_gene_logpost_diff", "get_state", "set_state", "preserved", "profile",
+                 "set_stream", "synchronize", "close"):
+        assert callable(getattr(bq.Sampler, name, None)), name
+    for name in ("simulate", "read_counts", "write_counts_binary", "autotune_chunk", "Batch", "estimate_buffers"):
+        assert callable(getattr(bq, name, None)), name
+
+
 def test_simulate_deterministic_and_model_shaped():
     a = bq.simulate([50, 40, 30], 400, 4, 123)
     b = bq.simulate([50, 40, 30], 400, 4, 123)
