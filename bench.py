@@ -16,10 +16,14 @@ A step is one full Gibbs sweep.  Reported:
   roofline   the dominant kernel's algorithmic bytes per launch over its mean
              CUDA-event duration, against the measured HBM copy bandwidth.
   cpu_baseline the FP64 OpenMP oracle (the CPU restatement of the same sweep)
-             on the host cores, on a bounded sample of the same data.
+             on the host cores: 20 full sweeps of the same data, timed as
+             they run (no cell sample, no scaling).
 
 --impl reference runs the CPU arm only (the reference program has no CPU
-implementation of the sweep, so its CPU stand-in is the oracle port).
+implementation of the sweep, so its CPU stand-in is the oracle port): every
+step is one full oracle sweep of the whole workload, timed, unscaled.  Its
+input comes from the generator built on the checker side, so that process
+never maps the product library.
 Multi-GPU (--gpus N under torchrun): N independent chains, one per GPU
 (replicas: a BUSseq chain has no data-parallel split that avoids an
 all-reduce per sweep).
@@ -163,63 +167,69 @@ def whole_job_rate(steps_per_rank: int, world: int, seconds: float) -> float:
     return steps_per_rank * world / seconds
 
 
+def sim_params(cfg):
+    """Generator parameters of a workload (the BUSseq model's distributions)."""
+    import busseq_gpu_gb300 as bq  # the parameter table only; the library is not loaded
+    return dict(bq.CONFIG_SIM[cfg.get("sim", "default")])
+
+
 def make_data(seed, cfg=CFG1, n_b=None):
     import busseq_gpu_gb300 as bq
-    prm = bq.CONFIG_SIM[cfg.get("sim", "default")]
-    return bq.simulate(n_b if n_b is not None else cfg["n_b"], cfg["G"], cfg["K"], seed, **prm)
+    return bq.simulate(n_b if n_b is not None else cfg["n_b"], cfg["G"], cfg["K"], seed, **sim_params(cfg))
 
 
-def cpu_oracle_rate(Y, n_b, K, seed, cells_per_batch: int, sweeps: int):
-    """FP64 oracle sweeps/s on the first `cells_per_batch` cells of every batch,
-    scaled to the full cell count (the oracle's cost is linear in cells)."""
+def make_data_cpu(seed, cfg=CFG1, n_b=None):
+    """The same counts as make_data, from the generator built alone on the
+    checker side (oracle/lib/libsim.so): the CPU arms never map the product
+    library."""
     from oracle import pyoracle as po
-    off = np.concatenate([[0], np.cumsum(n_b)])
-    rows = np.concatenate([np.arange(off[b], off[b] + cells_per_batch) for b in range(len(n_b))])
-    Ys = np.ascontiguousarray(Y[rows])
-    st = po.State(Ys, [cells_per_batch] * len(n_b), K, seed)
-    st.init(0.25)
-    st.sweep(0, 1 << 30)  # warm caches / page in
+    return po.simulate(n_b if n_b is not None else cfg["n_b"], cfg["G"], cfg["K"], seed, sim_params(cfg))
+
+
+def cpu_oracle_rate(Y, n_b, K, seed, sweeps: int, warmup: int = 1):
+    """FP64 oracle sweeps/s over the whole data set: `warmup` sweeps untimed,
+    then `sweeps` timed full sweeps (no sampling, no scaling).  Returns
+    (sweeps/s, threads, timed seconds, init seconds)."""
+    from oracle import pyoracle as po
+    st = po.State(np.ascontiguousarray(Y), n_b, K, seed)
     t0 = time.perf_counter()
-    for it in range(1, sweeps + 1):
+    st.init(0.25)
+    init_s = time.perf_counter() - t0
+    for it in range(warmup):
+        st.sweep(it, 0)
+    t0 = time.perf_counter()
+    for it in range(warmup, warmup + sweeps):
         st.sweep(it, 0)
     dt = time.perf_counter() - t0
-    frac = len(rows) / float(sum(n_b))
-    return sweeps / dt * frac, po.num_threads(), dt
+    return sweeps / dt, po.num_threads(), dt, init_s
 
 
 def run_reference(args, rank):
     if rank != 0:
         return 0
     cfg = WORKLOADS[args.workload]
-    n_b, K = list(cfg["n_b"]), cfg["K"]
-    Y, _, _ = make_data(cfg["seed"], cfg)
-    from oracle import pyoracle as po
-    off = np.concatenate([[0], np.cumsum(n_b)])
-    cpb = 100  # cells per batch in each step's sample
-    rows = np.concatenate([np.arange(off[b], off[b] + cpb) for b in range(len(n_b))])
-    st = po.State(np.ascontiguousarray(Y[rows]), [cpb] * len(n_b), K, cfg["seed"])
-    st.init(0.25)
-    for it in range(args.warmup):
-        st.sweep(it, 0)
-    t0 = time.perf_counter()
-    for it in range(args.warmup, args.warmup + args.steps):
-        st.sweep(it, 0)
-    dt = time.perf_counter() - t0
-    frac = len(rows) / float(sum(n_b))
-    value = args.steps / dt * frac
-    sample = ("per step: one full FP64 oracle sweep over %d cells (first %d of each batch) x %d genes of the "
-              "%s data; sweeps/s scaled by %d/%d cells" % (len(rows), cpb, cfg["G"], args.workload, len(rows),
-                                                          sum(n_b)))
+    if args.workload == "config3":
+        cfg = dict(cfg, K=max(cfg["ks"]))
+    n_b, K, G = list(cfg["n_b"]), cfg["K"], cfg["G"]
+    if args.cells > 0:
+        n_b = [args.cells] * len(n_b)
+    Y, _ = make_data_cpu(cfg["seed"], cfg, n_b)
+    value, cores, dt, init_s = cpu_oracle_rate(Y, n_b, K, cfg["seed"], args.steps, args.warmup)
+    sample = ("every step one full FP64 oracle sweep over all %d cells x %d genes of the %s data (%d timed "
+              "sweeps, %.1f s, after %d untimed; no sampling or scaling)"
+              % (sum(n_b), G, args.workload, args.steps, dt, args.warmup))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (BUSseq generative model)",
         # the reference has only the random-walk sampler: its arm runs that on every workload
         "config": _config(args.workload, n_b, dict(cfg, hmc=0)),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": po.num_threads(), "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "init_s": init_s,
         "note": "the reference program has no CPU implementation of the sweep; this arm times the FP64 CPU "
-                "restatement of it (oracle/oracle.cpp) with all host threads",
+                "restatement of it (oracle/oracle.cpp) with all host threads; its input comes from the "
+                "generator built on the checker side, so the product library is never loaded",
     }
     print(json.dumps(line))
     return 0
@@ -622,14 +632,14 @@ def main():
             quality["vs_mh"] = {"beta_ess_per_s_median_ratio": ratio("beta"),
                                 "nu_ess_per_s_median_ratio": ratio("nu"), "ari_W_mh": mh["ari_W"], "mh": mh}
 
-    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------
+    # ---- CPU baseline (rank 0, N = 1 only): 20 full sweeps of the oracle ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpb = 250
-        rate, cores, secs = cpu_oracle_rate(Y, n_b, K, seed, cpb, 2)
+        nsw = 20
+        rate, cores, secs, _ = cpu_oracle_rate(Y, n_b, K, seed, nsw, 1)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "2 FP64 oracle sweeps over the first %d cells of each batch (%d cells x %d genes, %.1f s), "
-                         "scaled to N=%d cells" % (cpb, cpb * len(n_b), G, secs, N)}
+               "sample": "%d full FP64 oracle sweeps over all %d cells x %d genes (%.1f s) after one untimed "
+                         "sweep; no sampling or scaling" % (nsw, N, G, secs)}
 
     if rank == 0:
         line = {
@@ -646,7 +656,7 @@ def main():
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "ms_per_launch": ms_launch,
                          "launches_per_sweep": n_launch},
-            "kernels_ms": prof,
+            "kernels_ms": {k: v for k, v in prof.items() if v > 0},  # the kernels this sampler launches
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,

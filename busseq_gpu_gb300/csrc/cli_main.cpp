@@ -109,8 +109,11 @@ int main(int argc, char** argv) {
       }
       case 1010: hmc_gene = 1; break;
       default:
-        printf("Error Usage: %s [-B batch] [-N sample_size_file] [-G gene] [-K celltype] [-s seed] "
-               "[-c count_data_file] [-i iterations] [-b burnin] [-u unchanged_iterations] "
+        // The reference's usage line byte for byte (BUSseq_gpu.cu:1088), lower-case
+        // flag names and stray parenthesis included: its stdout is part of the
+        // drop-in contract.
+        printf("Error Usage: %s [-b batch] [-n sample_size_file] [-g gene] [-k celltype] "
+               "[-c count_data_file)] [-i iterations] [-b burnin] [-u unchanged_iterations] "
                "[-p print_preserved] [-o output_prefix] \n",
                argv[0]);
         exit(1);

@@ -70,13 +70,11 @@ extern "C" int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev,
   const int64_t G = dims->G;
   if (B < 1 || B > bq::MAX_B || K < 1 || K > bq::MAX_K || G < 1)
     return err(BUSSEQ_ERR_ARG, "busseq_bic_noalloc: B must be in 1..128, K in 1..64 and G positive");
-  BatchOffsets o{};
+  // The true total first (64-bit), so that the message below reports it.
   int64_t N = 0;
   for (int b = 0; b < B; ++b) {
     if (dims->n_b[b] < 1) return err(BUSSEQ_ERR_ARG, "busseq_bic_noalloc: every batch needs at least one cell");
-    o.off[b] = (int32_t)N;
     N += dims->n_b[b];
-    if (N > kMaxCells) break;
   }
   if (N > kMaxCells || N * (int64_t)K > kMaxDoubles) {
     char msg[256];
@@ -86,18 +84,28 @@ extern "C" int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev,
              (long long)N, K, (long long)kMaxCells, (long long)kMaxDoubles);
     return err(BUSSEQ_ERR_ARG, msg);
   }
-  o.off[B] = (int32_t)N;
+  BatchOffsets o{};
+  o.off[0] = 0;
+  for (int b = 0; b < B; ++b) o.off[b + 1] = o.off[b] + dims->n_b[b];
 
-  // Per-device set-up: the symbols' device addresses, taken with the caller's
-  // device current.  Host code may not use the arrays' names as addresses.
+  // The scratch's device addresses, taken with the caller's device current.
+  // Host code may not use the arrays' names as addresses.  The lookup is
+  // repeated on every call made outside stream capture, so that a module
+  // loaded again (after cudaDeviceReset, or in another context on the same
+  // device) is found at its new address; a call made during capture uses the
+  // address of the last call made outside capture on this device.
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return err(BUSSEQ_ERR_ARG, "busseq_bic_noalloc: device ordinal out of range");
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
   DeviceScratch sc;
   {
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev].ready) {
+    if (cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_bic_ll);
       if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
@@ -106,12 +114,29 @@ extern "C" int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev,
       if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
       g_scratch[dev].batch = static_cast<int32_t*>(p);
       g_scratch[dev].ready = true;
+    } else if (!g_scratch[dev].ready) {
+      return err(BUSSEQ_ERR_STATE,
+                 "busseq_bic_noalloc: the first call on a device must come before any stream capture");
     }
     sc = g_scratch[dev];
   }
 
+  // Every pointer must be device (or managed) memory that the current device
+  // can address: the kernels run on the current device.
+  const void* ptrs[] = {Y_dev, alpha_dev, beta_dev, nu_dev, delta_dev, phi_dev, gamma_dev, pi_dev, out_dev};
+  for (const void* q : ptrs) {
+    cudaPointerAttributes a{};
+    e = cudaPointerGetAttributes(&a, q);
+    if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
+    if (!((a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged))
+      return err(BUSSEQ_ERR_ARG,
+                 "busseq_bic_noalloc: every array must be device memory of the current device");
+  }
+
   // A view of the caller's arrays in the layout the BIC kernels read
-  // (row stride G, estimates in the reference's layouts).
+  // (row stride G, estimates in the reference's layouts).  k_bic_cell and
+  // k_bic_total read only B, K, G, N, Gp, Y, batch_of and batch_off of the
+  // state, so every other field of this view stays zero.
   bq::DevState s{};
   s.B = B;
   s.K = K;
@@ -131,7 +156,6 @@ extern "C" int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev,
   est.gamma = const_cast<double*>(gamma_dev);
   est.pi = const_cast<double*>(pi_dev);
 
-  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
   const int64_t nfill = N > B + 1 ? N : B + 1;
   k_noalloc_batches<<<(unsigned)((nfill + 255) / 256), 256, 0, st>>>(sc.batch, o, B, N, kMaxCells);
   // Every [k][i] entry of the scratch is written by k_bic_cell before

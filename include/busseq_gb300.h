@@ -191,9 +191,13 @@ int busseq_bic(busseq_handle* h, double* bic);
  * doubles (8 MB) plus BUSSEQ_NOALLOC_BIC_MAX_CELLS ints (1 MB), held by every
  * GPU that loads the library until the process exits.  Larger problems are
  * rejected (BUSSEQ_ERR_ARG).  All calls share that array: calls that overlap
- * on the GPU (other streams, other host threads) race.  The first call on a
- * device looks up the array's device address; make that first call before any
- * stream capture. */
+ * on the GPU (other streams, other host threads) race.  The kernels run on the
+ * calling thread's current device, which must own every pointer passed in
+ * (checked; BUSSEQ_ERR_ARG otherwise).  Each call made outside stream capture
+ * looks up the array's device address again (so a device reset, after which
+ * the library's module is loaded afresh, is followed); a call made during
+ * capture reuses the address found by the last call outside capture on that
+ * device, so make the first call on a device before any stream capture. */
 #define BUSSEQ_NOALLOC_BIC_MAX_TYPES_X_CELLS (1 << 20)
 #define BUSSEQ_NOALLOC_BIC_MAX_CELLS (1 << 18)
 int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev, const double* alpha_dev,

@@ -9,6 +9,8 @@
   is built where a driver is installed, i.e. on the GPU machine).
 * ``ref_sweep_timer`` -- oracle/ref_sweep_timer.cpp, which replays the
   reference's per-sweep launch sequence from that cubin to time it.
+* ``libsim.so``    -- the synthetic-data generator alone (oracle/sim_standalone.cpp),
+  so that bench.py's CPU arms never map the product library.
 
 Nothing in the product package imports this module.
 """
@@ -22,12 +24,16 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "lib")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SRC = "/root/reference/BUSseq_gpu.cu"
+# The reference checkout's single source file; BUSSEQ_REFERENCE_SRC points
+# elsewhere when the checkout lives somewhere else.
+REFERENCE_SRC = os.environ.get("BUSSEQ_REFERENCE_SRC", "/root/reference/BUSseq_gpu.cu")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 ORACLE_SO = os.path.join(LIB_DIR, "liborc.so")
 REF_CUBIN = os.path.join(REF_DIR, "busseq_ref.cubin")
 HARNESS_BIN = os.path.join(LIB_DIR, "ref_harness")
+SIM_SO = os.path.join(LIB_DIR, "libsim.so")
+ROOT = os.path.dirname(HERE)
 TIMER_BIN = os.path.join(LIB_DIR, "ref_sweep_timer")
 
 
@@ -55,6 +61,18 @@ def build_oracle(force: bool = False) -> str:
     if force or _stale(ORACLE_SO, [src]):
         _run(oracle_cmd())
     return ORACLE_SO
+
+
+def build_sim(force: bool = False) -> str:
+    """The generator of busseq_gpu_gb300/csrc/simulate.cpp as its own library."""
+    os.makedirs(LIB_DIR, exist_ok=True)
+    src = os.path.join(HERE, "sim_standalone.cpp")
+    csrc = os.path.join(ROOT, "busseq_gpu_gb300", "csrc")
+    inc = os.path.join(ROOT, "include")
+    deps = [src, os.path.join(csrc, "simulate.cpp"), os.path.join(csrc, "rng.h"), os.path.join(inc, "busseq_gb300.h")]
+    if force or _stale(SIM_SO, deps):
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-shared", "-I", inc, "-I", csrc, "-o", SIM_SO, src])
+    return SIM_SO
 
 
 def build_ref_cubin(force: bool = False) -> str | None:
@@ -104,7 +122,7 @@ def build_ref_timer(force: bool = False) -> str | None:
 
 
 def build_all(force: bool = False) -> dict:
-    out = {"oracle": build_oracle(force), "ref_cubin": build_ref_cubin(force)}
+    out = {"oracle": build_oracle(force), "sim": build_sim(force), "ref_cubin": build_ref_cubin(force)}
     if shutil.which("g++"):
         out["harness"] = build_harness(force)
         out["ref_timer"] = build_ref_timer(force)

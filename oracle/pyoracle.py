@@ -260,6 +260,39 @@ def sample_negbin(seed, mu, phi, n):
     return out
 
 
+class _SimParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("alpha_lo", "alpha_hi", "de_frac", "beta_lo", "beta_hi", "nu_step",
+                                          "nu_sd", "delta_sd", "phi_lo", "phi_hi", "pi_conc", "gamma0", "gamma1")]
+
+
+class _Dims(C.Structure):
+    _fields_ = [("B", C.c_int32), ("K", C.c_int32), ("G", C.c_int64), ("n_b", _PI32)]
+
+
+_sim = None
+
+
+def simulate(n_b, G: int, K: int, seed: int, params: dict):
+    """(Y [N, G], W_true [N]) from the generator built alone (oracle/lib/libsim.so):
+    the same counts as the product library's generator for the same seed and
+    parameters, without loading that library."""
+    global _sim
+    if _sim is None:
+        _sim = C.CDLL(_build.build_sim())
+        _sim.busseq_simulate.argtypes = [C.POINTER(_Dims), C.POINTER(_SimParams), C.c_uint64, _PI32, _PI32, _PI32]
+        _sim.sim_last_error.restype = C.c_char_p
+    n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+    N = int(n_b.sum())
+    Y = np.zeros((N, G), np.int32)
+    W = np.zeros(N, np.int32)
+    d = _Dims(len(n_b), int(K), int(G), _ptr(n_b, _PI32))
+    sp = _SimParams(**params)
+    rc = _sim.busseq_simulate(C.byref(d), C.byref(sp), int(seed), _ptr(Y, _PI32), _ptr(W, _PI32), None)
+    if rc != 0:
+        raise RuntimeError("simulate: %s" % _sim.sim_last_error().decode())
+    return Y, W
+
+
 def set_threads(n: int) -> None:
     lib().orc_set_threads(int(n))
 

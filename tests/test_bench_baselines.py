@@ -54,3 +54,37 @@ def test_sweep_roofline_counts_the_reference_passes():
     assert r["bytes_per_entry"] == 40.25 and r["bytes_per_sweep"] == 40.25e8
     assert abs(r["achieved"] - 40.25e8 * 594.0 / 1e9) < 1e-6 and abs(r["frac"] - r["achieved"] / 6786.2) < 1e-12
     assert bench.sweep_roofline(10000, 10000, 10, 1.0, 1.0)["bytes_per_entry"] == 64.25  # HMC, L = 10
+
+
+def test_checker_side_generator_matches_the_library():
+    import busseq_gpu_gb300 as bq
+    from oracle import pyoracle as po
+    n_b, G, K, seed = [13, 9, 11], 57, 4, 99
+    for name in ("default", "wide"):
+        Y, W, _ = bq.simulate(n_b, G, K, seed, **bq.CONFIG_SIM[name])
+        Y2, W2 = po.simulate(n_b, G, K, seed, bq.CONFIG_SIM[name])
+        assert np.array_equal(Y, Y2) and np.array_equal(W, W2)
+
+
+def test_reference_arm_is_unscaled_and_never_maps_the_product_library():
+    """The reference arm times full oracle sweeps of the whole (here shrunk)
+    workload, and its process holds only checker-side libraries."""
+    import json
+    import subprocess
+    import sys
+    code = ("import sys, json, io, contextlib; sys.argv = ['bench.py']; import bench\n"
+            "class A: workload = 'config1'; cells = 6; steps = 2; warmup = 3; gpus = 1\n"
+            "buf = io.StringIO()\n"
+            "with contextlib.redirect_stdout(buf): bench.run_reference(A, 0)\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print(json.dumps({'line': json.loads(buf.getvalue()), 'product': 'libbusseq_gb300' in maps, "
+            "'checker': 'liborc.so' in maps}))\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    line = out["line"]
+    assert out["checker"] and not out["product"]
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["value"] > 0
+    assert abs(line["ms_per_step"] - 1000.0 / line["value"]) < 1e-9
+    assert "no sampling or scaling" in line["cpu_baseline"]["sample"] and "all 24 cells" in line["cpu_baseline"]["sample"]

@@ -38,8 +38,10 @@ def _case(n_b, G, K, seed):
 def test_bic_noalloc_matches_busseq_bic_twice():
     torch = pytest.importorskip("torch")
     fn = _noalloc_fn()
-    cases = [([40, 30, 30], 150, 3, 5), ([25, 35], 90, 2, 6)]
-    for n_b, G, K, seed in cases:  # two calls in a row share the static scratch
+    # two calls in a row share the static scratch; the second one runs on a
+    # stream of the caller's (not the default stream)
+    cases = [([40, 30, 30], 150, 3, 5, False), ([25, 35], 90, 2, 6, True)]
+    for n_b, G, K, seed, own_stream in cases:
         Y, est, want = _case(n_b, G, K, seed)
         dev = torch.device("cuda", 0)
         t = {k: torch.from_numpy(np.ascontiguousarray(est[k], dtype=np.float64)).to(dev)
@@ -49,13 +51,21 @@ def test_bic_noalloc_matches_busseq_bic_twice():
         nb = np.array(n_b, np.int32)
         dims = bq.Dims(len(n_b), K, G, nb.ctypes.data_as(C.POINTER(C.c_int32)))
         torch.cuda.synchronize()
+        stream = torch.cuda.Stream(device=dev) if own_stream else None
         rc = fn(C.byref(dims), Yd.data_ptr(), t["alpha"].data_ptr(), t["beta"].data_ptr(), t["nu"].data_ptr(),
                 t["delta"].data_ptr(), t["phi"].data_ptr(), t["gamma"].data_ptr(), t["pi"].data_ptr(),
-                out.data_ptr(), None)
+                out.data_ptr(), stream.cuda_stream if stream is not None else None)
         assert rc == 0, bq.lib().busseq_last_error().decode()
+        if stream is not None:
+            stream.synchronize()
         torch.cuda.synchronize()
-        got = float(out[0].item())
+        got, ll = (float(v) for v in out.cpu())
         assert abs(got - want) <= BIC_RTOL * abs(want), (got, want)
+        # out[1] is the log-likelihood of the BIC: BIC = -2 LL + log(G N) * nparam
+        B, N = len(n_b), sum(n_b)
+        nparam = (B + G) * K + 2 * B + G * (2 * B - 1) + N - B
+        ll_want = -(want - np.log(G * N) * nparam) / 2.0
+        assert abs(ll - ll_want) <= BIC_RTOL * abs(want), (ll, ll_want)
 
 
 def test_bic_noalloc_rejects_oversize():
