@@ -45,7 +45,8 @@ class Dims(C.Structure):
 class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
                 ("device", C.c_int32), ("chunk_cells", C.c_int32), ("hmc_leapfrog", C.c_int32),
-                ("zx_summaries", C.c_int32), ("hmc_gene_accept", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("zx_summaries", C.c_int32), ("hmc_gene_accept", C.c_int32), ("test_nb_inv_cap", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Estimates(C.Structure):
@@ -138,6 +139,7 @@ def lib():
         "busseq_write_outputs": ([H, C.c_char_p, C.c_int32], C.c_int),
         "busseq_simulate": ([C.POINTER(Dims), C.POINTER(SimParams), C.c_uint64, _PI32, _PI32, _PI32], C.c_int),
         "busseq_last_error": ([], C.c_char_p),
+        "busseq_sample_draws": ([C.c_int32, C.c_double, C.c_double, C.c_uint64, C.c_int64, C.c_void_p], C.c_int),
         "busseq_version": ([], C.c_char_p),
     }
     for name, (args, res) in sigs.items():
@@ -178,6 +180,18 @@ def simulate(n_b, G: int, K: int, seed: int, **params):
     sp = SimParams(**prm)
     _check(lib().busseq_simulate(C.byref(d), C.byref(sp), int(seed), _p(Y, _PI32), _p(W, _PI32), _p(X, _PI32)))
     return Y, W, X
+
+
+SAMPLE_KINDS = {"gamma": (0, np.float32), "poisson": (1, np.int32), "negbin": (2, np.int32),
+                "negbin_gamma_poisson": (3, np.int32), "negbin_inversion": (4, np.int32)}
+
+
+def sample_draws(kind: str, a: float, b: float = 0.0, seed: int = 0, n: int = 100000) -> np.ndarray:
+    """n draws of one device sampler (busseq_sample_draws), for distribution tests."""
+    code, dt = SAMPLE_KINDS[kind]
+    out = np.zeros(n, dt)
+    _check(lib().busseq_sample_draws(code, float(a), float(b), int(seed), int(n), out.ctypes.data_as(C.c_void_p)))
+    return out
 
 
 def read_counts(path: str, N: int, G: int) -> np.ndarray:
@@ -279,7 +293,7 @@ class Sampler:
 
     def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
                  keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0,
-                 zx_summaries: bool = False, hmc_gene_accept: bool = False):
+                 zx_summaries: bool = False, hmc_gene_accept: bool = False, test_nb_inv_cap: int = 0):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -290,7 +304,7 @@ class Sampler:
         opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
                       keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells),
                       hmc_leapfrog=int(hmc_leapfrog), zx_summaries=int(bool(zx_summaries)),
-                      hmc_gene_accept=int(bool(hmc_gene_accept)))
+                      hmc_gene_accept=int(bool(hmc_gene_accept)), test_nb_inv_cap=int(test_nb_inv_cap))
         on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
         if on_dev:
             assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2

@@ -23,9 +23,10 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["gene_kernels.cu", "cell_kernels.cu", "init_kernels.cu", "hmc_kernels.cu", "correct_kernels.cu", "capi.cu", "checkpoint.cu", "batch.cu",
-              "format_kernels.cu", "noalloc.cu"]
+              "format_kernels.cu", "noalloc.cu", "sampler_draws.cu"]
 CPP_SOURCES = ["host_io.cpp", "simulate.cpp"]
-HEADERS = ["busseq_dev.h", "rng.h", "kernels.h", "kernels_common.cuh", "correct_math.h", "capi_internal.h"]
+HEADERS = ["busseq_dev.h", "rng.h", "kernels.h", "kernels_common.cuh", "correct_math.h", "capi_internal.h",
+           "bic_series.h"]
 
 
 def _run(cmd):

@@ -1,0 +1,90 @@
+// The dropout-marginal likelihood of a zero count, in double precision.
+//
+// For Y = 0 the reference (BUSseq_gpu.cu:990-1003) sums, in log space,
+//   S = NB(0) + sum_{x=1}^{x_max-1} NB(x) sigmoid(g0 + g1 x),   x_max = floor(3 mu),
+// with NB(x) = Gamma(phi + x) / (Gamma(phi) x!) p^x (1-p)^phi, p = mu / (mu + phi),
+// one lgamma-based term and one log-add per x, and the clamps log p >= -250,
+// log(1-p) >= -250 (:977-986).  Here the same sum is formed without any
+// logarithm inside the loop: with r_x = NB(x) sigmoid(s_x) / NB(0),
+// s_x = g0 + g1 x and F_x = exp(s_x),
+//   r_x = r_{x-1} a_x b_x,  a_x = (phi + x - 1) / x * p,
+//   b_x = e^{g1} (1 + F_{x-1}) / (1 + F_x)     (= sigmoid(s_x) / sigmoid(s_{x-1})),
+// kept as R * exp(off) with R rescaled by 2^+-930 whenever it leaves
+// [2^-930, 2^930], so neither the NB mode (r can reach e^700) nor a vanishing
+// sigmoid under- or overflows.  log S = phi log(1-p) + log(1 + exp(off) sum R).
+//
+// Early exit, without changing the sum beyond double rounding: for g1 < 0,
+// b_y = e^{g1} (1 + F_{y-1}) / (1 + e^{g1} F_{y-1}) grows with F_{y-1}, and F
+// decreases, so b_y <= b_{x+1} for every y > x; a_y decreases in y when
+// phi > 1 and is at most p when phi <= 1.  So with rho = a_{x+1} b_{x+1} (p
+// b_{x+1} when phi <= 1) below 1, every later term is at most r_x rho^k and
+// the rest of the series at most r_x rho / (1 - rho).  The loop stops when
+// that bound falls below 2^-60 of the running sum (a quarter of double
+// precision's rounding unit), or when r has underflowed to exactly 0.
+#pragma once
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define BQ_BIC_HD __host__ __device__ __forceinline__
+#else
+#define BQ_BIC_HD inline
+#endif
+
+namespace bq {
+
+constexpr int BIC_SERIES_MAX_TERMS = 1 << 24;  // x_max is capped there (mu beyond 5.6e6)
+
+// The same sum term by term in log space (the reference's form, with the NB
+// term by its recurrence): used only where the recurrence above does not
+// apply, g1 >= 0 (the model's gamma1 is negative) or exp(g0 + g1) beyond 1e300.
+BQ_BIC_HD double bic_zero_series_logspace(int x_max, double logp, double lw0, double phi, double g0, double g1) {
+  double sacc = lw0, lnb = lw0;
+  for (int x = 1; x < x_max; ++x) {
+    lnb += log((phi + (double)(x - 1)) / (double)x) + logp;
+    const double sx = g0 + g1 * (double)x;
+    const double t = (sx > 0.0 ? -log1p(exp(-sx)) : sx - log1p(exp(sx))) + lnb;
+    sacc = t > sacc ? t + log1p(exp(sacc - t)) : sacc + log1p(exp(t - sacc));
+  }
+  return sacc;
+}
+
+// log S for a zero count; logp and log1mp already clamped as the reference does.
+BQ_BIC_HD double bic_zero_series(double mu, double logp, double log1mp, double phi, double g0, double g1) {
+  const double lw0 = phi * log1mp;  // log NB(0)
+  const double xm = 3.0 * mu;
+  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+  if (x_max <= 1) return lw0;
+  if (!(g1 < 0.0) || g0 + g1 > 690.0) return bic_zero_series_logspace(x_max, logp, lw0, phi, g0, g1);
+  const double p = exp(logp);
+  const double c = exp(g1);                 // e^{g1}
+  const double big = 8.7e279, small = 1.0 / 8.7e279;  // 2^930, 2^-930
+  const double ln_big = 930.0 * 0.69314718055994530942;
+  // x = 1: r_1 = phi p sigmoid(s_1), in log form (the only logarithms of the series)
+  const double s1 = g0 + g1;
+  const double lsig1 = s1 > 0.0 ? -log1p(exp(-s1)) : s1 - log1p(exp(s1));
+  double off = log(phi) + logp + lsig1;
+  double R = 1.0, acc = 1.0;
+  double F = exp(s1);  // F_1; it only decreases (g1 < 0), and once it underflows b_x is e^{g1}
+  for (int x = 1; x + 1 < x_max; ++x) {
+    // the factors of step x + 1
+    const double xd = (double)x;
+    const double a = (phi + xd) / (xd + 1.0) * p;
+    const double Fn = F * c;
+    const double b = c * (1.0 + F) / (1.0 + Fn);
+    const double rho = (phi > 1.0 ? a : p) * b;
+    if (R == 0.0 || (rho < 1.0 && R * rho < 8.673617379884035e-19 * acc * (1.0 - rho))) break;  // 2^-60
+    F = Fn;
+    R *= a * b;
+    acc += R;
+    if (acc > big) {                        // rescale the frame
+      R *= small;
+      acc *= small;
+      off += ln_big;
+    }
+  }
+  // log(1 + exp(off) acc), the x = 0 term being 1 in this frame
+  const double l1 = off + log(acc);
+  return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
+}
+
+}  // namespace bq

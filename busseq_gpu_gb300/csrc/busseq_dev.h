@@ -115,6 +115,7 @@ struct DevState {
   int n_static;     // CTAs evaluating the static (Y > 0) gamma terms
   int ymax;         // largest observed count
   int w_update;     // 0: MH with uniform proposal (reference), 1: K-way Gibbs
+  int nb_inv_cap;   // search cap of the NB inversion in k_zx (NB_INV_MAX_K unless a test lowers it)
   int n_burnin, n_unchanged, keep_draws, n_kept;
   uint64_t seed;
 

@@ -1,6 +1,7 @@
 // C ABI of the GB300 BUSseq sampler: memory, initialisation, CUDA-graph
 // sweeps, stages, summaries.  See include/busseq_gb300.h for the contract.
 #include "capi_internal.h"
+#include "rng.h"
 #include "correct_math.h"
 #include "kernels.h"
 
@@ -581,6 +582,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       s.cap_c += h->n_b[b] / bq::CELL_TILE + K;
     }
     s.w_update = opt.w_update == BUSSEQ_W_GIBBS ? BUSSEQ_W_GIBBS : BUSSEQ_W_MH;
+    s.nb_inv_cap = opt.test_nb_inv_cap > 0 ? std::min(opt.test_nb_inv_cap, bq::NB_INV_MAX_K) : bq::NB_INV_MAX_K;
     s.seed = opt.seed;
     s.n_burnin = 0;
     s.n_unchanged = INT_MAX;

@@ -388,7 +388,8 @@ __global__ void __launch_bounds__(CELL_THREADS) k_w_gibbs(DevState s) {
       if (target < cum) { pick = kk; break; }
     }
     s.W[i] = pick;
-    s.lr_W[i] = 0.0;
+    // diagnostic: log weight of the drawn type relative to the current one
+    s.lr_W[i] = sh_lp[tid][pick] - sh_lp[tid][k];
   }
 }
 

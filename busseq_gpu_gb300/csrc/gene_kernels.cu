@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
                                q_w[3][qw][slot], xo == 0);
     int err = 0;
     const float mu = q_mu[qw][slot], ph = q_ph[qw][slot];
-    const int xn = is_inv ? negbin_inversion(st, mu, ph, &err) : negbin_gamma_poisson(st, mu, ph, &err);
+    const int xn = is_inv ? negbin_inversion(st, mu, ph, &err, s.nb_inv_cap) : negbin_gamma_poisson(st, mu, ph, &err);
     const float ua = st.uniform();
     // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
     const float spo = (unsigned)xo < (unsigned)ZX_HIST ? sp_tab[xo] : softplusf(-g0 - g1 * (float)xo);

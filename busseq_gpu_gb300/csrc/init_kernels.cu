@@ -12,6 +12,7 @@
 // Summaries: k_finalize (posterior means, P(L=1), W mode; :1557-1608) and
 // k_bic_cell + k_bic_total (:967-1024, :1815-1843).
 #include "kernels_common.cuh"
+#include "bic_series.h"
 
 namespace bq {
 
@@ -420,33 +421,12 @@ __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
 
 // ---------------------------------------------------------------------------
 // BIC.  Per cell i and type k: sum over genes of the dropout-marginal
-// log-likelihood of Y (BUSseq_gpu.cu:967-1007), with the estimates.
-// For Y = 0 the reference sums NB(x) * P(drop | x) over x = 0 .. floor(3 mu)-1
-// in log space; here the same sum is evaluated with the NB recurrence
-//   log NB(x) = log NB(x-1) + log((phi + x - 1) / x) + log p
-// and stops once the terms are past the NB mode and 30 nats below the running
-// sum (the summand is then decreasing, so the rest cannot matter in float).
+// log-likelihood of Y (BUSseq_gpu.cu:967-1007), with the estimates, in double
+// precision throughout.  For Y = 0 the reference's series over
+// x = 0 .. floor(3 mu)-1 is bic_zero_series (bic_series.h): the same sum by a
+// log-free double recurrence, stopped only once the rest is provably below a
+// quarter of double rounding.
 // ---------------------------------------------------------------------------
-__device__ double bic_zero_term(double mu, double logp, double log1mp, float phi, float g0, float g1) {
-  const double x_max_d = 3.0 * mu;
-  // the series is cut at 2^24 terms (it is negligible long before, unless mu is absurd)
-  const int x_max = x_max_d > 16777216.0 ? 16777216 : (int)x_max_d;
-  float sacc = (float)(phi * log1mp);
-  float lnb = sacc;
-  const float lp = (float)logp;
-  const double mode_d = phi > 1.0f ? floor((phi - 1.0) * mu / phi) : 0.0;
-  for (int x = 1; x < x_max; ++x) {
-    lnb += logf((phi + (float)(x - 1)) / (float)x) + lp;
-    const float s = fmaf(g1, (float)x, g0);
-    const float ls = s - softplusf(s);  // log(sigmoid(g0 + g1 x))
-    const float tt = ls + lnb;
-    if (tt > sacc) sacc = tt + log1pf(expf(sacc - tt));
-    else sacc = sacc + log1pf(expf(tt - sacc));
-    if (g1 < 0.0f && (double)x > mode_d && tt < sacc - 30.0f) break;
-  }
-  return (double)sacc;
-}
-
 __global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik) {
   __shared__ double sh[8 * MAX_K];
   const int64_t i = blockIdx.x;
@@ -477,7 +457,7 @@ __global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, doubl
       if (logp < -250.0) logp = -250.0;
       if (log1mp < -250.0) log1mp = -250.0;
       if (y) acc[k] += base + y * logp + phi * log1mp;
-      else acc[k] += bic_zero_term(mu, logp, log1mp, (float)phi, (float)g0, (float)g1);
+      else acc[k] += bic_zero_series(mu, logp, log1mp, phi, g0, g1);
     }
   }
   for (int k = 0; k < K; ++k) {

@@ -59,7 +59,10 @@ enum StreamId : uint32_t {
   SID_CORRECT = 17,      // entry i*G+g : randomised PIT of the batch-corrected count (two words)
   SID_INIT_W = 20,       // cell i      : initial cell type
   SID_INIT_L = 21,       // k*G+g       : initial indicator L
-  SID_SIM = 30           // synthetic-data generator (not used by the sampler)
+  SID_SIM = 30,          // synthetic-data generator (not used by the sampler)
+  SID_TEST_GAMMA = 40,   // draw j      : busseq_sample_draws (distribution tests), the
+  SID_TEST_POISSON = 41, //               same streams as the oracle's sample functions
+  SID_TEST_NEGBIN = 42
 };
 
 // Iteration caps of the rejection samplers.  Hitting one sets an error bit.
@@ -395,14 +398,15 @@ enum : int { ERR_NB_INV_CAP = 4 };
 
 BQ_HD bool negbin_use_inversion(float mu, float phi) { return mu < NB_INV_MU && phi >= 1.0f; }
 
-BQ_HD int negbin_inversion(Stream& s, float mu, float phi, int* err) {
+// max_k lowers the search cap (a test of the failure path passes a small one).
+BQ_HD int negbin_inversion(Stream& s, float mu, float phi, int* err, int max_k = NB_INV_MAX_K) {
   const float q = mu / (phi + mu);
   float p = expf(phi * log1p_fast(-q));
   float F = p;
   const float u = s.uniform();
   int k = 0;
   while (u > F) {
-    if (k >= NB_INV_MAX_K) { *err |= ERR_NB_INV_CAP; break; }
+    if (k >= max_k) { *err |= ERR_NB_INV_CAP; break; }
     p = p * (q * fast_div(phi + (float)k, (float)(k + 1)));
     ++k;
     const float Fn = F + p;

@@ -79,7 +79,11 @@ typedef struct busseq_options {
                            change (the block posterior factorises over genes
                            given delta); delta then takes the random-walk step.
                            0: one decision for the whole block, delta included */
-  int32_t reserved[5];
+  int32_t test_nb_inv_cap; /* tests of the failure path only: > 0 lowers the search
+                           cap of the Z/X update's NB inversion (default and
+                           maximum 1024), so that the cap is reached and the run
+                           reports BUSSEQ_ERR_SAMPLER; 0 for every real run      */
+  int32_t reserved[4];
 } busseq_options;
 
 /* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
@@ -143,7 +147,8 @@ typedef struct busseq_log_ratios {
   double* nu;       /* [B*G] (b >= 1) */
   double* delta;    /* [N]   */
   double* phi;      /* [B*G] */
-  double* W;        /* [N]   (MH only) */
+  double* W;        /* [N]   MH: the log ratio of the proposal; K-way draw: the
+                       log weight of the drawn type minus that of the current one */
 } busseq_log_ratios;
 
 /* ---- lifecycle ------------------------------------------------------------ */
@@ -206,6 +211,19 @@ int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev, const doub
                        void* cuda_stream);
 
 /* ---- state access, single stages, diagnostics ----------------------------- */
+
+/* n draws from one of the device samplers that the sweep kernels use, into
+ * host memory, for distribution tests.  Draw j uses the Philox stream (seed,
+ * 40 + family, j, 0), the streams of the FP64 oracle's sample functions.
+ *   kind 0: Gamma(shape a, scale 1), Marsaglia-Tsang         out: float[n]
+ *   kind 1: Poisson(a), inversion / PTRS                      out: int32[n]
+ *   kind 2: NB(mean a, size b) as the Z/X update draws it     out: int32[n]
+ *   kind 3: NB(mean a, size b), Gamma-Poisson always          out: int32[n]
+ *   kind 4: NB(mean a, size b), inversion always (b >= 1)     out: int32[n]
+ * No counterpart in the reference, whose samplers (BUSseq_gpu.cu:34-218) are
+ * only called inside its update kernels.  Returns BUSSEQ_ERR_SAMPLER when a
+ * sampler cap was reached. */
+int busseq_sample_draws(int32_t kind, double a, double b, uint64_t seed, int64_t n, void* out);
 
 /* Batch-corrected counts [N*G] (cells x genes, the layout of Y): each imputed
  * count of the last sweep (_post_X) mapped by randomised quantile matching

@@ -9,6 +9,9 @@
   is built where a driver is installed, i.e. on the GPU machine).
 * ``ref_sweep_timer`` -- oracle/ref_sweep_timer.cpp, which replays the
   reference's per-sweep launch sequence from that cubin to time it.
+* ``ref_chain``    -- oracle/ref_chain.cpp, which runs a whole chain (init,
+  burn-in, kept sweeps) with the reference's kernels from that cubin, for the
+  chain-level comparison of oracle/ref_chain.py.
 * ``libsim.so``    -- the synthetic-data generator alone (oracle/sim_standalone.cpp),
   so that bench.py's CPU arms never map the product library.
 
@@ -35,6 +38,7 @@ HARNESS_BIN = os.path.join(LIB_DIR, "ref_harness")
 SIM_SO = os.path.join(LIB_DIR, "libsim.so")
 ROOT = os.path.dirname(HERE)
 TIMER_BIN = os.path.join(LIB_DIR, "ref_sweep_timer")
+CHAIN_BIN = os.path.join(LIB_DIR, "ref_chain")
 
 
 def _run(cmd: list[str]) -> None:
@@ -104,13 +108,13 @@ def build_harness(force: bool = False) -> str | None:
     return HARNESS_BIN
 
 
-def build_ref_timer(force: bool = False) -> str | None:
-    """Build the reference sweep timer (driver API; needs libcuda, like the harness)."""
-    src = os.path.join(HERE, "ref_sweep_timer.cpp")
+def _driver_api_tool(src_name: str, out: str, force: bool) -> str | None:
+    """A driver-API program (needs libcuda; None where it cannot be linked)."""
+    src = os.path.join(HERE, src_name)
     os.makedirs(LIB_DIR, exist_ok=True)
-    if not force and not _stale(TIMER_BIN, [src]):
-        return TIMER_BIN
-    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(CUDA_HOME, "include"), "-o", TIMER_BIN, src]
+    if not force and not _stale(out, [src]):
+        return out
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(CUDA_HOME, "include"), "-o", out, src]
     for d in (os.path.join(CUDA_HOME, "lib64"), os.path.join(CUDA_HOME, "lib64", "stubs")):
         cmd += ["-L", d]
     cmd += ["-lcuda"]
@@ -118,7 +122,17 @@ def build_ref_timer(force: bool = False) -> str | None:
         _run(cmd)
     except RuntimeError:
         return None
-    return TIMER_BIN
+    return out
+
+
+def build_ref_timer(force: bool = False) -> str | None:
+    """Build the reference sweep timer (driver API; needs libcuda, like the harness)."""
+    return _driver_api_tool("ref_sweep_timer.cpp", TIMER_BIN, force)
+
+
+def build_ref_chain(force: bool = False) -> str | None:
+    """Build the reference chain runner (driver API; needs libcuda)."""
+    return _driver_api_tool("ref_chain.cpp", CHAIN_BIN, force)
 
 
 def build_all(force: bool = False) -> dict:
@@ -126,6 +140,7 @@ def build_all(force: bool = False) -> dict:
     if shutil.which("g++"):
         out["harness"] = build_harness(force)
         out["ref_timer"] = build_ref_timer(force)
+        out["ref_chain"] = build_ref_chain(force)
     return out
 
 

@@ -666,6 +666,7 @@ static void stage_W(orc_state* st, int iter, int w_update, orc_debug* dbg) {
         if (!done && target < cum) { pick = kk; done = true; }
       }
       if (dbg && dbg->mg_W) dbg->mg_W[i] = mg;
+      if (dbg && dbg->lr_W) dbg->lr_W[i] = lp[pick] - lp[k];  // log weight of the draw relative to the current type
       st->W[i] = pick;
     }
   }

@@ -23,13 +23,20 @@ CASES = {
     "ragged_warm": ([9, 61, 17, 33, 5], 333, 5, 7, 15),
     "minimal_warm": ([12, 9], 97, 2, 3, 10),                      # B = 2, K = 2
     "many_types_warm": ([20, 35, 50, 25, 40, 30], 150, 12, 9, 10),  # B = 6, K = 12
+    # the headline shape (4 batches, G = 10^4, K = 8) on a cell subset the oracle runs in seconds
+    "config1_shape": ([250, 250, 250, 250], 10000, 8, 13580, 20),
+    # the large uneven workload's shape: 6 batches in its 2:5:8:12:20:3 ratio, G = 2*10^4,
+    # K = 12, 15 % differential genes and phi ~ U(2, 30) ("wide" generator)
+    "config4_shape": ([80, 200, 320, 480, 800, 120], 20000, 12, 13583, 10),
 }
+WIDE = {"config4_shape"}
 
 
 @pytest.fixture(scope="module", params=list(CASES))
 def case(request):
     n_b, G, K, seed, warm = CASES[request.param]
-    Y, W_true, _ = bq.simulate(n_b, G, K, seed)
+    sim = bq.CONFIG_SIM["wide" if request.param in WIDE else "default"]
+    Y, W_true, _ = bq.simulate(n_b, G, K, seed, **sim)
     s = bq.Sampler(Y, n_b, K, seed=seed, p0=0.3)
     if warm:
         s.begin(warm, warm, 0)
@@ -79,11 +86,13 @@ def test_stage_zx_gamma_alpha_L_ptau(case):
     # L from the old beta, p, tau0 (BUSseq_gpu.cu:634-648)
     o.step("L", it, debug=d)
     check_discrete("L", g["L"][1:], o.L[1:], d.mg_L[1:], report=rep)
-    # p, tau0 from the kernels' L (BUSseq_gpu.cu:650-668)
+    # p, tau0 from the kernels' L (BUSseq_gpu.cu:650-668): each is compared unless its
+    # own Gamma rejection step is a certified near-tie (margin <= 1e-5)
     o.L[:] = g["L"]
     o.step("ptau", it, debug=d)
-    if np.all(d.mg_ptau > 1e-5):
-        np.testing.assert_allclose(g["p_tau0"], o.p_tau0, rtol=1e-5)
+    checked = d.mg_ptau > 1e-5
+    np.testing.assert_allclose(g["p_tau0"][checked], o.p_tau0[checked], rtol=1e-5)
+    rep["p_tau0_checked"] = int(checked.sum())
     print(c["name"], rep, "gamma0 flips", f0)
 
 
@@ -160,13 +169,25 @@ def test_stage_W_gibbs(case):
         s.set_state(c["st"])
         s.run_stage(4, it)
         g = s.get_state()
+        lr = s.log_ratios()
     finally:
         s.close()
     o = oracle_state(Y, c["n_b"], c["K"], c["seed"], c["st"])
     d = po.Debug(o)
     o.step("W", it, w_update=1, debug=d)
-    rep = {}
-    check_discrete("W_gibbs", g["W"], o.W, d.mg_W, tol=2e-3, max_frac=1e-2, report=rep)
+    # Where both drew the same type, the log weight of that type relative to the
+    # current one (K sums over the genes in float) must agree within the log-ratio
+    # tolerance; the largest such error eps measured on this very case bounds how
+    # far a boundary of the categorical distribution function can move (by at
+    # most max |d log w_j - d log w_k| <= 2 eps), so a differing draw is a
+    # certified near-tie only where the oracle's uniform lies within 2 eps of a
+    # boundary, and such draws are at most 0.1 % of the cells.
+    same = g["W"] == o.W
+    dlr = np.abs(lr["W"] - d.lr_W)
+    assert np.all(dlr[same] <= LR_ATOL + LR_RTOL * np.abs(d.lr_W[same])), dlr[same].max()
+    eps = float(dlr[same].max()) if same.any() else LR_ATOL
+    rep = {"max_dlr": eps}
+    check_discrete("W_gibbs", g["W"], o.W, d.mg_W, tol=2.0 * eps + 1e-9, max_frac=1e-3, report=rep)
     print(c["name"], rep)
 
 
