@@ -314,7 +314,7 @@ def run_batch(args, cfg, rank, world, local):
         return torch.cuda.Event(enable_timing=True)
 
     # ---- sequential arm: every chain alone, on its own stream ----------------
-    seq_ms = {}
+    seq_ms, busy_ms = {}, {}
     stream = torch.cuda.Stream(device=local)
     for K, c in zip(ks, chains()):
         c.set_stream(stream.cuda_stream)
@@ -327,6 +327,8 @@ def run_batch(args, cfg, rank, world, local):
         e1.record(stream)
         torch.cuda.synchronize()
         seq_ms[K] = e0.elapsed_time(e1)
+        # the chain's kernels alone: summed event-timed durations per sweep
+        busy_ms[K] = sum(c.profile(10).values())
         c.close()
     seq_total = sum(seq_ms.values())
 
@@ -394,6 +396,19 @@ def run_batch(args, cfg, rank, world, local):
                            "ms_per_chain": {str(K): v for K, v in seq_ms.items()},
                            "note": "each chain alone for the same %d sweeps" % args.steps},
             "batched_vs_sequential": value / seq_value,
+            # What a merged multi-chain launch could recover: it can remove the gaps
+            # between kernels (launch latency, tails, idle SMs) but not the kernels'
+            # own busy time.  sequential / busy is the speed-up of removing every gap;
+            # batched / busy below 1 means the concurrent kernels already overlap.
+            "kernel_busy": {
+                "ms_per_sweep": {str(K): v for K, v in busy_ms.items()},
+                "busy_ms_per_sweep_all_chains": sum(busy_ms.values()),
+                "sequential_ms_per_sweep_all_chains": seq_total / args.steps,
+                "batched_ms_per_sweep_all_chains": bat_ms / args.steps,
+                "gap_free_bound_vs_sequential": (seq_total / args.steps) / sum(busy_ms.values()),
+                "batched_over_busy": (bat_ms / args.steps) / sum(busy_ms.values()),
+                "note": "busy = sum of each kernel's event-timed duration when its chain runs alone (burn-in "
+                        "sweeps, 10 timed)"},
             # per chain-sweep, every chain passes over its own copy of the tensor
             "sweep_roofline": sweep_roofline(N, G, 0, value / world, _peak_hbm()[0]),
             "autotune": {"seconds": tune_s, "ms_per_sweep": {str(K): {str(c): m for c, m in tuned[K][1].items()}

@@ -36,7 +36,10 @@
 // reference's [scalar][kept sweep] layout, are written to <out_dir> as raw
 // little-endian files (preserved_<name>.bin) and summarised by
 // oracle/ref_chain.py.  The state right after initialisation is written too
-// (init_<name>.bin), so that the other chain can start from it.
+// (init_<name>.bin), so that the other chain can start from it.  With
+// REF_CHAIN_INIT_ONLY set the program stops after writing it; with
+// REF_CHAIN_START_DIR=<dir> the chain starts instead from the state in <dir>
+// (start_<name>.bin), keeping the priors of its own initialisation.
 //
 // usage: ref_chain <cubin> <Y.i32> <G> <K> <seed> <n_iter> <n_burnin>
 //                  <n_unchanged> <out_dir> <n_1> ... <n_B>
@@ -317,6 +320,38 @@ int main(int argc, char** argv) {
     for (const Out& o : outs) {
       std::vector<char> h = down<char>(o.p, o.bytes);
       wrote &= write_file(out_dir + "/init_" + o.name + ".bin", h.data(), h.size());
+    }
+  }
+
+  // Only the initial state wanted (REF_CHAIN_INIT_ONLY): stop here.
+  if (getenv("REF_CHAIN_INIT_ONLY")) {
+    printf("{\"impl\": \"reference .cu kernels, BUSseq_gpu.cu:1163-1244\", \"init_only\": true, \"p0\": %.17g, "
+           "\"init_s\": %.3f, \"files_written\": %s}\n", p0, init_s, wrote ? "true" : "false");
+    return wrote ? 0 : 3;
+  }
+  // A given starting state (REF_CHAIN_START_DIR): after the reference's own
+  // initialisation (which fixes the priors mu_alpha, mu_nu and mu_delta), the
+  // chain state is replaced by the one in that directory (start_<name>.bin:
+  // X, Z [N*G] int32; W [N] int32; L [K*G] int32; alpha [G], beta [K*G],
+  // nu [B*G], delta [N], phi [B*G], gamma [2B], pi [B*K], p [2] double).
+  if (const char* sd = getenv("REF_CHAIN_START_DIR")) {
+    struct In { const char* name; CUdeviceptr p; size_t bytes; };
+    const In ins[] = {
+        {"X", d_X, 4ull * NG}, {"Z", d_Z, 4ull * NG}, {"W", d_W, 4ull * N}, {"L", d_L, 4ull * K * G},
+        {"alpha", d_alpha, 8ull * G}, {"beta", d_beta, 8ull * K * G}, {"nu", d_nu, 8ull * B * G},
+        {"delta", d_delta, 8ull * N}, {"phi", d_phi, 8ull * B * G}, {"gamma", d_gamma, 16ull * B},
+        {"pi", d_pi, 8ull * B * K}, {"p", d_p, 16},
+    };
+    for (const In& in : ins) {
+      std::vector<char> h(in.bytes);
+      const std::string path = std::string(sd) + "/start_" + in.name + ".bin";
+      FILE* f = fopen(path.c_str(), "rb");
+      if (!f || fread(h.data(), 1, h.size(), f) != h.size()) {
+        fprintf(stderr, "ref_chain: cannot read %zu bytes from %s\n", h.size(), path.c_str());
+        return 1;
+      }
+      fclose(f);
+      CK(cuMemcpyHtoD(in.p, h.data(), h.size()));
     }
   }
 

@@ -42,24 +42,97 @@ sys.path.insert(0, ROOT)
 CONFIG0 = dict(n_b=[300, 300, 200, 200], G=3000, K=5, seed=13579)
 
 
-def run_reference(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeout):
+def _ref_binary(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeout, env=None):
     from oracle import build
     cubin = build.build_ref_cubin()
     exe = build.build_ref_chain()
     if not cubin or not os.path.exists(cubin) or not exe:
         raise RuntimeError("the reference cubin or oracle/lib/ref_chain is not available")
     ypath = os.path.join(workdir, "Y.i32")
-    np.ascontiguousarray(Y, dtype=np.int32).tofile(ypath)
+    if not os.path.exists(ypath):
+        np.ascontiguousarray(Y, dtype=np.int32).tofile(ypath)
     G = Y.shape[1]
     cmd = [exe, cubin, ypath, str(G), str(K), str(seed), str(n_iter), str(n_burnin), str(n_unchanged), workdir,
            *[str(n) for n in n_b]]
     t0 = time.perf_counter()
-    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=timeout)
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=timeout,
+                       env=dict(os.environ, **(env or {})))
     wall = time.perf_counter() - t0
     info = json.loads(r.stdout.strip().splitlines()[-1]) if r.stdout.strip() else {}
     if r.returncode != 0:
         raise RuntimeError("ref_chain failed (rc %d): %s %s" % (r.returncode, r.stderr[-2000:], info))
     info["wall_s"] = wall
+    return info
+
+
+def _read_init(workdir, Y, B, K, G):
+    def ini(name, dtype):
+        return np.fromfile(os.path.join(workdir, "init_%s.bin" % name), dtype=dtype)
+
+    return {"X": np.ascontiguousarray(Y, dtype=np.int32), "Z": np.zeros(Y.shape, np.uint8),
+            "W": ini("W", np.int32), "L": ini("L", np.int32).astype(np.int8).reshape(K, G),
+            "alpha": ini("alpha", np.float64), "mu_alpha": ini("mu_alpha", np.float64),
+            "beta": ini("beta", np.float64).reshape(K, G), "nu": ini("nu", np.float64).reshape(B, G),
+            "mu_nu": np.concatenate([[0.0], ini("mu_nu", np.float64)]), "delta": ini("delta", np.float64),
+            "mu_delta": ini("mu_delta", np.float64), "phi": ini("phi", np.float64).reshape(B, G),
+            "gamma": ini("gamma", np.float64).reshape(2, B), "pi": ini("pi", np.float64).reshape(B, K),
+            "p_tau0": ini("p", np.float64)}
+
+
+def _read_preserved(workdir, n_b, K, G, n):
+    B, N = len(n_b), int(sum(n_b))
+
+    def rd(name, dtype, rows):
+        return np.fromfile(os.path.join(workdir, "preserved_%s.bin" % name), dtype=dtype).reshape(rows, n)
+
+    return {"gamma": rd("gamma", np.float64, 2 * B), "alpha": rd("alpha", np.float64, G),
+            "L": rd("L", np.int32, (K - 1) * G), "beta": rd("beta", np.float64, (K - 1) * G),
+            "p_tau0": rd("p", np.float64, 2), "nu": rd("nu", np.float64, (B - 1) * G),
+            "delta": rd("delta", np.float64, N), "phi": rd("phi", np.float64, B * G),
+            "W": rd("W", np.int32, N), "pi": rd("pi", np.float64, B * K)}
+
+
+def _write_start(workdir, st):
+    """A state of this sampler as the reference runner's start files."""
+    files = {"X": (st["X"], np.int32), "Z": (st["Z"], np.int32), "W": (st["W"], np.int32), "L": (st["L"], np.int32),
+             "alpha": (st["alpha"], np.float64), "beta": (st["beta"], np.float64), "nu": (st["nu"], np.float64),
+             "delta": (st["delta"], np.float64), "phi": (st["phi"], np.float64), "gamma": (st["gamma"], np.float64),
+             "pi": (st["pi"], np.float64), "p": (st["p_tau0"], np.float64)}
+    for name, (v, dt) in files.items():
+        np.ascontiguousarray(v, dtype=dt).ravel().tofile(os.path.join(workdir, "start_%s.bin" % name))
+
+
+def run_stationary(Y, n_b, K, seed, start_sweeps, n_iter, n_burnin, timeout):
+    """Both samplers from one state in the posterior's bulk: this sampler runs
+    `start_sweeps` sweeps from the reference's initial state; from the state it
+    reaches, each sampler then runs n_iter sweeps (n_burnin not kept) with p and
+    tau0 updated throughout, and the kept draws are compared."""
+    import busseq_gpu_gb300 as bq
+    B, G = len(n_b), Y.shape[1]
+    with tempfile.TemporaryDirectory() as wd:
+        info0 = _ref_binary(Y, n_b, K, seed, 1, 0, 0, wd, timeout, env={"REF_CHAIN_INIT_ONLY": "1"})
+        init = _read_init(wd, Y, B, K, G)
+        t0 = time.perf_counter()
+        s = bq.Sampler(Y, n_b, K, seed=seed, p0=info0["p0"], keep_draws=True)
+        s.set_state(init)
+        s.begin(start_sweeps + n_iter, start_sweeps + n_burnin, 0)
+        s.sweeps(start_sweeps)
+        s.synchronize()
+        start = s.get_state()
+        s.sweeps(n_iter)
+        s.finish()
+        ours_wall = time.perf_counter() - t0
+        ours = s.preserved()
+        s.close()
+        _write_start(wd, start)
+        info = _ref_binary(Y, n_b, K, seed, n_iter, n_burnin, 0, wd, timeout, env={"REF_CHAIN_START_DIR": wd})
+        ref = _read_preserved(wd, n_b, K, G, n_iter - n_burnin)
+    info["start"] = {"sweeps_of_this_sampler_from_the_reference_init": start_sweeps}
+    return ref, info, ours, {"wall_s": ours_wall, "sweeps_per_s": (start_sweeps + n_iter) / ours_wall}
+
+
+def run_reference(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeout):
+    info = _ref_binary(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeout)
     B, N, n = len(n_b), int(sum(n_b)), n_iter - n_burnin
 
     def rd(name, dtype, rows):
@@ -71,18 +144,7 @@ def run_reference(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeo
             "delta": rd("delta", np.float64, N), "phi": rd("phi", np.float64, B * G),
             "W": rd("W", np.int32, N), "pi": rd("pi", np.float64, B * K)}
 
-    def ini(name, dtype):
-        return np.fromfile(os.path.join(workdir, "init_%s.bin" % name), dtype=dtype)
-
-    init = {"X": np.ascontiguousarray(Y, dtype=np.int32), "Z": np.zeros(Y.shape, np.uint8),
-            "W": ini("W", np.int32), "L": ini("L", np.int32).astype(np.int8).reshape(K, G),
-            "alpha": ini("alpha", np.float64), "mu_alpha": ini("mu_alpha", np.float64),
-            "beta": ini("beta", np.float64).reshape(K, G), "nu": ini("nu", np.float64).reshape(B, G),
-            "mu_nu": np.concatenate([[0.0], ini("mu_nu", np.float64)]), "delta": ini("delta", np.float64),
-            "mu_delta": ini("mu_delta", np.float64), "phi": ini("phi", np.float64).reshape(B, G),
-            "gamma": ini("gamma", np.float64).reshape(2, B), "pi": ini("pi", np.float64).reshape(B, K),
-            "p_tau0": ini("p", np.float64)}
-    return pres, info, init
+    return pres, info, _read_init(workdir, Y, B, K, G)
 
 
 def run_ours(Y, n_b, K, seed, p0, n_iter, n_burnin, n_unchanged, init=None):
@@ -108,6 +170,10 @@ def main():
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     ap.add_argument("--name", default="config0")
     ap.add_argument("--timeout", type=int, default=3000, help="seconds allowed for the reference chain")
+    ap.add_argument("--start-sweeps", type=int, default=0,
+                    help="> 0: compare the stationary chains: this sampler first runs this many sweeps from the "
+                         "reference's initial state, then both samplers run --iters sweeps from the state reached "
+                         "(--unchanged is then 0)")
     ap.add_argument("--own-init", action="store_true",
                     help="start this sampler from its own initialisation instead of the reference's initial state")
     args = ap.parse_args()
@@ -119,22 +185,31 @@ def main():
     B = len(n_b)
     Y, W_true, _ = bq.simulate(n_b, G, K, seed)
     os.makedirs(args.out, exist_ok=True)
-    with tempfile.TemporaryDirectory() as wd:
-        ref_pres, ref_info, init = run_reference(Y, n_b, K, seed, args.iters, args.burnin, args.unchanged, wd,
-                                                 args.timeout)
-    ours_pres, ours_info = run_ours(Y, n_b, K, seed, ref_info["p0"], args.iters, args.burnin, args.unchanged,
-                                    None if args.own_init else init)
+    if args.start_sweeps > 0:
+        ref_pres, ref_info, ours_pres, ours_info = run_stationary(Y, n_b, K, seed, args.start_sweeps, args.iters,
+                                                                  args.burnin, args.timeout)
+    else:
+        with tempfile.TemporaryDirectory() as wd:
+            ref_pres, ref_info, init = run_reference(Y, n_b, K, seed, args.iters, args.burnin, args.unchanged, wd,
+                                                     args.timeout)
+        ours_pres, ours_info = run_ours(Y, n_b, K, seed, ref_info["p0"], args.iters, args.burnin, args.unchanged,
+                                        None if args.own_init else init)
     sa = cc.summarise(ref_pres, B, K, G)
     sb = cc.summarise(ours_pres, B, K, G)
     rec = cc.compare(sa, sb, B, K, G, W_true)
     rec.update({
         "what": "whole-chain comparison: the reference's kernels (a) against this sampler (b), same data, run "
                 "lengths, seed and initial p; z = (mean_a - mean_b) / sqrt(se_a^2 + se_b^2) per scalar",
-        "start": ("both chains from their own initialisation" if args.own_init else
+        "start": (("both chains from one state in the posterior's bulk: this sampler ran %d sweeps from the "
+                   "reference's initial state, and both samplers continue from the state it reached (X, Z, W, L and "
+                   "every parameter; the priors of the reference's initialisation); p and tau0 updated throughout"
+                   % args.start_sweeps) if args.start_sweeps > 0 else
+                  "both chains from their own initialisation" if args.own_init else
                   "this sampler started from the reference chain's initial state (W, L, every parameter, X = Y, "
                   "Z = 0), so both chains have the same distribution at every sweep"),
         "data": "BUSseq generative model, batches %s, G = %d, K = %d, seed %d" % (n_b, G, K, seed),
-        "n_iter": args.iters, "n_burnin": args.burnin, "n_unchanged": args.unchanged,
+        "n_iter": args.iters, "n_burnin": args.burnin,
+        "n_unchanged": 0 if args.start_sweeps > 0 else args.unchanged,
         "reference": ref_info, "ours": ours_info,
         "pi_in_reference_chain": "host Dirichlet(count + 2) draws; update_pi (BUSseq_gpu.cu:866-890) not launched",
     })
