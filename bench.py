@@ -52,6 +52,8 @@ CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=1358
 # steps (--gene-accept 1: per-gene decisions)
 CFG2 = dict(CFG1, hmc=10)
 CFG3 = dict(CFG1, ks=list(range(3, 11)))  # config-1 data fitted by 8 chains, K = 3 .. 10
+# the gradient-based sampler whose mixing the config-1 line reports beside the plain sampler's
+HMC_QUALITY = dict(hmc=10, gene=False, w_update="mh")
 WORKLOADS = {"config1": CFG1, "config2": CFG2, "config3": CFG3, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
 UNIT = "sweeps/s"
@@ -426,7 +428,7 @@ def run_batch(args, cfg, rank, world, local):
     return 0
 
 
-def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=False):
+def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=False, w_update="mh"):
     """One whole job with kept draws: ESS (Geyer, initial monotone sequence) of
     every beta (k >= 1) and nu (b >= 1) coordinate, ESS/s over the wall time of
     the whole job (upload, init, burn-in, kept sweeps, estimates), and the ARI
@@ -435,7 +437,8 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=Fal
     from busseq_gpu_gb300.diagnostics import adjusted_rand_index, ess_geyer
 
     t0 = time.perf_counter()
-    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True, hmc_leapfrog=hmc, hmc_gene_accept=gene and hmc > 0)
+    s = bq.Sampler(Y, n_b, K, seed=seed + 1, keep_draws=True, hmc_leapfrog=hmc, hmc_gene_accept=gene and hmc > 0,
+                   w_update=w_update)
     s.run(n_iter, n_burnin, min(500, n_burnin))
     est = s.estimates(with_XZ=False)
     wall = time.perf_counter() - t0
@@ -445,7 +448,8 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=Fal
     out = {"sweeps": n_iter, "burnin": n_burnin, "kept": n_iter - n_burnin, "wall_s": wall,
            "ari_W": adjusted_rand_index(est["W"], W_true), "estimator": "Geyer initial monotone sequence",
            "sampler": ("HMC, %d leapfrog steps%s" % (hmc, ", per-gene decisions" if gene else "")) if hmc
-           else "random-walk MH (the reference's)"}
+           else "random-walk MH (the reference's)",
+           "w_update": "K-way Gibbs draw" if w_update == "gibbs" else "Metropolis, uniform proposal (the reference's)"}
     if hstats:
         out["hmc"] = {k: float(v) for k, v in hstats.items()}
     for name in ("beta", "nu"):
@@ -470,6 +474,8 @@ def main():
     ap.add_argument("--cells", type=int, default=0,
                     help="cells per batch (default 2500, the config-1 size); smaller only for profiler captures")
     ap.add_argument("--no-ess", action="store_true", help="skip the ESS / ARI run")
+    ap.add_argument("--no-hmc-quality", action="store_true",
+                    help="config1: skip the gradient-based sampler's ESS / ARI run beside the plain sampler's")
     ap.add_argument("--leapfrog", type=int, default=0,
                     help="leapfrog steps of the HMC block update (overrides the workload's; 0 keeps it)")
     ap.add_argument("--gene-accept", type=int, default=None, choices=[0, 1],
@@ -646,6 +652,23 @@ def main():
 
             quality["vs_mh"] = {"beta_ess_per_s_median_ratio": ratio("beta"),
                                 "nu_ess_per_s_median_ratio": ratio("nu"), "ari_W_mh": mh["ari_W"], "mh": mh}
+        elif args.workload == "config1" and not args.no_hmc_quality:
+            # the gradient-based update on the same data and whole job (the config-2
+            # sampler): its ESS/s against this plain sampler's, at equal ARI
+            hq = ess_run(Y, W_true, n_b, K, seed, hmc=HMC_QUALITY["hmc"], gene=HMC_QUALITY["gene"],
+                         w_update=HMC_QUALITY["w_update"])
+
+            def ratio(name):
+                a, r = hq[name]["ess_per_s_median"], quality[name]["ess_per_s_median"]
+                return a / r if a and r else None
+
+            quality["hmc_vs_mh"] = {
+                "beta_ess_per_s_median_ratio": ratio("beta"), "nu_ess_per_s_median_ratio": ratio("nu"),
+                "ari_W_hmc": hq["ari_W"], "ari_W_mh": quality["ari_W"], "ari_diff": hq["ari_W"] - quality["ari_W"],
+                "target": "both ratios >= 5 with the ARI within 0.01 of the plain sampler's or better",
+                "met": bool((ratio("beta") or 0) >= 5 and (ratio("nu") or 0) >= 5 and
+                            hq["ari_W"] >= quality["ari_W"] - 0.01),
+                "hmc": hq}
 
     # ---- CPU baseline (rank 0, N = 1 only): 20 full sweeps of the oracle ----
     cpu = None

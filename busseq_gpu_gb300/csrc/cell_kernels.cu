@@ -122,13 +122,16 @@ __global__ void __launch_bounds__(CELL_THREADS, 4) k_delta(DevState s) {
   const int64_t Gp = s.Gp, G = s.G;
   DeltaRing ring{xbuf, bar, s.X, sh_i, Gp, len, (int)((Gp + DELTA_WIDTH - 1) / DELTA_WIDTH)};
   ring.init(tid);
+  float cd = 0.0f;
   if (tid < CELL_TILE) {
     const int i = s.perm[start + (tid < len ? tid : 0)];
     sh_i[tid] = i;
     sh_D[tid] = s.Dexp[i];
-    sh_c[tid] = tid < len ? expm1f(s.delta_p[i] - s.delta[i]) : 0.0f;
+    cd = tid < len ? expm1f(s.delta_p[i] - s.delta[i]) : 0.0f;
+    sh_c[tid] = cd;
   }
-  __syncthreads();
+  // every cell's |expm1(step)| <= 1/2: the terms by log1p_shift (one reciprocal)
+  const bool fast = __syncthreads_and(fabsf(cd) <= 0.5f) != 0;
   ring.prologue(tid);
   float acc[CELL_TILE];
 #pragma unroll
@@ -155,10 +158,14 @@ __global__ void __launch_bounds__(CELL_THREADS, 4) k_delta(DevState s) {
           const int2 xv = *reinterpret_cast<const int2*>(ring.row(step, r) + tid * 2);
           const float D = sh_D[r], c = sh_c[r];
           const float mu0 = e.x * D, mu1 = e.y * D;
-          float a = (ph.x + (float)xv.x) * log1p_near0(c * fast_div(mu0, ph.x + mu0));
+          const float l0 = fast ? log1p_shift(c * mu0, fmaf(2.0f + c, mu0, 2.0f * ph.x))
+                                : log1p_near0(c * fast_div(mu0, ph.x + mu0));
+          float a = (ph.x + (float)xv.x) * l0;
           int sxv = xv.x;
           if (two) {
-            a += (ph.y + (float)xv.y) * log1p_near0(c * fast_div(mu1, ph.y + mu1));
+            const float l1 = fast ? log1p_shift(c * mu1, fmaf(2.0f + c, mu1, 2.0f * ph.y))
+                                  : log1p_near0(c * fast_div(mu1, ph.y + mu1));
+            a = fmaf(ph.y + (float)xv.y, l1, a);
             sxv += xv.y;
           }
           sxi[r] += sxv;

@@ -481,7 +481,31 @@ __device__ __forceinline__ int stage_chunk(const DevState& s, int start, int len
   return len8;
 }
 
-// alpha: sum of x and of (phi + x) log1p(expm1(alpha' - alpha) p) over the chunk
+// alpha: sum of x and of (phi + x) log1p(expm1(alpha' - alpha) p) over the chunk.
+// FAST: |c| <= 1/2, the term by log1p_shift (one reciprocal); otherwise the
+// general form (a random-walk step beyond 0.405, about four of its sd).
+template <bool FAST>
+__device__ __forceinline__ void alpha_sums(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D,
+                                           int len8, float M, float ph, float ca, int64_t& sx, KahanF& la) {
+  const float c2 = 2.0f + ca, ph2 = 2.0f * ph;
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    float f = 0.0f;
+    int s8 = 0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const float mu = M * dv[u];
+      s8 += xr[u];
+      const float l = FAST ? log1p_shift(ca * mu, fmaf(c2, mu, ph2)) : log1p_near0(ca * fast_div(mu, ph + mu));
+      f = fmaf(ph + (float)xr[u], l, f);
+    }
+    sx += s8;
+    la.add(f);
+  }
+}
+
 __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
   __shared__ __align__(16) int s_i[MAX_CG];
   __shared__ __align__(16) float s_D[MAX_CG];
@@ -501,32 +525,21 @@ __global__ void __launch_bounds__(GENE_TILE) k_alpha(DevState s) {
   const float ca = expm1f(s.alpha_p[g] - s.alpha[g]);
   int64_t sx = 0;
   KahanF la;
-  for (int j0 = 0; j0 < len8; j0 += 8) {
-    int xr[8];
-    float dv[8];
-    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
-    float f = 0.0f;
-    int s8 = 0;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const float mu = M * dv[u];
-      s8 += xr[u];
-      f += (ph + (float)xr[u]) * log1p_near0(ca * fast_div(mu, ph + mu));
-    }
-    sx += s8;
-    la.add(f);
-  }
+  if (fabsf(ca) <= 0.5f) alpha_sums<true>(Xg, row_bytes, s_i, s_D, len8, M, ph, ca, sx, la);
+  else alpha_sums<false>(Xg, row_bytes, s_i, s_D, len8, M, ph, ca, sx, la);
   double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
   pr[0] = (double)sx;
   pr[Gp] = la.value();
 }
 
 // Chunk sums of k_beta_nu for one CTA-uniform case: HB = the chunk's type
-// has a beta (k > 0), HN = its batch has a nu (b > 0).
-template <bool HB, bool HN>
+// has a beta (k > 0), HN = its batch has a nu (b > 0).  FAST: both shifts'
+// |expm1(step)| <= 1/2, every term by log1p_shift.
+template <bool HB, bool HN, bool FAST>
 __device__ __forceinline__ void beta_nu_sums(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D,
                                              int len8, float M, float ph, float cb, float fb, float cn, int64_t& sx,
                                              KahanF& lb, KahanF& ln0, KahanF& ln1) {
+  const float cb2 = 2.0f + cb, cn2 = 2.0f + cn, ph2 = 2.0f * ph;
   for (int j0 = 0; j0 < len8; j0 += 8) {
     int xr[8];
     float dv[8];
@@ -538,14 +551,25 @@ __device__ __forceinline__ void beta_nu_sums(const char* Xg, uint32_t row_bytes,
       const int x = xr[u];
       const float mu = M * dv[u];
       const float w = ph + (float)x;
-      const float p = fast_div(mu, ph + mu);
       s8 += x;
-      if (HB) lbf += w * log1p_near0(cb * p);
-      if (HN) {
-        ln0f += w * log1p_near0(cn * p);
-        if (HB) {
-          const float mu1 = mu * fb;
-          ln1f += w * log1p_near0(cn * fast_div(mu1, ph + mu1));
+      if (FAST) {
+        if (HB) lbf = fmaf(w, log1p_shift(cb * mu, fmaf(cb2, mu, ph2)), lbf);
+        if (HN) {
+          ln0f = fmaf(w, log1p_shift(cn * mu, fmaf(cn2, mu, ph2)), ln0f);
+          if (HB) {
+            const float mu1 = mu * fb;
+            ln1f = fmaf(w, log1p_shift(cn * mu1, fmaf(cn2, mu1, ph2)), ln1f);
+          }
+        }
+      } else {
+        const float p = fast_div(mu, ph + mu);
+        if (HB) lbf += w * log1p_near0(cb * p);
+        if (HN) {
+          ln0f += w * log1p_near0(cn * p);
+          if (HB) {
+            const float mu1 = mu * fb;
+            ln1f += w * log1p_near0(cn * fast_div(mu1, ph + mu1));
+          }
         }
       }
     }
@@ -554,6 +578,18 @@ __device__ __forceinline__ void beta_nu_sums(const char* Xg, uint32_t row_bytes,
     if (HN) ln0.add(ln0f);
     if (HB && HN) ln1.add(ln1f);
   }
+}
+
+template <bool FAST>
+__device__ __forceinline__ void beta_nu_case(int b, int k, const char* Xg, uint32_t row_bytes, const int* s_i,
+                                             const float* s_D, int len8, float M, float ph, float cb, float fb,
+                                             float cn, int64_t& sx, KahanF& lb, KahanF& ln0, KahanF& ln1) {
+  if (k > 0 && b > 0)
+    beta_nu_sums<true, true, FAST>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  else if (k > 0)
+    beta_nu_sums<true, false, FAST>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  else
+    beta_nu_sums<false, true, FAST>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
 }
 
 __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
@@ -579,14 +615,45 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   const float cn = expm1f(en);
   int64_t sx = 0;
   KahanF lb, ln0, ln1;
-  if (k > 0 && b > 0) beta_nu_sums<true, true>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
-  else if (k > 0) beta_nu_sums<true, false>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
-  else beta_nu_sums<false, true>(Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  if (fabsf(cb) <= 0.5f && fabsf(cn) <= 0.5f)
+    beta_nu_case<true>(b, k, Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
+  else
+    beta_nu_case<false>(b, k, Xg, row_bytes, s_i, s_D, len8, M, ph, cb, fb, cn, sx, lb, ln0, ln1);
   double* pr = s.part + (int64_t)row * NSLOT * Gp + g;
   pr[0] = (double)sx;
   pr[Gp] = lb.value();
   pr[2 * Gp] = ln0.value();
   pr[3 * Gp] = ln1.value();
+}
+
+template <bool FAST>
+__device__ __forceinline__ void phi_sums(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D,
+                                         int len8, const uint32_t* ym, int64_t Gw, int bit,
+                                         const float (*tab)[GENE_TILE], int tid, float M, float ph, float pp,
+                                         float dl, float lgd0, float c1, float iph, KahanF& acc) {
+  const float sig = pp + ph;
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    uint32_t zw[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
+    float f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int x = xr[u];
+      const float mu = M * dv[u];
+      const float xf = (float)x;
+      const bool y0 = (zw[u] >> bit) & 1u;
+      float hx = y0 && (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : 0.0f;
+      // an imputed count past the table (rare): both arguments are past the shift range
+      if (y0 && x >= PHI_TAB) hx = lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
+      const float l1 = FAST ? two_atanh_small(fast_div(dl, fmaf(2.0f, mu, sig))) : log_ratio(pp + mu, ph + mu, dl);
+      f += hx - (pp + xf) * l1 + c1 - dl * log1p_fast(mu * iph);
+    }
+    acc.add(f);
+  }
 }
 
 __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
@@ -625,27 +692,12 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   const int64_t Gw = s.Gw;
   const int bit = (int)(g & 31);
   KahanF acc;
-  for (int j0 = 0; j0 < len8; j0 += 8) {
-    int xr[8];
-    float dv[8];
-    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
-    uint32_t zw[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
-    float f = 0.0f;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int x = xr[u];
-      const float mu = M * dv[u];
-      const float xf = (float)x;
-      const bool y0 = (zw[u] >> bit) & 1u;
-      float hx = y0 && (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : 0.0f;
-      // an imputed count past the table (rare): both arguments are past the shift range
-      if (y0 && x >= PHI_TAB) hx = lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
-      f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
-    }
-    acc.add(f);
-  }
+  // log((pp + mu) / (ph + mu)) = 2 atanh(dl / (pp + ph + 2 mu)); while
+  // |dl| <= (pp + ph) / 3 the argument stays within 1/3 for every mu and the
+  // short series applies (one reciprocal), else the general log_ratio
+  if (fabsf(dl) * 3.0f <= pp + ph) phi_sums<true>(Xg, row_bytes, s_i, s_D, len8, ym, Gw, bit, tab, tid, M, ph, pp, dl,
+                                                   lgd0, c1, iph, acc);
+  else phi_sums<false>(Xg, row_bytes, s_i, s_D, len8, ym, Gw, bit, tab, tid, M, ph, pp, dl, lgd0, c1, iph, acc);
   s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
 }
 

@@ -129,7 +129,22 @@ def compare(a: dict, b: dict, B: int, K: int, G: int, W_true=None) -> dict:
             z = np.where(se > 0, d / np.where(se > 0, se, 1.0), np.where(d == 0, 0.0, np.inf))
             stats[kind] = {"frac_abs_z_gt_3": float(np.mean(np.abs(z) > 3)), "median_abs_z": float(np.median(np.abs(z))),
                            "max_abs_z": float(np.max(np.abs(z)))}
-        sd = np.sqrt(0.5 * (sa["sd"] ** 2 + permute_block(name, sb["sd"], perm, B, K, G) ** 2))
+        # the same test where both chains' ESS (sd / MCSE)^2 reach a floor: the
+        # MCSE of a chain with only a few effective draws is itself unreliable
+        sb_se = permute_block(name, sb["se_ess"], perm, B, K, G)
+        sb_sd = permute_block(name, sb["sd"], perm, B, K, G)
+        ess_a = np.where(sa["se_ess"] > 0, (sa["sd"] / np.where(sa["se_ess"] > 0, sa["se_ess"], 1.0)) ** 2, 0.0)
+        ess_b = np.where(sb_se > 0, (sb_sd / np.where(sb_se > 0, sb_se, 1.0)) ** 2, 0.0)
+        se = np.sqrt(sa["se_ess"] ** 2 + sb_se ** 2)
+        z = np.where(se > 0, (sa["mean"] - mb) / np.where(se > 0, se, 1.0), 0.0)
+        stats["median_ess"] = [float(np.median(ess_a)), float(np.median(ess_b))]
+        for floor in (30, 100):
+            m = (ess_a >= floor) & (ess_b >= floor) & (se > 0)
+            stats["ess_ge_%d" % floor] = {"coords": int(m.sum()),
+                                          "frac_abs_z_gt_3": float(np.mean(np.abs(z[m]) > 3)) if m.any() else None,
+                                          "mean_z": float(np.mean(z[m])) if m.any() else None}
+        stats["mean_z"] = float(np.mean(z[se > 0])) if (se > 0).any() else 0.0
+        sd = np.sqrt(0.5 * (sa["sd"] ** 2 + sb_sd ** 2))
         dd = np.abs(sa["mean"] - mb)
         rel = dd[sd > 0] / sd[sd > 0]
         stats["coords"] = int(sa["mean"].size)

@@ -244,6 +244,11 @@ static inline double nb_shift_term(double xold, double xnew, double m, double ph
   return (xnew - xold) * X + (phi + X) * (log(phi + exp(m + xold)) - log(phi + exp(m + xnew)));
 }
 
+// The absolute sizes of nb_shift_term's two pieces.
+static inline double nb_shift_scale(double xold, double xnew, double m, double phi, int X) {
+  return fabs((xnew - xold) * X) + fabs((phi + X) * (log(phi + exp(m + xold)) - log(phi + exp(m + xnew))));
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -295,6 +300,20 @@ typedef struct orc_debug {
   double* mg_W;       // [N]
   double* mg_ptau;    // [2]
   double* mg_pi;      // [B*K]
+  // Size of the single-precision pieces behind each log ratio: the sum over
+  // its entries of the absolute values of the parts a float kernel evaluates
+  // term by term (for the eta shifts |(new - old) X| + |(phi + X) log ratio|;
+  // for gamma the softplus differences; for phi the lgamma difference, the two
+  // log ratios and pn log(pn / po)).  A float evaluation errs by a few units in
+  // the last place of each piece, so this bounds the error a correct kernel
+  // can make.
+  double* sc_gamma;   // [2B]
+  double* sc_alpha;   // [G]
+  double* sc_beta;    // [K*G]
+  double* sc_nu;      // [B*G]
+  double* sc_delta;   // [N]
+  double* sc_phi;     // [B*G]
+  double* sc_W;       // [N]
 } orc_debug;
 
 // Stages group the reference's sweep order (BUSseq_gpu.cu:1267-1398) the way
@@ -379,31 +398,36 @@ static void stage_gamma(orc_state* st, int iter, orc_debug* dbg) {
     const double g1n = -gamma_mt(sg, -10.0 * g1, nullptr) * 0.1;
     const int64_t lo = off[b] * G, hi = off[b + 1] * G;
     // gamma0: sum of (g0n - g0) Z - [sp(g0n + g1 X) - sp(g0 + g1 X)]
-    double lr0 = 0.0;
-#pragma omp parallel for reduction(+ : lr0)
+    double lr0 = 0.0, sc0 = 0.0;
+#pragma omp parallel for reduction(+ : lr0, sc0)
     for (int64_t pos = lo; pos < hi; ++pos) {
       const int X = st->X[pos], Z = st->Z[pos];
       double prop, prev, t;
       t = g0n + g1 * X;
       prop = g0n * Z - softplus(t);
+      const double spn = softplus(t);
       t = g0 + g1 * X;
       prev = g0 * Z - softplus(t);
       lr0 += prop - prev;
+      sc0 += fabs(spn - softplus(t));
     }
+    if (dbg && dbg->sc_gamma) dbg->sc_gamma[b] = sc0;
     const double prior0 = (g0 * g0 - g0n * g0n) / (2.0 * SIGMA2_GAMMA0);
     const double l0 = log(ua0);
     if (dbg && dbg->lr_gamma) dbg->lr_gamma[b] = lr0 + prior0;
     if (dbg && dbg->mg_gamma) dbg->mg_gamma[b] = fabs(l0 - (prior0 + lr0));
     if (l0 <= prior0 + lr0) { g0 = g0n; st->gamma[b] = g0n; }
     // gamma1 with the updated gamma0
-    double lr1 = 0.0;
-#pragma omp parallel for reduction(+ : lr1)
+    double lr1 = 0.0, sc1 = 0.0;
+#pragma omp parallel for reduction(+ : lr1, sc1)
     for (int64_t pos = lo; pos < hi; ++pos) {
       const int X = st->X[pos], Z = st->Z[pos];
       const double prop = g1n * X * Z - softplus(g0 + g1n * X);
       const double prev = g1 * X * Z - softplus(g0 + g1 * X);
       lr1 += prop - prev;
+      sc1 += fabs(softplus(g0 + g1n * X) - softplus(g0 + g1 * X));
     }
+    if (dbg && dbg->sc_gamma) dbg->sc_gamma[B + b] = sc1;
     const double pv = -g1, nv = -g1n;
     const double prior1 = (KAPPA_GAMMA1 - 1.0) * (log(nv) - log(pv)) + TAU_GAMMA1 * (pv - nv) -
                           lgamma(10.0 * nv) + (10.0 * nv - 1.0) * log(pv) + 10.0 * nv * (log(10.0) + 1.0) +
@@ -428,13 +452,15 @@ static void stage_alpha(orc_state* st, int iter, orc_debug* dbg) {
     const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
     const double ua = s.unif();
     const double a = st->alpha[g], an = a + 0.1 * z;
-    double lr = 0.0;
+    double lr = 0.0, sc = 0.0;
     for (int64_t i = 0; i < N; ++i) {
       const int b = bat[i];
       const double phi = st->phi[b * G + g];
       const double m = st->beta[(int64_t)st->W[i] * G + g] + st->nu[b * G + g] + st->delta[i];
       lr += nb_shift_term(a, an, m, phi, st->X[i * G + g]);
+      sc += nb_shift_scale(a, an, m, phi, st->X[i * G + g]);
     }
+    if (dbg && dbg->sc_alpha) dbg->sc_alpha[g] = sc;
     const double ma = st->mu_alpha[g];
     const double prior = ((a - ma) * (a - ma) - (an - ma) * (an - ma)) / (2.0 * SIGMA2_ALPHA);
     const double lu = log(ua);
@@ -503,13 +529,17 @@ static void stage_beta(orc_state* st, int iter, orc_debug* dbg) {
       ua[k] = s.unif();
       bn[k] = st->beta[k * G + g] + 0.1 * z;
     }
+    std::vector<double> sc(K, 0.0);
     for (int64_t i = 0; i < N; ++i) {
       const int k = st->W[i];
       if (k == 0) continue;
       const int b = bat[i];
       const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
       lr[k] += nb_shift_term(st->beta[k * G + g], bn[k], m, st->phi[b * G + g], st->X[i * G + g]);
+      sc[k] += nb_shift_scale(st->beta[k * G + g], bn[k], m, st->phi[b * G + g], st->X[i * G + g]);
     }
+    if (dbg && dbg->sc_beta)
+      for (int k = 1; k < K; ++k) dbg->sc_beta[k * G + g] = sc[k];
     for (int k = 1; k < K; ++k) {
       const int64_t pos = k * G + g;
       const double bo = st->beta[pos];
@@ -537,11 +567,13 @@ static void stage_nu(orc_state* st, int iter, orc_debug* dbg) {
       const double z = sqrt(-2.0 * log(u0)) * cos(6.283185307179586476925 * u1);
       const double ua = s.unif();
       const double vo = st->nu[pos], vn = vo + 0.1 * z;
-      double lr = 0.0;
+      double lr = 0.0, sc = 0.0;
       for (int64_t i = off[b]; i < off[b + 1]; ++i) {
         const double m = st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->delta[i];
         lr += nb_shift_term(vo, vn, m, st->phi[pos], st->X[i * G + g]);
+        sc += nb_shift_scale(vo, vn, m, st->phi[pos], st->X[i * G + g]);
       }
+      if (dbg && dbg->sc_nu) dbg->sc_nu[pos] = sc;
       const double mn = st->mu_nu[b];
       const double prior = ((vo - mn) * (vo - mn) - (vn - mn) * (vn - mn)) / (2.0 * SIGMA2_NU);
       const double lu = log(ua);
@@ -566,11 +598,13 @@ static void stage_delta(orc_state* st, int iter, orc_debug* dbg) {
     const double ua = s.unif();
     const double dn = st->delta[i] + 0.1 * z, d = st->delta[i];
     const int k = st->W[i];
-    double lr = 0.0;
+    double lr = 0.0, sc = 0.0;
     for (int64_t g = 0; g < G; ++g) {
       const double m = st->alpha[g] + st->beta[(int64_t)k * G + g] + st->nu[b * G + g];
       lr += nb_shift_term(d, dn, m, st->phi[b * G + g], st->X[i * G + g]);
+      sc += nb_shift_scale(d, dn, m, st->phi[b * G + g], st->X[i * G + g]);
     }
+    if (dbg && dbg->sc_delta) dbg->sc_delta[i] = sc;
     const double md = st->mu_delta[i];
     const double prior = ((d - md) * (d - md) - (dn - md) * (dn - md)) / (2.0 * SIGMA2_DELTA);
     const double lu = log(ua);
@@ -594,13 +628,18 @@ static void stage_phi(orc_state* st, int iter, orc_debug* dbg) {
       const double pn = gamma_mt(sp, po, nullptr);
       Stream sa(st->seed, SID_PHI_ACC, (uint64_t)pos, (uint32_t)iter);
       const double ua = sa.unif();
-      double lr = 0.0;
+      double lr = 0.0, sc = 0.0;
+      const double dl = pn - po, c1 = pn * log(pn / po);
       for (int64_t i = off[b]; i < off[b + 1]; ++i) {
         const int X = st->X[i * G + g];
         const double eta = exp(st->alpha[g] + st->beta[(int64_t)st->W[i] * G + g] + st->nu[pos] + st->delta[i]);
         lr += lgamma(pn + X) + pn * log(pn) - lgamma(pn) - (pn + X) * log(pn + eta) + lgamma(po) +
               (po + X) * log(po + eta) - lgamma(po + X) - po * log(po);
+        // the same term as a float kernel forms it: h - (pn + X) l1 + c1 - dl l2
+        const double h = (lgamma(pn + X) - lgamma(pn)) - (lgamma(po + X) - lgamma(po));
+        sc += fabs(h) + fabs((pn + X) * log((pn + eta) / (po + eta))) + fabs(c1) + fabs(dl * log1p(eta / po));
       }
+      if (dbg && dbg->sc_phi) dbg->sc_phi[pos] = sc;
       const double prior = (KAPPA_PHI - po) * log(pn) - (KAPPA_PHI - pn) * log(po) + (1.0 - TAU_PHI) * (pn - po) +
                            lgamma(po) - lgamma(pn);
       const double lu = log(ua);
@@ -625,12 +664,15 @@ static void stage_W(orc_state* st, int iter, int w_update, orc_debug* dbg) {
       const uint32_t r0 = s.u32();
       const int kn = (int)(((uint64_t)r0 * (uint64_t)K) >> 32);
       const double ua = s.unif();
-      double lr = 0.0;
+      double lr = 0.0, sc = 0.0;
       for (int64_t g = 0; g < G; ++g) {
         const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
         lr += nb_shift_term(st->beta[(int64_t)k * G + g], st->beta[(int64_t)kn * G + g], m, st->phi[b * G + g],
                             st->X[i * G + g]);
+        sc += nb_shift_scale(st->beta[(int64_t)k * G + g], st->beta[(int64_t)kn * G + g], m, st->phi[b * G + g],
+                             st->X[i * G + g]);
       }
+      if (dbg && dbg->sc_W) dbg->sc_W[i] = sc;
       const double rhs = log(st->pi[b * K + kn] / st->pi[b * K + k]) + lr;
       const double lu = log(ua);
       if (dbg && dbg->lr_W) dbg->lr_W[i] = rhs;
@@ -667,6 +709,15 @@ static void stage_W(orc_state* st, int iter, int w_update, orc_debug* dbg) {
       }
       if (dbg && dbg->mg_W) dbg->mg_W[i] = mg;
       if (dbg && dbg->lr_W) dbg->lr_W[i] = lp[pick] - lp[k];  // log weight of the draw relative to the current type
+      if (dbg && dbg->sc_W) {  // size of that log weight's float pieces
+        double sc = 0.0;
+        for (int64_t g = 0; g < G && pick != k; ++g) {
+          const double m = st->alpha[g] + st->nu[b * G + g] + st->delta[i];
+          sc += nb_shift_scale(st->beta[(int64_t)k * G + g], st->beta[(int64_t)pick * G + g], m, st->phi[b * G + g],
+                               st->X[i * G + g]);
+        }
+        dbg->sc_W[i] = sc;
+      }
       st->W[i] = pick;
     }
   }

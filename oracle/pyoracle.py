@@ -38,7 +38,8 @@ class OrcState(C.Structure):
 
 _DEBUG_FIELDS = ["lr_gamma", "lr_alpha", "lr_beta", "lr_nu", "lr_delta", "lr_phi", "lr_W",
                  "mg_zx", "mg_gamma", "mg_alpha", "mg_L", "mg_beta", "mg_nu", "mg_delta",
-                 "mg_phi", "mg_W", "mg_ptau", "mg_pi"]
+                 "mg_phi", "mg_W", "mg_ptau", "mg_pi",
+                 "sc_gamma", "sc_alpha", "sc_beta", "sc_nu", "sc_delta", "sc_phi", "sc_W"]
 
 
 class OrcDebug(C.Structure):
@@ -217,9 +218,11 @@ class Debug:
             "lr_phi": (B, G), "lr_W": (N,), "mg_zx": (N, G), "mg_gamma": (2, B), "mg_alpha": (G,),
             "mg_L": (K, G), "mg_beta": (K, G), "mg_nu": (B, G), "mg_delta": (N,), "mg_phi": (B, G),
             "mg_W": (N,), "mg_ptau": (2,), "mg_pi": (B, K),
+            "sc_gamma": (2, B), "sc_alpha": (G,), "sc_beta": (K, G), "sc_nu": (B, G), "sc_delta": (N,),
+            "sc_phi": (B, G), "sc_W": (N,),
         }
         for k, shp in shapes.items():
-            setattr(self, k, np.full(shp, np.inf if k.startswith("mg") else np.nan))
+            setattr(self, k, np.full(shp, np.inf if k.startswith("mg") else 0.0 if k.startswith("sc") else np.nan))
 
     def c(self) -> OrcDebug:
         d = OrcDebug()

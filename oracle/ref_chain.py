@@ -40,6 +40,10 @@ ROOT = os.path.dirname(HERE)
 sys.path.insert(0, ROOT)
 
 CONFIG0 = dict(n_b=[300, 300, 200, 200], G=3000, K=5, seed=13579)
+# a small problem on which the reference's sweep takes ~0.1 s, so that long
+# chains give every block enough effective draws for a Monte Carlo error test
+SMALL = dict(n_b=[60, 50, 40, 50], G=300, K=4, seed=2468)
+CASES = {"config0": CONFIG0, "small": SMALL}
 
 
 def _ref_binary(Y, n_b, K, seed, n_iter, n_burnin, n_unchanged, workdir, timeout, env=None):
@@ -169,6 +173,8 @@ def main():
     ap.add_argument("--unchanged", type=int, default=300)
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     ap.add_argument("--name", default="config0")
+    ap.add_argument("--data", default="config0", choices=sorted(CASES),
+                    help="config0: 300/300/200/200 cells, G = 3000, K = 5; small: 60/50/40/50 cells, G = 300, K = 4")
     ap.add_argument("--timeout", type=int, default=3000, help="seconds allowed for the reference chain")
     ap.add_argument("--start-sweeps", type=int, default=0,
                     help="> 0: compare the stationary chains: this sampler first runs this many sweeps from the "
@@ -180,7 +186,7 @@ def main():
     from oracle import chain_compare as cc
     import busseq_gpu_gb300 as bq
 
-    cfg = CONFIG0
+    cfg = CASES[args.data]
     n_b, G, K, seed = cfg["n_b"], cfg["G"], cfg["K"], cfg["seed"]
     B = len(n_b)
     Y, W_true, _ = bq.simulate(n_b, G, K, seed)
@@ -207,7 +213,7 @@ def main():
                   "both chains from their own initialisation" if args.own_init else
                   "this sampler started from the reference chain's initial state (W, L, every parameter, X = Y, "
                   "Z = 0), so both chains have the same distribution at every sweep"),
-        "data": "BUSseq generative model, batches %s, G = %d, K = %d, seed %d" % (n_b, G, K, seed),
+        "data": "BUSseq generative model, batches %s, G = %d, K = %d, seed %d (%s)" % (n_b, G, K, seed, args.data),
         "n_iter": args.iters, "n_burnin": args.burnin,
         "n_unchanged": 0 if args.start_sweeps > 0 else args.unchanged,
         "reference": ref_info, "ours": ours_info,
@@ -222,9 +228,10 @@ def main():
         json.dump(rec, f, indent=1)
     print(json.dumps({k: rec[k] for k in ("ari_a", "ari_b", "ari_diff", "ari_a_vs_b", "baseline_type_matched")}))
     for name, st in rec["blocks"].items():
-        print("%-9s coords %6d  |z|>3 (batch means) %.4f  (ESS) %.4f  median |d|/sd %.3f"
-              % (name, st["coords"], st["se_bm"]["frac_abs_z_gt_3"], st["se_ess"]["frac_abs_z_gt_3"],
-                 st["median_abs_diff_over_sd"]))
+        e30 = st["ess_ge_30"]
+        print("%-9s coords %6d  |z|>3 (batch means) %.4f  (ESS) %.4f  ESS>=30: %d coords %s  median ESS %.0f/%.0f"
+              % (name, st["coords"], st["se_bm"]["frac_abs_z_gt_3"], st["se_ess"]["frac_abs_z_gt_3"], e30["coords"],
+                 "%.4f" % e30["frac_abs_z_gt_3"] if e30["frac_abs_z_gt_3"] is not None else "-", *st["median_ess"]))
     print("reference %.3f s/sweep (%s), ours %.1f sweeps/s" % (ref_info["seconds_per_sweep"],
                                                               "graphs" if ref_info["graphs"] else "launches",
                                                               ours_info["sweeps_per_s"]))
