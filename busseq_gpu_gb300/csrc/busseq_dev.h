@@ -62,7 +62,9 @@ constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
 constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
-constexpr int ZX_PER_CTA = 1024;   // zero entries per Z/X CTA
+constexpr int ZX_UNIT = 256;       // zero entries per Z/X work unit (one warp, one partial)
+constexpr int ZX_HIST = 128;       // counts below this read the gamma terms from a per-batch table
+constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's launch bound)
 
 // ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
 enum Stage : int {
@@ -209,7 +211,7 @@ struct DevState {
   const int2* zij;          // [nz0] {cell, gene}
   uint8_t* zval;            // [nz0] Z
   int64_t nz0;
-  const int2* zcta;         // [n_zcta] {first entry, count}, each run inside one batch
+  const int2* zcta;         // [n_zcta] Z/X work units {first entry, count}, each inside one batch
   const int32_t* zcta_batch;
   const int32_t* zfirst;    // [B+1] first run of each batch
   int n_zcta;
@@ -219,6 +221,10 @@ struct DevState {
   double* part;    // [cap_g][NSLOT][Gp]
   double* gpart;   // [n_zcta][GSLOT]
   double* gstat;   // [n_static][4]
+  float4* zx_gtab;    // [B][ZX_HIST] per count x < ZX_HIST: softplus(-g0 - g1 x) and the three gamma
+                      // terms of the sweep's proposals (built by k_propose)
+  unsigned* zx_ctr;   // [2] Z/X work-unit counter and finished-warp counter (zero between launches)
+  int zx_ctas;        // Z/X CTAs per launch (resident on every SM)
   double* tpart;   // [n_tiles][2]
   unsigned* cnt_tile;  // [n_tiles]
   unsigned* cnt_glob;  // [4]

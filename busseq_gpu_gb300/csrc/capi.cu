@@ -91,8 +91,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_propose");
       break;
     case 1:
-      k_zx<<<(unsigned)(s.n_zcta + s.n_static) > 0 ? (unsigned)(s.n_zcta + s.n_static) : 1u, ZX_THREADS, 0, st>>>(
-          s, kept);
+      k_zx<<<(unsigned)s.zx_ctas, ZX_THREADS, 0, st>>>(s, kept);
       LAUNCH_CHECK("k_zx");
       break;
     case 2:
@@ -725,9 +724,9 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     for (int b = 0; b < B; ++b) {
       zfirst_h[b] = (int32_t)zcta_h.size();
       const int64_t lo = rowoff_h[h->off[b]], hi = rowoff_h[h->off[b + 1]];
-      for (int64_t e = lo; e < hi; e += bq::ZX_PER_CTA) {
+      for (int64_t e = lo; e < hi; e += bq::ZX_UNIT) {
         if (e > INT_MAX) return fail(BUSSEQ_ERR_ARG, "too many zero counts (more than 2^31)");
-        zcta_h.push_back(make_int2((int)e, (int)std::min<int64_t>(bq::ZX_PER_CTA, hi - e)));
+        zcta_h.push_back(make_int2((int)e, (int)std::min<int64_t>(bq::ZX_UNIT, hi - e)));
         zbatch_h.push_back(b);
       }
     }
@@ -743,6 +742,15 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&zbatch, std::max(1, s.n_zcta)));
     TRY(h->alloc(&zfirst, B + 1));
     TRY(h->alloc(&s.gpart, (int64_t)std::max(1, s.n_zcta) * bq::GSLOT));
+    TRY(h->alloc(&s.zx_gtab, (int64_t)B * bq::ZX_HIST));
+    TRY(h->alloc(&s.zx_ctr, 2));
+    {  // the Z/X launch: ZX_CTAS_PER_SM CTAs on every SM (and at least one per static-term slice)
+      int nsm = 0;
+      CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, opt.device));
+      const int64_t want = (s.n_zcta + bq::ZX_THREADS / 32 - 1) / (bq::ZX_THREADS / 32);
+      s.zx_ctas = (int)std::max<int64_t>({(int64_t)s.n_static, std::min<int64_t>(want, (int64_t)nsm * bq::ZX_CTAS_PER_SM),
+                                          (int64_t)1});
+    }
     CUDA_TRY(cudaMemcpyAsync(rowoff, rowoff_h.data(), (N + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
     if (s.n_zcta) {
       CUDA_TRY(cudaMemcpyAsync(zcta, zcta_h.data(), zcta_h.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));

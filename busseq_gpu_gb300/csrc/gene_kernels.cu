@@ -2,11 +2,11 @@
 // per-gene Metropolis updates alpha, beta, nu, phi with their decisions.
 //
 //   k_propose       every random-walk / Gamma proposal of the sweep
-//   k_zx            Z/X update (BUSseq_gpu.cu:484-512), one thread per entry of
-//                   the static list of Y == 0 entries, with the per-batch
-//                   sufficient statistics of the gamma updates (:514-600); extra
-//                   CTAs evaluate the gamma terms of the Y > 0 entries from the
-//                   histogram of Y
+//   k_zx            Z/X update (BUSseq_gpu.cu:484-512) over the static list of
+//                   Y == 0 entries, warps taking work units of 256 entries,
+//                   with the per-batch sufficient statistics of the gamma
+//                   updates (:514-600); its first CTAs also evaluate the gamma
+//                   terms of the Y > 0 entries from the histogram of Y
 //   k_alpha         alpha sums (:602-623)
 //   k_decide_alpha  alpha decisions, L redraw (:634-648), p and tau0 (:650-668)
 //                   in the last gene CTA, gamma0 / gamma1 decisions in one CTA per
@@ -136,11 +136,35 @@ __global__ void k_propose(DevState s, int mask) {
       if (cnt) s.phi_static[b * Gp + g] = stat.value();
       s.phi_lgd0[b * Gp + g] = lgamma_diff(ph, pn, dl);
     }
+    return;
+  }
+  t -= (int64_t)s.B * G;
+  if (t < (int64_t)s.B * ZX_HIST) {
+    // The Z/X update's table for count x of batch b: softplus(-g0 - g1 x) (its
+    // MH ratio) and the three gamma terms of the sweep's proposals
+    // (BUSseq_gpu.cu:524-576).  The proposals are drawn again from their own
+    // streams, exactly as the batch's thread above draws them.
+    if (mask & PROP_GAMMA) {
+      const int b = (int)(t / ZX_HIST), x = (int)(t % ZX_HIST);
+      Stream st(s.seed, SID_GAMMA, (uint64_t)b, iter);
+      const float g0 = s.gamma[b], g1 = s.gamma[s.B + b];
+      const float g0p = __fmaf_rn(RW_STEP, normal(st), g0);
+      Stream sg(s.seed, SID_GAMMA1_PROP, (uint64_t)b, iter);
+      int err = 0;
+      float g1p = -(gamma_mt(sg, -10.0f * g1, &err) * 0.1f);
+      if (!(g1p < 0.0f)) g1p = -1.0e-30f;
+      const float xf = (float)x;
+      const float tt = fmaf(g1, xf, g0), d1 = (g1p - g1) * xf;
+      s.zx_gtab[(int64_t)b * ZX_HIST + x] =
+          make_float4(softplusf(-g0 - g1 * xf), softplus_diff(tt, g0p - g0), softplus_diff(tt, d1),
+                      softplus_diff(fmaf(g1, xf, g0p), d1));
+    }
   }
 }
 
 int64_t propose_count(const DevState& s) {
-  return (int64_t)s.B + s.G + (int64_t)(s.K - 1) * s.G + (int64_t)(s.B - 1) * s.G + s.N + (int64_t)s.B * s.G;
+  return (int64_t)s.B + s.G + (int64_t)(s.K - 1) * s.G + (int64_t)(s.B - 1) * s.G + s.N + (int64_t)s.B * s.G +
+         (int64_t)s.B * ZX_HIST;
 }
 
 // ---------------------------------------------------------------------------
@@ -194,271 +218,245 @@ struct GammaTerms {
   }
 };
 
-// Work unit: a run of <= ZX_PER_CTA list entries of one batch (built at
-// initialisation); CTAs past n_zcta evaluate the static gamma terms.
+// Work units: runs of <= ZX_UNIT list entries of one batch (built at
+// initialisation).  The launch holds ZX_CTAS_PER_SM CTAs on every SM; each
+// warp takes units from a counter until none are left, so no warp ever waits
+// for another (a unit rich in slow Gamma-Poisson draws only delays its own
+// warp, which then takes fewer units).  The first n_static CTAs first
+// evaluate the static gamma terms of the Y > 0 entries.  The counter resets
+// itself: the last warp to finish zeroes it for the next launch.
 //
-// Phase 1 (each warp, 128 entries, all lanes busy): the entry's loads, block 0
-// of its Philox stream (an entry with X = 0 reads its Z uniform there, and
-// every NB proposal starts there) and the Z draw.  Entries that need an NB
-// proposal are staged in shared memory with their block 0 and a cost class:
-// class 0 for Gamma-Poisson draws, classes 1..31 for CDF inversions ordered
-// by the expected length of the search, mu (-log(1 - u)) with u the uniform
-// the inversion will use, longest first.
-// Phase 2: a counting sort over (class, warp, rank) - all counts come from
-// ballots and match masks, so the order is deterministic - lays the staged
-// entries out as one CTA-wide queue.
-// Phase 3: warps claim 32 consecutive queue positions at a time from a shared
-// counter.  The rare, expensive Gamma-Poisson draws thus share a few warps
-// instead of idling most lanes of every warp, the warps that drew them take
-// fewer of the inversions, and lanes of one warp run inversion searches of
-// similar length.
-// Phase 4: the gamma statistics of the drawn values, in a fixed order.
-//
-// The gamma terms depend on the entry only through x, so values below ZX_HIST
-// are counted in a shared histogram and each bin's terms are evaluated once;
-// the MH ratio reads softplus(-g0 - g1 x) from a table for the same range.
+// A unit is done in two halves of 128 entries (4 per lane):
+// Phase 1 (all lanes busy): the entry's loads, block 0 of its Philox stream
+// (an entry with X = 0 reads its Z uniform there, and every NB proposal starts
+// there) and the Z draw.  Entries that need an NB proposal are staged in the
+// warp's shared queue with their block 0 and a cost class: class 0 for
+// Gamma-Poisson draws, classes 1..31 for CDF inversions ordered by the
+// expected length of the search, mu (-log(1 - u)) with u the uniform the
+// inversion will use, longest first.
+// Phase 2: a counting sort over (class, rank) - counts from ballots and match
+// masks, so the order is deterministic - lays the queue out in class order.
+// Phase 3: the lanes take the sorted queue 32 entries at a time, so lanes of
+// one warp run searches of similar length; each entry's draws come from its
+// own stream.  The gamma statistics of the drawn values are summed per lane
+// (counts below ZX_HIST read their terms from the per-batch table that
+// k_propose built; the MH ratio reads softplus(-g0 - g1 x) there too) and
+// reduced over the warp into the unit's partial, in a fixed order.
 constexpr int ZX_WARPS = ZX_THREADS / 32;
-constexpr int ZX_PER_WARP = ZX_PER_CTA / ZX_WARPS;
-constexpr int ZX_PER_LANE = ZX_PER_WARP / 32;
-constexpr int ZX_HIST = 128;
+constexpr int ZX_HALF = 128;
+constexpr int ZX_PER_LANE = ZX_HALF / 32;
 constexpr int ZX_NCLS = 32;
-static_assert(ZX_HIST <= ZX_THREADS, "one thread per histogram bin");
-static_assert(ZX_NCLS <= 32 && ZX_PER_WARP <= 128 && ZX_WARPS <= 8, "queue index packing");
+static_assert(ZX_UNIT == 2 * ZX_HALF && ZX_NCLS == 32, "unit and queue layout");
 
 __device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
   if (!inv) return 0;
-  const float key = mu * -log_fast(1.0f - u_nb);  // 1 - u is exact for u = (2m+1) 2^-24
+  // a sort key only (the draws do not depend on it): the hardware logarithm
+  const float key = mu * -__log2f(1.0f - u_nb) * 0.6931471805599453f;  // 1 - u is exact for u = (2m+1) 2^-24
   const int bin = key < 60.0f ? (int)(key * 0.5f) : 30;
   return 31 - bin;
 }
 
-__global__ void __launch_bounds__(ZX_THREADS, 4) k_zx(DevState s, int kept) {
-  __shared__ double sh[(ZX_THREADS / 32) * 6];
-  __shared__ FF shf[ZX_WARPS * 3];
-  __shared__ long long shn[ZX_WARPS * 3];
-  __shared__ float q_mu[ZX_WARPS][ZX_PER_WARP], q_ph[ZX_WARPS][ZX_PER_WARP];
-  __shared__ int q_xo[ZX_WARPS][ZX_PER_WARP], q_kr[ZX_WARPS][ZX_PER_WARP];
-  __shared__ uint16_t q_e[ZX_WARPS][ZX_PER_WARP];
-  __shared__ int q_i[ZX_WARPS][ZX_PER_WARP], q_g[ZX_WARPS][ZX_PER_WARP];
-  __shared__ uint32_t q_w[4][ZX_WARPS][ZX_PER_WARP];
-  __shared__ uint16_t perm[ZX_PER_CTA];
-  __shared__ int cnt_w[ZX_WARPS][ZX_NCLS], off[ZX_NCLS][ZX_WARPS], n_need_w[ZX_WARPS];
-  __shared__ int n_queue, q_next;
-  __shared__ float sp_tab[ZX_HIST];
-  __shared__ int xhist[ZX_HIST];
-  const int c = blockIdx.x;
-  if (c >= s.n_zcta) {
-    gamma_static_cta(s, c - s.n_zcta, sh);
-    return;
-  }
+// One warp's staging area for half a unit.
+struct ZxQueue {
+  float mu[ZX_HALF], ph[ZX_HALF];
+  int xo[ZX_HALF], kr[ZX_HALF], i[ZX_HALF], g[ZX_HALF];
+  uint32_t w[4][ZX_HALF];
+  uint16_t e[ZX_HALF];
+  uint8_t perm[ZX_HALF];
+  int cnt[ZX_NCLS];
+};
+
+__global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, int kept) {
+  __shared__ double sh[ZX_WARPS * 3];
+  __shared__ ZxQueue qs[ZX_WARPS];
+  if ((int)blockIdx.x < s.n_static) gamma_static_cta(s, blockIdx.x, sh);  // the whole CTA, before any unit
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ZxQueue& q = qs[warp];
   const uint32_t iter = (uint32_t)*s.iter;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int2 run = s.zcta[c];
-  const int b = s.zcta_batch[c];
   const int64_t Gp = s.Gp;
   const uint64_t G64 = (uint64_t)s.G;
-  GammaTerms gt;
-  gt.g0 = s.gamma[b];
-  gt.g1 = s.gamma[s.B + b];
-  gt.g0p = s.gamma_p[b];
-  gt.dg0 = gt.g0p - gt.g0;
-  gt.dg1 = s.gamma_p[s.B + b] - gt.g1;
-  const float g0 = gt.g0, g1 = gt.g1;
-  const float zthr = 1.0f / (1.0f + expf(g0));
   const uint32_t k0 = (uint32_t)s.seed, k1 = (uint32_t)(s.seed >> 32);
-  if (tid < ZX_HIST) {
-    sp_tab[tid] = softplusf(-g0 - g1 * (float)tid);
-    xhist[tid] = 0;
-  }
-  if (lane < ZX_NCLS) cnt_w[warp][lane] = 0;
-  __syncthreads();
-
-  // ---- phase 1: Z for the warp's entries; stage the ones that need NB -------
-  // All loads of the warp's four rounds are issued before any of the
-  // ballot / match bookkeeping, so their latencies overlap.
-  int ei[ZX_PER_LANE], eg[ZX_PER_LANE], exo[ZX_PER_LANE];
-  float emu[ZX_PER_LANE], eph[ZX_PER_LANE];
-#pragma unroll
-  for (int u = 0; u < ZX_PER_LANE; ++u) {
-    const int e = warp * ZX_PER_WARP + u * 32 + lane;
-    const int2 ig = e < run.y ? s.zij[(int64_t)run.x + e] : make_int2(-1, 0);
-    ei[u] = ig.x;
-    eg[u] = ig.y;
-  }
-  int ew[ZX_PER_LANE];
-  float eD[ZX_PER_LANE];
-#pragma unroll
-  for (int u = 0; u < ZX_PER_LANE; ++u) {
-    if (ei[u] >= 0) {
-      const int64_t i = ei[u], g = eg[u];
-      ew[u] = s.W[i];
-      eD[u] = s.Dexp[i];
-      eph[u] = s.phi[(int64_t)b * Gp + g];
-      exo[u] = s.X[i * Gp + g];
-    } else {
-      ew[u] = 0;
-      eD[u] = 0.0f;
-      eph[u] = 1.0f;
-      exo[u] = 0;
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < ZX_PER_LANE; ++u)
-    emu[u] = ei[u] >= 0 ? s.E[((int64_t)b * s.K + ew[u]) * Gp + eg[u]] * eD[u] : 0.0f;
-
-  int n_need = 0;
-  long long n0 = 0;
   const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int u = 0; u < ZX_PER_LANE; ++u) {
-    const int e = warp * ZX_PER_WARP + u * 32 + lane;
-    bool need = false;
-    int cls = -1;
-    const float mu = emu[u], ph = eph[u];
-    const int xo = exo[u];
-    U32x4 r{0u, 0u, 0u, 0u};
-    if (ei[u] >= 0) {
-      const uint64_t ent = (uint64_t)ei[u] * G64 + (uint64_t)eg[u];
-      r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0, k1);
-      const bool z = xo != 0 || u32_to_unit(r.x) > zthr;
-      if (z) {
-        need = true;
-        cls = zx_class(negbin_use_inversion(mu, ph), mu, u32_to_unit(xo == 0 ? r.y : r.x));
-      } else {
-        s.zval[(int64_t)run.x + e] = 0;  // Z = 0 and X stays 0
-        ++n0;
-      }
-    }
-    const unsigned nm = __ballot_sync(0xffffffffu, need);
-    const unsigned grp = __match_any_sync(0xffffffffu, cls);
-    if (need) {
-      const int slot = n_need + __popc(nm & lt);
-      const int rank = cnt_w[warp][cls] + __popc(grp & lt);
-      q_mu[warp][slot] = mu;
-      q_ph[warp][slot] = ph;
-      q_xo[warp][slot] = xo;
-      q_e[warp][slot] = (uint16_t)e;
-      q_i[warp][slot] = ei[u];
-      q_g[warp][slot] = eg[u];
-      q_kr[warp][slot] = (cls << 16) | rank;
-      q_w[0][warp][slot] = r.x;
-      q_w[1][warp][slot] = r.y;
-      q_w[2][warp][slot] = r.z;
-      q_w[3][warp][slot] = r.w;
-    }
-    __syncwarp();
-    if (need && (grp & lt) == 0) cnt_w[warp][cls] += __popc(grp);  // the class group's first lane
-    __syncwarp();
-    n_need += __popc(nm);
-  }
-  if (lane == 0) n_need_w[warp] = n_need;
-  __syncthreads();
-
-  // ---- phase 2: queue offsets per (class, warp), then the CTA-wide order ---
-  if (warp == 0) {
-    int tot = 0;
-    if (lane < ZX_NCLS)
-      for (int w = 0; w < ZX_WARPS; ++w) tot += cnt_w[w][lane];
-    int incl = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    if (lane < ZX_NCLS) {
-      int base = incl - tot;
-      for (int w = 0; w < ZX_WARPS; ++w) {
-        off[lane][w] = base;
-        base += cnt_w[w][lane];
-      }
-    }
-    if (lane == ZX_NCLS - 1) n_queue = incl;
-    if (lane == 0) q_next = 0;
-  }
-  __syncthreads();
-  for (int q = lane; q < n_need_w[warp]; q += 32) {
-    const int kr = q_kr[warp][q];
-    perm[off[kr >> 16][warp] + (kr & 0xFFFF)] = (uint16_t)((warp << 7) | q);
-  }
-  __syncthreads();
-
-  // ---- phase 3: the queued imputations, X ~ NB independence MH
-  //      (BUSseq_gpu.cu:497-506).  Warps claim 32 consecutive queue positions
-  //      at a time, so the warp that drew the Gamma-Poisson entries at the head
-  //      of the queue takes fewer of the rest.  Each entry's draws come from
-  //      its own stream, so the result does not depend on which warp takes
-  //      it; the drawn x goes back into q_xo for phase 4.
-  const int nq = n_queue;
   for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&q_next, 32);
-    base = __shfl_sync(0xffffffffu, base, 0);  // warp-uniform: the whole warp leaves together
-    if (base >= nq) break;
-    const int q = base + lane;
-    if (q >= nq) continue;
-    const int ws = perm[q];
-    const int qw = ws >> 7, slot = ws & 127;
-    const bool is_inv = (q_kr[qw][slot] >> 16) != 0;
-    const int e = q_e[qw][slot];
-    const int xo = q_xo[qw][slot];
-    const int64_t j = (int64_t)run.x + e;
-    const int2 ig = make_int2(q_i[qw][slot], q_g[qw][slot]);
-    const uint64_t ent = (uint64_t)ig.x * G64 + (uint64_t)ig.y;
-    Stream st = Stream::resume(s.seed, SID_ZX, ent, iter, q_w[0][qw][slot], q_w[1][qw][slot], q_w[2][qw][slot],
-                               q_w[3][qw][slot], xo == 0);
-    int err = 0;
-    const float mu = q_mu[qw][slot], ph = q_ph[qw][slot];
-    const int xn = is_inv ? negbin_inversion(st, mu, ph, &err, s.nb_inv_cap) : negbin_gamma_poisson(st, mu, ph, &err);
-    const float ua = st.uniform();
-    // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
-    const float spo = (unsigned)xo < (unsigned)ZX_HIST ? sp_tab[xo] : softplusf(-g0 - g1 * (float)xo);
-    const float spn = (unsigned)xn < (unsigned)ZX_HIST ? sp_tab[xn] : softplusf(-g0 - g1 * (float)xn);
-    const int x = log_fast(ua) <= spo - spn ? xn : xo;
-    if (err) atomicOr(s.err, err);
-    if (x != xo) s.X[(int64_t)ig.x * Gp + ig.y] = x;
-    s.zval[j] = 1;
-    if (kept && s.acc_zn) {  // posterior summaries (entries with Z = 0 keep X = 0 and add nothing)
-      s.acc_zn[j] += 1;
-      s.acc_xs[j] += x;
+    int unit = 0;
+    if (lane == 0) unit = (int)atomicAdd(&s.zx_ctr[0], 1u);
+    unit = __shfl_sync(0xffffffffu, unit, 0);  // warp-uniform: the whole warp leaves together
+    if (unit >= s.n_zcta) break;
+    const int2 run = s.zcta[unit];
+    const int b = s.zcta_batch[unit];
+    const float4* gtab = s.zx_gtab + (int64_t)b * ZX_HIST;
+    GammaTerms gt;
+    gt.g0 = s.gamma[b];
+    gt.g1 = s.gamma[s.B + b];
+    gt.g0p = s.gamma_p[b];
+    gt.dg0 = gt.g0p - gt.g0;
+    gt.dg1 = s.gamma_p[s.B + b] - gt.g1;
+    const float g0 = gt.g0, g1 = gt.g1;
+    const float zthr = 1.0f / (1.0f + expf(g0));
+    long long nz = 0, xz = 0, n0 = 0;
+    float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
+    for (int half = 0; half * ZX_HALF < run.y; ++half) {
+      const int hb = half * ZX_HALF;
+      q.cnt[lane] = 0;
+      __syncwarp();
+      // ---- phase 1: loads hoisted over the lane's four entries ------------
+      int ei[ZX_PER_LANE], eg[ZX_PER_LANE], exo[ZX_PER_LANE];
+      float emu[ZX_PER_LANE], eph[ZX_PER_LANE];
+#pragma unroll
+      for (int u = 0; u < ZX_PER_LANE; ++u) {
+        const int e = hb + u * 32 + lane;
+        const int2 ig = e < run.y ? s.zij[(int64_t)run.x + e] : make_int2(-1, 0);
+        ei[u] = ig.x;
+        eg[u] = ig.y;
+      }
+      int ew[ZX_PER_LANE];
+      float eD[ZX_PER_LANE];
+#pragma unroll
+      for (int u = 0; u < ZX_PER_LANE; ++u) {
+        if (ei[u] >= 0) {
+          const int64_t i = ei[u], g = eg[u];
+          ew[u] = s.W[i];
+          eD[u] = s.Dexp[i];
+          eph[u] = s.phi[(int64_t)b * Gp + g];
+          exo[u] = s.X[i * Gp + g];
+        } else {
+          ew[u] = 0;
+          eD[u] = 0.0f;
+          eph[u] = 1.0f;
+          exo[u] = 0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < ZX_PER_LANE; ++u)
+        emu[u] = ei[u] >= 0 ? s.E[((int64_t)b * s.K + ew[u]) * Gp + eg[u]] * eD[u] : 0.0f;
+      int n_need = 0;
+#pragma unroll
+      for (int u = 0; u < ZX_PER_LANE; ++u) {
+        const int e = hb + u * 32 + lane;
+        bool need = false;
+        int cls = -1;
+        const float mu = emu[u], ph = eph[u];
+        const int xo = exo[u];
+        U32x4 r{0u, 0u, 0u, 0u};
+        if (ei[u] >= 0) {
+          const uint64_t ent = (uint64_t)ei[u] * G64 + (uint64_t)eg[u];
+          r = philox4x32_10(U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0,
+                            k1);
+          const bool z = xo != 0 || u32_to_unit(r.x) > zthr;
+          if (z) {
+            need = true;
+            cls = zx_class(negbin_use_inversion(mu, ph), mu, u32_to_unit(xo == 0 ? r.y : r.x));
+          } else {
+            s.zval[(int64_t)run.x + e] = 0;  // Z = 0 and X stays 0
+            ++n0;
+          }
+        }
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        const unsigned grp = __match_any_sync(0xffffffffu, cls);
+        if (need) {
+          const int slot = n_need + __popc(nm & lt);
+          q.mu[slot] = mu;
+          q.ph[slot] = ph;
+          q.xo[slot] = xo;
+          q.e[slot] = (uint16_t)e;
+          q.i[slot] = ei[u];
+          q.g[slot] = eg[u];
+          q.kr[slot] = (cls << 16) | (q.cnt[cls] + __popc(grp & lt));
+          q.w[0][slot] = r.x;
+          q.w[1][slot] = r.y;
+          q.w[2][slot] = r.z;
+          q.w[3][slot] = r.w;
+        }
+        __syncwarp();
+        if (need && (grp & lt) == 0) q.cnt[cls] += __popc(grp);  // the class group's first lane
+        __syncwarp();
+        n_need += __popc(nm);
+      }
+      // ---- phase 2: class offsets (lane = class), then the queue order ----
+      {
+        const int tot = q.cnt[lane];
+        int incl = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        __syncwarp();
+        q.cnt[lane] = incl - tot;
+        __syncwarp();
+        for (int j = lane; j < n_need; j += 32) {
+          const int kr = q.kr[j];
+          q.perm[q.cnt[kr >> 16] + (kr & 0xFFFF)] = (uint8_t)j;
+        }
+        __syncwarp();
+      }
+      // ---- phase 3: the queued imputations, X ~ NB independence MH
+      //      (BUSseq_gpu.cu:497-506), 32 queue positions at a time -----------
+      for (int p0 = 0; p0 < n_need; p0 += 32) {
+        const int p = p0 + lane;
+        if (p >= n_need) continue;
+        const int j = q.perm[p];
+        const bool is_inv = (q.kr[j] >> 16) != 0;
+        const int xo = q.xo[j];
+        const int64_t jj = (int64_t)run.x + q.e[j];
+        const int i = q.i[j], g = q.g[j];
+        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+        Stream st = Stream::resume(s.seed, SID_ZX, ent, iter, q.w[0][j], q.w[1][j], q.w[2][j], q.w[3][j], xo == 0);
+        int err = 0;
+        const float mu = q.mu[j], ph = q.ph[j];
+        const int xn = is_inv ? negbin_inversion(st, mu, ph, &err, s.nb_inv_cap) : negbin_gamma_poisson(st, mu, ph, &err);
+        const float ua = st.uniform();
+        // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
+        const float spo = (unsigned)xo < (unsigned)ZX_HIST ? __ldg(&gtab[xo].x) : softplusf(-g0 - g1 * (float)xo);
+        const float spn = (unsigned)xn < (unsigned)ZX_HIST ? __ldg(&gtab[xn].x) : softplusf(-g0 - g1 * (float)xn);
+        const int x = log_fast(ua) <= spo - spn ? xn : xo;
+        if (err) atomicOr(s.err, err);
+        if (x != xo) s.X[(int64_t)i * Gp + g] = x;
+        s.zval[jj] = 1;
+        if (kept && s.acc_zn) {  // posterior summaries (entries with Z = 0 keep X = 0 and add nothing)
+          s.acc_zn[jj] += 1;
+          s.acc_xs[jj] += x;
+        }
+        // gamma statistics of the drawn value
+        ++nz;
+        xz += x;
+        if (x == 0) {
+          ++n0;
+        } else if (x < ZX_HIST) {
+          const float4 t = __ldg(&gtab[x]);
+          d0 += t.y;
+          d1a += t.z;
+          d1b += t.w;
+        } else {
+          gt.add(x, 1.0f, d0, d1a, d1b);
+        }
+      }
+      __syncwarp();  // the queue is reused by the next half
     }
-    q_xo[qw][slot] = x;
-  }
-  __syncthreads();
-
-  // ---- phase 4: gamma statistics of the imputed entries, thread t taking
-  //      queue positions t, t + 256, ... (a fixed order: the float sums are
-  //      bit-reproducible)
-  long long nz = 0, xz = 0;
-  float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-  for (int q = tid; q < nq; q += ZX_THREADS) {
-    const int ws = perm[q];
-    const int x = q_xo[ws >> 7][ws & 127];
-    ++nz;
-    xz += x;
-    if (x == 0) {
-      ++n0;
-    } else if (x < ZX_HIST) {
-      atomicAdd(&xhist[x], 1);
-    } else {
-      gt.add(x, 1.0f, d0, d1a, d1b);
+    // ---- the unit's partial: a fixed-order warp reduction -----------------
+    const FF f0 = ff_warp_sum(FF{d0, 0.0f}), f1 = ff_warp_sum(FF{d1a, 0.0f}), f2 = ff_warp_sum(FF{d1b, 0.0f});
+    nz = i64_warp_sum(nz);
+    xz = i64_warp_sum(xz);
+    n0 = i64_warp_sum(n0);
+    if (lane == 0) {
+      double* gp = s.gpart + (int64_t)unit * GSLOT;
+      gp[0] = (double)nz;
+      gp[1] = (double)xz;
+      gp[2] = (double)n0;
+      gp[3] = ff_value(f0);
+      gp[4] = ff_value(f1);
+      gp[5] = ff_value(f2);
     }
   }
-  __syncthreads();  // histogram complete
-  if (tid > 0 && tid < ZX_HIST) {
-    const int cnt = xhist[tid];
-    if (cnt) gt.add(tid, (float)cnt, d0, d1a, d1b);
-  }
-  FF f[3] = {FF{d0, 0.0f}, FF{d1a, 0.0f}, FF{d1b, 0.0f}};
-  long long n[3] = {nz, xz, n0};
-  block_sum_ff<3, 3>(f, n, shf, shn);
-  if (tid == 0) {
-    double* gp = s.gpart + (int64_t)c * GSLOT;
-    gp[0] = (double)n[0];
-    gp[1] = (double)n[1];
-    gp[2] = (double)n[2];
-    gp[3] = ff_value(f[0]);
-    gp[4] = ff_value(f[1]);
-    gp[5] = ff_value(f[2]);
+  // the last warp to finish zeroes both counters for the next launch
+  if (lane == 0) {
+    __threadfence();
+    const unsigned total = gridDim.x * (unsigned)ZX_WARPS;
+    if (atomicAdd(&s.zx_ctr[1], 1u) == total - 1u) {
+      s.zx_ctr[0] = 0u;
+      s.zx_ctr[1] = 0u;
+      __threadfence();
+    }
   }
 }
 
