@@ -53,7 +53,7 @@ CFG4 = dict(n_b=[2000, 5000, 8000, 12000, 20000, 3000], G=20000, K=12, seed=1358
 CFG2 = dict(CFG1, hmc=10)
 CFG3 = dict(CFG1, ks=list(range(3, 11)))  # config-1 data fitted by 8 chains, K = 3 .. 10
 # the gradient-based sampler whose mixing the config-1 line reports beside the plain sampler's
-HMC_QUALITY = dict(hmc=10, gene=False, w_update="mh")
+HMC_QUALITY = dict(hmc=10, gene=True, w_update="mh")
 WORKLOADS = {"config1": CFG1, "config2": CFG2, "config3": CFG3, "config4": CFG4}
 METRIC = "gibbs_iters_per_s"
 UNIT = "sweeps/s"
@@ -464,6 +464,42 @@ def ess_run(Y, W_true, n_b, K, seed, n_iter=2000, n_burnin=1000, hmc=0, gene=Fal
     return out
 
 
+def hmc_vs_mh(Y, W_true, n_b, K, seed, mh_first, seed_offsets=(0, 1000, 2000)):
+    """The gradient-based sampler (HMC_QUALITY) against the plain sampler on the
+    same data, each run as a whole job of 2000 sweeps (1000 kept) from three
+    seeds.  The ARI of a single chain depends on which local mode of the cell
+    types the chain settles in (the plain sampler alone ranges 0.81-0.96 over
+    these seeds), so the ARIs are compared as means over the three chains of
+    each sampler; the ESS/s ratios are the medians of the three per-seed ratios
+    (per seed: median over the coordinates, whole-job wall time)."""
+    runs = []
+    for k, off in enumerate(seed_offsets):
+        mh = mh_first if k == 0 else ess_run(Y, W_true, n_b, K, seed + off, hmc=0)
+        hq = ess_run(Y, W_true, n_b, K, seed + off, hmc=HMC_QUALITY["hmc"], gene=HMC_QUALITY["gene"],
+                     w_update=HMC_QUALITY["w_update"])
+        r = {"seed_offset": off, "ari_W_mh": mh["ari_W"], "ari_W_hmc": hq["ari_W"],
+             "wall_s_mh": mh["wall_s"], "wall_s_hmc": hq["wall_s"]}
+        for name in ("beta", "nu"):
+            a, b = hq[name]["ess_per_s_median"], mh[name]["ess_per_s_median"]
+            r[name + "_ess_per_s_median_ratio"] = a / b if a and b else None
+            r[name + "_ess_median_hmc"] = hq[name]["ess_median"]
+            r[name + "_ess_median_mh"] = mh[name]["ess_median"]
+        if hq.get("hmc"):
+            r["hmc"] = hq["hmc"]
+        runs.append(r)
+    med = {name: float(np.median([r[name + "_ess_per_s_median_ratio"] or 0.0 for r in runs])) for name in ("beta", "nu")}
+    ari_mh = float(np.mean([r["ari_W_mh"] for r in runs]))
+    ari_hmc = float(np.mean([r["ari_W_hmc"] for r in runs]))
+    return {"sampler": "HMC, %d leapfrog steps%s, W by %s" % (HMC_QUALITY["hmc"],
+                                                            ", per-gene decisions" if HMC_QUALITY["gene"] else "",
+                                                            HMC_QUALITY["w_update"]),
+            "beta_ess_per_s_median_ratio": med["beta"], "nu_ess_per_s_median_ratio": med["nu"],
+            "ari_W_hmc_mean": ari_hmc, "ari_W_mh_mean": ari_mh, "ari_diff_mean": ari_hmc - ari_mh,
+            "target": "both ESS/s ratios >= 5 with the mean ARI within 0.01 of the plain sampler's or better",
+            "met": bool(med["beta"] >= 5 and med["nu"] >= 5 and ari_hmc >= ari_mh - 0.01),
+            "runs": runs}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -653,22 +689,7 @@ def main():
             quality["vs_mh"] = {"beta_ess_per_s_median_ratio": ratio("beta"),
                                 "nu_ess_per_s_median_ratio": ratio("nu"), "ari_W_mh": mh["ari_W"], "mh": mh}
         elif args.workload == "config1" and not args.no_hmc_quality:
-            # the gradient-based update on the same data and whole job (the config-2
-            # sampler): its ESS/s against this plain sampler's, at equal ARI
-            hq = ess_run(Y, W_true, n_b, K, seed, hmc=HMC_QUALITY["hmc"], gene=HMC_QUALITY["gene"],
-                         w_update=HMC_QUALITY["w_update"])
-
-            def ratio(name):
-                a, r = hq[name]["ess_per_s_median"], quality[name]["ess_per_s_median"]
-                return a / r if a and r else None
-
-            quality["hmc_vs_mh"] = {
-                "beta_ess_per_s_median_ratio": ratio("beta"), "nu_ess_per_s_median_ratio": ratio("nu"),
-                "ari_W_hmc": hq["ari_W"], "ari_W_mh": quality["ari_W"], "ari_diff": hq["ari_W"] - quality["ari_W"],
-                "target": "both ratios >= 5 with the ARI within 0.01 of the plain sampler's or better",
-                "met": bool((ratio("beta") or 0) >= 5 and (ratio("nu") or 0) >= 5 and
-                            hq["ari_W"] >= quality["ari_W"] - 0.01),
-                "hmc": hq}
+            quality["hmc_vs_mh"] = hmc_vs_mh(Y, W_true, n_b, K, seed, quality)
 
     # ---- CPU baseline (rank 0, N = 1 only): 20 full sweeps of the oracle ----
     cpu = None

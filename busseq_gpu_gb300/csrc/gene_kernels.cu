@@ -624,36 +624,6 @@ __global__ void __launch_bounds__(GENE_TILE) k_beta_nu(DevState s) {
   pr[3 * Gp] = ln1.value();
 }
 
-template <bool FAST>
-__device__ __forceinline__ void phi_sums(const char* Xg, uint32_t row_bytes, const int* s_i, const float* s_D,
-                                         int len8, const uint32_t* ym, int64_t Gw, int bit,
-                                         const float (*tab)[GENE_TILE], int tid, float M, float ph, float pp,
-                                         float dl, float lgd0, float c1, float iph, KahanF& acc) {
-  const float sig = pp + ph;
-  for (int j0 = 0; j0 < len8; j0 += 8) {
-    int xr[8];
-    float dv[8];
-    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
-    uint32_t zw[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
-    float f = 0.0f;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int x = xr[u];
-      const float mu = M * dv[u];
-      const float xf = (float)x;
-      const bool y0 = (zw[u] >> bit) & 1u;
-      float hx = y0 && (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : 0.0f;
-      // an imputed count past the table (rare): both arguments are past the shift range
-      if (y0 && x >= PHI_TAB) hx = lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
-      const float l1 = FAST ? two_atanh_small(fast_div(dl, fmaf(2.0f, mu, sig))) : log_ratio(pp + mu, ph + mu, dl);
-      f += hx - (pp + xf) * l1 + c1 - dl * log1p_fast(mu * iph);
-    }
-    acc.add(f);
-  }
-}
-
 __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   __shared__ float tab[PHI_TAB][GENE_TILE];
   __shared__ __align__(16) int s_i[MAX_CG];
@@ -690,12 +660,27 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi(DevState s) {
   const int64_t Gw = s.Gw;
   const int bit = (int)(g & 31);
   KahanF acc;
-  // log((pp + mu) / (ph + mu)) = 2 atanh(dl / (pp + ph + 2 mu)); while
-  // |dl| <= (pp + ph) / 3 the argument stays within 1/3 for every mu and the
-  // short series applies (one reciprocal), else the general log_ratio
-  if (fabsf(dl) * 3.0f <= pp + ph) phi_sums<true>(Xg, row_bytes, s_i, s_D, len8, ym, Gw, bit, tab, tid, M, ph, pp, dl,
-                                                   lgd0, c1, iph, acc);
-  else phi_sums<false>(Xg, row_bytes, s_i, s_D, len8, ym, Gw, bit, tab, tid, M, ph, pp, dl, lgd0, c1, iph, acc);
+  for (int j0 = 0; j0 < len8; j0 += 8) {
+    int xr[8];
+    float dv[8];
+    load8(Xg, row_bytes, s_i, s_D, j0, xr, dv);
+    uint32_t zw[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) zw[u] = ym[(int64_t)s_i[j0 + u] * Gw];
+    float f = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int x = xr[u];
+      const float mu = M * dv[u];
+      const float xf = (float)x;
+      const bool y0 = (zw[u] >> bit) & 1u;
+      float hx = y0 && (unsigned)x < (unsigned)PHI_TAB ? tab[x][tid] : 0.0f;
+      // an imputed count past the table (rare): both arguments are past the shift range
+      if (y0 && x >= PHI_TAB) hx = lgamma_diff_large(ph + xf, pp + xf, dl) - lgd0;
+      f += hx - (pp + xf) * log_ratio(pp + mu, ph + mu, dl) + c1 - dl * log1p_fast(mu * iph);
+    }
+    acc.add(f);
+  }
   s.part[(int64_t)row * NSLOT * Gp + g] = acc.value();
 }
 
@@ -741,7 +726,21 @@ __global__ void __launch_bounds__(256) k_phi_static(DevState s) {
 // gamma0 then gamma1 of batch b, one CTA (BUSseq_gpu.cu:514-600).
 __device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double* sh) {
   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int c = s.zfirst[b] + threadIdx.x; c < s.zfirst[b + 1]; c += blockDim.x) {
+  // the batch's Z/X work-unit partials, eight units' loads in flight per thread
+  const int c_end = s.zfirst[b + 1], stride = (int)blockDim.x;
+  int c = s.zfirst[b] + (int)threadIdx.x;
+  for (; c + 7 * stride < c_end; c += 8 * stride) {
+    double t[8][6];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) t[u][q] = __ldg(&s.gpart[(int64_t)(c + u * stride) * GSLOT + q]);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) v[q] += t[u][q];
+  }
+  for (; c < c_end; c += stride) {
 #pragma unroll
     for (int q = 0; q < 6; ++q) v[q] += s.gpart[(int64_t)c * GSLOT + q];
   }
