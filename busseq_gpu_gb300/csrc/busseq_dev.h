@@ -62,7 +62,7 @@ constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
 constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
-constexpr int ZX_UNIT = 256;       // zero entries per Z/X work unit (one warp, one partial)
+constexpr int ZX_UNIT = 512;       // zero entries per Z/X work unit (one warp, one partial)
 constexpr int ZX_HIST = 128;       // counts below this read the gamma terms from a per-batch table
 constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's launch bound)
 

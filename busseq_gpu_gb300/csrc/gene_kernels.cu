@@ -3,7 +3,7 @@
 //
 //   k_propose       every random-walk / Gamma proposal of the sweep
 //   k_zx            Z/X update (BUSseq_gpu.cu:484-512) over the static list of
-//                   Y == 0 entries, warps taking work units of 256 entries,
+//                   Y == 0 entries, warps taking work units of 512 entries,
 //                   with the per-batch sufficient statistics of the gamma
 //                   updates (:514-600); its first CTAs also evaluate the gamma
 //                   terms of the Y > 0 entries from the histogram of Y
@@ -226,7 +226,7 @@ struct GammaTerms {
 // evaluate the static gamma terms of the Y > 0 entries.  The counter resets
 // itself: the last warp to finish zeroes it for the next launch.
 //
-// A unit is done in two halves of 128 entries (4 per lane):
+// A unit is done in quarters of 128 entries (4 per lane):
 // Phase 1 (all lanes busy): the entry's loads, block 0 of its Philox stream
 // (an entry with X = 0 reads its Z uniform there, and every NB proposal starts
 // there) and the Z draw.  Entries that need an NB proposal are staged in the
@@ -246,7 +246,7 @@ constexpr int ZX_WARPS = ZX_THREADS / 32;
 constexpr int ZX_HALF = 128;
 constexpr int ZX_PER_LANE = ZX_HALF / 32;
 constexpr int ZX_NCLS = 32;
-static_assert(ZX_UNIT == 2 * ZX_HALF && ZX_NCLS == 32, "unit and queue layout");
+static_assert(ZX_UNIT % ZX_HALF == 0 && ZX_UNIT <= 65536 && ZX_NCLS == 32, "unit and queue layout");
 
 __device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
   if (!inv) return 0;
@@ -256,7 +256,7 @@ __device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
   return 31 - bin;
 }
 
-// One warp's staging area for half a unit.
+// One warp's staging area for a quarter of a unit (128 entries).
 struct ZxQueue {
   float mu[ZX_HALF], ph[ZX_HALF];
   int xo[ZX_HALF], kr[ZX_HALF], i[ZX_HALF], g[ZX_HALF];
@@ -295,8 +295,8 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
     const float zthr = 1.0f / (1.0f + expf(g0));
     long long nz = 0, xz = 0, n0 = 0;
     float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-    for (int half = 0; half * ZX_HALF < run.y; ++half) {
-      const int hb = half * ZX_HALF;
+    for (int part = 0; part * ZX_HALF < run.y; ++part) {
+      const int hb = part * ZX_HALF;
       q.cnt[lane] = 0;
       __syncwarp();
       // ---- phase 1: loads hoisted over the lane's four entries ------------
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
           gt.add(x, 1.0f, d0, d1a, d1b);
         }
       }
-      __syncwarp();  // the queue is reused by the next half
+      __syncwarp();  // the queue is reused by the next quarter
     }
     // ---- the unit's partial: a fixed-order warp reduction -----------------
     const FF f0 = ff_warp_sum(FF{d0, 0.0f}), f1 = ff_warp_sum(FF{d1a, 0.0f}), f2 = ff_warp_sum(FF{d1b, 0.0f});
