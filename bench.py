@@ -86,18 +86,20 @@ def sweep_roofline(N: int, G: int, hmc: int, sweeps_per_s: float, peak_gbs: floa
 
 def _traffic(kernel: str, workload: str = "config1"):
     """DRAM bytes per launch of `kernel` from the committed ncu summary of this
-    workload, or None."""
+    workload, or None.  For k_zx: k_zx and k_zx_gp together (the Z/X update)."""
     p = os.path.join(ROOT, "profiles", "dram_traffic_%s.txt" % workload)
     if not os.path.exists(p):
         return None
+    want = ("k_zx", "k_zx_gp") if kernel == "k_zx" else (kernel,)
+    got = {}
     for line in open(p):
         parts = line.split()
-        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+        if len(parts) >= 2 and parts[0] in want and not line.startswith("#"):
             try:
-                return float(parts[1])
+                got[parts[0]] = float(parts[1])
             except ValueError:
                 return None
-    return None
+    return sum(got.values()) if len(got) == len(want) else None
 
 
 class ClockSampler:
@@ -618,11 +620,13 @@ def main():
     prof = s.profile(20)
     big = {k: v for k, v in prof.items() if k in ("k_zx", "k_alpha", "k_beta_nu", "k_delta", "k_phi", "k_w",
                                                   "k_hmc_grad", "k_hmc_dll")}
+    # the Z/X update is two launches: k_zx and the Gamma-Poisson draws it leaves to k_zx_gp
+    big["k_zx"] = prof.get("k_zx", 0.0) + prof.get("k_zx_gp", 0.0)
     dom = max(big, key=big.get)
     kid = [bq.lib().busseq_kernel_name(i).decode() for i in range(64)].index(dom)
     alg_bytes = s.kernel_bytes(kid)
     n_launch = hmc if dom == "k_hmc_grad" else 1  # launches of the kernel per sweep (one per leapfrog step)
-    ms_launch = prof[dom] / n_launch
+    ms_launch = big[dom] / n_launch
     achieved = alg_bytes / (ms_launch / 1000.0) / 1e9
     peak, peak_kind = _peak_hbm()
     traffic = _traffic(dom, args.workload) if args.cells <= 0 else None
@@ -711,7 +715,7 @@ def main():
                     "note": "one job per run: pinned-host upload, init, %d sweeps, posterior, all estimates "
                             "(and the last sweep's X and Z) to pinned host buffers" % args.steps},
             "sweep_roofline": sweep_roofline(N, G, hmc, value / world, peak),  # per GPU: replicas
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": "k_zx + k_zx_gp" if dom == "k_zx" else dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "alg_bytes_per_launch": alg_bytes, "ms_per_launch": ms_launch,
                          "launches_per_sweep": n_launch},

@@ -65,6 +65,8 @@ constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
 constexpr int ZX_UNIT = 512;       // zero entries per Z/X work unit (one warp, one partial)
 constexpr int ZX_HIST = 128;       // counts below this read the gamma terms from a per-batch table
 constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's launch bound)
+constexpr int ZGP_UNITS = 4;       // Z/X work units per chunk of the Gamma-Poisson pass
+constexpr int ZGP_CTAS_PER_SM = 3;  // resident k_zx_gp CTAs per SM (its launch bound)
 
 // ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
 enum Stage : int {
@@ -223,8 +225,17 @@ struct DevState {
   double* gstat;   // [n_static][4]
   float4* zx_gtab;    // [B][ZX_HIST] per count x < ZX_HIST: softplus(-g0 - g1 x) and the three gamma
                       // terms of the sweep's proposals (built by k_propose)
-  unsigned* zx_ctr;   // [2] Z/X work-unit counter and finished-warp counter (zero between launches)
+  unsigned* zx_ctr;   // [4] work counter and finished-warp counter of k_zx, then of k_zx_gp
+                      // (zero between launches)
   int zx_ctas;        // Z/X CTAs per launch (resident on every SM)
+  // The NB proposals drawn as Gamma-Poisson mixtures, left by k_zx to k_zx_gp:
+  uint16_t* zgp;            // [n_zcta][ZX_UNIT] their positions in each unit, in unit order
+  int32_t* zgp_cnt;         // [n_zcta] how many each unit has
+  const int4* zgchunk;      // [n_gchunk] {first unit, units, batch, 0}: ZGP_UNITS units of one batch
+  const int32_t* gfirst;    // [B+1] first chunk of each batch
+  double* gpart_gp;         // [n_gchunk][GSLOT] gamma statistics of each chunk's draws
+  int n_gchunk;
+  int zgp_ctas;             // k_zx_gp CTAs per launch
   double* tpart;   // [n_tiles][2]
   unsigned* cnt_tile;  // [n_tiles]
   unsigned* cnt_glob;  // [4]

@@ -46,8 +46,8 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
                                     "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static",
-                                    "k_hmc_accept_genes"};
-constexpr int kNumKernels = 34;
+                                    "k_hmc_accept_genes", "k_zx_gp"};
+constexpr int kNumKernels = 35;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -55,7 +55,8 @@ enum : int {
   KID_HMC_LEAP = 17, KID_HMC_E = 18, KID_HMC_DLL = 19, KID_HMC_ENERGY = 20, KID_HMC_ACCEPT = 21,
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
-  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32, KID_HMC_ACCEPT_GENES = 33
+  KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32, KID_HMC_ACCEPT_GENES = 33,
+  KID_ZX_GP = 34
 };
 
 }  // namespace
@@ -93,6 +94,10 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
     case 1:
       k_zx<<<(unsigned)s.zx_ctas, ZX_THREADS, 0, st>>>(s, kept);
       LAUNCH_CHECK("k_zx");
+      break;
+    case KID_ZX_GP:
+      k_zx_gp<<<(unsigned)s.zgp_ctas, ZX_THREADS, 0, st>>>(s, kept);
+      LAUNCH_CHECK("k_zx_gp");
       break;
     case 2:
       k_alpha<<<gene_grid, GENE_TILE, 0, st>>>(s);
@@ -239,7 +244,8 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
     const bool blocks = h->s.hmc_nb > 0;
-    q = {KID_PROPOSE, KID_ZX, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START, KID_HMC_MASS};
+    q = {KID_PROPOSE, KID_ZX, KID_ZX_GP, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START,
+         KID_HMC_MASS};
     if (blocks) q.push_back(KID_HMC_METRIC_BLOCKS);
     q.push_back(KID_HMC_START);
     if (blocks) q.push_back(KID_HMC_START_BLOCKS);
@@ -264,6 +270,7 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
     for (int k = 0; k <= KID_SORT_PI; ++k) {
       if (k == KID_PHI) q.push_back(KID_PHI_STATIC);
       q.push_back(k);
+      if (k == KID_ZX) q.push_back(KID_ZX_GP);
     }
   }
   if (kept) q.push_back(KID_POSTERIOR);
@@ -743,14 +750,40 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     TRY(h->alloc(&zfirst, B + 1));
     TRY(h->alloc(&s.gpart, (int64_t)std::max(1, s.n_zcta) * bq::GSLOT));
     TRY(h->alloc(&s.zx_gtab, (int64_t)B * bq::ZX_HIST));
-    TRY(h->alloc(&s.zx_ctr, 2));
-    {  // the Z/X launch: ZX_CTAS_PER_SM CTAs on every SM (and at least one per static-term slice)
+    TRY(h->alloc(&s.zx_ctr, 4));
+    // the Gamma-Poisson lists of the units and the chunks of k_zx_gp (ZGP_UNITS units of one batch)
+    std::vector<int4> zgchunk_h;
+    std::vector<int32_t> gfirst_h(B + 1, 0);
+    for (int b = 0; b < B; ++b) {
+      gfirst_h[b] = (int32_t)zgchunk_h.size();
+      for (int u = zfirst_h[b]; u < zfirst_h[b + 1]; u += bq::ZGP_UNITS)
+        zgchunk_h.push_back(make_int4(u, std::min(bq::ZGP_UNITS, zfirst_h[b + 1] - u), b, 0));
+    }
+    gfirst_h[B] = (int32_t)zgchunk_h.size();
+    s.n_gchunk = (int)zgchunk_h.size();
+    int4* zgchunk;
+    int32_t* gfirst;
+    TRY(h->alloc(&s.zgp, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
+    TRY(h->alloc(&s.zgp_cnt, std::max(1, s.n_zcta)));
+    TRY(h->alloc(&zgchunk, std::max(1, s.n_gchunk)));
+    TRY(h->alloc(&gfirst, B + 1));
+    TRY(h->alloc(&s.gpart_gp, (int64_t)std::max(1, s.n_gchunk) * bq::GSLOT));
+    {  // the Z/X launches: ZX_CTAS_PER_SM CTAs on every SM (and at least one per static-term slice)
       int nsm = 0;
       CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, opt.device));
       const int64_t want = (s.n_zcta + bq::ZX_THREADS / 32 - 1) / (bq::ZX_THREADS / 32);
       s.zx_ctas = (int)std::max<int64_t>({(int64_t)s.n_static, std::min<int64_t>(want, (int64_t)nsm * bq::ZX_CTAS_PER_SM),
                                           (int64_t)1});
+      const int64_t want_gp = (s.n_gchunk + bq::ZX_THREADS / 32 - 1) / (bq::ZX_THREADS / 32);
+      s.zgp_ctas = (int)std::max<int64_t>(std::min<int64_t>(want_gp, (int64_t)nsm * bq::ZGP_CTAS_PER_SM), 1);
     }
+    if (s.n_gchunk) {
+      CUDA_TRY(cudaMemcpyAsync(zgchunk, zgchunk_h.data(), zgchunk_h.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                               h->stream));
+    }
+    CUDA_TRY(cudaMemcpyAsync(gfirst, gfirst_h.data(), (B + 1) * 4, cudaMemcpyHostToDevice, h->stream));
+    s.zgchunk = zgchunk;
+    s.gfirst = gfirst;
     CUDA_TRY(cudaMemcpyAsync(rowoff, rowoff_h.data(), (N + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
     if (s.n_zcta) {
       CUDA_TRY(cudaMemcpyAsync(zcta, zcta_h.data(), zcta_h.size() * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
@@ -1173,7 +1206,7 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
     case BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA);
       LAUNCH_CHECK("k_propose");
-      TRY(run({1, 2, 3}));
+      TRY(run({KID_ZX, KID_ZX_GP, 2, 3}));
       break;
     case BUSSEQ_STAGE_BETA_NU:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU);

@@ -7,6 +7,7 @@
 //                   with the per-batch sufficient statistics of the gamma
 //                   updates (:514-600); its first CTAs also evaluate the gamma
 //                   terms of the Y > 0 entries from the histogram of Y
+//   k_zx_gp         the NB proposals of k_zx drawn as Gamma-Poisson mixtures
 //   k_alpha         alpha sums (:602-623)
 //   k_decide_alpha  alpha decisions, L redraw (:634-648), p and tau0 (:650-668)
 //                   in the last gene CTA, gamma0 / gamma1 decisions in one CTA per
@@ -221,50 +222,89 @@ struct GammaTerms {
 // Work units: runs of <= ZX_UNIT list entries of one batch (built at
 // initialisation).  The launch holds ZX_CTAS_PER_SM CTAs on every SM; each
 // warp takes units from a counter until none are left, so no warp ever waits
-// for another (a unit rich in slow Gamma-Poisson draws only delays its own
-// warp, which then takes fewer units).  The first n_static CTAs first
-// evaluate the static gamma terms of the Y > 0 entries.  The counter resets
-// itself: the last warp to finish zeroes it for the next launch.
+// for another (a unit rich in slow draws only delays its own warp, which then
+// takes fewer units).  The first n_static CTAs first evaluate the static gamma
+// terms of the Y > 0 entries.  The counter resets itself: the last warp to
+// finish zeroes it for the next launch.
 //
-// A unit is done in quarters of 128 entries (4 per lane):
+// A unit is read in parts of 128 entries (4 per lane):
 // Phase 1 (all lanes busy): the entry's loads, block 0 of its Philox stream
 // (an entry with X = 0 reads its Z uniform there, and every NB proposal starts
-// there) and the Z draw.  Entries that need an NB proposal are staged in the
-// warp's shared queue with their block 0 and a cost class: class 0 for
-// Gamma-Poisson draws, classes 1..31 for CDF inversions ordered by the
-// expected length of the search, mu (-log(1 - u)) with u the uniform the
-// inversion will use, longest first.
+// there) and the Z draw.  An entry that needs an NB proposal by inversion of
+// the distribution function is staged in the warp's queue with the two words
+// it will use and a cost class, 0..30 by the expected length of the search,
+// mu (-log(1 - u)) with u the inversion's uniform, longest first.  An entry
+// that needs a Gamma-Poisson draw is listed, by its position, for k_zx_gp.
 // Phase 2: a counting sort over (class, rank) - counts from ballots and match
 // masks, so the order is deterministic - lays the queue out in class order.
 // Phase 3: the lanes take the sorted queue 32 entries at a time, so lanes of
-// one warp run searches of similar length; each entry's draws come from its
-// own stream.  The gamma statistics of the drawn values are summed per lane
-// (counts below ZX_HIST read their terms from the per-batch table that
-// k_propose built; the MH ratio reads softplus(-g0 - g1 x) there too) and
-// reduced over the warp into the unit's partial, in a fixed order.
+// one warp run searches of similar length.  Only full rounds of 32 run before
+// the unit's last part: the shortest searches wait for the next part, so a
+// round leaves lanes idle only at the end of a unit.  Each entry's draws come
+// from its own stream, so neither the order nor the round changes them.  The
+// gamma statistics of the drawn values are summed per lane (counts below
+// ZX_HIST read their terms from the per-batch table that k_propose built; the
+// MH ratio reads softplus(-g0 - g1 x) there too) and reduced over the warp
+// into the unit's partial, in a fixed order.
 constexpr int ZX_WARPS = ZX_THREADS / 32;
-constexpr int ZX_HALF = 128;
-constexpr int ZX_PER_LANE = ZX_HALF / 32;
+constexpr int ZX_PART = 128;
+constexpr int ZX_PER_LANE = ZX_PART / 32;
 constexpr int ZX_NCLS = 32;
-static_assert(ZX_UNIT % ZX_HALF == 0 && ZX_UNIT <= 65536 && ZX_NCLS == 32, "unit and queue layout");
+constexpr int ZX_Q = ZX_PART + 32;  // fewer than 32 entries carried over plus one part
+static_assert(ZX_UNIT % ZX_PART == 0 && ZX_UNIT <= 65536 && ZX_NCLS == 32 && ZX_Q <= 256,
+              "unit and queue layout");
 
-__device__ __forceinline__ int zx_class(bool inv, float mu, float u_nb) {
-  if (!inv) return 0;
+__device__ __forceinline__ int zx_class(float mu, float u_nb) {
   // a sort key only (the draws do not depend on it): the hardware logarithm
   const float key = mu * -__log2f(1.0f - u_nb) * 0.6931471805599453f;  // 1 - u is exact for u = (2m+1) 2^-24
   const int bin = key < 60.0f ? (int)(key * 0.5f) : 30;
-  return 31 - bin;
+  return 30 - bin;
 }
 
-// One warp's staging area for a quarter of a unit (128 entries).
+// One warp's staging area: the inversion queue.
 struct ZxQueue {
-  float mu[ZX_HALF], ph[ZX_HALF];
-  int xo[ZX_HALF], kr[ZX_HALF], i[ZX_HALF], g[ZX_HALF];
-  uint32_t w[4][ZX_HALF];
-  uint16_t e[ZX_HALF];
-  uint8_t perm[ZX_HALF];
+  float mu[ZX_Q], ph[ZX_Q];
+  int xo[ZX_Q], kr[ZX_Q];
+  uint32_t wu[ZX_Q], wa[ZX_Q];  // the inversion's uniform and the MH uniform
+  uint16_t e[ZX_Q];             // position in the unit
+  uint8_t perm[ZX_Q];
   int cnt[ZX_NCLS];
 };
+
+// Per-lane sums of one unit.
+struct ZxAcc {
+  long long nz = 0, xz = 0, n0 = 0;
+  float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
+};
+
+// The MH decision of an NB proposal (BUSseq_gpu.cu:497-506), the entry's
+// writes and its gamma statistics.
+__device__ __forceinline__ void zx_finish(const DevState& s, int kept, const float4* gtab, const GammaTerms& gt,
+                                          int64_t jj, int2 ig, int xo, int xn, float ua, int err, ZxAcc& a) {
+  // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
+  const float spo = (unsigned)xo < (unsigned)ZX_HIST ? __ldg(&gtab[xo].x) : softplusf(-gt.g0 - gt.g1 * (float)xo);
+  const float spn = (unsigned)xn < (unsigned)ZX_HIST ? __ldg(&gtab[xn].x) : softplusf(-gt.g0 - gt.g1 * (float)xn);
+  const int x = log_fast(ua) <= spo - spn ? xn : xo;
+  if (err) atomicOr(s.err, err);
+  if (x != xo) s.X[(int64_t)ig.x * s.Gp + ig.y] = x;
+  s.zval[jj] = 1;
+  if (kept && s.acc_zn) {  // posterior summaries (entries with Z = 0 keep X = 0 and add nothing)
+    s.acc_zn[jj] += 1;
+    s.acc_xs[jj] += x;
+  }
+  ++a.nz;
+  a.xz += x;
+  if (x == 0) {
+    ++a.n0;
+  } else if (x < ZX_HIST) {
+    const float4 t = __ldg(&gtab[x]);
+    a.d0 += t.y;
+    a.d1a += t.z;
+    a.d1b += t.w;
+  } else {
+    gt.add(x, 1.0f, a.d0, a.d1a, a.d1b);
+  }
+}
 
 __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, int kept) {
   __shared__ double sh[ZX_WARPS * 3];
@@ -285,20 +325,22 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
     const int2 run = s.zcta[unit];
     const int b = s.zcta_batch[unit];
     const float4* gtab = s.zx_gtab + (int64_t)b * ZX_HIST;
+    const int64_t eoff = (int64_t)b * s.K;
     GammaTerms gt;
     gt.g0 = s.gamma[b];
     gt.g1 = s.gamma[s.B + b];
     gt.g0p = s.gamma_p[b];
     gt.dg0 = gt.g0p - gt.g0;
     gt.dg1 = s.gamma_p[s.B + b] - gt.g1;
-    const float g0 = gt.g0, g1 = gt.g1;
-    const float zthr = 1.0f / (1.0f + expf(g0));
-    long long nz = 0, xz = 0, n0 = 0;
-    float d0 = 0.0f, d1a = 0.0f, d1b = 0.0f;
-    for (int part = 0; part * ZX_HALF < run.y; ++part) {
-      const int hb = part * ZX_HALF;
-      q.cnt[lane] = 0;
-      __syncwarp();
+    const float zthr = 1.0f / (1.0f + expf(gt.g0));
+    ZxAcc acc;
+    int n_iq = 0, n_gq = 0;  // warp-uniform: the queue's length, the Gamma-Poisson entries listed
+    uint16_t* gpl = s.zgp + (int64_t)unit * ZX_UNIT;
+    q.cnt[lane] = 0;
+    __syncwarp();
+    for (int part = 0; part * ZX_PART < run.y; ++part) {
+      const int hb = part * ZX_PART;
+      const bool last = hb + ZX_PART >= run.y;
       // ---- phase 1: loads hoisted over the lane's four entries ------------
       int ei[ZX_PER_LANE], eg[ZX_PER_LANE], exo[ZX_PER_LANE];
       float emu[ZX_PER_LANE], eph[ZX_PER_LANE];
@@ -328,12 +370,11 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
       }
 #pragma unroll
       for (int u = 0; u < ZX_PER_LANE; ++u)
-        emu[u] = ei[u] >= 0 ? s.E[((int64_t)b * s.K + ew[u]) * Gp + eg[u]] * eD[u] : 0.0f;
-      int n_need = 0;
+        emu[u] = ei[u] >= 0 ? s.E[(eoff + ew[u]) * Gp + eg[u]] * eD[u] : 0.0f;
 #pragma unroll
       for (int u = 0; u < ZX_PER_LANE; ++u) {
         const int e = hb + u * 32 + lane;
-        bool need = false;
+        bool inv = false, gpn = false;
         int cls = -1;
         const float mu = emu[u], ph = eph[u];
         const int xo = exo[u];
@@ -344,33 +385,36 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
                             k1);
           const bool z = xo != 0 || u32_to_unit(r.x) > zthr;
           if (z) {
-            need = true;
-            cls = zx_class(negbin_use_inversion(mu, ph), mu, u32_to_unit(xo == 0 ? r.y : r.x));
+            if (negbin_use_inversion(mu, ph)) {
+              inv = true;
+              cls = zx_class(mu, u32_to_unit(xo == 0 ? r.y : r.x));
+            } else {
+              gpn = true;
+            }
           } else {
             s.zval[(int64_t)run.x + e] = 0;  // Z = 0 and X stays 0
-            ++n0;
+            ++acc.n0;
           }
         }
-        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        const unsigned im = __ballot_sync(0xffffffffu, inv);
+        const unsigned gm = __ballot_sync(0xffffffffu, gpn);
         const unsigned grp = __match_any_sync(0xffffffffu, cls);
-        if (need) {
-          const int slot = n_need + __popc(nm & lt);
+        if (inv) {
+          const int slot = n_iq + __popc(im & lt);
           q.mu[slot] = mu;
           q.ph[slot] = ph;
           q.xo[slot] = xo;
           q.e[slot] = (uint16_t)e;
-          q.i[slot] = ei[u];
-          q.g[slot] = eg[u];
           q.kr[slot] = (cls << 16) | (q.cnt[cls] + __popc(grp & lt));
-          q.w[0][slot] = r.x;
-          q.w[1][slot] = r.y;
-          q.w[2][slot] = r.z;
-          q.w[3][slot] = r.w;
+          q.wu[slot] = xo == 0 ? r.y : r.x;
+          q.wa[slot] = xo == 0 ? r.z : r.y;
         }
+        if (gpn) gpl[n_gq + __popc(gm & lt)] = (uint16_t)e;
         __syncwarp();
-        if (need && (grp & lt) == 0) q.cnt[cls] += __popc(grp);  // the class group's first lane
+        if (inv && (grp & lt) == 0) q.cnt[cls] += __popc(grp);  // the class group's first lane
         __syncwarp();
-        n_need += __popc(nm);
+        n_iq += __popc(im);
+        n_gq += __popc(gm);
       }
       // ---- phase 2: class offsets (lane = class), then the queue order ----
       {
@@ -384,62 +428,163 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
         __syncwarp();
         q.cnt[lane] = incl - tot;
         __syncwarp();
-        for (int j = lane; j < n_need; j += 32) {
+        for (int j = lane; j < n_iq; j += 32) {
           const int kr = q.kr[j];
           q.perm[q.cnt[kr >> 16] + (kr & 0xFFFF)] = (uint8_t)j;
         }
         __syncwarp();
       }
-      // ---- phase 3: the queued imputations, X ~ NB independence MH
+      // ---- phase 3a: the inversions, X ~ NB independence MH
       //      (BUSseq_gpu.cu:497-506), 32 queue positions at a time -----------
-      for (int p0 = 0; p0 < n_need; p0 += 32) {
+      const int n_run = last ? n_iq : (n_iq & ~31);
+      for (int p0 = 0; p0 < n_run; p0 += 32) {
         const int p = p0 + lane;
-        if (p >= n_need) continue;
+        if (p >= n_run) continue;
         const int j = q.perm[p];
-        const bool is_inv = (q.kr[j] >> 16) != 0;
-        const int xo = q.xo[j];
         const int64_t jj = (int64_t)run.x + q.e[j];
-        const int i = q.i[j], g = q.g[j];
-        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
-        Stream st = Stream::resume(s.seed, SID_ZX, ent, iter, q.w[0][j], q.w[1][j], q.w[2][j], q.w[3][j], xo == 0);
+        const int2 ig = s.zij[jj];  // for the write of X, loaded ahead of the search
+        const int xo = q.xo[j];
         int err = 0;
-        const float mu = q.mu[j], ph = q.ph[j];
-        const int xn = is_inv ? negbin_inversion(st, mu, ph, &err, s.nb_inv_cap) : negbin_gamma_poisson(st, mu, ph, &err);
-        const float ua = st.uniform();
-        // log[(1 + e^{-g0 - g1 x_old}) / (1 + e^{-g0 - g1 x_new})]
-        const float spo = (unsigned)xo < (unsigned)ZX_HIST ? __ldg(&gtab[xo].x) : softplusf(-g0 - g1 * (float)xo);
-        const float spn = (unsigned)xn < (unsigned)ZX_HIST ? __ldg(&gtab[xn].x) : softplusf(-g0 - g1 * (float)xn);
-        const int x = log_fast(ua) <= spo - spn ? xn : xo;
-        if (err) atomicOr(s.err, err);
-        if (x != xo) s.X[(int64_t)i * Gp + g] = x;
-        s.zval[jj] = 1;
-        if (kept && s.acc_zn) {  // posterior summaries (entries with Z = 0 keep X = 0 and add nothing)
-          s.acc_zn[jj] += 1;
-          s.acc_xs[jj] += x;
-        }
-        // gamma statistics of the drawn value
-        ++nz;
-        xz += x;
-        if (x == 0) {
-          ++n0;
-        } else if (x < ZX_HIST) {
-          const float4 t = __ldg(&gtab[x]);
-          d0 += t.y;
-          d1a += t.z;
-          d1b += t.w;
-        } else {
-          gt.add(x, 1.0f, d0, d1a, d1b);
-        }
+        const int xn = negbin_invert_u(u32_to_unit(q.wu[j]), q.mu[j], q.ph[j], &err, s.nb_inv_cap);
+        zx_finish(s, kept, gtab, gt, jj, ig, xo, xn, u32_to_unit(q.wa[j]), err, acc);
       }
-      __syncwarp();  // the queue is reused by the next quarter
+      __syncwarp();
+      // ---- carry the shortest searches (fewer than 32) to the next part ----
+      if (!last) {
+        const int left = n_iq - n_run;
+        const bool has = lane < left;
+        float cmu = 0.0f, cph = 0.0f;
+        int cxo = 0, ckr = 0;
+        uint32_t cwu = 0u, cwa = 0u;
+        uint16_t ce = 0;
+        if (has) {
+          const int j = q.perm[n_run + lane];
+          cmu = q.mu[j];
+          cph = q.ph[j];
+          cxo = q.xo[j];
+          ckr = q.kr[j];
+          cwu = q.wu[j];
+          cwa = q.wa[j];
+          ce = q.e[j];
+        }
+        const int cc = has ? (ckr >> 16) : 64 + lane;
+        const unsigned grp = __match_any_sync(0xffffffffu, cc);
+        __syncwarp();
+        q.cnt[lane] = 0;
+        __syncwarp();
+        if (has) {
+          q.mu[lane] = cmu;
+          q.ph[lane] = cph;
+          q.xo[lane] = cxo;
+          q.kr[lane] = (cc << 16) | __popc(grp & lt);
+          q.wu[lane] = cwu;
+          q.wa[lane] = cwa;
+          q.e[lane] = ce;
+          if ((grp & lt) == 0) q.cnt[cc] = __popc(grp);
+        }
+        __syncwarp();
+        n_iq = left;
+      }
     }
+    if (lane == 0) s.zgp_cnt[unit] = n_gq;
     // ---- the unit's partial: a fixed-order warp reduction -----------------
-    const FF f0 = ff_warp_sum(FF{d0, 0.0f}), f1 = ff_warp_sum(FF{d1a, 0.0f}), f2 = ff_warp_sum(FF{d1b, 0.0f});
-    nz = i64_warp_sum(nz);
-    xz = i64_warp_sum(xz);
-    n0 = i64_warp_sum(n0);
+    const FF f0 = ff_warp_sum(FF{acc.d0, 0.0f}), f1 = ff_warp_sum(FF{acc.d1a, 0.0f}),
+             f2 = ff_warp_sum(FF{acc.d1b, 0.0f});
+    const long long nz = i64_warp_sum(acc.nz), xz = i64_warp_sum(acc.xz), n0 = i64_warp_sum(acc.n0);
     if (lane == 0) {
       double* gp = s.gpart + (int64_t)unit * GSLOT;
+      gp[0] = (double)nz;
+      gp[1] = (double)xz;
+      gp[2] = (double)n0;
+      gp[3] = ff_value(f0);
+      gp[4] = ff_value(f1);
+      gp[5] = ff_value(f2);
+    }
+    __syncwarp();  // the queue's counts are reset by the next unit
+  }
+  // the last warp to finish zeroes both counters for the next launch
+  if (lane == 0) {
+    __threadfence();
+    const unsigned total = gridDim.x * (unsigned)ZX_WARPS;
+    if (atomicAdd(&s.zx_ctr[1], 1u) == total - 1u) {
+      s.zx_ctr[0] = 0u;
+      s.zx_ctr[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// The NB proposals that k_zx listed for Gamma-Poisson draws (phi < 1 or
+// mu >= NB_INV_MU: BUSseq_gpu.cu:199-210's method), in a pass of their own so
+// that every lane of a round runs the same sampler and k_zx carries none of
+// its code.  Warps take chunks of ZGP_UNITS units of one batch from a counter
+// and draw the chunk's listed entries 32 at a time in unit order; each lane
+// reloads its entry, generates blocks 0 and 1 of the entry's stream with the
+// other lanes, draws the Gamma-Poisson proposal and decides it as k_zx
+// decides an inversion's.  The gamma statistics go to the chunk's partial in
+// a fixed order, so the sums do not depend on which warp took the chunk.
+__global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState s, int kept) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t iter = (uint32_t)*s.iter;
+  const int64_t Gp = s.Gp;
+  const uint64_t G64 = (uint64_t)s.G;
+  const uint32_t k0 = (uint32_t)s.seed, k1 = (uint32_t)(s.seed >> 32);
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = (int)atomicAdd(&s.zx_ctr[2], 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= s.n_gchunk) break;
+    const int4 ch = s.zgchunk[c];  // {first unit, units (<= 32), batch}
+    const int b = ch.z;
+    // the units' list lengths and their exclusive prefix (lane = unit of the chunk)
+    const int cnt = lane < ch.y ? s.zgp_cnt[ch.x + lane] : 0;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - cnt;
+    const float4* gtab = s.zx_gtab + (int64_t)b * ZX_HIST;
+    const int64_t eoff = (int64_t)b * s.K;
+    GammaTerms gt;
+    gt.g0 = s.gamma[b];
+    gt.g1 = s.gamma[s.B + b];
+    gt.g0p = s.gamma_p[b];
+    gt.dg0 = gt.g0p - gt.g0;
+    gt.dg1 = s.gamma_p[s.B + b] - gt.g1;
+    ZxAcc acc;
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      // the unit holding list position p: the last one whose prefix is <= p
+      // (an empty unit shares its prefix with the next one)
+      int uu = 0;
+      for (int t = 1; t < ch.y; ++t)
+        if (p >= __shfl_sync(0xffffffffu, excl, t)) uu = t;
+      const int base = __shfl_sync(0xffffffffu, excl, uu);
+      if (p < total) {
+        const int unit = ch.x + uu;
+        const int64_t jj = (int64_t)s.zcta[unit].x + s.zgp[(int64_t)unit * ZX_UNIT + (p - base)];
+        const int2 ig = s.zij[jj];
+        const int64_t i = ig.x, g = ig.y;
+        const int xo = s.X[i * Gp + g];
+        const float ph = s.phi[(int64_t)b * Gp + g];
+        const float mu = s.E[(eoff + s.W[i]) * Gp + g] * s.Dexp[i];
+        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+        const U32x4 r = philox4x32_10(
+            U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0, k1);
+        StreamAhead st(Stream::resume(s.seed, SID_ZX, ent, iter, r.x, r.y, r.z, r.w, xo == 0));
+        int err = 0;
+        const int xn = negbin_gamma_poisson(st, mu, ph, &err);
+        zx_finish(s, kept, gtab, gt, jj, ig, xo, xn, st.uniform(), err, acc);
+      }
+    }
+    const FF f0 = ff_warp_sum(FF{acc.d0, 0.0f}), f1 = ff_warp_sum(FF{acc.d1a, 0.0f}),
+             f2 = ff_warp_sum(FF{acc.d1b, 0.0f});
+    const long long nz = i64_warp_sum(acc.nz), xz = i64_warp_sum(acc.xz), n0 = i64_warp_sum(acc.n0);
+    if (lane == 0) {
+      double* gp = s.gpart_gp + (int64_t)c * GSLOT;
       gp[0] = (double)nz;
       gp[1] = (double)xz;
       gp[2] = (double)n0;
@@ -452,9 +597,9 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
   if (lane == 0) {
     __threadfence();
     const unsigned total = gridDim.x * (unsigned)ZX_WARPS;
-    if (atomicAdd(&s.zx_ctr[1], 1u) == total - 1u) {
-      s.zx_ctr[0] = 0u;
-      s.zx_ctr[1] = 0u;
+    if (atomicAdd(&s.zx_ctr[3], 1u) == total - 1u) {
+      s.zx_ctr[2] = 0u;
+      s.zx_ctr[3] = 0u;
       __threadfence();
     }
   }
@@ -743,6 +888,11 @@ __device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double
   for (; c < c_end; c += stride) {
 #pragma unroll
     for (int q = 0; q < 6; ++q) v[q] += s.gpart[(int64_t)c * GSLOT + q];
+  }
+  // and the partials of the batch's Gamma-Poisson chunks
+  for (int h = s.gfirst[b] + (int)threadIdx.x; h < s.gfirst[b + 1]; h += stride) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) v[q] += s.gpart_gp[(int64_t)h * GSLOT + q];
   }
   const int slices = (s.ymax + ZX_THREADS - 1) / ZX_THREADS;
   for (int c = b * slices + threadIdx.x; c < (b + 1) * slices && c < s.n_static; c += blockDim.x) {

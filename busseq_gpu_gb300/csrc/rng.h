@@ -154,6 +154,31 @@ struct Stream {
   }
 };
 
+// A Stream whose next block is generated ahead of need, at the point of
+// construction.  A sampler that runs past the buffered words at different
+// draws in different lanes of a warp (a rejection, the U^(1/a) boost, a second
+// Poisson try) then takes those words from registers instead of running
+// Philox in a divergent branch.  The words and their order are Stream's.
+struct StreamAhead {
+  Stream s;
+  uint32_t a0, a1, a2, a3;
+  bool ahead;
+  BQ_HD explicit StreamAhead(const Stream& base) : s(base), ahead(true) {
+    const U32x4 r = philox4x32_10(U32x4{s.c0, s.c1, s.blk, s.it}, s.k0, s.k1);
+    a0 = r.x; a1 = r.y; a2 = r.z; a3 = r.w;
+  }
+  BQ_HD uint32_t next_u32() {
+    if (s.n == 0 && ahead) {
+      s.b0 = a0; s.b1 = a1; s.b2 = a2; s.b3 = a3;
+      s.n = 4;
+      ++s.blk;
+      ahead = false;
+    }
+    return s.next_u32();
+  }
+  BQ_HD float uniform() { return u32_to_unit(next_u32()); }
+};
+
 // ---------------------------------------------------------------------------
 // Single-precision math shims (device intrinsics vs. host libm)
 // ---------------------------------------------------------------------------
@@ -331,7 +356,8 @@ BQ_HD float log_factorial(float k) {
 // Samplers
 // ---------------------------------------------------------------------------
 // Standard normal: z = sqrt(-2 log u1) cos(2 pi u2).  Consumes 2 uniforms.
-BQ_HD float normal(Stream& s) {
+template <class S>
+BQ_HD float normal(S& s) {
   const float u1 = s.uniform();
   const float u2 = s.uniform();
   return sqrtf(-2.0f * log_fast(u1)) * cospi2f(u2);
@@ -340,7 +366,8 @@ BQ_HD float normal(Stream& s) {
 // Gamma(shape a, scale 1), Marsaglia and Tsang (2000).  Each try consumes a
 // normal (2 uniforms) and, unless 1 + c z <= 0, one more uniform.  Shapes
 // below one draw Gamma(a+1) and multiply by U^(1/a) (one more uniform).
-BQ_HD float gamma_mt(Stream& s, float a, int* err) {
+template <class S>
+BQ_HD float gamma_mt(S& s, float a, int* err) {
   if (!(a > 0.0f)) return 0.0f;
   const bool boost = a < 1.0f;
   const float aa = boost ? a + 1.0f : a;
@@ -368,7 +395,8 @@ BQ_HD float gamma_mt(Stream& s, float a, int* err) {
 
 // Poisson(lambda).  Inversion below 10 (one uniform), PTRS above (two
 // uniforms per try).
-BQ_HD int poisson(Stream& s, float lam, int* err) {
+template <class S>
+BQ_HD int poisson(S& s, float lam, int* err) {
   if (!(lam > 0.0f)) return 0;
   if (lam > POISSON_MAX_LAMBDA) lam = POISSON_MAX_LAMBDA;
   if (lam < 10.0f) {
@@ -420,25 +448,48 @@ enum : int { ERR_NB_INV_CAP = 4 };
 
 BQ_HD bool negbin_use_inversion(float mu, float phi) { return mu < NB_INV_MU && phi >= 1.0f; }
 
-// max_k lowers the search cap (a test of the failure path passes a small one).
-BQ_HD int negbin_inversion(Stream& s, float mu, float phi, int* err, int max_k = NB_INV_MAX_K) {
-  const float q = mu / (phi + mu);
-  float p = expf(phi * log1p_fast(-q));
-  float F = p;
-  const float u = s.uniform();
-  int k = 0;
-  while (u > F) {
-    if (k >= max_k) { *err |= ERR_NB_INV_CAP; break; }
-    p = p * (q * fast_div(phi + (float)k, (float)(k + 1)));
-    ++k;
-    const float Fn = F + p;
-    if (Fn == F) break;  // the distribution function stopped growing
-    F = Fn;
-  }
-  return k;
+// e^x from the hardware base-2 exponential (a few ulp, plus the rounding of
+// x log2(e): below 1e-5 relative for |x| < 100).
+BQ_HD float exp_fast(float x) {
+#if defined(__CUDA_ARCH__)
+  return __expf(x);
+#else
+  return expf(x);
+#endif
 }
 
-BQ_HD int negbin_gamma_poisson(Stream& s, float mu, float phi, int* err) {
+// The search of the inversion for a given uniform u: the smallest k with
+// u <= F(k), F summed from P(0) = (1 - q)^phi by P(k+1) = P(k) q (phi + k) /
+// (k + 1), q = mu / (phi + mu).  The counter is kept in float (exact below
+// 2^24).  The search also stops where F no longer grows in single precision
+// (u within 2^-24 of 1 past the last representable step); max_k caps it and
+// raises ERR_NB_INV_CAP (a test of the failure path passes a small cap).
+BQ_HD int negbin_invert_u(float u, float mu, float phi, int* err, int max_k = NB_INV_MAX_K) {
+  const float q = fast_div(mu, phi + mu);
+  const float qphi = q * phi;
+  const float cap = (float)max_k;
+  float p = exp_fast(phi * log1p_fast(-q));
+  float F = p, k = 0.0f;
+  bool grow = true, go = u > F;
+  while (go) {
+    const float k1 = k + 1.0f;
+    p = p * (fmaf(q, k, qphi) * fast_rcp(k1));
+    k = k1;
+    const float Fn = F + p;
+    grow = Fn != F;
+    go = u > Fn && grow && k < cap;
+    F = Fn;
+  }
+  if (grow && u > F) *err |= ERR_NB_INV_CAP;  // stopped by the cap
+  return (int)k;
+}
+
+BQ_HD int negbin_inversion(Stream& s, float mu, float phi, int* err, int max_k = NB_INV_MAX_K) {
+  return negbin_invert_u(s.uniform(), mu, phi, err, max_k);
+}
+
+template <class S>
+BQ_HD int negbin_gamma_poisson(S& s, float mu, float phi, int* err) {
   const float g = gamma_mt(s, phi, err);
   return poisson(s, g * (mu / phi), err);
 }
