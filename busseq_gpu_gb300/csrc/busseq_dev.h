@@ -229,7 +229,8 @@ struct DevState {
                       // (zero between launches)
   int zx_ctas;        // Z/X CTAs per launch (resident on every SM)
   // The NB proposals drawn as Gamma-Poisson mixtures, left by k_zx to k_zx_gp:
-  uint16_t* zgp;            // [n_zcta][ZX_UNIT] their positions in each unit, in unit order
+  int4* zgp_rec;            // [n_zcta][ZX_UNIT] each unit's, in unit order: {list entry, cell, gene, X}
+  float2* zgp_mp;           // [n_zcta][ZX_UNIT] and their {mu, phi}
   int32_t* zgp_cnt;         // [n_zcta] how many each unit has
   const int4* zgchunk;      // [n_gchunk] {first unit, units, batch, 0}: ZGP_UNITS units of one batch
   const int32_t* gfirst;    // [B+1] first chunk of each batch

@@ -763,7 +763,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.n_gchunk = (int)zgchunk_h.size();
     int4* zgchunk;
     int32_t* gfirst;
-    TRY(h->alloc(&s.zgp, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
+    TRY(h->alloc(&s.zgp_rec, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
+    TRY(h->alloc(&s.zgp_mp, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
     TRY(h->alloc(&s.zgp_cnt, std::max(1, s.n_zcta)));
     TRY(h->alloc(&zgchunk, std::max(1, s.n_gchunk)));
     TRY(h->alloc(&gfirst, B + 1));

@@ -234,7 +234,8 @@ struct GammaTerms {
 // the distribution function is staged in the warp's queue with the two words
 // it will use and a cost class, 0..30 by the expected length of the search,
 // mu (-log(1 - u)) with u the inversion's uniform, longest first.  An entry
-// that needs a Gamma-Poisson draw is listed, by its position, for k_zx_gp.
+// that needs a Gamma-Poisson draw is listed for k_zx_gp with its cell, gene,
+// X, mu and phi.
 // Phase 2: a counting sort over (class, rank) - counts from ballots and match
 // masks, so the order is deterministic - lays the queue out in class order.
 // Phase 3: the lanes take the sorted queue 32 entries at a time, so lanes of
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
     const float zthr = 1.0f / (1.0f + expf(gt.g0));
     ZxAcc acc;
     int n_iq = 0, n_gq = 0;  // warp-uniform: the queue's length, the Gamma-Poisson entries listed
-    uint16_t* gpl = s.zgp + (int64_t)unit * ZX_UNIT;
+    const int64_t gpo = (int64_t)unit * ZX_UNIT;
     q.cnt[lane] = 0;
     __syncwarp();
     for (int part = 0; part * ZX_PART < run.y; ++part) {
@@ -409,7 +410,11 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
           q.wu[slot] = xo == 0 ? r.y : r.x;
           q.wa[slot] = xo == 0 ? r.z : r.y;
         }
-        if (gpn) gpl[n_gq + __popc(gm & lt)] = (uint16_t)e;
+        if (gpn) {  // the record k_zx_gp draws from, with what was loaded for it here
+          const int64_t o = gpo + n_gq + __popc(gm & lt);
+          s.zgp_rec[o] = make_int4(run.x + e, ei[u], eg[u], xo);
+          s.zgp_mp[o] = make_float2(mu, ph);
+        }
         __syncwarp();
         if (inv && (grp & lt) == 0) q.cnt[cls] += __popc(grp);  // the class group's first lane
         __syncwarp();
@@ -519,14 +524,15 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
 // that every lane of a round runs the same sampler and k_zx carries none of
 // its code.  Warps take chunks of ZGP_UNITS units of one batch from a counter
 // and draw the chunk's listed entries 32 at a time in unit order; each lane
-// reloads its entry, generates blocks 0 and 1 of the entry's stream with the
-// other lanes, draws the Gamma-Poisson proposal and decides it as k_zx
-// decides an inversion's.  The gamma statistics go to the chunk's partial in
-// a fixed order, so the sums do not depend on which warp took the chunk.
+// reads its entry's record, generates blocks 0 and 1 of the entry's stream
+// with the other lanes, draws the Gamma-Poisson proposal and decides it as
+// k_zx decides an inversion's.  The chunk's partial is its units' partials from
+// k_zx plus the gamma statistics of these draws, summed in a fixed order, so
+// the sums do not depend on which warp took the chunk; the gamma decisions
+// then read one partial per chunk.
 __global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState s, int kept) {
   const int lane = threadIdx.x & 31;
   const uint32_t iter = (uint32_t)*s.iter;
-  const int64_t Gp = s.Gp;
   const uint64_t G64 = (uint64_t)s.G;
   const uint32_t k0 = (uint32_t)s.seed, k1 = (uint32_t)(s.seed >> 32);
   for (;;) {
@@ -547,7 +553,6 @@ __global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState 
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - cnt;
     const float4* gtab = s.zx_gtab + (int64_t)b * ZX_HIST;
-    const int64_t eoff = (int64_t)b * s.K;
     GammaTerms gt;
     gt.g0 = s.gamma[b];
     gt.g1 = s.gamma[s.B + b];
@@ -564,14 +569,14 @@ __global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState 
         if (p >= __shfl_sync(0xffffffffu, excl, t)) uu = t;
       const int base = __shfl_sync(0xffffffffu, excl, uu);
       if (p < total) {
-        const int unit = ch.x + uu;
-        const int64_t jj = (int64_t)s.zcta[unit].x + s.zgp[(int64_t)unit * ZX_UNIT + (p - base)];
-        const int2 ig = s.zij[jj];
-        const int64_t i = ig.x, g = ig.y;
-        const int xo = s.X[i * Gp + g];
-        const float ph = s.phi[(int64_t)b * Gp + g];
-        const float mu = s.E[(eoff + s.W[i]) * Gp + g] * s.Dexp[i];
-        const uint64_t ent = (uint64_t)i * G64 + (uint64_t)g;
+        const int64_t o = (int64_t)(ch.x + uu) * ZX_UNIT + (p - base);
+        const int4 ra = s.zgp_rec[o];
+        const float2 rb = s.zgp_mp[o];
+        const int64_t jj = ra.x;
+        const int2 ig = make_int2(ra.y, ra.z);
+        const int xo = ra.w;
+        const float mu = rb.x, ph = rb.y;
+        const uint64_t ent = (uint64_t)ra.y * G64 + (uint64_t)ra.z;
         const U32x4 r = philox4x32_10(
             U32x4{(uint32_t)ent, ((uint32_t)(ent >> 32) & 0xFFFFu) | (SID_ZX << 16), 0u, iter}, k0, k1);
         StreamAhead st(Stream::resume(s.seed, SID_ZX, ent, iter, r.x, r.y, r.z, r.w, xo == 0));
@@ -583,14 +588,19 @@ __global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState 
     const FF f0 = ff_warp_sum(FF{acc.d0, 0.0f}), f1 = ff_warp_sum(FF{acc.d1a, 0.0f}),
              f2 = ff_warp_sum(FF{acc.d1b, 0.0f});
     const long long nz = i64_warp_sum(acc.nz), xz = i64_warp_sum(acc.xz), n0 = i64_warp_sum(acc.n0);
+    // (the warp sums are lane 0's) the chunk's unit partials first, in unit order
     if (lane == 0) {
+      double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int t = 0; t < ch.y; ++t)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) v[q] += s.gpart[(int64_t)(ch.x + t) * GSLOT + q];
       double* gp = s.gpart_gp + (int64_t)c * GSLOT;
-      gp[0] = (double)nz;
-      gp[1] = (double)xz;
-      gp[2] = (double)n0;
-      gp[3] = ff_value(f0);
-      gp[4] = ff_value(f1);
-      gp[5] = ff_value(f2);
+      gp[0] = v[0] + (double)nz;
+      gp[1] = v[1] + (double)xz;
+      gp[2] = v[2] + (double)n0;
+      gp[3] = v[3] + ff_value(f0);
+      gp[4] = v[4] + ff_value(f1);
+      gp[5] = v[5] + ff_value(f2);
     }
   }
   // the last warp to finish zeroes both counters for the next launch
@@ -871,28 +881,24 @@ __global__ void __launch_bounds__(256) k_phi_static(DevState s) {
 // gamma0 then gamma1 of batch b, one CTA (BUSseq_gpu.cu:514-600).
 __device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double* sh) {
   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  // the batch's Z/X work-unit partials, eight units' loads in flight per thread
-  const int c_end = s.zfirst[b + 1], stride = (int)blockDim.x;
-  int c = s.zfirst[b] + (int)threadIdx.x;
-  for (; c + 7 * stride < c_end; c += 8 * stride) {
-    double t[8][6];
+  // the batch's Z/X chunk partials (k_zx_gp folds the units' partials into
+  // them), four chunks' loads in flight per thread
+  const int c_end = s.gfirst[b + 1], stride = (int)blockDim.x;
+  int c = s.gfirst[b] + (int)threadIdx.x;
+  for (; c + 3 * stride < c_end; c += 4 * stride) {
+    double t[4][6];
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int q = 0; q < 6; ++q) t[u][q] = __ldg(&s.gpart[(int64_t)(c + u * stride) * GSLOT + q]);
+      for (int q = 0; q < 6; ++q) t[u][q] = __ldg(&s.gpart_gp[(int64_t)(c + u * stride) * GSLOT + q]);
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int q = 0; q < 6; ++q) v[q] += t[u][q];
   }
   for (; c < c_end; c += stride) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) v[q] += s.gpart[(int64_t)c * GSLOT + q];
-  }
-  // and the partials of the batch's Gamma-Poisson chunks
-  for (int h = s.gfirst[b] + (int)threadIdx.x; h < s.gfirst[b + 1]; h += stride) {
-#pragma unroll
-    for (int q = 0; q < 6; ++q) v[q] += s.gpart_gp[(int64_t)h * GSLOT + q];
+    for (int q = 0; q < 6; ++q) v[q] += __ldg(&s.gpart_gp[(int64_t)c * GSLOT + q]);
   }
   const int slices = (s.ymax + ZX_THREADS - 1) / ZX_THREADS;
   for (int c = b * slices + threadIdx.x; c < (b + 1) * slices && c < s.n_static; c += blockDim.x) {
