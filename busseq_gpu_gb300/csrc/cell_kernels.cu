@@ -48,9 +48,11 @@ __device__ __forceinline__ void cell_reduce_i(long long (&acc)[CELL_TILE], long 
 
 // X rows of a cell tile, streamed through shared memory: a ring of NST stages,
 // each holding the tile's rows over WIDTH consecutive genes, filled by bulk
-// asynchronous copies that thread 0 issues NST stages ahead of the compute.
-// Row starts are 16-byte aligned (Gp is a multiple of GENE_TILE) and every
-// copy is a multiple of 16 bytes.
+// asynchronous copies that warp 0 issues NST stages ahead of the compute (lane
+// 0 arms the stage's barrier, lane r copies row r, so the warp that also
+// computes spends little time on the copies).  Row starts are 16-byte aligned
+// (Gp is a multiple of GENE_TILE) and every copy is a multiple of 16 bytes.
+static_assert(CELL_TILE <= 32, "one lane of warp 0 per row of a tile");
 template <int WIDTH, int NST>
 struct XRowRing {
   int* buf;       // [NST][CELL_TILE][WIDTH]
@@ -68,25 +70,27 @@ struct XRowRing {
       mbar_init_fence();
     }
   }
-  __device__ void issue(int step) const {
+  // Called by all of warp 0 (lane = its lane).
+  __device__ void issue(int step, int lane) const {
     const int st = step % NST;
     const int64_t g0 = (int64_t)step * WIDTH;
     const uint32_t nb = (uint32_t)((Gp - g0 < WIDTH ? Gp - g0 : WIDTH) * (int64_t)sizeof(int));
-    mbar_arrive_expect_tx(&bar[st], nb * (uint32_t)len);
-    for (int r = 0; r < len; ++r)
-      bulk_copy_g2s(buf + (st * CELL_TILE + r) * WIDTH, X + (int64_t)rows[r] * Gp + g0, nb, &bar[st]);
+    if (lane == 0) mbar_arrive_expect_tx(&bar[st], nb * (uint32_t)len);
+    __syncwarp();
+    if (lane < len)
+      bulk_copy_g2s(buf + (st * CELL_TILE + lane) * WIDTH, X + (int64_t)rows[lane] * Gp + g0, nb, &bar[st]);
   }
   __device__ void prologue(int tid) const {
-    if (tid == 0)
-      for (int q = 0; q < NST && q < n_steps; ++q) issue(q);
+    if (tid < 32)
+      for (int q = 0; q < NST && q < n_steps; ++q) issue(q, tid);
   }
   __device__ bool wait(int step) { return mbar_wait(&bar[step % NST], (uint32_t)((step / NST) & 1)); }
   __device__ const int* row(int step, int r) const { return buf + ((step % NST) * CELL_TILE + r) * WIDTH; }
   // After every thread finished reading stage `step`: refill it.
   __device__ void advance(int tid, int step) const {
-    if (tid == 0 && step + NST < n_steps) {
+    if (tid < 32 && step + NST < n_steps) {
       fence_proxy_async_smem();
-      issue(step + NST);
+      issue(step + NST, tid);
     }
   }
   // Failure at `step`: flag it and let the copies in flight land before the
