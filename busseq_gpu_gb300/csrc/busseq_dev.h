@@ -67,6 +67,7 @@ constexpr int ZX_HIST = 128;       // counts below this read the gamma terms fro
 constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's launch bound)
 constexpr int ZGP_UNITS = 4;       // Z/X work units per chunk of the Gamma-Poisson pass
 constexpr int ZGP_CTAS_PER_SM = 3;  // resident k_zx_gp CTAs per SM (its launch bound)
+constexpr int DECIDE_GAMMA_THREADS = 256;  // threads of a gamma-decision CTA (one per batch)
 
 // ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
 enum Stage : int {

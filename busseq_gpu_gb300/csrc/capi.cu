@@ -46,8 +46,8 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
                                     "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static",
-                                    "k_hmc_accept_genes", "k_zx_gp"};
-constexpr int kNumKernels = 35;
+                                    "k_hmc_accept_genes", "k_zx_gp", "k_decide_gamma"};
+constexpr int kNumKernels = 36;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -56,7 +56,7 @@ enum : int {
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
   KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32, KID_HMC_ACCEPT_GENES = 33,
-  KID_ZX_GP = 34
+  KID_ZX_GP = 34, KID_DECIDE_GAMMA = 35
 };
 
 }  // namespace
@@ -99,12 +99,16 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       k_zx_gp<<<(unsigned)s.zgp_ctas, ZX_THREADS, 0, st>>>(s, kept);
       LAUNCH_CHECK("k_zx_gp");
       break;
+    case KID_DECIDE_GAMMA:
+      k_decide_gamma<<<s.B, DECIDE_GAMMA_THREADS, 0, st>>>(s);
+      LAUNCH_CHECK("k_decide_gamma");
+      break;
     case 2:
       k_alpha<<<gene_grid, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_alpha");
       break;
     case 3:
-      k_decide_alpha<<<s.n_tiles + s.B, GENE_TILE, 0, st>>>(s);
+      k_decide_alpha<<<s.n_tiles, GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_decide_alpha");
       break;
     case 4:
@@ -244,8 +248,8 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   std::vector<int> q;
   if (h->s.hmc_L > 0) {
     const bool blocks = h->s.hmc_nb > 0;
-    q = {KID_PROPOSE, KID_ZX, KID_ZX_GP, KID_DECIDE_ALPHA, KID_HMC_GRAD_START, KID_HMC_ASSEMBLE_START,
-         KID_HMC_MASS};
+    q = {KID_PROPOSE, KID_ZX, KID_ZX_GP, KID_DECIDE_GAMMA, KID_DECIDE_ALPHA, KID_HMC_GRAD_START,
+         KID_HMC_ASSEMBLE_START, KID_HMC_MASS};
     if (blocks) q.push_back(KID_HMC_METRIC_BLOCKS);
     q.push_back(KID_HMC_START);
     if (blocks) q.push_back(KID_HMC_START_BLOCKS);
@@ -270,16 +274,50 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
     for (int k = 0; k <= KID_SORT_PI; ++k) {
       if (k == KID_PHI) q.push_back(KID_PHI_STATIC);
       q.push_back(k);
-      if (k == KID_ZX) q.push_back(KID_ZX_GP);
+      if (k == KID_ZX) {
+        q.push_back(KID_ZX_GP);
+        q.push_back(KID_DECIDE_GAMMA);
+      }
     }
   }
   if (kept) q.push_back(KID_POSTERIOR);
   return q;
 }
 
+// One sweep, enqueued while `st` is being captured into a graph.  Two
+// kernels leave the main line on the handle's side stream: k_phi_static needs
+// only k_propose's phi proposals and is read by k_decide_phi; the gamma
+// decisions need the Z/X partials of k_zx_gp and are read only by the next
+// sweep (and the posterior accumulation).  Both run beside the main line,
+// filling the SMs that its small decision kernels leave idle; the branch
+// joins before k_decide_phi, or at the end of the sweep.
 int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
-  for (int k : sweep_sequence(h, kept)) TRY(launch_kernel(h, k, st, kept, h->s));
-  return BUSSEQ_OK;
+  const std::vector<int> seq = sweep_sequence(h, kept);
+  cudaStream_t side = h->side_stream;
+  bool open = false;  // the side branch has work that the main line has not joined
+  auto fork = [&](int which, int ev) -> int {
+    CUDA_TRY(cudaEventRecord(h->ev_fork[ev], st));
+    CUDA_TRY(cudaStreamWaitEvent(side, h->ev_fork[ev], 0));
+    TRY(launch_kernel(h, which, side, kept, h->s));
+    open = true;
+    return BUSSEQ_OK;
+  };
+  auto join = [&]() -> int {
+    if (!open) return BUSSEQ_OK;
+    CUDA_TRY(cudaEventRecord(h->ev_join, side));
+    CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
+    open = false;
+    return BUSSEQ_OK;
+  };
+  const bool has_static = std::find(seq.begin(), seq.end(), (int)KID_PHI_STATIC) != seq.end();
+  for (int k : seq) {
+    if (k == KID_PHI_STATIC || k == KID_DECIDE_GAMMA) continue;
+    if (k == KID_DECIDE_PHI || k == KID_POSTERIOR) TRY(join());
+    TRY(launch_kernel(h, k, st, kept, h->s));
+    if (k == KID_PROPOSE && has_static) TRY(fork(KID_PHI_STATIC, 0));
+    if (k == KID_ZX_GP) TRY(fork(KID_DECIDE_GAMMA, 1));
+  }
+  return join();
 }
 
 // Z as a bit mask [N][Gw] in s.zm, from the per-entry zval (for transfers).
@@ -563,9 +601,13 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
   busseq_handle* h = new busseq_handle();
   h->device = opt.device;
   h->opt = opt;
-  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     delete h;
-    return fail(BUSSEQ_ERR_CUDA, "cudaStreamCreate failed");
+    return fail(BUSSEQ_ERR_CUDA, "cudaStreamCreate / cudaEventCreate failed");
   }
   h->stream = h->own_stream;
   h->n_b.assign(dims->n_b, dims->n_b + B);
@@ -1207,7 +1249,7 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
     case BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA);
       LAUNCH_CHECK("k_propose");
-      TRY(run({KID_ZX, KID_ZX_GP, 2, 3}));
+      TRY(run({KID_ZX, KID_ZX_GP, KID_DECIDE_GAMMA, 2, 3}));
       break;
     case BUSSEQ_STAGE_BETA_NU:
       k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU);

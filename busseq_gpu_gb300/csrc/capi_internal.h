@@ -44,6 +44,10 @@ struct busseq_handle {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // a captured sweep's side branch (k_phi_static, the gamma decisions) and
+  // its fork and join events
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
   bq::DevState s{};
   busseq_options opt{};
   std::vector<int32_t> n_b, off;
@@ -64,6 +68,10 @@ struct busseq_handle {
     if (g_keep) cudaGraphExecDestroy(g_keep);
     for (void* p : run_allocs) cudaFree(p);
     for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t e : ev_fork)
+      if (e) cudaEventDestroy(e);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side_stream) cudaStreamDestroy(side_stream);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 

@@ -9,9 +9,10 @@
 //                   terms of the Y > 0 entries from the histogram of Y
 //   k_zx_gp         the NB proposals of k_zx drawn as Gamma-Poisson mixtures
 //   k_alpha         alpha sums (:602-623)
+//   k_decide_gamma  gamma0 / gamma1 decisions, one CTA per batch (a branch of
+//                   the sweep's graph beside the alpha and beta passes)
 //   k_decide_alpha  alpha decisions, L redraw (:634-648), p and tau0 (:650-668)
-//                   in the last gene CTA, gamma0 / gamma1 decisions in one CTA per
-//                   batch
+//                   in the last gene CTA
 //   k_beta_nu       beta sums (:676-694) and the nu sums (:715-728) under both
 //                   outcomes of the beta of the cell's type
 //   k_decide_beta   beta decisions (:696-707)
@@ -930,17 +931,19 @@ __device__ void gamma_decide_cta(const DevState& s, int b, uint32_t iter, double
   if ((double)logf(u1) <= lr1 + prior1) s.gamma[s.B + b] = g1p;
 }
 
-// Gene CTAs (blockIdx.x < n_tiles): alpha decisions and L; the last of them
-// draws p and tau0.  CTAs n_tiles .. n_tiles + B - 1: gamma of one batch.
+// gamma0 and gamma1 of batch blockIdx.x.
+__global__ void __launch_bounds__(DECIDE_GAMMA_THREADS) k_decide_gamma(DevState s) {
+  __shared__ double sh[(DECIDE_GAMMA_THREADS / 32) * 9];
+  gamma_decide_cta(s, blockIdx.x, (uint32_t)*s.iter, sh);
+}
+
+// One CTA per gene tile: alpha decisions and L; the last of them draws p and
+// tau0.
 __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
-  __shared__ double sh[(GENE_TILE / 32) * 9];
+  __shared__ double sh[(GENE_TILE / 32) * 2];
   __shared__ int sh_flag;
   const uint32_t iter = (uint32_t)*s.iter;
   const int tid = threadIdx.x;
-  if ((int)blockIdx.x >= s.n_tiles) {
-    gamma_decide_cta(s, blockIdx.x - s.n_tiles, iter, sh);
-    return;
-  }
   const int tile = blockIdx.x;
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;

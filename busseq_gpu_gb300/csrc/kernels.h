@@ -20,6 +20,7 @@ struct CorrTables {
 __global__ void k_propose(DevState s, int mask);
 __global__ void k_zx(DevState s, int kept);
 __global__ void k_zx_gp(DevState s, int kept);
+__global__ void k_decide_gamma(DevState s);
 __global__ void k_zx_summary(DevState s, int n_kept, float* x_mean, float* z_prob);
 __global__ void k_zx_summary_zeros(DevState s, int n_kept, float* x_mean, float* z_prob);
 __global__ void k_alpha(DevState s);
