@@ -238,7 +238,7 @@ struct DevState {
   double* gpart_gp;         // [n_gchunk][GSLOT] gamma statistics of each chunk's draws
   int n_gchunk;
   int zgp_ctas;             // k_zx_gp CTAs per launch
-  double* tpart;   // [n_tiles][2]
+  double* tpart;   // per-CTA sums: [n_tiles][MAX_B] at initialisation, [ceil(G / 32)][2] in k_decide_alpha
   unsigned* cnt_tile;  // [n_tiles]
   unsigned* cnt_glob;  // [4]
 

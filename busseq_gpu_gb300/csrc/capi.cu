@@ -108,7 +108,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_alpha");
       break;
     case 3:
-      k_decide_alpha<<<s.n_tiles, GENE_TILE, 0, st>>>(s);
+      k_decide_alpha<<<blocks_for(s.G, 32), GENE_TILE, 0, st>>>(s);
       LAUNCH_CHECK("k_decide_alpha");
       break;
     case 4:
@@ -711,7 +711,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       bq::k_hmc_unit_mass<<<blocks_for(s.hmc_D, 256), 256, 0, h->stream>>>(s);
       LAUNCH_CHECK("k_hmc_unit_mass");
     }
-    TRY(h->alloc(&s.tpart, (int64_t)s.n_tiles * bq::MAX_B));
+    TRY(h->alloc(&s.tpart, std::max<int64_t>((int64_t)s.n_tiles * bq::MAX_B, 2 * (int64_t)blocks_for(G, 32))));
     TRY(h->alloc(&s.cnt_tile, s.n_tiles));
     TRY(h->alloc(&s.cnt_glob, 8));
     TRY(h->alloc(&s.iter, 1));

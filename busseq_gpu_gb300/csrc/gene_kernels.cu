@@ -937,42 +937,60 @@ __global__ void __launch_bounds__(DECIDE_GAMMA_THREADS) k_decide_gamma(DevState 
   gamma_decide_cta(s, blockIdx.x, (uint32_t)*s.iter, sh);
 }
 
-// One CTA per gene tile: alpha decisions and L; the last of them draws p and
-// tau0.
+// One CTA per 32 genes: alpha decisions and L; the last CTA draws p and tau0.
+// The CTA's four warps split each gene's chunk partials (chunks c = w, w + 4,
+// ...) so that more loads are in flight, and add the four slices in a fixed
+// order; they split the types of the L redraw the same way.
+constexpr int DA_SLICES = GENE_TILE / 32;
 __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
   __shared__ double sh[(GENE_TILE / 32) * 2];
+  __shared__ double s_sum[DA_SLICES][2][32];
   __shared__ int sh_flag;
   const uint32_t iter = (uint32_t)*s.iter;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, sl = tid >> 5;
   const int tile = blockIdx.x;
   const int64_t Gp = s.Gp;
-  const int64_t g = (int64_t)tile * GENE_TILE + tid;
-  double lv[2] = {0.0, 0.0};
-  if (g < s.G && s.hmc_L == 0) {  // alpha: random-walk MH (the HMC block updates it otherwise)
+  const int64_t g = (int64_t)tile * 32 + lane;
+  if (s.hmc_L == 0) {  // alpha: random-walk MH (the HMC block updates it otherwise)
     double Sx = 0.0, La = 0.0;
-#pragma unroll 8
-    for (int c = 0; c < s.cap_g; ++c) {  // unrolled: eight chunks' loads in flight
-      const bool used = s.gchunk[c].w > 0;
-      const double a0 = __ldg(&s.part[((int64_t)c * NSLOT + 0) * Gp + g]);
-      const double a1 = __ldg(&s.part[((int64_t)c * NSLOT + 1) * Gp + g]);
-      Sx += used ? a0 : 0.0;
-      La += used ? a1 : 0.0;
+    if (g < s.G) {
+#pragma unroll 4
+      for (int c = sl; c < s.cap_g; c += DA_SLICES) {
+        const bool used = s.gchunk[c].w > 0;
+        const double a0 = __ldg(&s.part[((int64_t)c * NSLOT + 0) * Gp + g]);
+        const double a1 = __ldg(&s.part[((int64_t)c * NSLOT + 1) * Gp + g]);
+        Sx += used ? a0 : 0.0;
+        La += used ? a1 : 0.0;
+      }
     }
-    const float a = s.alpha[g], ap = s.alpha_p[g];
-    const double ma = s.mu_alpha[g];
-    const double lr = (double)(ap - a) * Sx - La;
-    const double prior = (((double)a - ma) * ((double)a - ma) - ((double)ap - ma) * ((double)ap - ma)) /
-                         (2.0 * SIGMA2_ALPHA);
-    const float ua = uniform_at(s.seed, SID_ALPHA, (uint64_t)g, iter, 2);
-    s.lr_alpha[g] = lr + prior;
-    if ((double)logf(ua) <= lr + prior) s.alpha[g] = ap;
+    s_sum[sl][0][lane] = Sx;
+    s_sum[sl][1][lane] = La;
+    __syncthreads();
+    if (sl == 0 && g < s.G) {
+      Sx = s_sum[0][0][lane];
+      La = s_sum[0][1][lane];
+#pragma unroll
+      for (int w = 1; w < DA_SLICES; ++w) {
+        Sx += s_sum[w][0][lane];
+        La += s_sum[w][1][lane];
+      }
+      const float a = s.alpha[g], ap = s.alpha_p[g];
+      const double ma = s.mu_alpha[g];
+      const double lr = (double)(ap - a) * Sx - La;
+      const double prior = (((double)a - ma) * ((double)a - ma) - ((double)ap - ma) * ((double)ap - ma)) /
+                           (2.0 * SIGMA2_ALPHA);
+      const float ua = uniform_at(s.seed, SID_ALPHA, (uint64_t)g, iter, 2);
+      s.lr_alpha[g] = lr + prior;
+      if ((double)logf(ua) <= lr + prior) s.alpha[g] = ap;
+    }
   }
+  double lv[2] = {0.0, 0.0};
   if (g < s.G) {
     // L from the current beta, p and tau0 (BUSseq_gpu.cu:634-648)
     const float p = s.p_tau0[0], tau0 = s.p_tau0[1];
     const float base = logf(p) - logf(1.0f - p) - (logf((float)TAU1) - logf(tau0)) * 0.5f;
     const float qd = 1.0f / (2.0f * tau0) - 1.0f / (2.0f * (float)TAU1);
-    for (int kk = 1; kk < s.K; ++kk) {
+    for (int kk = 1 + sl; kk < s.K; kk += DA_SLICES) {
       const float bt = s.beta[(int64_t)kk * Gp + g];
       const float lo = base + bt * bt * qd;
       const float u = uniform_at(s.seed, SID_L, (uint64_t)(kk - 1) * (uint64_t)s.G + (uint64_t)g, iter, 0);
@@ -987,11 +1005,11 @@ __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
     s.tpart[2 * tile] = lv[0];
     s.tpart[2 * tile + 1] = lv[1];
   }
-  if (!arrive_last(&s.cnt_glob[0], (unsigned)s.n_tiles, &sh_flag)) return;
+  if (!arrive_last(&s.cnt_glob[0], gridDim.x, &sh_flag)) return;
   if ((int)iter < s.n_unchanged) return;
   // p ~ Beta(sum L + 1, G(K-1) - sum L + 3), tau0 = 1 / Gamma(...) (BUSseq_gpu.cu:650-668)
   double v[2] = {0.0, 0.0};
-  for (int t = tid; t < s.n_tiles; t += blockDim.x) {
+  for (int t = tid; t < (int)gridDim.x; t += blockDim.x) {
     v[0] += __ldcg(&s.tpart[2 * t]);
     v[1] += __ldcg(&s.tpart[2 * t + 1]);
   }
