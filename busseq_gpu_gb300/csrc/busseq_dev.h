@@ -68,6 +68,7 @@ constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's lau
 constexpr int ZGP_UNITS = 4;       // Z/X work units per chunk of the Gamma-Poisson pass
 constexpr int ZGP_CTAS_PER_SM = 3;  // resident k_zx_gp CTAs per SM (its launch bound)
 constexpr int DECIDE_GAMMA_THREADS = 256;  // threads of a gamma-decision CTA (one per batch)
+constexpr int DEC_THREADS = 256;   // per-gene decision CTAs: 32 genes x 8 warps splitting their segments
 
 // ---- stages (groups of the reference's sweep order, BUSseq_gpu.cu:1267-1398)
 enum Stage : int {

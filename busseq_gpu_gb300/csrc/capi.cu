@@ -116,11 +116,11 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_beta_nu");
       break;
     case 5:
-      k_decide_beta<<<blocks_for((int64_t)std::max(1, s.K - 1) * s.G, 256), 256, 0, st>>>(s);
+      k_decide_beta<<<blocks_for((int64_t)std::max(1, s.K - 1) * s.G, 32), DEC_THREADS, 0, st>>>(s);
       LAUNCH_CHECK("k_decide_beta");
       break;
     case 6:
-      k_decide_nu_E<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      k_decide_nu_E<<<blocks_for((int64_t)s.B * s.G, 32), DEC_THREADS, 0, st>>>(s);
       LAUNCH_CHECK("k_decide_nu_E");
       break;
     case 7:
@@ -142,7 +142,7 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
       LAUNCH_CHECK("k_hmc_dll_static");
       break;
     case 9:
-      k_decide_phi<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s);
+      k_decide_phi<<<blocks_for((int64_t)s.B * s.G, 32), DEC_THREADS, 0, st>>>(s);
       LAUNCH_CHECK("k_decide_phi");
       break;
     case 10:

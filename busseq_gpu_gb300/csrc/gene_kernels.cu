@@ -1032,18 +1032,63 @@ __global__ void __launch_bounds__(GENE_TILE) k_decide_alpha(DevState s) {
 }
 
 // beta_gk for k >= 1: one thread per (k, g) (BUSseq_gpu.cu:696-707).
-__global__ void k_decide_beta(DevState s) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t G = s.G, Gp = s.Gp;
-  if (t >= (int64_t)(s.K - 1) * G) return;
-  const uint32_t iter = (uint32_t)*s.iter;
-  const int k = 1 + (int)(t / G);
-  const int64_t g = t % G;
-  double Sx = 0.0, Lb = 0.0;
-  for (int b = 0; b < s.B; ++b) {
-    Sx += seg_sum(s, b, k, 0, g);
-    Lb += seg_sum(s, b, k, 1, g);
+// The per-gene decisions below take 32 genes per CTA, each gene split over
+// DEC_SLICES warps: warp w sums the chunk partials of the segments w, w +
+// DEC_SLICES, ... (batches for beta, types for nu and phi) with both slots'
+// loads in flight, and warp 0 adds the slices in a fixed order and decides.
+// A thread per gene with one segment after the other would wait for every
+// segment's loads in turn.
+constexpr int DEC_SLICES = DEC_THREADS / 32;
+
+// Both slots' sums over the chunks c of range r of gene g.
+__device__ __forceinline__ void chunk_sums2(const DevState& s, int2 r, int slot_a, int slot_b, int64_t g, double& a,
+                                            double& b) {
+  const int64_t Gp = s.Gp;
+#pragma unroll 2
+  for (int c = r.x; c < r.x + r.y; ++c) {
+    a += __ldg(&s.part[((int64_t)c * NSLOT + slot_a) * Gp + g]);
+    b += __ldg(&s.part[((int64_t)c * NSLOT + slot_b) * Gp + g]);
   }
+}
+
+// One slot's sum over the chunks c of range r of gene g.
+__device__ __forceinline__ void chunk_sums1(const DevState& s, int2 r, int slot, int64_t g, double& a) {
+  const int64_t Gp = s.Gp;
+#pragma unroll 4
+  for (int c = r.x; c < r.x + r.y; ++c) a += __ldg(&s.part[((int64_t)c * NSLOT + slot) * Gp + g]);
+}
+
+// The slices' two sums of gene lane, added in slice order (valid in warp 0).
+__device__ __forceinline__ void dec_combine(double (&sm)[DEC_SLICES][2][32], int sl, int lane, double& a, double& b) {
+  sm[sl][0][lane] = a;
+  sm[sl][1][lane] = b;
+  __syncthreads();
+  if (sl == 0) {
+    a = sm[0][0][lane];
+    b = sm[0][1][lane];
+#pragma unroll
+    for (int w = 1; w < DEC_SLICES; ++w) {
+      a += sm[w][0][lane];
+      b += sm[w][1][lane];
+    }
+  }
+}
+
+// beta_k,g for k >= 1 (BUSseq_gpu.cu:696-707); slices over batches.
+__global__ void __launch_bounds__(DEC_THREADS) k_decide_beta(DevState s) {
+  __shared__ double sm[DEC_SLICES][2][32];
+  const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * 32 + lane;
+  const int64_t G = s.G, Gp = s.Gp;
+  const bool live = t < (int64_t)(s.K - 1) * G;
+  const int k = live ? 1 + (int)(t / G) : 1;
+  const int64_t g = live ? t % G : 0;
+  double Sx = 0.0, Lb = 0.0;
+  if (live)
+    for (int b = sl; b < s.B; b += DEC_SLICES) chunk_sums2(s, s.seg_chunk[b * s.K + k], 0, 1, g, Sx, Lb);
+  dec_combine(sm, sl, lane, Sx, Lb);
+  if (sl != 0 || !live) return;
+  const uint32_t iter = (uint32_t)*s.iter;
   const int64_t pos = (int64_t)k * Gp + g;
   const float bo = s.beta[pos], bn = s.beta_p[pos];
   const double var = s.L[pos] == 1 ? TAU1 : (double)s.p_tau0[1];
@@ -1056,46 +1101,65 @@ __global__ void k_decide_beta(DevState s) {
   s.beta_acc[pos] = acc ? 1 : 0;
 }
 
-// nu_bg for b >= 1 (BUSseq_gpu.cu:730-737), then E[b][.][g] for every b.
-__global__ void k_decide_nu_E(DevState s) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// nu_b,g for b >= 1 (BUSseq_gpu.cu:730-737), then the table
+// E = exp(alpha + beta + nu) of every type for the new nu; slices over types.
+__global__ void __launch_bounds__(DEC_THREADS) k_decide_nu_E(DevState s) {
+  __shared__ double sm[DEC_SLICES][2][32];
+  __shared__ float s_nu[32];
+  const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * 32 + lane;
   const int64_t G = s.G, Gp = s.Gp;
-  if (t >= (int64_t)s.B * G) return;
-  const uint32_t iter = (uint32_t)*s.iter;
-  const int b = (int)(t / G);
-  const int64_t g = t % G;
+  const bool live = t < (int64_t)s.B * G;
+  const int b = live ? (int)(t / G) : 0;
+  const int64_t g = live ? t % G : 0;
   const int64_t pos = (int64_t)b * Gp + g;
-  if (b > 0) {
-    double Sx = 0.0, Ln = 0.0;
-    for (int k = 0; k < s.K; ++k) {
-      Sx += seg_sum(s, b, k, 0, g);
+  double Sx = 0.0, Ln = 0.0;
+  if (live && b > 0)
+    for (int k = sl; k < s.K; k += DEC_SLICES) {
       const bool bacc = k > 0 && s.beta_acc[(int64_t)k * Gp + g];
-      Ln += seg_sum(s, b, k, bacc ? 3 : 2, g);
+      chunk_sums2(s, s.seg_chunk[b * s.K + k], 0, bacc ? 3 : 2, g, Sx, Ln);
     }
-    const float vo = s.nu[pos], vn = s.nu_p[pos];
-    const double mn = s.mu_nu[b];
-    const double lr = (double)(vn - vo) * Sx - Ln;
-    const double prior = (((double)vo - mn) * ((double)vo - mn) - ((double)vn - mn) * ((double)vn - mn)) /
-                         (2.0 * SIGMA2_NU);
-    const float u = uniform_at(s.seed, SID_NU, (uint64_t)(b - 1) * (uint64_t)G + (uint64_t)g, iter, 2);
-    s.lr_nu[(int64_t)b * G + g] = lr + prior;
-    if ((double)logf(u) <= lr + prior) s.nu[pos] = vn;
+  dec_combine(sm, sl, lane, Sx, Ln);
+  if (sl == 0 && live) {
+    float nv = s.nu[pos];
+    if (b > 0) {
+      const uint32_t iter = (uint32_t)*s.iter;
+      const float vn = s.nu_p[pos];
+      const double mn = s.mu_nu[b];
+      const double lr = (double)(vn - nv) * Sx - Ln;
+      const double prior = (((double)nv - mn) * ((double)nv - mn) - ((double)vn - mn) * ((double)vn - mn)) /
+                           (2.0 * SIGMA2_NU);
+      const float u = uniform_at(s.seed, SID_NU, (uint64_t)(b - 1) * (uint64_t)G + (uint64_t)g, iter, 2);
+      s.lr_nu[(int64_t)b * G + g] = lr + prior;
+      if ((double)logf(u) <= lr + prior) {
+        s.nu[pos] = vn;
+        nv = vn;
+      }
+    }
+    s_nu[lane] = nv;
   }
-  const float a = s.alpha[g], nv = s.nu[pos];
-  for (int k = 0; k < s.K; ++k)
+  __syncthreads();
+  if (!live) return;
+  const float a = s.alpha[g], nv = s_nu[lane];
+  for (int k = sl; k < s.K; k += DEC_SLICES)
     s.E[((int64_t)b * s.K + k) * Gp + g] = exp_sum3(a, s.beta[(int64_t)k * Gp + g], nv);
 }
 
-// phi_bg (BUSseq_gpu.cu:806-818).
-__global__ void k_decide_phi(DevState s) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// phi_b,g (BUSseq_gpu.cu:806-818); slices over types.
+__global__ void __launch_bounds__(DEC_THREADS) k_decide_phi(DevState s) {
+  __shared__ double sm[DEC_SLICES][2][32];
+  const int lane = threadIdx.x & 31, sl = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * 32 + lane;
   const int64_t G = s.G, Gp = s.Gp;
-  if (t >= (int64_t)s.B * G) return;
+  const bool live = t < (int64_t)s.B * G;
+  const int b = live ? (int)(t / G) : 0;
+  const int64_t g = live ? t % G : 0;
+  double S = 0.0, unused = 0.0;
+  if (live)
+    for (int k = sl; k < s.K; k += DEC_SLICES) chunk_sums1(s, s.seg_chunk[b * s.K + k], 0, g, S);
+  dec_combine(sm, sl, lane, S, unused);
+  if (sl != 0 || !live) return;
   const uint32_t iter = (uint32_t)*s.iter;
-  const int b = (int)(t / G);
-  const int64_t g = t % G;
-  double S = 0.0;
-  for (int k = 0; k < s.K; ++k) S += seg_sum(s, b, k, 0, g);
   const int64_t pos = (int64_t)b * Gp + g;
   S += s.phi_static[pos];
   const float ph = s.phi[pos], pp = s.phi_p[pos];
