@@ -863,7 +863,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.phi_static, B * Gp));
       int64_t* nbig;
       TRY(h->alloc(&nbig, nbg));
-      bq::k_phi_hist<<<blocks_for(nbg, 256), 256, 0, h->stream>>>(s, nbig, 0);
+      const dim3 hist_grid((unsigned)s.n_tiles, (unsigned)B);
+      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, 0);
       LAUNCH_CHECK("k_phi_hist");
       std::vector<int64_t> off_h(nbg + 1, 0);
       CUDA_TRY(cudaMemcpyAsync(off_h.data() + 1, nbig, nbg * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
@@ -873,7 +874,7 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       TRY(h->alloc(&s.phi_big_y, std::max<int64_t>(1, off_h[nbg])));
       CUDA_TRY(cudaMemcpyAsync(s.phi_big_off, off_h.data(), (nbg + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
                                h->stream));
-      bq::k_phi_hist<<<blocks_for(nbg, 256), 256, 0, h->stream>>>(s, nbig, 1);
+      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, 1);
       LAUNCH_CHECK("k_phi_hist");
       CUDA_TRY(cudaStreamSynchronize(h->stream));  // off_h leaves scope
     }

@@ -138,17 +138,33 @@ __global__ void k_y_fingerprint(DevState s, unsigned long long* out) {
 
 // Histogram of Y > 0 per batch; warp-aggregated so that repeated small values
 // cost one atomic per distinct value per warp.
-__global__ void k_init_hist(DevState s, int32_t* hist) {
+// One CTA per cell: counts below HIST_SMEM_BINS go to a shared-memory
+// histogram (one shared atomic per distinct value of a warp's 32 counts) and
+// the CTA adds its non-zero bins to the batch's histogram; larger counts go
+// to the global histogram directly.  Counts are integers, so the result does
+// not depend on the order of the additions.
+constexpr int HIST_SMEM_BINS = 4096;
+__global__ void __launch_bounds__(256) k_init_hist(DevState s, int32_t* hist) {
+  __shared__ int sh[HIST_SMEM_BINS];
   const int64_t i = blockIdx.x;
   const int b = s.batch_of[i];
   const int lane = threadIdx.x & 31;
   int32_t* h = hist + (int64_t)b * (s.ymax + 1);
+  const int nbins = min(HIST_SMEM_BINS, s.ymax + 1);
+  for (int t = threadIdx.x; t < nbins; t += blockDim.x) sh[t] = 0;
+  __syncthreads();
   for (int64_t g0 = (int64_t)(threadIdx.x & ~31); g0 < s.Gp; g0 += blockDim.x) {
     const int64_t g = g0 + lane;
     const int y = g < s.G ? s.Y[i * s.Gp + g] : 0;
     const unsigned same = __match_any_sync(0xffffffffu, y);
-    if (y > 0 && __ffs(same) - 1 == lane) atomicAdd(&h[y], __popc(same));
+    if (y > 0 && __ffs(same) - 1 == lane) {
+      if (y < nbins) atomicAdd(&sh[y], __popc(same));
+      else atomicAdd(&h[y], __popc(same));
+    }
   }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nbins; t += blockDim.x)
+    if (sh[t]) atomicAdd(&h[t], sh[t]);
 }
 
 __global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell) {
@@ -306,26 +322,39 @@ __global__ void k_init_finish(DevState s, int fresh) {
 // and the number of larger values into n_big; fill = 1: the larger values
 // into phi_big_y from phi_big_off, in cell order (so every sum over them has a
 // fixed order).
-__global__ void k_phi_hist(DevState s, int64_t* n_big, int fill) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)s.B * s.G) return;
-  const int b = (int)(t / s.G);
-  const int64_t g = t % s.G, Gp = s.Gp;
-  int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
-  int64_t pos = fill ? s.phi_big_off[t] : 0;
+// fill = 0: per (batch, gene), the counts of Y = 1 .. PHI_TAB - 1 (into
+// phi_cnt) and how many Y >= PHI_TAB there are; fill = 1: those larger Y in
+// cell order, at the offsets the host summed from the first pass.  One CTA per
+// (batch, tile of GENE_TILE genes), a thread per gene walking the batch's
+// cells; the first pass counts in shared memory (each thread its own column)
+// and writes the table out once.
+__global__ void __launch_bounds__(GENE_TILE) k_phi_hist(DevState s, int64_t* n_big, int fill) {
+  __shared__ int sc[PHI_TAB][GENE_TILE];
+  const int b = blockIdx.y, tid = threadIdx.x;
+  const int64_t g = (int64_t)blockIdx.x * GENE_TILE + tid, Gp = s.Gp;
+  const bool live = g < s.G;
+  const int64_t t = (int64_t)b * s.G + g;
+  if (!fill)
+    for (int y = 0; y < PHI_TAB; ++y) sc[y][tid] = 0;
+  int64_t pos = fill && live ? s.phi_big_off[t] : 0;
   int64_t nb = 0;
   const int i1 = s.batch_off[b + 1];
+  if (live) {
 #pragma unroll 4
-  for (int i = s.batch_off[b]; i < i1; ++i) {
-    const int y = s.Y[(int64_t)i * Gp + g];
-    if (y >= PHI_TAB) {
-      if (fill) s.phi_big_y[pos++] = y;
-      ++nb;
-    } else if (y > 0 && !fill) {
-      ++cnt[(int64_t)y * Gp];
+    for (int i = s.batch_off[b]; i < i1; ++i) {
+      const int y = s.Y[(int64_t)i * Gp + g];
+      if (y >= PHI_TAB) {
+        if (fill) s.phi_big_y[pos++] = y;
+        ++nb;
+      } else if (y > 0 && !fill) {
+        ++sc[y][tid];
+      }
     }
   }
-  if (!fill) n_big[t] = nb;
+  if (fill || !live) return;
+  int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
+  for (int y = 1; y < PHI_TAB; ++y) cnt[(int64_t)y * Gp] = sc[y][tid];
+  n_big[t] = nb;
 }
 
 // Posterior summaries of the imputation as dense [N][G] tables: E[X] and
