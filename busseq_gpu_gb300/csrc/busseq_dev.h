@@ -60,6 +60,7 @@ constexpr int MAX_B = 128;
 constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
 constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
+constexpr int PHI_HIST_SLICES = 8;  // slices of a batch's cells in the initial count tables of phi
 constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
 constexpr int ZX_UNIT = 512;       // zero entries per Z/X work unit (one warp, one partial)

@@ -334,17 +334,37 @@ int zmask_from_zval(busseq_handle* h) {
 
 // Z as a dense host table [N][G] of int32 (esize 4) or uint8 (esize 1),
 // unpacked from the bit mask on the device.
-int z_to_host(busseq_handle* h, void* dst, int esize) {
+// Z as a dense [N][G] table of int32 (esize 4) or uint8 (esize 1) in a
+// stream-ordered device allocation, enqueued on the handle's stream (the
+// caller copies it and frees it there).
+int z_dense_async(busseq_handle* h, int esize, void** out) {
   const bq::DevState& s = h->s;
-  TRY(zmask_from_zval(h));
-  const size_t bytes = (size_t)s.N * s.G * esize;
+  *out = nullptr;
+  CUDA_TRY(cudaMemsetAsync(s.zm, 0, (size_t)s.N * s.Gw * sizeof(uint32_t), h->stream));
+  if (s.nz0 > 0) {
+    bq::k_zmask_from_zval<<<blocks_for(s.nz0, 256), 256, 0, h->stream>>>(s);
+    LAUNCH_CHECK("k_zmask_from_zval");
+  }
   void* d = nullptr;
-  CUDA_TRY(cudaMallocAsync(&d, bytes, h->stream));
+  CUDA_TRY(cudaMallocAsync(&d, (size_t)s.N * s.G * esize, h->stream));
   const unsigned grid = std::min<unsigned>(blocks_for(s.N * s.Gw, 256), 152 * 16);
   if (esize == 4) bq::k_z_dense_i32<<<grid, 256, 0, h->stream>>>(s, static_cast<int32_t*>(d), s.G);
   else bq::k_z_dense_u8<<<grid, 256, 0, h->stream>>>(s, static_cast<uint8_t*>(d), s.G);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, h->stream);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFreeAsync(d, h->stream);
+    return fail(BUSSEQ_ERR_CUDA, "Z table: %s", cudaGetErrorString(e));
+  }
+  *out = d;
+  return BUSSEQ_OK;
+}
+
+int z_to_host(busseq_handle* h, void* dst, int esize) {
+  const bq::DevState& s = h->s;
+  const size_t bytes = (size_t)s.N * s.G * esize;
+  void* d = nullptr;
+  TRY(z_dense_async(h, esize, &d));
+  cudaError_t e = cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, h->stream);
   const cudaError_t e2 = cudaFreeAsync(d, h->stream);
   if (e == cudaSuccess) e = e2;
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -861,20 +881,32 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       const int64_t nbg = (int64_t)B * G;
       TRY(h->alloc(&s.phi_cnt, (int64_t)B * bq::PHI_TAB * Gp));
       TRY(h->alloc(&s.phi_static, B * Gp));
-      int64_t* nbig;
-      TRY(h->alloc(&nbig, nbg));
-      const dim3 hist_grid((unsigned)s.n_tiles, (unsigned)B);
-      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, 0);
+      const int nsl = bq::PHI_HIST_SLICES;
+      int64_t *nbig, *soff;
+      TRY(h->alloc(&nbig, nsl * nbg, true));
+      TRY(h->alloc(&soff, nsl * nbg, true));
+      const dim3 hist_grid((unsigned)s.n_tiles, (unsigned)B, (unsigned)nsl);
+      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, nullptr, 0);
       LAUNCH_CHECK("k_phi_hist");
-      std::vector<int64_t> off_h(nbg + 1, 0);
-      CUDA_TRY(cudaMemcpyAsync(off_h.data() + 1, nbig, nbg * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+      std::vector<int64_t> n_h((size_t)nsl * nbg), off_h(nbg + 1, 0), soff_h((size_t)nsl * nbg);
+      CUDA_TRY(cudaMemcpyAsync(n_h.data(), nbig, n_h.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
       CUDA_TRY(cudaStreamSynchronize(h->stream));
-      for (int64_t t = 0; t < nbg; ++t) off_h[t + 1] += off_h[t];
+      // the large values of (batch, gene) t in cell order: slice after slice
+      for (int64_t t = 0; t < nbg; ++t) {
+        int64_t p = off_h[t];
+        for (int q = 0; q < nsl; ++q) {
+          soff_h[(size_t)q * nbg + t] = p;
+          p += n_h[(size_t)q * nbg + t];
+        }
+        off_h[t + 1] = p;
+      }
       TRY(h->alloc(&s.phi_big_off, nbg + 1));
       TRY(h->alloc(&s.phi_big_y, std::max<int64_t>(1, off_h[nbg])));
       CUDA_TRY(cudaMemcpyAsync(s.phi_big_off, off_h.data(), (nbg + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
                                h->stream));
-      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, 1);
+      CUDA_TRY(cudaMemcpyAsync(soff, soff_h.data(), soff_h.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               h->stream));
+      bq::k_phi_hist<<<hist_grid, bq::GENE_TILE, 0, h->stream>>>(s, nbig, soff, 1);
       LAUNCH_CHECK("k_phi_hist");
       CUDA_TRY(cudaStreamSynchronize(h->stream));  // off_h leaves scope
     }
@@ -1012,8 +1044,15 @@ int busseq_get_estimates(busseq_handle* h, busseq_estimates* o) {
   const int64_t G = s.G, N = s.N;
   const int B = s.B, K = s.K;
   const bq::Estimates& e = h->est;
+  // Z is unpacked on the handle's stream while the estimates and X go to the
+  // host on the side stream, so the two large reads overlap the unpacking.
+  cudaStream_t side = h->side_stream;
+  CUDA_TRY(cudaEventRecord(h->ev_fork[0], h->stream));
+  CUDA_TRY(cudaStreamWaitEvent(side, h->ev_fork[0], 0));
+  void* zdev = nullptr;
+  if (o->Z) TRY(z_dense_async(h, 4, &zdev));
   auto cp = [&](void* dst, const void* src, size_t bytes) -> int {
-    if (dst) CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    if (dst) CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, side));
     return BUSSEQ_OK;
   };
   TRY(cp(o->gamma, e.gamma, 2 * B * sizeof(double)));
@@ -1026,8 +1065,18 @@ int busseq_get_estimates(busseq_handle* h, busseq_estimates* o) {
   TRY(cp(o->phi, e.phi, B * G * sizeof(double)));
   TRY(cp(o->W, e.W, N * sizeof(int32_t)));
   TRY(cp(o->pi, e.pi, B * K * sizeof(double)));
-  if (o->X) CUDA_TRY(cudaMemcpy2D(o->X, G * 4, s.X, s.Gp * 4, G * 4, N, cudaMemcpyDeviceToHost));
-  if (o->Z) TRY(z_to_host(h, o->Z, 4));
+  if (o->X) CUDA_TRY(cudaMemcpy2DAsync(o->X, G * 4, s.X, s.Gp * 4, G * 4, N, cudaMemcpyDeviceToHost, side));
+  cudaError_t ez = cudaSuccess;
+  if (zdev) {
+    ez = cudaMemcpyAsync(o->Z, zdev, (size_t)N * G * 4, cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t ef = cudaFreeAsync(zdev, h->stream);
+    if (ez == cudaSuccess) ez = ef;
+  }
+  const cudaError_t e1 = cudaStreamSynchronize(side);
+  const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  if (ez != cudaSuccess || e1 != cudaSuccess || e2 != cudaSuccess)
+    return fail(BUSSEQ_ERR_CUDA, "estimates to the host: %s",
+                cudaGetErrorString(ez != cudaSuccess ? ez : e1 != cudaSuccess ? e1 : e2));
   return BUSSEQ_OK;
 }
 

@@ -95,6 +95,7 @@ int check_device_error(busseq_handle* h);
 int launch_sweep(busseq_handle* h, cudaStream_t st, int kept);
 std::vector<int> sweep_sequence(const busseq_handle* h, int kept);
 int zmask_from_zval(busseq_handle* h);
+int z_dense_async(busseq_handle* h, int esize, void** out);
 int z_to_host(busseq_handle* h, void* dst, int esize);
 int capture(busseq_handle* h, int kept, cudaGraphExec_t* out);
 int ensure_estimates(busseq_handle* h);

@@ -322,27 +322,31 @@ __global__ void k_init_finish(DevState s, int fresh) {
 // and the number of larger values into n_big; fill = 1: the larger values
 // into phi_big_y from phi_big_off, in cell order (so every sum over them has a
 // fixed order).
-// fill = 0: per (batch, gene), the counts of Y = 1 .. PHI_TAB - 1 (into
-// phi_cnt) and how many Y >= PHI_TAB there are; fill = 1: those larger Y in
-// cell order, at the offsets the host summed from the first pass.  One CTA per
-// (batch, tile of GENE_TILE genes), a thread per gene walking the batch's
-// cells; the first pass counts in shared memory (each thread its own column)
-// and writes the table out once.
-__global__ void __launch_bounds__(GENE_TILE) k_phi_hist(DevState s, int64_t* n_big, int fill) {
+// fill = 0: per (batch, gene), the counts of Y = 1 .. PHI_TAB - 1 (added
+// into phi_cnt) and, per slice of the batch's cells, how many Y >= PHI_TAB
+// there are (n_big[slice][batch * G + gene]); fill = 1: those larger Y in cell
+// order, each slice from the offset `off` the host summed from the first
+// pass.  One CTA per (tile of GENE_TILE genes, batch, slice of the cells), a
+// thread per gene walking its slice; the first pass counts in shared memory
+// (each thread its own column) and adds the table to phi_cnt once (integer
+// additions: the order does not matter).
+__global__ void __launch_bounds__(GENE_TILE) k_phi_hist(DevState s, int64_t* n_big, const int64_t* off, int fill) {
   __shared__ int sc[PHI_TAB][GENE_TILE];
-  const int b = blockIdx.y, tid = threadIdx.x;
+  const int b = blockIdx.y, sl = blockIdx.z, tid = threadIdx.x;
   const int64_t g = (int64_t)blockIdx.x * GENE_TILE + tid, Gp = s.Gp;
   const bool live = g < s.G;
-  const int64_t t = (int64_t)b * s.G + g;
+  const int64_t t = (int64_t)b * s.G + g, slot = (int64_t)sl * s.B * s.G + t;
   if (!fill)
     for (int y = 0; y < PHI_TAB; ++y) sc[y][tid] = 0;
-  int64_t pos = fill && live ? s.phi_big_off[t] : 0;
+  int64_t pos = fill && live ? off[slot] : 0;
   int64_t nb = 0;
-  const int i1 = s.batch_off[b + 1];
+  const int c0 = s.batch_off[b], nc = s.batch_off[b + 1] - c0;
+  const int i0 = c0 + (int)((int64_t)nc * sl / PHI_HIST_SLICES);
+  const int i1 = c0 + (int)((int64_t)nc * (sl + 1) / PHI_HIST_SLICES);
   if (live) {
-#pragma unroll 4
-    for (int i = s.batch_off[b]; i < i1; ++i) {
-      const int y = s.Y[(int64_t)i * Gp + g];
+#pragma unroll 8
+    for (int i = i0; i < i1; ++i) {
+      const int y = __ldg(s.Y + (int64_t)i * Gp + g);  // read-only: the loads may pass the stores below
       if (y >= PHI_TAB) {
         if (fill) s.phi_big_y[pos++] = y;
         ++nb;
@@ -353,8 +357,9 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi_hist(DevState s, int64_t* n_b
   }
   if (fill || !live) return;
   int32_t* cnt = s.phi_cnt + (int64_t)b * PHI_TAB * Gp + g;
-  for (int y = 1; y < PHI_TAB; ++y) cnt[(int64_t)y * Gp] = sc[y][tid];
-  n_big[t] = nb;
+  for (int y = 1; y < PHI_TAB; ++y)
+    if (sc[y][tid]) atomicAdd(cnt + (int64_t)y * Gp, sc[y][tid]);
+  n_big[slot] = nb;
 }
 
 // Posterior summaries of the imputation as dense [N][G] tables: E[X] and

@@ -30,7 +30,7 @@ __global__ void k_decide_beta(DevState s);
 __global__ void k_decide_nu_E(DevState s);
 __global__ void k_phi(DevState s);
 __global__ void k_phi_static(DevState s);
-__global__ void k_phi_hist(DevState s, int64_t* n_big, int fill);
+__global__ void k_phi_hist(DevState s, int64_t* n_big, const int64_t* off, int fill);
 __global__ void k_decide_phi(DevState s);
 __global__ void k_delta(DevState s);
 __global__ void k_w_mh(DevState s);
