@@ -46,7 +46,7 @@ class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("p0", C.c_double), ("w_update", C.c_int32), ("keep_draws", C.c_int32),
                 ("device", C.c_int32), ("chunk_cells", C.c_int32), ("hmc_leapfrog", C.c_int32),
                 ("zx_summaries", C.c_int32), ("hmc_gene_accept", C.c_int32), ("test_nb_inv_cap", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("zx_unit", C.c_int32), ("zx_ctas_per_sm", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Estimates(C.Structure):
@@ -118,6 +118,7 @@ def lib():
         "busseq_batch_destroy": ([H], None),
         "busseq_autotune_chunk": ([C.POINTER(Dims), C.c_void_p, C.c_int32, C.POINTER(Options), _PI32, C.c_int32,
                                    C.c_int32, _PI32, _PD], C.c_int),
+        "busseq_autotune": ([C.POINTER(Dims), C.c_void_p, C.c_int32, C.POINTER(Options), C.c_int32, _PD], C.c_int),
         "busseq_get_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_set_state": ([H, C.POINTER(State)], C.c_int),
         "busseq_run_stage": ([H, C.c_int32, C.c_int32, C.c_int32], C.c_int),
@@ -232,6 +233,28 @@ def autotune_chunk(Y, n_b, K: int, seed: int = 0, candidates=(64, 128, 192, 256)
     return int(best.value), {int(c): float(m) for c, m in zip(cand, ms)}
 
 
+def autotune(Y, n_b, K: int, seed: int = 0, sweeps: int = 8, hmc_leapfrog: int = 0, device: int = 0) -> dict:
+    """Launch shapes (gene-pass chunk length, Z/X work-unit length, Z/X CTAs
+    per SM) chosen by busseq_autotune's coordinate descent over burn-in sweeps
+    of scratch chains.  Returns the keyword arguments for Sampler and the
+    time per sweep they gave: {"chunk_cells", "zx_unit", "zx_ctas_per_sm",
+    "ms_per_sweep"}."""
+    n_b = np.ascontiguousarray(n_b, dtype=np.int32)
+    on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
+    if on_dev:
+        yptr, G = C.c_void_p(Y.data_ptr()), int(Y.shape[1])
+    else:
+        Yh = np.ascontiguousarray(Y, dtype=np.int32)
+        yptr, G = Yh.ctypes.data_as(C.c_void_p), int(Yh.shape[1])
+    dims = Dims(len(n_b), int(K), G, _p(n_b, _PI32))
+    opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=0.25, w_update=W_MH, keep_draws=0, device=int(device),
+                  chunk_cells=0, hmc_leapfrog=int(hmc_leapfrog))
+    ms = C.c_double()
+    _check(lib().busseq_autotune(C.byref(dims), yptr, int(on_dev), C.byref(opt), int(sweeps), C.byref(ms)))
+    return {"chunk_cells": int(opt.chunk_cells), "zx_unit": int(opt.zx_unit),
+            "zx_ctas_per_sm": int(opt.zx_ctas_per_sm), "ms_per_sweep": float(ms.value)}
+
+
 def estimate_buffers(B: int, K: int, G: int, N: int, with_XZ: bool = True, alloc=np.zeros) -> dict:
     """Arrays of the shapes and types Sampler.estimates() fills; ``alloc(shape,
     dtype)`` may return pinned host memory (for instance through torch) to speed
@@ -293,7 +316,8 @@ class Sampler:
 
     def __init__(self, Y, n_b, K: int, seed: int = 0, p0: float = 0.25, w_update: str | int = "mh",
                  keep_draws: bool = False, device: int = 0, chunk_cells: int = 0, hmc_leapfrog: int = 0,
-                 zx_summaries: bool = False, hmc_gene_accept: bool = False, test_nb_inv_cap: int = 0):
+                 zx_summaries: bool = False, hmc_gene_accept: bool = False, test_nb_inv_cap: int = 0,
+                 zx_unit: int = 0, zx_ctas_per_sm: int = 0):
         L = lib()
         self.n_b = np.ascontiguousarray(n_b, dtype=np.int32)
         self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
@@ -304,7 +328,8 @@ class Sampler:
         opt = Options(seed=int(seed) & 0xFFFFFFFFFFFFFFFF, p0=float(p0), w_update=int(w_update),
                       keep_draws=int(bool(keep_draws)), device=int(device), chunk_cells=int(chunk_cells),
                       hmc_leapfrog=int(hmc_leapfrog), zx_summaries=int(bool(zx_summaries)),
-                      hmc_gene_accept=int(bool(hmc_gene_accept)), test_nb_inv_cap=int(test_nb_inv_cap))
+                      hmc_gene_accept=int(bool(hmc_gene_accept)), test_nb_inv_cap=int(test_nb_inv_cap),
+                      zx_unit=int(zx_unit), zx_ctas_per_sm=int(zx_ctas_per_sm))
         on_dev = hasattr(Y, "data_ptr") and getattr(Y, "is_cuda", False)
         if on_dev:
             assert Y.dtype.__str__().endswith("int32") and Y.is_contiguous() and Y.dim() == 2

@@ -1,5 +1,5 @@
-// Batches of chains launched as one CUDA graph per sweep, and the gene-pass
-// chunk autotuner (neither in the reference).
+// Batches of chains launched as one CUDA graph per sweep, and the autotuners
+// of the launch shapes (neither in the reference).
 #include "capi_internal.h"
 
 #include <vector>
@@ -142,8 +142,34 @@ void busseq_batch_destroy(busseq_batch* b) {
   delete b;
 }
 
+// Milliseconds per sweep of `sweeps` timed burn-in sweeps (after `warm`
+// untimed ones) of a scratch handle with options `o` on the given counts.
+static int time_sweeps(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, busseq_options o,
+                       int32_t sweeps, double* ms_per_sweep) {
+  const int warm = 3;
+  o.keep_draws = 0;
+  busseq_handle* h = nullptr;
+  TRY(busseq_create(dims, Y, Y_is_device, &o, &h));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int r = busseq_begin(h, warm + sweeps, warm + sweeps, 0);
+  if (r == BUSSEQ_OK) r = busseq_sweeps(h, warm);
+  if (r == BUSSEQ_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    r = fail(BUSSEQ_ERR_CUDA, "cudaEventCreate failed");
+  float ms = 0.0f;
+  if (r == BUSSEQ_OK && cudaEventRecord(e0, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
+  if (r == BUSSEQ_OK) r = busseq_sweeps(h, sweeps);
+  if (r == BUSSEQ_OK && cudaEventRecord(e1, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
+  if (r == BUSSEQ_OK) r = check_device_error(h);
+  if (r == BUSSEQ_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event time");
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  busseq_destroy(h);
+  if (r == BUSSEQ_OK) *ms_per_sweep = (double)ms / sweeps;
+  return r;
+}
+
 // Gene-pass chunk length by measurement: for every candidate, a scratch
-// handle on the same counts (a device copy when Y is on the host) runs `warm`
+// handle on the same counts (a device copy when Y is on the host) runs three
 // untimed and `sweeps` timed burn-in sweeps; the fastest candidate wins.  The
 // scratch handles use the options' seed, so the caller's chains are untouched.
 int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, const busseq_options* opt,
@@ -151,7 +177,6 @@ int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_i
                           double* ms_per_sweep) {
   if (!dims || !Y || !opt || !candidates || n_cand <= 0 || sweeps <= 0 || !best)
     return fail(BUSSEQ_ERR_ARG, "bad autotune arguments");
-  const int warm = 3;
   double best_ms = 0.0;
   *best = 0;
   for (int c = 0; c < n_cand; ++c) {
@@ -159,31 +184,57 @@ int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_i
       return fail(BUSSEQ_ERR_ARG, "chunk candidate %d outside 1..%d", candidates[c], bq::MAX_CG);
     busseq_options o = *opt;
     o.chunk_cells = candidates[c];
-    o.keep_draws = 0;
-    busseq_handle* h = nullptr;
-    TRY(busseq_create(dims, Y, Y_is_device, &o, &h));
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int r = busseq_begin(h, warm + sweeps, warm + sweeps, 0);
-    if (r == BUSSEQ_OK) r = busseq_sweeps(h, warm);
-    if (r == BUSSEQ_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
-      r = fail(BUSSEQ_ERR_CUDA, "cudaEventCreate failed");
-    float ms = 0.0f;
-    if (r == BUSSEQ_OK && cudaEventRecord(e0, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
-    if (r == BUSSEQ_OK) r = busseq_sweeps(h, sweeps);
-    if (r == BUSSEQ_OK && cudaEventRecord(e1, h->stream) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event record");
-    if (r == BUSSEQ_OK) r = check_device_error(h);
-    if (r == BUSSEQ_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(BUSSEQ_ERR_CUDA, "event time");
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    busseq_destroy(h);
-    if (r != BUSSEQ_OK) return r;
-    const double per = (double)ms / sweeps;
+    double per = 0.0;
+    TRY(time_sweeps(dims, Y, Y_is_device, o, sweeps, &per));
     if (ms_per_sweep) ms_per_sweep[c] = per;
     if (*best == 0 || per < best_ms) {
       best_ms = per;
       *best = candidates[c];
     }
   }
+  return BUSSEQ_OK;
+}
+
+// Launch shapes by coordinate descent: the chunk length, then the Z/X unit
+// length, then the Z/X CTAs per SM, each set to its fastest candidate with the
+// others held; the pass is repeated once if it moved any of them.
+int busseq_autotune(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, busseq_options* opt,
+                    int32_t sweeps, double* ms_per_sweep) {
+  if (!dims || !Y || !opt || sweeps <= 0) return fail(BUSSEQ_ERR_ARG, "bad autotune arguments");
+  static const int32_t chunk_c[] = {64, 128, 192, 256};
+  static const int32_t unit_c[] = {128, 256, 384, 512};
+  static const int32_t ctas_c[] = {2, 3, 4};
+  busseq_options cur = *opt;
+  if (cur.chunk_cells <= 0) cur.chunk_cells = bq::MAX_CG;
+  if (cur.zx_unit <= 0) cur.zx_unit = bq::ZX_UNIT;
+  if (cur.zx_ctas_per_sm <= 0) cur.zx_ctas_per_sm = bq::ZX_CTAS_PER_SM;
+  double best_ms = 0.0;
+  TRY(time_sweeps(dims, Y, Y_is_device, cur, sweeps, &best_ms));
+  for (int pass = 0; pass < 2; ++pass) {
+    bool moved = false;
+    for (int knob = 0; knob < 3; ++knob) {
+      const int32_t* cand = knob == 0 ? chunk_c : knob == 1 ? unit_c : ctas_c;
+      const int n = knob == 2 ? 3 : 4;
+      for (int c = 0; c < n; ++c) {
+        busseq_options o = cur;
+        int32_t* field = knob == 0 ? &o.chunk_cells : knob == 1 ? &o.zx_unit : &o.zx_ctas_per_sm;
+        if (*field == cand[c]) continue;
+        *field = cand[c];
+        double per = 0.0;
+        TRY(time_sweeps(dims, Y, Y_is_device, o, sweeps, &per));
+        if (per < best_ms) {
+          best_ms = per;
+          cur = o;
+          moved = true;
+        }
+      }
+    }
+    if (!moved) break;
+  }
+  opt->chunk_cells = cur.chunk_cells;
+  opt->zx_unit = cur.zx_unit;
+  opt->zx_ctas_per_sm = cur.zx_ctas_per_sm;
+  if (ms_per_sweep) *ms_per_sweep = best_ms;
   return BUSSEQ_OK;
 }
 

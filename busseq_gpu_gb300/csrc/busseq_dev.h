@@ -63,7 +63,7 @@ constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
 constexpr int PHI_HIST_SLICES = 8;  // slices of a batch's cells in the initial count tables of phi
 constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
-constexpr int ZX_UNIT = 512;       // zero entries per Z/X work unit (one warp, one partial)
+constexpr int ZX_UNIT = 512;       // most zero entries per Z/X work unit (one warp, one partial)
 constexpr int ZX_HIST = 128;       // counts below this read the gamma terms from a per-batch table
 constexpr int ZX_CTAS_PER_SM = 4;  // resident Z/X CTAs per SM (the kernel's launch bound)
 constexpr int ZGP_UNITS = 4;       // Z/X work units per chunk of the Gamma-Poisson pass
@@ -232,8 +232,9 @@ struct DevState {
                       // (zero between launches)
   int zx_ctas;        // Z/X CTAs per launch (resident on every SM)
   // The NB proposals drawn as Gamma-Poisson mixtures, left by k_zx to k_zx_gp:
-  int4* zgp_rec;            // [n_zcta][ZX_UNIT] each unit's, in unit order: {list entry, cell, gene, X}
-  float2* zgp_mp;           // [n_zcta][ZX_UNIT] and their {mu, phi}
+  int4* zgp_rec;            // [nz0] each unit's, in unit order from the unit's first list entry on:
+                            // {list entry, cell, gene, X}
+  float2* zgp_mp;           // [nz0] and their {mu, phi}
   int32_t* zgp_cnt;         // [n_zcta] how many each unit has
   const int4* zgchunk;      // [n_gchunk] {first unit, units, batch, 0}: ZGP_UNITS units of one batch
   const int32_t* gfirst;    // [B+1] first chunk of each batch

@@ -788,14 +788,16 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     std::vector<int64_t> rowoff_h(N + 1, 0);
     for (int64_t i = 0; i < N; ++i) rowoff_h[i + 1] = rowoff_h[i] + rowcnt_h[i];
     s.nz0 = rowoff_h[N];
+    // work units of zx_unit entries (the options' launch shape, at most ZX_UNIT)
+    const int64_t zx_unit = opt.zx_unit > 0 ? std::max(16, std::min(opt.zx_unit, bq::ZX_UNIT)) : bq::ZX_UNIT;
     std::vector<int2> zcta_h;
     std::vector<int32_t> zbatch_h, zfirst_h(B + 1, 0);
     for (int b = 0; b < B; ++b) {
       zfirst_h[b] = (int32_t)zcta_h.size();
       const int64_t lo = rowoff_h[h->off[b]], hi = rowoff_h[h->off[b + 1]];
-      for (int64_t e = lo; e < hi; e += bq::ZX_UNIT) {
+      for (int64_t e = lo; e < hi; e += zx_unit) {
         if (e > INT_MAX) return fail(BUSSEQ_ERR_ARG, "too many zero counts (more than 2^31)");
-        zcta_h.push_back(make_int2((int)e, (int)std::min<int64_t>(bq::ZX_UNIT, hi - e)));
+        zcta_h.push_back(make_int2((int)e, (int)std::min<int64_t>(zx_unit, hi - e)));
         zbatch_h.push_back(b);
       }
     }
@@ -825,8 +827,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.n_gchunk = (int)zgchunk_h.size();
     int4* zgchunk;
     int32_t* gfirst;
-    TRY(h->alloc(&s.zgp_rec, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
-    TRY(h->alloc(&s.zgp_mp, (int64_t)std::max(1, s.n_zcta) * bq::ZX_UNIT));
+    TRY(h->alloc(&s.zgp_rec, std::max<int64_t>(1, s.nz0)));
+    TRY(h->alloc(&s.zgp_mp, std::max<int64_t>(1, s.nz0)));
     TRY(h->alloc(&s.zgp_cnt, std::max(1, s.n_zcta)));
     TRY(h->alloc(&zgchunk, std::max(1, s.n_gchunk)));
     TRY(h->alloc(&gfirst, B + 1));
@@ -835,7 +837,8 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
       int nsm = 0;
       CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, opt.device));
       const int64_t want = (s.n_zcta + bq::ZX_THREADS / 32 - 1) / (bq::ZX_THREADS / 32);
-      s.zx_ctas = (int)std::max<int64_t>({(int64_t)s.n_static, std::min<int64_t>(want, (int64_t)nsm * bq::ZX_CTAS_PER_SM),
+      const int per_sm = opt.zx_ctas_per_sm > 0 ? std::min(opt.zx_ctas_per_sm, bq::ZX_CTAS_PER_SM) : bq::ZX_CTAS_PER_SM;
+      s.zx_ctas = (int)std::max<int64_t>({(int64_t)s.n_static, std::min<int64_t>(want, (int64_t)nsm * per_sm),
                                           (int64_t)1});
       const int64_t want_gp = (s.n_gchunk + bq::ZX_THREADS / 32 - 1) / (bq::ZX_THREADS / 32);
       s.zgp_ctas = (int)std::max<int64_t>(std::min<int64_t>(want_gp, (int64_t)nsm * bq::ZGP_CTAS_PER_SM), 1);

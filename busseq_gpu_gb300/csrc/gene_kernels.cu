@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(ZX_THREADS, ZX_CTAS_PER_SM) k_zx(DevState s, i
     const float zthr = 1.0f / (1.0f + expf(gt.g0));
     ZxAcc acc;
     int n_iq = 0, n_gq = 0;  // warp-uniform: the queue's length, the Gamma-Poisson entries listed
-    const int64_t gpo = (int64_t)unit * ZX_UNIT;
+    const int64_t gpo = run.x;  // the unit's record slots: one per entry of the unit
     q.cnt[lane] = 0;
     __syncwarp();
     for (int part = 0; part * ZX_PART < run.y; ++part) {
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(ZX_THREADS, ZGP_CTAS_PER_SM) k_zx_gp(DevState 
         if (p >= __shfl_sync(0xffffffffu, excl, t)) uu = t;
       const int base = __shfl_sync(0xffffffffu, excl, uu);
       if (p < total) {
-        const int64_t o = (int64_t)(ch.x + uu) * ZX_UNIT + (p - base);
+        const int64_t o = (int64_t)s.zcta[ch.x + uu].x + (p - base);
         const int4 ra = s.zgp_rec[o];
         const float2 rb = s.zgp_mp[o];
         const int64_t jj = ra.x;

@@ -83,7 +83,12 @@ typedef struct busseq_options {
                            cap of the Z/X update's NB inversion (default and
                            maximum 1024), so that the cap is reached and the run
                            reports BUSSEQ_ERR_SAMPLER; 0 for every real run      */
-  int32_t reserved[4];
+  int32_t zx_unit;      /* Y == 0 entries per Z/X work unit (a warp's claim),
+                           16..512; 0 = default (512).  Launch shape only: the
+                           draws do not depend on it                          */
+  int32_t zx_ctas_per_sm; /* resident Z/X CTAs per SM, 1..4; 0 = default (4).
+                           Launch shape only                                   */
+  int32_t reserved[2];
 } busseq_options;
 
 /* Posterior estimates (BUSseq_gpu.cu:1557-1813).  Every pointer is a
@@ -322,6 +327,19 @@ int busseq_batch_sweeps(busseq_batch* b, int32_t count);
 int busseq_batch_synchronize(busseq_batch* b);
 void* busseq_batch_stream(busseq_batch* b);  /* the cudaStream_t the batch launches on */
 void busseq_batch_destroy(busseq_batch* b);
+
+/* Autotuner of the launch shapes: by coordinate descent over the gene-pass
+ * chunk length (64, 128, 192, 256 cells), the Z/X work-unit length (128, 256,
+ * 384, 512 entries) and the resident Z/X CTAs per SM (2, 3, 4), each candidate
+ * timed over `sweeps` burn-in sweeps (after 3 untimed ones) of a scratch
+ * handle on the same counts, from the starting values in *opt (0 = default).
+ * Writes the fastest shape into opt->chunk_cells, opt->zx_unit and
+ * opt->zx_ctas_per_sm and its time per sweep into *ms_per_sweep (may be NULL).
+ * None of the three changes a draw: a chain run with the tuned options draws
+ * what it draws with the defaults (up to the order of floating-point partial
+ * sums). */
+int busseq_autotune(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, busseq_options* opt,
+                    int32_t sweeps, double* ms_per_sweep);
 
 /* Autotuner of the gene-pass chunk length (cells of one (batch, type) segment
  * per CTA): times `sweeps` burn-in sweeps of a scratch handle for each of the

@@ -116,7 +116,8 @@ def test_documented_python_api_exists():
                  "hmc_logpost_diff", "hmc_gene_logpost_diff", "get_state", "set_state", "preserved", "profile",
                  "set_stream", "synchronize", "close"):
         assert callable(getattr(bq.Sampler, name, None)), name
-    for name in ("simulate", "read_counts", "write_counts_binary", "autotune_chunk", "Batch", "estimate_buffers"):
+    for name in ("simulate", "read_counts", "write_counts_binary", "autotune_chunk", "autotune", "Batch",
+                 "estimate_buffers"):
         assert callable(getattr(bq, name, None)), name
 
 

@@ -1,5 +1,5 @@
 """Batches of chains (one CUDA graph per sweep holding every chain) and the
-gene-pass chunk autotuner.
+launch-shape autotuners.
 
 A chain run inside a batch must make exactly the draws it makes alone: the
 batch only changes how its kernels are launched (graph branches that run
@@ -111,3 +111,26 @@ def test_autotune_picks_a_candidate_and_the_choice_is_a_valid_chain(data):
     est = s.estimates(with_XZ=False)
     s.close()
     assert np.all(np.isfinite(est["alpha"])) and np.all(np.isfinite(est["phi"]))
+
+
+def test_launch_shape_autotune_and_shapes_keep_the_draws(data):
+    """busseq_autotune returns shapes from its candidate sets; a chain with other
+    Z/X unit lengths and CTA counts imputes exactly the same X and Z in its
+    first sweep (the draws come from each entry's own stream; only the order
+    of the gamma statistics' partial sums moves, which the first sweep's Z/X
+    update does not read)."""
+    Y = data
+    t = bq.autotune(Y, N_B, 4, seed=3, sweeps=3)
+    assert t["chunk_cells"] in (64, 128, 192, 256) and t["zx_unit"] in (128, 256, 384, 512)
+    assert t["zx_ctas_per_sm"] in (2, 3, 4) and t["ms_per_sweep"] > 0
+    states = []
+    for kw in ({}, {"zx_unit": 48, "zx_ctas_per_sm": 1}, {"zx_unit": t["zx_unit"], "zx_ctas_per_sm": t["zx_ctas_per_sm"]}):
+        s = bq.Sampler(Y, N_B, 4, seed=3, **kw)
+        s.begin(4, 4, 0)
+        s.sweeps(1)
+        s.synchronize()
+        states.append(s.get_state())
+        s.close()
+    for st in states[1:]:
+        np.testing.assert_array_equal(st["X"], states[0]["X"])
+        np.testing.assert_array_equal(st["Z"], states[0]["Z"])
