@@ -87,4 +87,93 @@ BQ_BIC_HD double bic_zero_series(double mu, double logp, double log1mp, double p
   return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
 }
 
+// ---------------------------------------------------------------------------
+// The same recurrence in float-float arithmetic (an unevaluated sum hi + lo of
+// two floats, 48 bits of significand): products exact by fmaf, sums exact by
+// TwoSum (Knuth), each result renormalised.  GB300 runs FP64 at a small
+// fraction of its FP32 rate, and the double loop above does two divisions per
+// term; here a term is about sixty FP32 operations.  Each operation errs by a
+// few units of 2^-48 relative, so over the few hundred terms a series takes
+// the sum S errs by below 1e-12 relative and log S by below 1e-12 absolute
+// (tests/test_bic_series.py checks it against the reference's log-space form).
+// The frame is rescaled by 2^+-100 (float range); the loop, its early exit and
+// the x = 1 logarithms are the double version's.  Where the float range does
+// not hold (exp(g0 + g1) above 2^110, phi above 1e6) it defers to the double
+// version.
+struct BicFF {
+  float hi, lo;
+};
+
+BQ_BIC_HD BicFF bff(double v) {
+  const float h = (float)v;
+  return BicFF{h, (float)(v - (double)h)};
+}
+
+BQ_BIC_HD BicFF bff_norm(float s, float e) {  // FastTwoSum, |s| >= |e|
+  const float h = s + e;
+  return BicFF{h, e - (h - s)};
+}
+
+BQ_BIC_HD BicFF bff_add(BicFF a, BicFF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);  // TwoSum error
+  return bff_norm(s, e + (a.lo + b.lo));
+}
+
+BQ_BIC_HD BicFF bff_add1(BicFF a) {  // a + 1
+  return bff_add(a, BicFF{1.0f, 0.0f});
+}
+
+BQ_BIC_HD BicFF bff_mul(BicFF a, BicFF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);  // the product's rounding error, exactly
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return bff_norm(p, e);
+}
+
+BQ_BIC_HD BicFF bff_rcp(BicFF d) {  // 1 / d: the float reciprocal and one correction step
+  const float r = 1.0f / d.hi;
+  const float e = fmaf(-d.hi, r, 1.0f) - d.lo * r;  // 1 - d r
+  return bff_norm(r, r * e);
+}
+
+BQ_BIC_HD BicFF bff_scale(BicFF a, float f) { return BicFF{a.hi * f, a.lo * f}; }  // f a power of two
+
+BQ_BIC_HD double bic_zero_series_ff(double mu, double logp, double log1mp, double phi, double g0, double g1) {
+  const double lw0 = phi * log1mp;  // log NB(0)
+  const double xm = 3.0 * mu;
+  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+  if (x_max <= 1) return lw0;
+  if (!(g1 < 0.0) || g0 + g1 > 76.0 || phi > 1.0e6) return bic_zero_series(mu, logp, log1mp, phi, g0, g1);
+  const double p = exp(logp);
+  const BicFF pf = bff(p), cf = bff(exp(g1)), phif = bff(phi);
+  const float big = 1.2676506e30f, small = 7.888609e-31f;  // 2^100, 2^-100
+  const double ln_big = 100.0 * 0.69314718055994530942;
+  const double s1 = g0 + g1;
+  const double lsig1 = s1 > 0.0 ? -log1p(exp(-s1)) : s1 - log1p(exp(s1));
+  double off = log(phi) + logp + lsig1;
+  BicFF R{1.0f, 0.0f}, acc{1.0f, 0.0f};
+  BicFF F = bff(exp(s1));
+  const bool big_phi = phi > 1.0;
+  for (int x = 1; x + 1 < x_max; ++x) {
+    const float xf = (float)x;  // exact: x < 2^24
+    const BicFF a = bff_mul(bff_mul(bff_add(phif, BicFF{xf, 0.0f}), bff_rcp(BicFF{xf + 1.0f, 0.0f})), pf);
+    const BicFF Fn = bff_mul(F, cf);
+    const BicFF b = bff_mul(bff_mul(cf, bff_add1(F)), bff_rcp(bff_add1(Fn)));
+    const float rho = (big_phi ? a.hi : pf.hi) * b.hi;
+    if (R.hi == 0.0f || (rho < 1.0f && R.hi * rho < 8.6736174e-19f * acc.hi * (1.0f - rho))) break;  // 2^-60
+    F = Fn;
+    R = bff_mul(R, bff_mul(a, b));
+    acc = bff_add(acc, R);
+    if (acc.hi > big) {  // rescale the frame
+      R = bff_scale(R, small);
+      acc = bff_scale(acc, small);
+      off += ln_big;
+    }
+  }
+  const double l1 = off + log((double)acc.hi + (double)acc.lo);
+  return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
+}
+
 }  // namespace bq

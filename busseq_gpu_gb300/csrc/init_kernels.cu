@@ -456,10 +456,11 @@ __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
 // ---------------------------------------------------------------------------
 // BIC.  Per cell i and type k: sum over genes of the dropout-marginal
 // log-likelihood of Y (BUSseq_gpu.cu:967-1007), with the estimates, in double
-// precision throughout.  For Y = 0 the reference's series over
-// x = 0 .. floor(3 mu)-1 is bic_zero_series (bic_series.h): the same sum by a
-// log-free double recurrence, stopped only once the rest is provably below a
-// quarter of double rounding.
+// precision.  For Y = 0 the reference's series over x = 0 .. floor(3 mu)-1 is
+// bic_zero_series_ff (bic_series.h): the same sum by a log-free recurrence in
+// float-float arithmetic (48-bit significands; FP64 runs at a small fraction
+// of the FP32 rate here), stopped only once the rest is provably below 2^-60
+// of the sum.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik) {
   __shared__ double sh[8 * MAX_K];
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, doubl
       if (logp < -250.0) logp = -250.0;
       if (log1mp < -250.0) log1mp = -250.0;
       if (y) acc[k] += base + y * logp + phi * log1mp;
-      else acc[k] += bic_zero_series(mu, logp, log1mp, phi, g0, g1);
+      else acc[k] += bic_zero_series_ff(mu, logp, log1mp, phi, g0, g1);
     }
   }
   for (int k = 0; k < K; ++k) {

@@ -1,5 +1,6 @@
-"""The double-precision series of the BIC's zero counts (bic_series.h) against
-the reference's own formula (BUSseq_gpu.cu:967-1003), on the CPU.
+"""The series of the BIC's zero counts (bic_series.h), in double precision and
+in the float-float arithmetic the device runs, against the reference's own
+formula (BUSseq_gpu.cu:967-1003), on the CPU.
 
 The header is compiled for the host with g++ and called through ctypes.  The
 reference sums, for Y = 0, log[ NB(0) + sum_{x=1}^{floor(3 mu)-1} NB(x)
@@ -7,7 +8,8 @@ sigmoid(g0 + g1 x) ] term by term in log space with lgamma; it is restated
 here in Python double precision.  The recurrence must agree to 1e-12
 relative (both sides round differently; the truncated tail is below 2^-60 of
 the sum) over means 0.1 to 1100, dispersions 0.4 to 400, and dropout slopes
-down to -2.7 and up to 0 (the log-space fallback).
+down to -2.7 and up to 0 (the log-space fallback); the float-float version to
+2e-12.
 """
 import ctypes as C
 import math
@@ -29,14 +31,19 @@ def series(tmp_path_factory):
     d = tmp_path_factory.mktemp("bic")
     src = d / "s.cpp"
     src.write_text('#include "bic_series.h"\nextern "C" double zs(double mu, double lp, double l1, double phi, '
-                   'double g0, double g1) { return bq::bic_zero_series(mu, lp, l1, phi, g0, g1); }\n')
+                   'double g0, double g1) { return bq::bic_zero_series(mu, lp, l1, phi, g0, g1); }\n'
+                   'extern "C" double zf(double mu, double lp, double l1, double phi, double g0, double g1) '
+                   '{ return bq::bic_zero_series_ff(mu, lp, l1, phi, g0, g1); }\n')
     so = str(d / "s.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I",
+    # no contraction of a * b + c into fma beyond the explicit fmaf calls: the
+    # float-float steps rely on IEEE rounding of each operation
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-I",
                     os.path.join(ROOT, "busseq_gpu_gb300", "csrc"), str(src), "-o", so], check=True)
-    f = C.CDLL(so).zs
-    f.restype = C.c_double
-    f.argtypes = [C.c_double] * 6
-    return f
+    lib = C.CDLL(so)
+    for f in (lib.zs, lib.zf):
+        f.restype = C.c_double
+        f.argtypes = [C.c_double] * 6
+    return lib
 
 
 def _clamped_logs(mu, phi):
@@ -68,11 +75,16 @@ def test_zero_count_series_matches_the_reference_formula(series):
     for _ in range(150):
         cases.append((float(np.exp(rng.uniform(-2.3, 7))), float(np.exp(rng.uniform(-0.9, 6))),
                       float(rng.normal(0, 2)), -float(np.exp(rng.uniform(-7, 1)))))
-    worst = 0.0
+    worst, worst_ff = 0.0, 0.0
     for mu, phi, g0, g1 in cases:
         want, logp, l1 = _reference(mu, phi, g0, g1)
-        got = series(mu, logp, l1, phi, g0, g1)
+        got = series.zs(mu, logp, l1, phi, g0, g1)
         err = abs(got - want) / max(1.0, abs(want))
         assert err <= 1e-12, (mu, phi, g0, g1, got, want)
         worst = max(worst, err)
-    print("worst relative difference", worst)
+        # the float-float version the device runs: the same sum to 48 bits
+        got_ff = series.zf(mu, logp, l1, phi, g0, g1)
+        err_ff = abs(got_ff - want) / max(1.0, abs(want))
+        assert err_ff <= 2e-12, (mu, phi, g0, g1, got_ff, want)
+        worst_ff = max(worst_ff, err_ff)
+    print("worst relative difference: double", worst, "float-float", worst_ff)
