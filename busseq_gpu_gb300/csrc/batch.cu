@@ -200,12 +200,17 @@ int busseq_autotune_chunk(const busseq_dims* dims, const int32_t* Y, int32_t Y_i
 // others held; the pass is repeated once if it moved any of them.
 int busseq_autotune(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device, busseq_options* opt,
                     int32_t sweeps, double* ms_per_sweep) {
-  if (!dims || !Y || !opt || sweeps <= 0) return fail(BUSSEQ_ERR_ARG, "bad autotune arguments");
+  if (!dims || !dims->n_b || dims->B < 1 || !Y || !opt || sweeps <= 0)
+    return fail(BUSSEQ_ERR_ARG, "bad autotune arguments");
   static const int32_t chunk_c[] = {64, 128, 192, 256};
   static const int32_t unit_c[] = {128, 256, 384, 512};
   static const int32_t ctas_c[] = {2, 3, 4};
   busseq_options cur = *opt;
-  if (cur.chunk_cells <= 0) cur.chunk_cells = bq::MAX_CG;
+  if (cur.chunk_cells <= 0) {  // the handle's default (busseq_create)
+    int64_t n = 0;
+    for (int b = 0; b < dims->B; ++b) n += dims->n_b[b];
+    cur.chunk_cells = n / std::max<int64_t>(1, (int64_t)dims->B * dims->K) < 512 ? 128 : bq::MAX_CG;
+  }
   if (cur.zx_unit <= 0) cur.zx_unit = bq::ZX_UNIT;
   if (cur.zx_ctas_per_sm <= 0) cur.zx_ctas_per_sm = bq::ZX_CTAS_PER_SM;
   double best_ms = 0.0;
