@@ -209,7 +209,8 @@ int busseq_autotune(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_devi
   if (cur.chunk_cells <= 0) {  // the handle's default (busseq_create)
     int64_t n = 0;
     for (int b = 0; b < dims->B; ++b) n += dims->n_b[b];
-    cur.chunk_cells = n / std::max<int64_t>(1, (int64_t)dims->B * dims->K) < 512 ? 128 : bq::MAX_CG;
+    cur.chunk_cells =
+        cur.hmc_leapfrog <= 0 && n / std::max<int64_t>(1, (int64_t)dims->B * dims->K) < 512 ? 128 : bq::MAX_CG;
   }
   if (cur.zx_unit <= 0) cur.zx_unit = bq::ZX_UNIT;
   if (cur.zx_ctas_per_sm <= 0) cur.zx_ctas_per_sm = bq::ZX_CTAS_PER_SM;

@@ -642,11 +642,14 @@ int busseq_create(const busseq_dims* dims, const int32_t* Y, int32_t Y_is_device
     s.Gp = round_up(G, bq::GENE_TILE);
     s.Gw = s.Gp / 32;
     s.n_tiles = (int)((G + bq::GENE_TILE - 1) / bq::GENE_TILE);
-    // default chunk length: 128 cells when a (batch, type) segment averages
-    // under 512 cells (measured at config 1: 1.8 % faster per sweep than 256),
-    // else 256 (config 4: 2 % faster than 128); busseq_autotune tunes it
+    // default chunk length: 128 cells for the random-walk sampler when a
+    // (batch, type) segment averages under 512 cells (config 1: 1.8 % faster
+    // per sweep than 256), else 256 (config 4: 2 % faster than 128; with the
+    // gradient-based update, whose passes build per-chunk digamma tables,
+    // config 2: 0.8 % faster); busseq_autotune tunes it
     const int64_t mean_seg = N / std::max<int64_t>(1, (int64_t)B * K);
-    s.CG = opt.chunk_cells > 0 ? std::min(opt.chunk_cells, bq::MAX_CG) : (mean_seg < 512 ? 128 : bq::MAX_CG);
+    s.CG = opt.chunk_cells > 0 ? std::min(opt.chunk_cells, bq::MAX_CG)
+                               : (opt.hmc_leapfrog <= 0 && mean_seg < 512 ? 128 : bq::MAX_CG);
     s.cap_g = 0;
     s.cap_c = 0;
     for (int b = 0; b < B; ++b) {

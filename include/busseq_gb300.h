@@ -65,9 +65,9 @@ typedef struct busseq_options {
   int32_t w_update;     /* BUSSEQ_W_MH (default) or BUSSEQ_W_GIBBS             */
   int32_t keep_draws;   /* store every kept draw (needed for reference -p)      */
   int32_t device;       /* CUDA device ordinal                                 */
-  int32_t chunk_cells;  /* cells per gene-pass chunk; 0 = default (128 when a
-                           (batch, type) segment averages under 512 cells,
-                           else 256)                                           */
+  int32_t chunk_cells;  /* cells per gene-pass chunk; 0 = default (128 for the
+                           random-walk sampler when a (batch, type) segment
+                           averages under 512 cells, else 256)                 */
   int32_t hmc_leapfrog; /* 0: random-walk MH for alpha, beta, nu, delta, phi (the
                            reference's sampler); L > 0: one Hamiltonian Monte Carlo
                            transition of that block per sweep with L leapfrog
