@@ -336,8 +336,13 @@ __global__ void __launch_bounds__(GENE_TILE) k_phi_hist(DevState s, int64_t* n_b
   const int64_t g = (int64_t)blockIdx.x * GENE_TILE + tid, Gp = s.Gp;
   const bool live = g < s.G;
   const int64_t t = (int64_t)b * s.G + g, slot = (int64_t)sl * s.B * s.G + t;
-  if (!fill)
+  if (fill) {
+    // only the slices that hold large values walk their cells again (a
+    // warp-uniform exit: the first pass's counts are in n_big)
+    if (!__any_sync(0xffffffffu, live && n_big[slot] > 0)) return;
+  } else {
     for (int y = 0; y < PHI_TAB; ++y) sc[y][tid] = 0;
+  }
   int64_t pos = fill && live ? off[slot] : 0;
   int64_t nb = 0;
   const int c0 = s.batch_off[b], nc = s.batch_off[b + 1] - c0;
