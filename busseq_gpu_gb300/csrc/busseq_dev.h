@@ -59,7 +59,7 @@ constexpr int W_SMEM = X_STAGES * CELL_TILE * W_WIDTH * (int)sizeof(int);
 constexpr int MAX_B = 128;
 constexpr int MAX_K = 64;
 constexpr int NSLOT = 4;           // partial-sum slots per (chunk, gene)
-constexpr int GSLOT = 8;           // gamma statistics per gene-pass CTA
+constexpr int GSLOT = 8;           // slots of a Z/X partial of the gamma statistics (6 used)
 constexpr int PHI_HIST_SLICES = 8;  // slices of a batch's cells in the initial count tables of phi
 constexpr int PHI_TAB = 64;        // counts below this read lgamma differences from a table
 constexpr int ZX_THREADS = 256;    // threads of a Z/X CTA
@@ -218,13 +218,13 @@ struct DevState {
   int64_t nz0;
   const int2* zcta;         // [n_zcta] Z/X work units {first entry, count}, each inside one batch
   const int32_t* zcta_batch;
-  const int32_t* zfirst;    // [B+1] first run of each batch
+  const int32_t* zfirst;    // [B+1] first unit of each batch
   int n_zcta;
   uint8_t* beta_acc;        // [K][Gp] accepted beta of the current sweep
 
   // scratch (partial sums and completion counters)
   double* part;    // [cap_g][NSLOT][Gp]
-  double* gpart;   // [n_zcta][GSLOT]
+  double* gpart;   // [n_zcta][GSLOT] each Z/X unit's gamma statistics (k_zx)
   double* gstat;   // [n_static][4]
   float4* zx_gtab;    // [B][ZX_HIST] per count x < ZX_HIST: softplus(-g0 - g1 x) and the three gamma
                       // terms of the sweep's proposals (built by k_propose)
@@ -238,7 +238,8 @@ struct DevState {
   int32_t* zgp_cnt;         // [n_zcta] how many each unit has
   const int4* zgchunk;      // [n_gchunk] {first unit, units, batch, 0}: ZGP_UNITS units of one batch
   const int32_t* gfirst;    // [B+1] first chunk of each batch
-  double* gpart_gp;         // [n_gchunk][GSLOT] gamma statistics of each chunk's draws
+  double* gpart_gp;         // [n_gchunk][GSLOT] each chunk's gamma statistics: its units' partials
+                            // plus its Gamma-Poisson draws (what k_decide_gamma reads)
   int n_gchunk;
   int zgp_ctas;             // k_zx_gp CTAs per launch
   double* tpart;   // per-CTA sums: [n_tiles][MAX_B] at initialisation, [ceil(G / 32)][2] in k_decide_alpha
