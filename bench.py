@@ -288,10 +288,11 @@ def _config(name="config1", n_b=None, cfg=None):
 
 def run_batch(args, cfg, rank, world, local):
     """Config 3: the config-1 data fitted by one chain per K = 3 .. 10 (the BIC
-    sweep over K).  Each chain's gene-pass chunk length comes from the
-    autotuner.  The sequential arm times each chain alone; the batched arm
-    launches one sweep of all chains as one CUDA graph.  Both arms run the same
-    sweeps of the same chains; the metric is chain-sweeps per second."""
+    sweep over K).  Each chain's launch shapes (gene-pass chunk length, Z/X
+    unit length and CTAs per SM) come from the autotuner.  The sequential arm
+    times each chain alone; the batched arm launches one sweep of all chains as
+    one CUDA graph.  Both arms run the same sweeps of the same chains; the
+    metric is chain-sweeps per second."""
     import torch
     import busseq_gpu_gb300 as bq
 
@@ -305,14 +306,14 @@ def run_batch(args, cfg, rank, world, local):
     ks = list(cfg["ks"])
     Yd = torch.from_numpy(Y).to(dev)
     t0 = time.perf_counter()
-    tuned = {K: bq.autotune_chunk(Yd, n_b, K, seed=seed, sweeps=6, device=local) for K in ks}
+    tuned = {K: bq.autotune(Yd, n_b, K, seed=seed, sweeps=6, device=local) for K in ks}
+    shape = {K: {k: v for k, v in tuned[K].items() if k != "ms_per_sweep"} for K in ks}
     tune_s = time.perf_counter() - t0
     total = args.warmup + args.steps
     burn = args.warmup + args.steps // 2
 
     def chains():
-        return [bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank + K, device=local, chunk_cells=tuned[K][0])
-                for K in ks]
+        return [bq.Sampler(Yd, n_b, K, seed=seed + 7919 * rank + K, device=local, **shape[K]) for K in ks]
 
     def ev():
         return torch.cuda.Event(enable_timing=True)
@@ -371,7 +372,7 @@ def run_batch(args, cfg, rank, world, local):
     Yh = Yp.numpy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    cs = [bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank + K, device=local, chunk_cells=tuned[K][0]) for K in ks]
+    cs = [bq.Sampler(Yh, n_b, K, seed=seed + 7919 * rank + K, device=local, **shape[K]) for K in ks]
     for c in cs:
         c.begin(args.steps, args.steps // 2, min(args.warmup, args.steps))
     with bq.Batch(cs) as b2:
@@ -394,7 +395,7 @@ def run_batch(args, cfg, rank, world, local):
             "data": "synthetic (BUSseq generative model, seed %d, K = 8)" % seed,
             "config": {"workload": "config3: the config-1 data (B=4 x %d cells, G=%d) fitted by %d chains, K = %s, "
                                    "batched: one CUDA graph per sweep of all chains" % (n_b[0], G, len(ks), ks),
-                       "N": N, "G": G, "Ks": ks, "chunk_cells": {str(K): tuned[K][0] for K in ks},
+                       "N": N, "G": G, "Ks": ks, "launch_shapes": {str(K): shape[K] for K in ks},
                        "l2": "no flush: every chain's X and Y are %.0f MB" % (N * G * 4 / 1e6)},
             "sequential": {"value": seq_value, "unit": "chain-sweeps/s", "ms": seq_total,
                            "ms_per_chain": {str(K): v for K, v in seq_ms.items()},
@@ -415,8 +416,7 @@ def run_batch(args, cfg, rank, world, local):
                         "sweeps, 10 timed)"},
             # per chain-sweep, every chain passes over its own copy of the tensor
             "sweep_roofline": sweep_roofline(N, G, 0, value / world, _peak_hbm()[0]),
-            "autotune": {"seconds": tune_s, "ms_per_sweep": {str(K): {str(c): m for c, m in tuned[K][1].items()}
-                                                             for K in ks}},
+            "autotune": {"seconds": tune_s, "ms_per_sweep": {str(K): tuned[K]["ms_per_sweep"] for K in ks}},
             "bic": {str(K): v for K, v in bic.items()}, "k_min_bic": k_best,
             "e2e": {"value": len(ks) * args.steps / e2e_s, "unit": "chain-sweeps/s",
                     "h2d_bytes_per_step": len(ks) * Y.nbytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,

@@ -46,8 +46,9 @@ const char* const kKernelNames[] = {"k_propose",      "k_zx",           "k_alpha
                                     "k_hmc_start_blocks", "k_hmc_leap_blocks0", "k_hmc_leap_blocks",
                                     "k_hmc_energy_blocks", "k_hmc_mass", "k_hmc_grad_start",
                                     "k_hmc_assemble_start", "k_phi_static", "k_hmc_dll_static",
-                                    "k_hmc_accept_genes", "k_zx_gp", "k_decide_gamma"};
-constexpr int kNumKernels = 36;
+                                    "k_hmc_accept_genes", "k_zx_gp", "k_decide_gamma",
+                                    "k_propose_phi"};
+constexpr int kNumKernels = 37;
 enum : int {
   KID_PROPOSE = 0, KID_ZX = 1, KID_ALPHA = 2, KID_DECIDE_ALPHA = 3, KID_BETA_NU = 4, KID_DECIDE_BETA = 5,
   KID_DECIDE_NU_E = 6, KID_DELTA = 7, KID_PHI = 8, KID_DECIDE_PHI = 9, KID_W = 10, KID_SORT_PI = 11,
@@ -56,7 +57,7 @@ enum : int {
   KID_HMC_FINISH = 22, KID_HMC_METRIC_BLOCKS = 23, KID_HMC_START_BLOCKS = 24, KID_HMC_LEAP_BLOCKS0 = 25,
   KID_HMC_LEAP_BLOCKS = 26, KID_HMC_ENERGY_BLOCKS = 27, KID_HMC_MASS = 28, KID_HMC_GRAD_START = 29,
   KID_HMC_ASSEMBLE_START = 30, KID_PHI_STATIC = 31, KID_HMC_DLL_STATIC = 32, KID_HMC_ACCEPT_GENES = 33,
-  KID_ZX_GP = 34, KID_DECIDE_GAMMA = 35
+  KID_ZX_GP = 34, KID_DECIDE_GAMMA = 35, KID_PROPOSE_PHI = 36
 };
 
 }  // namespace
@@ -87,9 +88,15 @@ int launch_kernel(busseq_handle* h, int which, cudaStream_t st, int kept, const 
   const dim3 gene_grid(s.n_tiles, s.cap_g);
   switch (which) {
     case 0:
+      // the random-walk sweep's phi proposals are KID_PROPOSE_PHI's
       k_propose<<<blocks_for(propose_count(s), 256), 256, 0, st>>>(
-          s, s.hmc_L > 0 ? (int)(s.hmc_gene ? PROP_GAMMA | PROP_DELTA : PROP_GAMMA) : (int)PROP_ALL);
+          s, s.hmc_L > 0 ? (int)(s.hmc_gene ? PROP_GAMMA | PROP_DELTA : PROP_GAMMA) : (int)(PROP_ALL & ~PROP_PHI),
+          0);
       LAUNCH_CHECK("k_propose");
+      break;
+    case KID_PROPOSE_PHI:
+      k_propose<<<blocks_for((int64_t)s.B * s.G, 256), 256, 0, st>>>(s, PROP_PHI, propose_phi_offset(s));
+      LAUNCH_CHECK("k_propose_phi");
       break;
     case 1:
       k_zx<<<(unsigned)s.zx_ctas, ZX_THREADS, 0, st>>>(s, kept);
@@ -274,6 +281,7 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
     for (int k = 0; k <= KID_SORT_PI; ++k) {
       if (k == KID_PHI) q.push_back(KID_PHI_STATIC);
       q.push_back(k);
+      if (k == KID_PROPOSE) q.push_back(KID_PROPOSE_PHI);
       if (k == KID_ZX) {
         q.push_back(KID_ZX_GP);
         q.push_back(KID_DECIDE_GAMMA);
@@ -284,13 +292,14 @@ std::vector<int> sweep_sequence(const busseq_handle* h, int kept) {
   return q;
 }
 
-// One sweep, enqueued while `st` is being captured into a graph.  Two
-// kernels leave the main line on the handle's side stream: k_phi_static needs
-// only k_propose's phi proposals and is read by k_decide_phi; the gamma
-// decisions need the Z/X partials of k_zx_gp and are read only by the next
-// sweep (and the posterior accumulation).  Both run beside the main line,
-// filling the SMs that its small decision kernels leave idle; the branch
-// joins before k_decide_phi, or at the end of the sweep.
+// One sweep, enqueued while `st` is being captured into a graph.  Three
+// kernels leave the main line on the handle's side stream: the phi proposals
+// with their lgamma tables and k_phi_static read only phi and the static
+// counts and are first read by k_phi; the gamma decisions need the Z/X
+// partials of k_zx_gp and are read only by the next sweep (and the posterior
+// accumulation).  They run beside the main line, filling the SMs that Z/X's
+// tail and the small decision kernels leave idle; the branch joins before
+// k_phi, or at the end of the sweep.
 int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
   const std::vector<int> seq = sweep_sequence(h, kept);
   cudaStream_t side = h->side_stream;
@@ -309,12 +318,15 @@ int launch_sweep(busseq_handle* h, cudaStream_t st, int kept) {
     open = false;
     return BUSSEQ_OK;
   };
-  const bool has_static = std::find(seq.begin(), seq.end(), (int)KID_PHI_STATIC) != seq.end();
+  const bool has_phi = std::find(seq.begin(), seq.end(), (int)KID_PROPOSE_PHI) != seq.end();
   for (int k : seq) {
-    if (k == KID_PHI_STATIC || k == KID_DECIDE_GAMMA) continue;
-    if (k == KID_DECIDE_PHI || k == KID_POSTERIOR) TRY(join());
+    if (k == KID_PROPOSE_PHI || k == KID_PHI_STATIC || k == KID_DECIDE_GAMMA) continue;
+    if (k == KID_PHI || k == KID_POSTERIOR) TRY(join());
     TRY(launch_kernel(h, k, st, kept, h->s));
-    if (k == KID_PROPOSE && has_static) TRY(fork(KID_PHI_STATIC, 0));
+    if (k == KID_PROPOSE && has_phi) {
+      TRY(fork(KID_PROPOSE_PHI, 0));
+      TRY(launch_kernel(h, KID_PHI_STATIC, side, kept, h->s));
+    }
     if (k == KID_ZX_GP) TRY(fork(KID_DECIDE_GAMMA, 1));
   }
   return join();
@@ -1307,22 +1319,22 @@ int busseq_run_stage(busseq_handle* h, int32_t stage, int32_t iter, int32_t n_un
   };
   switch (stage) {
     case BUSSEQ_STAGE_ZX_GAMMA_ALPHA_L:
-      k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA);
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_GAMMA | PROP_ALPHA, 0);
       LAUNCH_CHECK("k_propose");
       TRY(run({KID_ZX, KID_ZX_GP, KID_DECIDE_GAMMA, 2, 3}));
       break;
     case BUSSEQ_STAGE_BETA_NU:
-      k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU);
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_BETA | PROP_NU, 0);
       LAUNCH_CHECK("k_propose");
       TRY(run({4, 5, 6}));
       break;
     case BUSSEQ_STAGE_DELTA:
-      k_propose<<<pb, 256, 0, st>>>(s, PROP_DELTA);
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_DELTA, 0);
       LAUNCH_CHECK("k_propose");
       TRY(run({7}));
       break;
     case BUSSEQ_STAGE_PHI:
-      k_propose<<<pb, 256, 0, st>>>(s, PROP_PHI);
+      k_propose<<<pb, 256, 0, st>>>(s, PROP_PHI, 0);
       LAUNCH_CHECK("k_propose");
       TRY(run({KID_PHI_STATIC, 8, 9}));
       break;

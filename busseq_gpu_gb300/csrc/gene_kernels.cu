@@ -37,10 +37,12 @@ namespace bq {
 // ---------------------------------------------------------------------------
 // Proposals (all families of one sweep; `mask` selects families)
 // ---------------------------------------------------------------------------
-__global__ void k_propose(DevState s, int mask) {
+// t0: the first proposal of the launch (a launch of the phi proposals alone
+// starts at propose_phi_offset).
+__global__ void k_propose(DevState s, int mask, int64_t t0) {
   const uint32_t iter = (uint32_t)*s.iter;
   const int64_t G = s.G, Gp = s.Gp;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t t = t0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // [0,B) gamma | [.., +G) alpha | (K-1)G beta | (B-1)G nu | N delta | B G phi
   if (t < s.B) {
     if (mask & PROP_GAMMA) {
@@ -162,6 +164,10 @@ __global__ void k_propose(DevState s, int mask) {
                       softplus_diff(fmaf(g1, xf, g0p), d1));
     }
   }
+}
+
+int64_t propose_phi_offset(const DevState& s) {
+  return (int64_t)s.B + s.G + (int64_t)(s.K - 1) * s.G + (int64_t)(s.B - 1) * s.G + s.N;
 }
 
 int64_t propose_count(const DevState& s) {

@@ -17,7 +17,7 @@ struct CorrTables {
 };
 
 
-__global__ void k_propose(DevState s, int mask);
+__global__ void k_propose(DevState s, int mask, int64_t t0);
 __global__ void k_zx(DevState s, int kept);
 __global__ void k_zx_gp(DevState s, int kept);
 __global__ void k_decide_gamma(DevState s);
@@ -38,6 +38,7 @@ __global__ void k_w_gibbs(DevState s);
 __global__ void k_sort_pi(DevState s, int do_pi, int advance);
 __global__ void k_posterior(DevState s, int advance);
 int64_t propose_count(const DevState& s);
+int64_t propose_phi_offset(const DevState& s);  // the first phi proposal of k_propose
 
 __global__ void k_init_scan(DevState s, int64_t* libsize, int* ymax, int32_t* rowcnt);
 __global__ void k_init_hist(DevState s, int32_t* hist);
