@@ -23,6 +23,8 @@
 // precision's rounding unit), or when r has underflowed to exactly 0.
 #pragma once
 #include <math.h>
+#include <stdint.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define BQ_BIC_HD __host__ __device__ __forceinline__
@@ -140,22 +142,18 @@ BQ_BIC_HD BicFF bff_rcp(BicFF d) {  // 1 / d: the float reciprocal and one corre
 
 BQ_BIC_HD BicFF bff_scale(BicFF a, float f) { return BicFF{a.hi * f, a.lo * f}; }  // f a power of two
 
-BQ_BIC_HD double bic_zero_series_ff(double mu, double logp, double log1mp, double phi, double g0, double g1) {
-  const double lw0 = phi * log1mp;  // log NB(0)
-  const double xm = 3.0 * mu;
-  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
-  if (x_max <= 1) return lw0;
-  if (!(g1 < 0.0) || g0 + g1 > 76.0 || phi > 1.0e6) return bic_zero_series(mu, logp, log1mp, phi, g0, g1);
-  const double p = exp(logp);
-  const BicFF pf = bff(p), cf = bff(exp(g1)), phif = bff(phi);
+// The float-float recurrence from x = 1 (r_1 = 1 in the frame): returns the
+// frame's sum (the x = 0 term included, as 1) and the number of 2^100
+// rescales.  F is e^{s_1}, cf e^{g1}.
+struct BicSum {
+  BicFF acc;
+  int nres;
+};
+
+BQ_BIC_HD BicSum bic_ff_loop(int x_max, BicFF pf, BicFF phif, BicFF cf, BicFF F, bool big_phi) {
   const float big = 1.2676506e30f, small = 7.888609e-31f;  // 2^100, 2^-100
-  const double ln_big = 100.0 * 0.69314718055994530942;
-  const double s1 = g0 + g1;
-  const double lsig1 = s1 > 0.0 ? -log1p(exp(-s1)) : s1 - log1p(exp(s1));
-  double off = log(phi) + logp + lsig1;
   BicFF R{1.0f, 0.0f}, acc{1.0f, 0.0f};
-  BicFF F = bff(exp(s1));
-  const bool big_phi = phi > 1.0;
+  int nres = 0;
   for (int x = 1; x + 1 < x_max; ++x) {
     const float xf = (float)x;  // exact: x < 2^24
     const BicFF a = bff_mul(bff_mul(bff_add(phif, BicFF{xf, 0.0f}), bff_rcp(BicFF{xf + 1.0f, 0.0f})), pf);
@@ -169,10 +167,150 @@ BQ_BIC_HD double bic_zero_series_ff(double mu, double logp, double log1mp, doubl
     if (acc.hi > big) {  // rescale the frame
       R = bff_scale(R, small);
       acc = bff_scale(acc, small);
-      off += ln_big;
+      ++nres;
     }
   }
-  const double l1 = off + log((double)acc.hi + (double)acc.lo);
+  return BicSum{acc, nres};
+}
+
+BQ_BIC_HD double bic_zero_series_ff(double mu, double logp, double log1mp, double phi, double g0, double g1) {
+  const double lw0 = phi * log1mp;  // log NB(0)
+  const double xm = 3.0 * mu;
+  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+  if (x_max <= 1) return lw0;
+  if (!(g1 < 0.0) || g0 + g1 > 76.0 || phi > 1.0e6) return bic_zero_series(mu, logp, log1mp, phi, g0, g1);
+  const double s1 = g0 + g1;
+  const double lsig1 = s1 > 0.0 ? -log1p(exp(-s1)) : s1 - log1p(exp(s1));
+  const BicSum r = bic_ff_loop(x_max, bff(exp(logp)), bff(phi), bff(exp(g1)), bff(exp(s1)), phi > 1.0);
+  const double off = log(phi) + logp + lsig1 + r.nres * (100.0 * 0.69314718055994530942);
+  const double l1 = off + log((double)r.acc.hi + (double)r.acc.lo);
+  return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
+}
+
+// ---------------------------------------------------------------------------
+// Double-precision logarithm by table lookup (P. T. P. Tang, "Table-driven
+// implementation of the logarithm function in IEEE floating-point
+// arithmetic", ACM TOMS 16(4), 1990).  For a positive normal x = 2^e m,
+// m in [1, 2), with j the top seven bits of m's fraction, c_j = 1 + (j + 1/2)
+// / 128 the centre of m's interval and t_j = fl(1 / c_j):
+//   log x = e log 2 - log t_j + log(1 + r),   r = m t_j - 1 (one fma),
+// |r| <= 2^-8 (1 + 2^-52), and log(1 + r) = r - r^2/2 + r^3/3 - ... - r^6/6
+// leaves out less than |r|^7 / 7 < 2^-58.  log 2 is split as a 42-bit head
+// (so that e log 2_head is exact for |e| < 2^11) and its remainder.  The
+// result errs by a few units of 2^-53 times max(1, |log x|); it is summed into
+// the BIC's double sums, where the library logarithm errs alike.
+// The table (t_j, -log t_j) is built once per CTA in shared memory on the
+// device, once per process on the host.
+constexpr int BIC_LOG_TAB = 128;
+constexpr double BIC_LN2_HI = 0x1.62e42fefa38p-1;     // ln 2 rounded to 42 bits
+constexpr double BIC_LN2_LO = 5.497923018708371e-14;  // ln 2 - BIC_LN2_HI
+
+BQ_BIC_HD uint64_t bic_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+
+BQ_BIC_HD double bic_from_bits(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+
+// entry j of the table: tab[j] = t_j, tab[BIC_LOG_TAB + j] = -log t_j
+BQ_BIC_HD void bic_log_entry(double* tab, int j) {
+  const double t = 1.0 / (1.0 + ((double)j + 0.5) / (double)BIC_LOG_TAB);
+  tab[j] = t;
+  tab[BIC_LOG_TAB + j] = -log(t);
+}
+
+BQ_BIC_HD double bic_log(const double* tab, double x) {
+  if (!(x >= 2.2250738585072014e-308 && x <= 1.7976931348623157e308)) return log(x);  // not positive normal
+  const uint64_t u = bic_bits(x);
+  const int e = (int)(u >> 52) - 1023;
+  const int j = (int)((u >> 45) & (uint64_t)(BIC_LOG_TAB - 1));
+  const double m = bic_from_bits((u & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull);
+  const double r = fma(m, tab[j], -1.0);
+  double q = -1.0 / 6.0;
+  q = fma(q, r, 1.0 / 5.0);
+  q = fma(q, r, -1.0 / 4.0);
+  q = fma(q, r, 1.0 / 3.0);
+  q = fma(q, r, -1.0 / 2.0);
+  const double lp = fma(q * r, r, r);  // log(1 + r)
+  const double ed = (double)e;
+  return fma(ed, BIC_LN2_HI, tab[BIC_LOG_TAB + j]) + fma(ed, BIC_LN2_LO, lp);
+}
+
+// log(1 + s) for s >= 0, to a few units of 2^-53 times max(1, log(1 + s))
+// absolute: with w = fl(1 + s), log(1 + s) = log w + log(1 + c / w),
+// c = s - (w - 1) (exact while w <= 2; below half an ulp of w beyond), and
+// |c / w| <= 2^-53, so log(1 + c / w) = c / w to 2^-106 and a float
+// reciprocal of w suffices for it.
+BQ_BIC_HD double bic_log1p(const double* tab, double s) {
+  const double w = 1.0 + s;
+  if (w == 1.0) return s;
+  const double c = s - (w - 1.0);
+  return bic_log(tab, w) + c * (double)(1.0f / (float)w);
+}
+
+// ---------------------------------------------------------------------------
+// The zero-count term with its per-cell constants hoisted (the device BIC).
+// Per batch: s_1 = g0 + g1, log sigmoid(s_1), sigmoid(s_1), e^{g1} and
+// e^{s_1}; per entry the caller passes mu, q = mu + phi, the clamped logs and
+// log phi.  The series is bic_ff_loop; its closing log(1 + exp(off) acc) is
+// formed as one log1p of S = phi p sigmoid(s_1) acc (exp(off) itself is that
+// product), with p = mu / q from a reciprocal refined twice by Newton's step
+// (2^-52 relative), unless the frame was rescaled, when it takes the log form
+// of bic_zero_series_ff.  A tiny or subnormal S is absorbed by log1p(S) = S,
+// so its relative rounding never matters.
+struct BicCell {
+  double g0, g1, lsig1, sig1;
+  BicFF cf, F1;
+  bool ff;  // the float-float recurrence applies (g1 < 0, g0 + g1 <= 76)
+};
+
+BQ_BIC_HD BicCell bic_cell(double g0, double g1) {
+  BicCell c;
+  c.g0 = g0;
+  c.g1 = g1;
+  const double s1 = g0 + g1;
+  c.lsig1 = s1 > 0.0 ? -log1p(exp(-s1)) : s1 - log1p(exp(s1));
+  c.sig1 = exp(c.lsig1);
+  c.ff = g1 < 0.0 && s1 <= 76.0;
+  c.cf = bff(exp(g1));
+  c.F1 = bff(c.ff ? exp(s1) : 0.0);
+  return c;
+}
+
+// mu / q to 2^-52 relative, for 0 < q < 1e30 (the float reciprocal's range)
+BQ_BIC_HD double bic_quot(double mu, double q) {
+  if (!(q < 1.0e30)) return mu / q;
+  double r = (double)(1.0f / (float)q);
+  r = fma(r, fma(-q, r, 1.0), r);
+  r = fma(r, fma(-q, r, 1.0), r);
+  return mu * r;
+}
+
+BQ_BIC_HD double bic_zero_term(const BicCell& c, const double* tab, double mu, double q, double logp, double log1mp,
+                               double phi, double lphi) {
+  const double lw0 = phi * log1mp;  // log NB(0)
+  const double xm = 3.0 * mu;
+  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+  if (x_max <= 1) return lw0;
+  if (!c.ff || phi > 1.0e6) return bic_zero_series(mu, logp, log1mp, phi, c.g0, c.g1);
+  const double p = bic_quot(mu, q);
+  const BicSum r = bic_ff_loop(x_max, bff(p), bff(phi), c.cf, c.F1, phi > 1.0);
+  const double acc = (double)r.acc.hi + (double)r.acc.lo;
+  if (r.nres == 0) return lw0 + bic_log1p(tab, phi * p * c.sig1 * acc);
+  const double l1 = lphi + logp + c.lsig1 + r.nres * (100.0 * 0.69314718055994530942) + bic_log(tab, acc);
   return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
 }
 

@@ -291,6 +291,17 @@ struct Estimates {
   int32_t* W;
 };
 
+// Tables of the BIC (all null: every entry computes its own values).
+struct alignas(16) BicGene {  // per (batch, gene)
+  double ean, phi, lphi, lgphi;  // exp(alpha + nu), phi, log phi, lgamma phi
+};
+struct BicTabs {
+  double* eb;   // [K][G] exp(beta)
+  BicGene* bg;  // [B][G]
+  double* ty;   // [B][ny] -softplus(g0 + g1 y) - lgamma(1 + y)
+  int ny;
+};
+
 // eta = alpha + beta + nu, always summed in this order so that every kernel
 // rounds it identically.
 __device__ __forceinline__ float eta3(float a, float b, float n) { return (a + b) + n; }

@@ -1146,10 +1146,18 @@ int busseq_bic(busseq_handle* h, double* bic) {
   if (!h || !bic) return fail(BUSSEQ_ERR_ARG, "NULL argument");
   CUDA_TRY(cudaSetDevice(h->device));
   TRY(ensure_estimates(h));
-  bq::k_bic_cell<<<(unsigned)h->s.N, 256, 0, h->stream>>>(h->s, h->est, h->ll_ik);
+  const bq::DevState& s = h->s;
+  const int ny = bq::bic_table_counts(s);
+  char* scratch = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&scratch, (size_t)bq::bic_table_bytes(s, ny), h->stream));
+  bq::BicTabs tb;
+  tb.bg = reinterpret_cast<bq::BicGene*>(scratch);
+  tb.eb = reinterpret_cast<double*>(scratch + (size_t)s.B * s.G * sizeof(bq::BicGene));
+  tb.ty = tb.eb + (size_t)s.K * s.G;
+  tb.ny = ny;
+  bq::launch_bic(s, h->est, h->ll_ik, tb, h->bic_out, h->stream);
   LAUNCH_CHECK("k_bic_cell");
-  bq::k_bic_total<<<1, 1024, 0, h->stream>>>(h->s, h->est, h->ll_ik, h->bic_out);
-  LAUNCH_CHECK("k_bic_total");
+  CUDA_TRY(cudaFreeAsync(scratch, h->stream));
   double out[2];
   CUDA_TRY(cudaMemcpyAsync(out, h->bic_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));

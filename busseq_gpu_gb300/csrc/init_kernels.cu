@@ -461,54 +461,99 @@ __global__ void k_finalize(DevState s, Estimates e, int n_kept) {
 // ---------------------------------------------------------------------------
 // BIC.  Per cell i and type k: sum over genes of the dropout-marginal
 // log-likelihood of Y (BUSseq_gpu.cu:967-1007), with the estimates, in double
-// precision.  For Y = 0 the reference's series over x = 0 .. floor(3 mu)-1 is
-// bic_zero_series_ff (bic_series.h): the same sum by a log-free recurrence in
-// float-float arithmetic (48-bit significands; FP64 runs at a small fraction
-// of the FP32 rate here), stopped only once the rest is provably below 2^-60
-// of the sum.
+// precision.  FP64 runs at a small fraction of the FP32 rate here, so the
+// per-entry work is kept to one logarithm, log(mu + phi), by Tang's table
+// method (bic_series.h), two products for mu and a few sums:
+//   k_bic_tables  exp(beta) per (type, gene); exp(alpha + nu), phi, log phi
+//                 and lgamma(phi) per (batch, gene); -softplus(g0 + g1 y) -
+//                 lgamma(1 + y) per (batch, count)
+//   k_bic_cell    one CTA per cell: mu = exp(alpha + nu) e^delta e^beta, the
+//                 clamped log p and log(1 - p) (:977-986), the Y > 0 term and,
+//                 for Y = 0, the reference's series over x = 0 .. floor(3 mu)-1
+//                 (bic_zero_term: float-float recurrence, stopped once the
+//                 rest is provably below 2^-60 of the sum)
+// Without tables (the allocation-free entry point) each entry computes them.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik) {
-  __shared__ double sh[8 * MAX_K];
+__global__ void k_bic_tables(DevState s, Estimates e, BicTabs tb) {
+  const int64_t G = s.G, KG = (int64_t)s.K * G, BG = (int64_t)s.B * G, BY = (int64_t)s.B * tb.ny;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < KG + BG + BY; t += stride) {
+    if (t < KG) {
+      tb.eb[t] = exp(e.beta[t]);
+    } else if (t < KG + BG) {
+      const int64_t u = t - KG, g = u % G;
+      const double phi = e.phi[u];
+      tb.bg[u] = BicGene{exp(e.alpha[g] + e.nu[u]), phi, log(phi), lgamma(phi)};
+    } else {
+      const int64_t u = t - KG - BG;
+      const int b = (int)(u / tb.ny), y = (int)(u % tb.ny);
+      const double tt = e.gamma[b] + e.gamma[s.B + b] * y;
+      const double sp = tt > 0 ? tt + log1p(exp(-tt)) : log1p(exp(tt));
+      tb.ty[u] = -sp - lgamma(1.0 + y);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik, BicTabs tb) {
+  extern __shared__ double s_acc[];  // [K][blockDim.x] running sums
+  __shared__ double s_log[2 * BIC_LOG_TAB];
   const int64_t i = blockIdx.x;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, bd = blockDim.x;
   const int b = s.batch_of[i];
   const int B = s.B, K = s.K;
   const int64_t G = s.G, Gp = s.Gp;
-  const double g0 = e.gamma[b], g1 = e.gamma[B + b];
-  const double di = e.delta[i];
-  double acc[MAX_K];
-  for (int k = 0; k < K; ++k) acc[k] = 0.0;
-  for (int64_t g = tid; g < G; g += blockDim.x) {
+  for (int j = tid; j < BIC_LOG_TAB; j += bd) bic_log_entry(s_log, j);
+  for (int k = 0; k < K; ++k) s_acc[k * bd + tid] = 0.0;
+  const BicCell cc = bic_cell(e.gamma[b], e.gamma[B + b]);
+  const double g0 = cc.g0, g1 = cc.g1;
+  const double di = e.delta[i], edi = exp(di);
+  __syncthreads();
+  for (int64_t g = tid; g < G; g += bd) {
     const int y = s.Y[i * Gp + g];
-    const double phi = e.phi[(int64_t)b * G + g];
-    const double an = e.alpha[g] + e.nu[(int64_t)b * G + g] + di;
-    const double lphi = log(phi);
+    const int64_t bgi = (int64_t)b * G + g;
+    double phi, lphi, lgphi, ean;
+    if (tb.bg) {
+      const BicGene v = tb.bg[bgi];
+      ean = v.ean * edi;  // exp(alpha + nu + delta)
+      phi = v.phi;
+      lphi = v.lphi;
+      lgphi = v.lgphi;
+    } else {
+      phi = e.phi[bgi];
+      lphi = log(phi);
+      lgphi = lgamma(phi);
+      ean = 0.0;
+    }
+    const double an = e.alpha[g] + e.nu[bgi] + di;
     double base = 0.0;
     if (y) {
-      const double t = g0 + g1 * y;
-      const double sp = t > 0 ? t + log1p(exp(-t)) : log1p(exp(t));
-      base = -sp + lgamma(phi + y) - lgamma(1.0 + y) - lgamma(phi);
+      if (tb.ty && y < tb.ny) {
+        base = tb.ty[(int64_t)b * tb.ny + y] + lgamma(phi + y) - lgphi;
+      } else {
+        const double t = g0 + g1 * y;
+        const double sp = t > 0 ? t + log1p(exp(-t)) : log1p(exp(t));
+        base = -sp + lgamma(phi + y) - lgamma(1.0 + y) - lgphi;
+      }
     }
     for (int k = 0; k < K; ++k) {
       const double eta = an + e.beta[(int64_t)k * G + g];
-      const double mu = exp(eta);
-      const double lq = log(mu + phi);
+      const double mu = tb.eb ? ean * tb.eb[(int64_t)k * G + g] : exp(eta);
+      const double q = mu + phi;
+      const double lq = bic_log(s_log, q);
       double logp = eta - lq, log1mp = lphi - lq;
       if (logp < -250.0) logp = -250.0;
       if (log1mp < -250.0) log1mp = -250.0;
-      if (y) acc[k] += base + y * logp + phi * log1mp;
-      else acc[k] += bic_zero_series_ff(mu, logp, log1mp, phi, g0, g1);
+      const double v = y ? base + y * logp + phi * log1mp : bic_zero_term(cc, s_log, mu, q, logp, log1mp, phi, lphi);
+      s_acc[k * bd + tid] += v;
     }
   }
-  for (int k = 0; k < K; ++k) {
-    const double v = warp_sum(acc[k]);
-    if (lane == 0) sh[warp * MAX_K + k] = v;
-  }
   __syncthreads();
-  if (tid < K) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w * MAX_K + tid];
-    ll_ik[(int64_t)tid * s.N + i] = t;
+  // per type, a fixed-order sum over the CTA's threads
+  for (int k = warp; k < K; k += bd >> 5) {
+    double v = 0.0;
+    for (int t = lane; t < bd; t += 32) v += s_acc[k * bd + t];
+    v = warp_sum(v);
+    if (lane == 0) ll_ik[(int64_t)k * s.N + i] = v;
   }
 }
 
@@ -532,6 +577,29 @@ __global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double
     out[0] = -2.0 * v[0] + log(G * N) * nparam;
     out[1] = v[0];
   }
+}
+
+int bic_table_counts(const DevState& s) { return s.ymax + 1 < (1 << 16) ? s.ymax + 1 : (1 << 16); }
+
+int64_t bic_table_bytes(const DevState& s, int ny) {
+  return ((int64_t)s.K * s.G + (int64_t)s.B * ny) * (int64_t)sizeof(double) +
+         (int64_t)s.B * s.G * (int64_t)sizeof(BicGene);
+}
+
+// threads of a k_bic_cell CTA: the running sums (K per thread) and the log
+// table stay within the 48 KB of shared memory a launch gets by default
+int bic_cell_threads(int K) { return K <= 22 ? 256 : (K <= 44 ? 128 : 64); }
+
+void launch_bic(const DevState& s, const Estimates& e, double* ll_ik, const BicTabs& tb, double* out,
+                cudaStream_t st) {
+  const int64_t n_tab = tb.eb ? (int64_t)s.K * s.G + (int64_t)s.B * s.G + (int64_t)s.B * tb.ny : 0;
+  if (n_tab > 0) {
+    const int64_t nb = (n_tab + 255) / 256;
+    k_bic_tables<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, st>>>(s, e, tb);
+  }
+  const int bd = bic_cell_threads(s.K);
+  k_bic_cell<<<(unsigned)s.N, bd, (size_t)s.K * bd * sizeof(double), st>>>(s, e, ll_ik, tb);
+  k_bic_total<<<1, 1024, 0, st>>>(s, e, ll_ik, out);
 }
 
 }  // namespace bq

@@ -83,7 +83,16 @@ __global__ void k_fmt_row_len(FmtSrc src, int64_t cols, int64_t* row_len, int* b
 __global__ void k_fmt_rows(FmtSrc src, int64_t cols, const int64_t* row_off, char* out);
 __global__ void k_z_dense_i32(DevState s, int32_t* out, int64_t ld);
 __global__ void k_z_dense_u8(DevState s, uint8_t* out, int64_t ld);
-__global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik);
+__global__ void k_bic_cell(DevState s, Estimates e, double* ll_ik, BicTabs tb);
+__global__ void k_bic_tables(DevState s, Estimates e, BicTabs tb);
+// k_bic_tables (when tb has tables), k_bic_cell and k_bic_total on st; out
+// receives {BIC, log-likelihood}
+void launch_bic(const DevState& s, const Estimates& e, double* ll_ik, const BicTabs& tb, double* out,
+                cudaStream_t st);
+// bytes of the BIC tables: BicGene [B][G] first, then exp(beta) [K][G] and the
+// count terms [B][ny] as doubles
+int64_t bic_table_bytes(const DevState& s, int ny);
+int bic_table_counts(const DevState& s);  // ny: the counts 0 .. ny-1 that the count table covers
 __global__ void k_correct_prep(DevState s, Estimates e, CorrTables tb);
 __global__ void k_correct(DevState s, Estimates e, CorrTables tb, int32_t* out, int64_t ld);
 __global__ void k_bic_total(DevState s, Estimates e, const double* ll_ik, double* out);

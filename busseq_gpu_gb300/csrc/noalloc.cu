@@ -160,8 +160,8 @@ extern "C" int busseq_bic_noalloc(const busseq_dims* dims, const int32_t* Y_dev,
   k_noalloc_batches<<<(unsigned)((nfill + 255) / 256), 256, 0, st>>>(sc.batch, o, B, N, kMaxCells);
   // Every [k][i] entry of the scratch is written by k_bic_cell before
   // k_bic_total reads it, so nothing has to be cleared between calls.
-  bq::k_bic_cell<<<(unsigned)N, 256, 0, st>>>(s, est, sc.ll);
-  bq::k_bic_total<<<1, 1024, 0, st>>>(s, est, sc.ll, out_dev);
+  // no tables: each entry computes exp(beta), lgamma(phi) and the rest itself
+  bq::launch_bic(s, est, sc.ll, bq::BicTabs{}, out_dev, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return err(BUSSEQ_ERR_CUDA, cudaGetErrorString(e));
   return BUSSEQ_OK;
