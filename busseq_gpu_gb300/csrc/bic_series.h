@@ -35,6 +35,7 @@
 namespace bq {
 
 constexpr int BIC_SERIES_MAX_TERMS = 1 << 24;  // x_max is capped there (mu beyond 5.6e6)
+constexpr int BIC_CLASSES = 32;                // series length classes: floor(log2 x_max) < 32
 
 // The same sum term by term in log space (the reference's form, with the NB
 // term by its recurrence): used only where the recurrence above does not
@@ -264,13 +265,13 @@ BQ_BIC_HD double bic_log1p(const double* tab, double s) {
 // ---------------------------------------------------------------------------
 // The zero-count term with its per-cell constants hoisted (the device BIC).
 // Per batch: s_1 = g0 + g1, log sigmoid(s_1), sigmoid(s_1), e^{g1} and
-// e^{s_1}; per entry the caller passes mu, q = mu + phi, the clamped logs and
-// log phi.  The series is bic_ff_loop; its closing log(1 + exp(off) acc) is
-// formed as one log1p of S = phi p sigmoid(s_1) acc (exp(off) itself is that
-// product), with p = mu / q from a reciprocal refined twice by Newton's step
-// (2^-52 relative), unless the frame was rescaled, when it takes the log form
-// of bic_zero_series_ff.  A tiny or subnormal S is absorbed by log1p(S) = S,
-// so its relative rounding never matters.
+// e^{s_1}; per entry mu and phi (and the clamped logs for NB(0)).  The series
+// is bic_ff_loop; its closing log(1 + exp(off) acc) is formed as one log1p of
+// S = phi p sigmoid(s_1) acc (exp(off) itself is that product), with p = mu /
+// (mu + phi) from a reciprocal refined twice by Newton's step (2^-52
+// relative), unless the frame was rescaled, when it takes the log form of
+// bic_zero_series_ff.  A tiny or subnormal S is absorbed by log1p(S) = S, so
+// its relative rounding never matters.
 struct BicCell {
   double g0, g1, lsig1, sig1;
   BicFF cf, F1;
@@ -299,19 +300,33 @@ BQ_BIC_HD double bic_quot(double mu, double q) {
   return mu * r;
 }
 
-BQ_BIC_HD double bic_zero_term(const BicCell& c, const double* tab, double mu, double q, double logp, double log1mp,
-                               double phi, double lphi) {
+// The series part of a zero count's term, log(1 + exp(off) acc), for an entry
+// on the float-float path (c.ff, phi <= 1e6, floor(3 mu) >= 2).  Only a
+// rescaled frame (rare) takes logarithms of mu, phi and mu + phi.
+BQ_BIC_HD double bic_zero_close(const BicCell& c, const double* tab, double mu, double phi) {
+  const double q = mu + phi;
+  const double xm = 3.0 * mu;
+  const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+  const double p = bic_quot(mu, q);
+  const BicSum r = bic_ff_loop(x_max, bff(p), bff(phi), c.cf, c.F1, phi > 1.0);
+  const double acc = (double)r.acc.hi + (double)r.acc.lo;
+  if (r.nres == 0) return bic_log1p(tab, phi * p * c.sig1 * acc);
+  const double lq = bic_log(tab, q);
+  const double off = (bic_log(tab, phi) - lq) + bic_log(tab, mu) + c.lsig1;  // log(phi p sigmoid(s_1))
+  const double l1 = off + r.nres * (100.0 * 0.69314718055994530942) + bic_log(tab, acc);
+  return l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1));
+}
+
+// The whole zero-count term: NB(0) and the series (the reference's form where
+// the float-float recurrence does not apply).
+BQ_BIC_HD double bic_zero_term(const BicCell& c, const double* tab, double mu, double logp, double log1mp,
+                               double phi) {
   const double lw0 = phi * log1mp;  // log NB(0)
   const double xm = 3.0 * mu;
   const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
   if (x_max <= 1) return lw0;
   if (!c.ff || phi > 1.0e6) return bic_zero_series(mu, logp, log1mp, phi, c.g0, c.g1);
-  const double p = bic_quot(mu, q);
-  const BicSum r = bic_ff_loop(x_max, bff(p), bff(phi), c.cf, c.F1, phi > 1.0);
-  const double acc = (double)r.acc.hi + (double)r.acc.lo;
-  if (r.nres == 0) return lw0 + bic_log1p(tab, phi * p * c.sig1 * acc);
-  const double l1 = lphi + logp + c.lsig1 + r.nres * (100.0 * 0.69314718055994530942) + bic_log(tab, acc);
-  return lw0 + (l1 > 0.0 ? l1 + log1p(exp(-l1)) : log1p(exp(l1)));
+  return lw0 + bic_zero_close(c, tab, mu, phi);
 }
 
 }  // namespace bq

@@ -194,6 +194,8 @@ __global__ void k_init_w_delta(DevState s, const int64_t* libsize, int* bad_cell
 __global__ void __launch_bounds__(GENE_TILE) k_init_raw(DevState s) {
   __shared__ double sh[(GENE_TILE / 32) * MAX_B];
   __shared__ int sh_flag;
+  __shared__ int s_i[MAX_CG];
+  __shared__ float s_e[MAX_CG];  // exp(-delta) of the chunk's cells
   const int tid = threadIdx.x;
   const int tile = blockIdx.x, row = blockIdx.y;
   const int4 ch = s.gchunk[row];
@@ -201,15 +203,27 @@ __global__ void __launch_bounds__(GENE_TILE) k_init_raw(DevState s) {
   const int64_t Gp = s.Gp;
   const int64_t g = (int64_t)tile * GENE_TILE + tid;
   const bool valid = g < s.G;
+  if (len > 0) {  // uniform over the CTA
+    for (int j = tid; j < len; j += blockDim.x) {
+      const int i = s.perm[start + j];
+      s_i[j] = i;
+      s_e[j] = expf(-s.delta[i]);
+    }
+    __syncthreads();
+  }
   if (len > 0 && valid) {
     double acc = 0.0;
     for (int j0 = 0; j0 < len; j0 += 32) {
       const int jn = min(32, len - j0);
       float f = 0.0f;
-      for (int jj = 0; jj < jn; ++jj) {
-        const int i = s.perm[start + j0 + jj];
-        const float y = (float)s.Y[(int64_t)i * Gp + g];
-        f += log1pf(y * expf(-s.delta[i]));
+      for (int jj = 0; jj < jn; jj += 8) {  // eight rows' loads in flight, summed in cell order
+        float yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          yv[u] = jj + u < jn ? (float)__ldg(&s.Y[(int64_t)s_i[j0 + jj + u] * Gp + g]) : 0.0f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (jj + u < jn) f += log1pf(yv[u] * s_e[j0 + jj + u]);
       }
       acc += f;
     }
@@ -228,9 +242,9 @@ __global__ void __launch_bounds__(GENE_TILE) k_init_raw(DevState s) {
       double rsum = 0.0;
       for (int k = 0; k < K; ++k) {
         double sumbk = 0.0;
-        for (int c = 0; c < s.cap_g; ++c) {
-          const int4 cc = s.gchunk[c];
-          if (cc.w == 0 || cc.x != b || cc.y != k) continue;
+        const int2 sc = s.seg_chunk[b * K + k];  // the segment's chunks, in chunk order
+        for (int c = sc.x; c < sc.x + sc.y; ++c) {
+          if (s.gchunk[c].w == 0) continue;
           sumbk += __ldcg(&s.part[(int64_t)c * NSLOT * Gp + g]);
         }
         const int n = s.seg_cnt[b * K + k];
@@ -494,57 +508,142 @@ __global__ void k_bic_tables(DevState s, Estimates e, BicTabs tb) {
   }
 }
 
+// Shared memory of k_bic_cell beyond its static arrays: K running sums per
+// thread, then per job slot (K per thread) mu, phi, the result, the sorted
+// order and the length class.
+size_t bic_cell_smem(int K, int bd) {
+  const size_t slots = (size_t)K * bd;
+  return slots * sizeof(double) + slots * (3 * sizeof(double) + sizeof(uint16_t) + sizeof(uint8_t));
+}
+
+// One CTA per cell, the genes in passes of blockDim.x (one gene per thread,
+// all K types).  A pass first forms every term but the zero counts' series
+// (those entries add NB(0) and queue a job of mu and phi), then sorts the
+// pass's jobs by series length class (floor(log2 floor(3 mu)), longest
+// first) and hands them out in that order, so a warp's lanes run series of
+// similar length instead of waiting on one gene's long series; each result
+// returns to its job's slot and the owning thread adds its jobs in type order,
+// so the sums do not depend on the order the jobs ran in.
 __global__ void __launch_bounds__(256) k_bic_cell(DevState s, Estimates e, double* ll_ik, BicTabs tb) {
-  extern __shared__ double s_acc[];  // [K][blockDim.x] running sums
+  extern __shared__ double s_acc[];  // [K][blockDim.x] running sums, then the job arrays
   __shared__ double s_log[2 * BIC_LOG_TAB];
+  __shared__ int s_ccnt[BIC_CLASSES], s_cfill[BIC_CLASSES], s_njobs;
   const int64_t i = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, bd = blockDim.x;
   const int b = s.batch_of[i];
   const int B = s.B, K = s.K;
   const int64_t G = s.G, Gp = s.Gp;
+  const int slots = K * bd;
+  double* s_mu = s_acc + slots;
+  double* s_ph = s_mu + slots;
+  double* s_res = s_ph + slots;
+  uint16_t* s_perm = reinterpret_cast<uint16_t*>(s_res + slots);
+  uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_perm + slots);
   for (int j = tid; j < BIC_LOG_TAB; j += bd) bic_log_entry(s_log, j);
   for (int k = 0; k < K; ++k) s_acc[k * bd + tid] = 0.0;
+  if (tid < BIC_CLASSES) s_ccnt[tid] = 0;
   const BicCell cc = bic_cell(e.gamma[b], e.gamma[B + b]);
   const double g0 = cc.g0, g1 = cc.g1;
   const double di = e.delta[i], edi = exp(di);
   __syncthreads();
-  for (int64_t g = tid; g < G; g += bd) {
-    const int y = s.Y[i * Gp + g];
-    const int64_t bgi = (int64_t)b * G + g;
-    double phi, lphi, lgphi, ean;
-    if (tb.bg) {
-      const BicGene v = tb.bg[bgi];
-      ean = v.ean * edi;  // exp(alpha + nu + delta)
-      phi = v.phi;
-      lphi = v.lphi;
-      lgphi = v.lgphi;
-    } else {
-      phi = e.phi[bgi];
-      lphi = log(phi);
-      lgphi = lgamma(phi);
-      ean = 0.0;
-    }
-    const double an = e.alpha[g] + e.nu[bgi] + di;
-    double base = 0.0;
-    if (y) {
-      if (tb.ty && y < tb.ny) {
-        base = tb.ty[(int64_t)b * tb.ny + y] + lgamma(phi + y) - lgphi;
+  for (int64_t gbase = 0; gbase < G; gbase += bd) {
+    const int64_t g = gbase + tid;
+    uint64_t jmask = 0;  // types whose series this thread queued, in its slots tid * K + 0, 1, ...
+    if (g < G) {
+      const int y = s.Y[i * Gp + g];
+      const int64_t bgi = (int64_t)b * G + g;
+      double phi, lphi, lgphi, ean;
+      if (tb.bg) {
+        const BicGene v = tb.bg[bgi];
+        ean = v.ean * edi;  // exp(alpha + nu + delta)
+        phi = v.phi;
+        lphi = v.lphi;
+        lgphi = v.lgphi;
       } else {
-        const double t = g0 + g1 * y;
-        const double sp = t > 0 ? t + log1p(exp(-t)) : log1p(exp(t));
-        base = -sp + lgamma(phi + y) - lgamma(1.0 + y) - lgphi;
+        phi = e.phi[bgi];
+        lphi = log(phi);
+        lgphi = lgamma(phi);
+        ean = 0.0;
+      }
+      const double an = e.alpha[g] + e.nu[bgi] + di;
+      double base = 0.0;
+      if (y) {
+        if (tb.ty && y < tb.ny) {
+          base = tb.ty[(int64_t)b * tb.ny + y] + lgamma(phi + y) - lgphi;
+        } else {
+          const double t = g0 + g1 * y;
+          const double sp = t > 0 ? t + log1p(exp(-t)) : log1p(exp(t));
+          base = -sp + lgamma(phi + y) - lgamma(1.0 + y) - lgphi;
+        }
+      }
+      int nj = 0;
+      for (int k = 0; k < K; ++k) {
+        const double eta = an + e.beta[(int64_t)k * G + g];
+        const double mu = tb.eb ? ean * tb.eb[(int64_t)k * G + g] : exp(eta);
+        const double lq = bic_log(s_log, mu + phi);
+        double logp = eta - lq, log1mp = lphi - lq;
+        if (logp < -250.0) logp = -250.0;
+        if (log1mp < -250.0) log1mp = -250.0;
+        double v;
+        if (y) {
+          v = base + y * logp + phi * log1mp;
+        } else {
+          v = phi * log1mp;  // log NB(0)
+          const double xm = 3.0 * mu;
+          const int x_max = xm > (double)BIC_SERIES_MAX_TERMS ? BIC_SERIES_MAX_TERMS : (int)xm;
+          if (x_max > 1) {
+            if (cc.ff && phi <= 1.0e6) {
+              const int slot = tid * K + nj++;
+              s_mu[slot] = mu;
+              s_ph[slot] = phi;
+              const int cls = BIC_CLASSES - 1 - (31 - __clz(x_max));  // longest first
+              s_cls[slot] = (uint8_t)cls;
+              atomicAdd(&s_ccnt[cls], 1);
+              jmask |= 1ull << k;
+            } else {
+              v = bic_zero_series(mu, logp, log1mp, phi, g0, g1);
+            }
+          }
+        }
+        s_acc[k * bd + tid] += v;
       }
     }
-    for (int k = 0; k < K; ++k) {
-      const double eta = an + e.beta[(int64_t)k * G + g];
-      const double mu = tb.eb ? ean * tb.eb[(int64_t)k * G + g] : exp(eta);
-      const double q = mu + phi;
-      const double lq = bic_log(s_log, q);
-      double logp = eta - lq, log1mp = lphi - lq;
-      if (logp < -250.0) logp = -250.0;
-      if (log1mp < -250.0) log1mp = -250.0;
-      const double v = y ? base + y * logp + phi * log1mp : bic_zero_term(cc, s_log, mu, q, logp, log1mp, phi, lphi);
-      s_acc[k * bd + tid] += v;
+    __syncthreads();
+    if (warp == 0) {  // class offsets; the counts are cleared for the next pass
+      const int c0 = lane < BIC_CLASSES ? s_ccnt[lane] : 0;
+      int incl = c0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (lane < BIC_CLASSES) {
+        s_cfill[lane] = incl - c0;
+        s_ccnt[lane] = 0;
+      }
+      if (lane == 31) s_njobs = incl;
+    }
+    __syncthreads();
+    {
+      int m = 0;
+      for (uint64_t jm = jmask; jm; jm &= jm - 1, ++m) {
+        const int slot = tid * K + m;
+        s_perm[atomicAdd(&s_cfill[s_cls[slot]], 1)] = (uint16_t)slot;
+      }
+    }
+    __syncthreads();
+    const int nj_all = s_njobs;
+    for (int j = tid; j < nj_all; j += bd) {
+      const int slot = s_perm[j];
+      s_res[slot] = bic_zero_close(cc, s_log, s_mu[slot], s_ph[slot]);
+    }
+    __syncthreads();
+    {
+      int m = 0;
+      for (uint64_t jm = jmask; jm; jm &= jm - 1, ++m) {
+        const int k = __ffsll((long long)jm) - 1;
+        s_acc[k * bd + tid] += s_res[tid * K + m];
+      }
     }
   }
   __syncthreads();
@@ -586,9 +685,12 @@ int64_t bic_table_bytes(const DevState& s, int ny) {
          (int64_t)s.B * s.G * (int64_t)sizeof(BicGene);
 }
 
-// threads of a k_bic_cell CTA: the running sums (K per thread) and the log
-// table stay within the 48 KB of shared memory a launch gets by default
-int bic_cell_threads(int K) { return K <= 22 ? 256 : (K <= 44 ? 128 : 64); }
+// threads of a k_bic_cell CTA: at most 2048 job slots (K per thread), a
+// multiple of 32
+int bic_cell_threads(int K) {
+  const int bd = (2048 / K) & ~31;
+  return bd < 32 ? 32 : (bd > 256 ? 256 : bd);
+}
 
 void launch_bic(const DevState& s, const Estimates& e, double* ll_ik, const BicTabs& tb, double* out,
                 cudaStream_t st) {
@@ -598,7 +700,9 @@ void launch_bic(const DevState& s, const Estimates& e, double* ll_ik, const BicT
     k_bic_tables<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, st>>>(s, e, tb);
   }
   const int bd = bic_cell_threads(s.K);
-  k_bic_cell<<<(unsigned)s.N, bd, (size_t)s.K * bd * sizeof(double), st>>>(s, e, ll_ik, tb);
+  const size_t smem = bic_cell_smem(s.K, bd);
+  cudaFuncSetAttribute(k_bic_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_bic_cell<<<(unsigned)s.N, bd, smem, st>>>(s, e, ll_ik, tb);
   k_bic_total<<<1, 1024, 0, st>>>(s, e, ll_ik, out);
 }
 

@@ -36,7 +36,7 @@ extern "C" double zf(double mu, double lp, double l1, double phi, double g0, dou
   return bq::bic_zero_series_ff(mu, lp, l1, phi, g0, g1); }
 extern "C" double zt(double mu, double lp, double l1, double phi, double g0, double g1) {
   const bq::BicCell c = bq::bic_cell(g0, g1);
-  return bq::bic_zero_term(c, tab, mu, mu + phi, lp, l1, phi, bq::bic_log(tab, phi)); }
+  return bq::bic_zero_term(c, tab, mu, lp, l1, phi); }
 extern "C" double lg(double x) { return bq::bic_log(tab, x); }
 extern "C" double l1p(double x) { return bq::bic_log1p(tab, x); }
 """
