@@ -344,8 +344,6 @@ int zmask_from_zval(busseq_handle* h) {
   return BUSSEQ_OK;
 }
 
-// Z as a dense host table [N][G] of int32 (esize 4) or uint8 (esize 1),
-// unpacked from the bit mask on the device.
 // Z as a dense [N][G] table of int32 (esize 4) or uint8 (esize 1) in a
 // stream-ordered device allocation, enqueued on the handle's stream (the
 // caller copies it and frees it there).
