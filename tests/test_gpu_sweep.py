@@ -107,8 +107,14 @@ def test_posterior_summaries_match_draws():
     np.testing.assert_array_equal(e["W"], counts.argmax(0))
 
 
-def test_bic_matches_oracle():
-    n_b, G, K, seed = [60, 50, 40], 300, 3, 8
+@pytest.mark.parametrize("n_b,G,K,seed", [
+    ([60, 50, 40], 300, 3, 8),                   # 256 threads per cell, two gene passes
+    ([40, 55, 30, 45, 35, 50], 500, 12, 21),     # 160 threads (12 job slots each), four passes
+    ([70, 66, 80], 100, 64, 5),                  # the largest K: 32 threads, 2048 job slots
+])
+def test_bic_matches_oracle(n_b, G, K, seed):
+    """The BIC kernel forms its per-CTA thread count and job queue from K
+    (K slots per thread, at most 2048); each shape against the FP64 oracle."""
     Y, _, _ = bq.simulate(n_b, G, K, seed)
     s = bq.Sampler(Y, n_b, K, seed=seed)
     s.run(30, 15, 10)
