@@ -645,10 +645,9 @@ def main():
         cms = c0.elapsed_time(c1)
         corrected = {"ms": cms, "entries_per_s": N * G / (cms / 1000.0), "dtype": "f64",
                      "note": "one call: tables, k_correct over N x G entries, device output"}
-        if world == 1 and not args.no_cpu_baseline:
-            corrected["cpu_baseline"] = corrected_cpu_rate(s, n_b, seed + 7919 * rank)
         del cc
-    s.close()
+    # the finished run stays open for the corrected counts' CPU baseline, which
+    # runs after the end-to-end job: no host-side leg runs between the GPU timings
     del Yd
     torch.cuda.empty_cache()
 
@@ -677,6 +676,9 @@ def main():
     e2e_value = whole_job_rate(args.steps, world, max_over_ranks(e2e_s, dist, f"cuda:{local}"))
     h2d = Y.nbytes
     d2h = sum(v.nbytes for v in est.values())
+    if corrected is not None and world == 1 and not args.no_cpu_baseline:
+        corrected["cpu_baseline"] = corrected_cpu_rate(s, n_b, seed + 7919 * rank)
+    s.close()
 
     # ---- mixing and recovery: ESS of beta and nu, ARI of W (rank 0) -------
     quality = None
