@@ -700,9 +700,13 @@ void launch_bic(const DevState& s, const Estimates& e, double* ll_ik, const BicT
     k_bic_tables<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, st>>>(s, e, tb);
   }
   const int bd = bic_cell_threads(s.K);
-  const size_t smem = bic_cell_smem(s.K, bd);
-  cudaFuncSetAttribute(k_bic_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_bic_cell<<<(unsigned)s.N, bd, smem, st>>>(s, e, ll_ik, tb);
+  // every K's shape stays within 2048 job slots; the limit is raised to that
+  // size on calls made outside stream capture (the allocation-free entry point
+  // makes its first call on a device outside capture), so it holds for any K
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+    cudaFuncSetAttribute(k_bic_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bic_cell_smem(1, 2048));
+  k_bic_cell<<<(unsigned)s.N, bd, bic_cell_smem(s.K, bd), st>>>(s, e, ll_ik, tb);
   k_bic_total<<<1, 1024, 0, st>>>(s, e, ll_ik, out);
 }
 

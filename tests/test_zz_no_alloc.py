@@ -68,6 +68,47 @@ def test_bic_noalloc_matches_busseq_bic_twice():
         assert abs(ll - ll_want) <= BIC_RTOL * abs(want), (ll, ll_want)
 
 
+def test_bic_noalloc_in_a_captured_graph():
+    """A call made during stream capture, after one outside capture on the
+    device, records its launches into the graph; a replay computes the BIC.
+    The call outside capture has a smaller K (less shared memory per CTA) than
+    the captured one."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc_fn()
+    dev = torch.device("cuda", 0)
+
+    def prepared(n_b, G, K, seed):
+        Y, est, want = _case(n_b, G, K, seed)
+        t = {k: torch.from_numpy(np.ascontiguousarray(est[k], dtype=np.float64)).to(dev)
+             for k in ("alpha", "beta", "nu", "delta", "phi", "gamma", "pi")}
+        Yd = torch.from_numpy(Y).to(dev)
+        out = torch.full((2,), float("nan"), dtype=torch.float64, device=dev)
+        nb = np.array(n_b, np.int32)
+        dims = bq.Dims(len(n_b), K, G, nb.ctypes.data_as(C.POINTER(C.c_int32)))
+        args = [Yd.data_ptr()] + [t[k].data_ptr() for k in ("alpha", "beta", "nu", "delta", "phi", "gamma", "pi")]
+        keep = (Y, t, Yd, nb, dims)
+        return dims, args + [out.data_ptr()], out, want, keep
+
+    d1, a1, o1, w1, k1 = prepared([25, 30], 80, 2, 11)
+    torch.cuda.synchronize()
+    assert fn(C.byref(d1), *a1, None) == 0, bq.lib().busseq_last_error().decode()
+    torch.cuda.synchronize()
+    assert abs(float(o1[0].cpu()) - w1) <= BIC_RTOL * abs(w1)
+
+    d2, a2, o2, w2, k2 = prepared([30, 40, 35], 120, 8, 9)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = fn(C.byref(d2), *a2, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, bq.lib().busseq_last_error().decode()
+    torch.cuda.synchronize()
+    assert np.isnan(float(o2[0].cpu()))  # captured, not yet run
+    g.replay()
+    torch.cuda.synchronize()
+    got = float(o2[0].cpu())
+    assert abs(got - w2) <= BIC_RTOL * abs(w2), (got, w2)
+
+
 def test_bic_noalloc_rejects_oversize():
     fn = _noalloc_fn()
     nb = np.array([1 << 17, 1 << 17, 1 << 17], np.int32)  # N above the static limit
