@@ -1154,8 +1154,10 @@ int busseq_bic(busseq_handle* h, double* bic) {
   tb.ty = tb.eb + (size_t)s.K * s.G;
   tb.ny = ny;
   bq::launch_bic(s, h->est, h->ll_ik, tb, h->bic_out, h->stream);
-  LAUNCH_CHECK("k_bic_cell");
-  CUDA_TRY(cudaFreeAsync(scratch, h->stream));
+  cudaError_t e = cudaGetLastError();
+  const cudaError_t e2 = cudaFreeAsync(scratch, h->stream);  // also when a launch failed
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return fail(BUSSEQ_ERR_CUDA, "BIC kernels: %s", cudaGetErrorString(e));
   double out[2];
   CUDA_TRY(cudaMemcpyAsync(out, h->bic_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
